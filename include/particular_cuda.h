@@ -1,0 +1,116 @@
+/*
+ * particular_cuda.h -- C ABI of the GB300 (sm_103a) compute methods for particular.
+ *
+ * The library adds two compute methods beside particular's `sequential`, `parallel`
+ * and `gpu` ones:
+ *   cuda::BruteForce        all-pairs acceleration  (replaces gpu::BruteForce's wgpu
+ *                           dispatch, particular/src/gpu/mod.rs:179-208, and is the
+ *                           GPU counterpart of sequential::BruteForce,
+ *                           particular/src/sequential.rs:181-209)
+ *   cuda::BarnesHut{theta}  tree acceleration        (GPU counterpart of
+ *                           sequential::BarnesHut, particular/src/sequential.rs:456-543)
+ *
+ * Data layout at the boundary (the layout wgpu's padded types already use,
+ * particular/src/gravity/impls/mod.rs:430-434 and gravity/mod.rs:244-272):
+ *   affecting (sources) : float[4] per body = (x, y, z, mu)   -- GravitationalField<Vec3, f32>
+ *   affected  (targets) : float[4] per body = (x, y, z, unused)
+ *   output              : float[3] per affected body = acceleration
+ *
+ * The interaction is given by (softening, checked), mirroring
+ * Acceleration<CHECKED> (softening 0; gravity/newtonian/acceleration.rs:17-58) and
+ * AccelerationSoftened<f32, CHECKED> (gravity/newtonian/acceleration_softened.rs:17-63).
+ *
+ * Every entry point returns PT_OK (0) or a negative PT_ERR_* code and then sets a
+ * thread-local message readable with pt_last_error(). There is no CPU fallback: a
+ * failed call computes nothing. Calls taking host pointers are synchronous (like
+ * gpu::BruteForce, which blocks on the map, particular/src/gpu/mod.rs:200).
+ * Edge cases follow particular/src/gpu/resources.rs:272-280: n_aff == 0 computes
+ * nothing; n_src == 0 yields zero accelerations (the reference panics there on
+ * DynamicBuffer's len != 0 assert, resources.rs:24; this library does not).
+ */
+#ifndef PARTICULAR_CUDA_H
+#define PARTICULAR_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PT_OK 0
+#define PT_ERR_INVALID (-1)  /* bad argument (null pointer, size mismatch, bad flag) */
+#define PT_ERR_CUDA (-2)     /* a CUDA runtime call or kernel launch failed */
+#define PT_ERR_OOM (-3)      /* device or host allocation failed */
+#define PT_ERR_CAPACITY (-4) /* request exceeds the context's capacity limit */
+#define PT_ERR_TIMEOUT (-5)  /* a bounded device-side wait gave up */
+#define PT_ERR_DEPTH (-6)    /* tree deeper than the supported key resolution */
+
+/* Flags for pt_bf_accel_*. */
+/* Bit-identical to sequential::BruteForce: per-body sequential sum over j in
+ * ascending order, IEEE sqrt and divide, no contraction. Slower; it is the
+ * drop-in for callers that need the reference's exact f32 result. */
+#define PT_BF_EXACT 0x1u
+
+/* Opaque context: device, stream and grow-only device buffers. It plays the role
+ * of gpu::GpuResources (particular/src/gpu/mod.rs:84-143): create it once and
+ * reuse it across calls. One context must not be used by two threads at once. */
+typedef struct pt_ctx pt_ctx;
+
+/* Creates a context on `device` (a CUDA ordinal). Replaces GpuResources::new
+ * (particular/src/gpu/mod.rs:96-98) + the lazy init at :128-142. */
+int pt_ctx_create(pt_ctx **ctx, int device);
+/* Frees every device buffer the context owns. NULL is accepted. */
+void pt_ctx_destroy(pt_ctx *ctx);
+/* Message of the last failed call on this thread ("" if none). */
+const char *pt_last_error(void);
+/* Enqueue subsequent work on `stream` (a cudaStream_t; NULL = the context's own
+ * stream). Used to interleave with other CUDA work, e.g. for event timing. */
+int pt_ctx_set_stream(pt_ctx *ctx, void *stream);
+/* Caps the bytes of device memory the context may hold (0 = unlimited). A call
+ * that would grow past it fails with PT_ERR_CAPACITY and computes nothing. */
+int pt_ctx_set_capacity_limit(pt_ctx *ctx, size_t bytes);
+/* Bytes of device memory currently held by the context. */
+size_t pt_ctx_device_bytes(const pt_ctx *ctx);
+/* Number of kernels this context has launched so far. */
+uint64_t pt_ctx_launch_count(const pt_ctx *ctx);
+/* Number of SMs of the context's device. */
+int pt_ctx_sm_count(const pt_ctx *ctx);
+
+/* cuda::BruteForce over host buffers: for each affected body i,
+ *   out[i] = sum_j a(x_i, affecting_j), a from gravity/impls/mod.rs:150-166.
+ * Replaces gpu::BruteForce::compute (particular/src/gpu/mod.rs:186-207), whose
+ * per-body result is sequential::BruteForce's fold (sequential.rs:189-193).
+ * Default path: FP32 with rsqrt on the FMA pipe and compensated (two-sum) per-tile
+ * accumulation; flags = PT_BF_EXACT for the bit-identical path. */
+int pt_bf_accel_f32(pt_ctx *ctx, const float *affected, size_t n_aff, const float *affecting,
+                    size_t n_src, float softening, int checked, uint32_t flags, float *out_xyz);
+
+/* Same computation on device-resident buffers (no copies, asynchronous on the
+ * context's stream). Pointers must be 16-byte aligned device pointers. */
+int pt_bf_accel_f32_device(pt_ctx *ctx, const float *d_affected, size_t n_aff,
+                           const float *d_affecting, size_t n_src, float softening, int checked,
+                           uint32_t flags, float *d_out_xyz);
+
+/* FP64 brute force of the same formula on device buffers (f32 inputs widened to
+ * f64, double accumulation): the error judge for the FP32 methods. It has no
+ * counterpart in the reference, which reports no accuracy figures. */
+int pt_bf_accel_f64_device(pt_ctx *ctx, const float *d_affected, size_t n_aff,
+                           const float *d_affecting, size_t n_src, double softening, int checked,
+                           double *d_out_xyz);
+
+/* Overrides the brute-force launch plan of subsequent calls made from this
+ * thread: targets per thread (1, 2 or 4) and number of j-slices; 0 restores the
+ * automatic choice. Tuning and test knob; results do not depend on it beyond
+ * FP32 summation order. */
+int pt_bf_set_plan(pt_ctx *ctx, int targets_per_thread, int slices);
+
+/* Blocks until all work enqueued by the context has finished; reports any
+ * asynchronous kernel error as PT_ERR_CUDA. */
+int pt_ctx_synchronize(pt_ctx *ctx);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* PARTICULAR_CUDA_H */

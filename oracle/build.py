@@ -1,0 +1,34 @@
+"""Builds the C oracle (oracle/pt_oracle.c) into oracle/_build/liboracle.so.
+
+Test infrastructure only. The flags matter: -ffp-contract=off keeps every f32
+multiply and add separately rounded, as Rust evaluates them (rustc never
+contracts a*b+c into an FMA); -fno-fast-math keeps IEEE semantics; OpenMP gives
+the multi-threaded restatement of particular's rayon methods that the CPU
+baseline times.
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "liboracle.so")
+SRC = os.path.join(HERE, "pt_oracle.c")
+
+CFLAGS = ["-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+          "-fopenmp", "-Wall", "-Wno-unknown-pragmas"]
+
+
+def build(force=False):
+    os.makedirs(OUT_DIR, exist_ok=True)
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= os.path.getmtime(SRC)):
+        return LIB
+    cc = os.environ.get("CC", "gcc")
+    tmp = LIB + ".tmp"
+    subprocess.check_call([cc, *CFLAGS, SRC, "-o", tmp, "-lm"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True))

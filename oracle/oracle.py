@@ -1,0 +1,148 @@
+"""ctypes wrapper over the C oracle (test infrastructure only).
+
+Every function takes packed float32 arrays: sources (n, 4) = (x, y, z, mu),
+targets (n, 4) or (n, 3) = positions. See oracle/pt_oracle.c for the reference
+file:line each restated function follows.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_u32p = ctypes.c_void_p
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not os.path.exists(path):
+            _build.build()
+        L = ctypes.CDLL(path)
+        L.oracle_bf_f32.argtypes = [_f32p, ctypes.c_size_t, _f32p, ctypes.c_size_t,
+                                    ctypes.c_float, ctypes.c_int, _f32p, ctypes.c_int]
+        L.oracle_bf_f64.argtypes = [_f32p, ctypes.c_size_t, _f32p, ctypes.c_size_t,
+                                    ctypes.c_double, ctypes.c_int, _f64p, ctypes.c_int]
+        L.oracle_bh_build.argtypes = [_f32p, ctypes.c_size_t, ctypes.c_int]
+        L.oracle_bh_build.restype = ctypes.c_void_p
+        L.oracle_tree_free.argtypes = [ctypes.c_void_p]
+        L.oracle_tree_node_count.argtypes = [ctypes.c_void_p]
+        L.oracle_tree_node_count.restype = ctypes.c_size_t
+        L.oracle_tree_max_depth.argtypes = [ctypes.c_void_p]
+        L.oracle_tree_export.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 6
+        L.oracle_bh_walk.argtypes = [ctypes.c_void_p, _f32p, ctypes.c_size_t, ctypes.c_float,
+                                     ctypes.c_float, ctypes.c_int, _f32p, _u32p, ctypes.c_int]
+        L.oracle_bh_f32.argtypes = [_f32p, ctypes.c_size_t, _f32p, ctypes.c_size_t,
+                                    ctypes.c_float, ctypes.c_float, ctypes.c_int, _f32p, _u32p,
+                                    ctypes.c_int]
+        L.oracle_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _targets(a):
+    a = np.asarray(a, dtype=np.float32)
+    if a.ndim != 2 or a.shape[1] not in (3, 4):
+        raise ValueError("targets must be (n, 3) or (n, 4)")
+    if a.shape[1] == 3:
+        a = np.concatenate([a, np.zeros((a.shape[0], 1), np.float32)], axis=1)
+    return np.ascontiguousarray(a)
+
+
+def _sources(s):
+    s = np.ascontiguousarray(np.asarray(s, dtype=np.float32))
+    if s.ndim != 2 or s.shape[1] != 4:
+        raise ValueError("sources must be (n, 4) = (x, y, z, mu)")
+    return s
+
+
+def max_threads():
+    return lib().oracle_max_threads()
+
+
+def bf_f32(targets, sources, softening=0.0, checked=True, threads=0):
+    """sequential::BruteForce / parallel::BruteForce (bit-identical per body)."""
+    t, s = _targets(targets), _sources(sources)
+    out = np.zeros((t.shape[0], 3), np.float32)
+    rc = lib().oracle_bf_f32(t, t.shape[0], s, s.shape[0], softening, int(checked), out, threads)
+    if rc:
+        raise RuntimeError(f"oracle_bf_f32 failed: {rc}")
+    return out
+
+
+def bf_f64(targets, sources, softening=0.0, checked=True, threads=0):
+    """FP64 brute force of the same formula: the error judge."""
+    t, s = _targets(targets), _sources(sources)
+    out = np.zeros((t.shape[0], 3), np.float64)
+    rc = lib().oracle_bf_f64(t, t.shape[0], s, s.shape[0], softening, int(checked), out, threads)
+    if rc:
+        raise RuntimeError(f"oracle_bf_f64 failed: {rc}")
+    return out
+
+
+def bh_f32(targets, sources, theta, softening=0.0, checked=True, threads=0, accepted=False):
+    """sequential::BarnesHut (tree over `sources`, walk for every target)."""
+    t, s = _targets(targets), _sources(sources)
+    out = np.zeros((t.shape[0], 3), np.float32)
+    acc = np.zeros(t.shape[0], np.uint32) if accepted else None
+    rc = lib().oracle_bh_f32(t, t.shape[0], s, s.shape[0], theta, softening, int(checked), out,
+                             acc.ctypes.data if accepted else None, threads)
+    if rc:
+        raise RuntimeError(f"oracle_bh_f32 failed: {rc}")
+    return (out, acc) if accepted else out
+
+
+class Tree:
+    """The reference orthtree built over `sources` (tree/mod.rs:91-138)."""
+
+    def __init__(self, sources, max_depth=0):
+        self._s = _sources(sources)
+        self._h = lib().oracle_bh_build(self._s, self._s.shape[0], max_depth)
+        if not self._h:
+            raise MemoryError("oracle_bh_build failed")
+        if lib().oracle_tree_max_depth(self._h) < 0:
+            lib().oracle_tree_free(self._h)
+            self._h = None
+            raise RuntimeError("oracle_bh_build: depth limit reached")
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_tree_free(self._h)
+            self._h = None
+
+    @property
+    def node_count(self):
+        return lib().oracle_tree_node_count(self._h)
+
+    @property
+    def max_depth(self):
+        return lib().oracle_tree_max_depth(self._h)
+
+    def export(self):
+        n = self.node_count
+        internal = np.zeros(n, np.int32)
+        child = np.zeros((n, 8), np.int32)
+        box = np.zeros((n, 6), np.float32)
+        data = np.zeros((n, 4), np.float32)
+        rng = np.zeros((n, 2), np.int32)
+        perm = np.zeros(self._s.shape[0], np.uint32)
+        lib().oracle_tree_export(self._h, internal.ctypes.data, child.ctypes.data,
+                                 box.ctypes.data, data.ctypes.data, rng.ctypes.data,
+                                 perm.ctypes.data)
+        return dict(internal=internal, child=child, box=box, data=data, range=rng, perm=perm)
+
+    def walk(self, targets, theta, softening=0.0, checked=True, threads=0, accepted=False):
+        t = _targets(targets)
+        out = np.zeros((t.shape[0], 3), np.float32)
+        acc = np.zeros(t.shape[0], np.uint32) if accepted else None
+        rc = lib().oracle_bh_walk(self._h, t, t.shape[0], theta, softening, int(checked), out,
+                                  acc.ctypes.data if accepted else None, threads)
+        if rc:
+            raise RuntimeError(f"oracle_bh_walk failed: {rc}")
+        return (out, acc) if accepted else out

@@ -1,0 +1,103 @@
+"""Loads libparticular_cuda.so (the C ABI of include/particular_cuda.h) with ctypes.
+
+There is no fallback: if the library is missing or a call fails, a CudaError is
+raised, as particular's gpu method panics on a failed device call
+(particular/src/gpu/resources.rs:345, gpu/mod.rs:200).
+"""
+import ctypes
+import os
+import re
+
+from . import build_native
+
+PT_OK = 0
+PT_ERR_INVALID = -1
+PT_ERR_CUDA = -2
+PT_ERR_OOM = -3
+PT_ERR_CAPACITY = -4
+PT_ERR_TIMEOUT = -5
+PT_ERR_DEPTH = -6
+
+PT_BF_EXACT = 0x1
+
+_NAMES = {PT_ERR_INVALID: "PT_ERR_INVALID", PT_ERR_CUDA: "PT_ERR_CUDA", PT_ERR_OOM: "PT_ERR_OOM",
+          PT_ERR_CAPACITY: "PT_ERR_CAPACITY", PT_ERR_TIMEOUT: "PT_ERR_TIMEOUT",
+          PT_ERR_DEPTH: "PT_ERR_DEPTH"}
+
+HEADER = os.path.join(build_native.ROOT, "include", "particular_cuda.h")
+
+
+class CudaError(RuntimeError):
+    """A failed call into libparticular_cuda.so (status code + message)."""
+
+    def __init__(self, code, message):
+        self.code = code
+        super().__init__(f"{_NAMES.get(code, code)}: {message}")
+
+
+_lib = None
+
+c_size = ctypes.c_size_t
+c_ptr = ctypes.c_void_p
+
+
+def _declare(L):
+    sig = {
+        "pt_ctx_create": (ctypes.c_int, [ctypes.POINTER(c_ptr), ctypes.c_int]),
+        "pt_ctx_destroy": (None, [c_ptr]),
+        "pt_last_error": (ctypes.c_char_p, []),
+        "pt_ctx_set_stream": (ctypes.c_int, [c_ptr, c_ptr]),
+        "pt_ctx_set_capacity_limit": (ctypes.c_int, [c_ptr, c_size]),
+        "pt_ctx_device_bytes": (c_size, [c_ptr]),
+        "pt_ctx_launch_count": (ctypes.c_uint64, [c_ptr]),
+        "pt_ctx_sm_count": (ctypes.c_int, [c_ptr]),
+        "pt_ctx_synchronize": (ctypes.c_int, [c_ptr]),
+        "pt_bf_accel_f32": (ctypes.c_int, [c_ptr, c_ptr, c_size, c_ptr, c_size, ctypes.c_float,
+                                           ctypes.c_int, ctypes.c_uint32, c_ptr]),
+        "pt_bf_accel_f32_device": (ctypes.c_int, [c_ptr, c_ptr, c_size, c_ptr, c_size,
+                                                  ctypes.c_float, ctypes.c_int, ctypes.c_uint32,
+                                                  c_ptr]),
+        "pt_bf_accel_f64_device": (ctypes.c_int, [c_ptr, c_ptr, c_size, c_ptr, c_size,
+                                                  ctypes.c_double, ctypes.c_int, c_ptr]),
+        "pt_bf_set_plan": (ctypes.c_int, [c_ptr, ctypes.c_int, ctypes.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def lib_path():
+    return build_native.LIB
+
+
+def lib():
+    """The loaded native library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        path = build_native.LIB
+        if not os.path.exists(path):
+            raise CudaError(PT_ERR_CUDA, f"{path} is not built: run "
+                            "`python -c 'import __graft_entry__ as g; g.build()'` first")
+        L = ctypes.CDLL(path)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def last_error():
+    msg = lib().pt_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(rc):
+    if rc != PT_OK:
+        raise CudaError(rc, last_error())
+    return rc
+
+
+def header_functions():
+    """Names of every function the C header declares."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pt_[a-z0-9_]+)\s*\(", text)))

@@ -1,0 +1,453 @@
+// cuda::BruteForce: all-pairs gravitational acceleration on sm_103a.
+//
+// Computes, for every affected body i, out_i = sum_j a(x_i, s_j) with the
+// per-pair kernel of particular/src/gravity/impls/mod.rs:150-166:
+//     d = x_j - x_i;  n = |d|^2;  checked && n == 0 -> d;
+//     else a = d * (mu_j / (n_s * sqrt(n_s))),  n_s = n + eps^2
+// (the sum that sequential::BruteForce folds, particular/src/sequential.rs:189-193,
+// and that the wgpu shader tiles, particular/src/gpu/bruteforce_shared.wgsl:16-28).
+//
+// Three kernels:
+//  * bf_fast  : the throughput path. CTAs own an i-block of THREADS*K targets (K
+//               targets per thread) and a j-slice; source tiles of TILE float4
+//               are staged in shared memory by cp.async through a STAGES-deep
+//               ring; every thread reads each tile entry as a warp broadcast and
+//               evaluates K pairs with rsqrt on the MUFU unit and 12 FP32 FMA-pipe
+//               instructions per pair. Sums are plain FP32 inside a tile and
+//               compensated (two-sum) across tiles. j-slices (grid.y) keep all SMs
+//               busy at small N; their partials are combined by bf_fixup in a fixed
+//               order, so the result is deterministic.
+//  * bf_exact : one thread per target, sequential j order, IEEE sqrt/div and no
+//               contraction: bit-identical to sequential::BruteForce.
+//  * bf_f64   : the same formula in double, the error judge.
+#include "pt_common.cuh"
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+
+namespace pt {
+namespace bf {
+
+constexpr int THREADS = 128;
+constexpr int TILE = 256;  // sources per stage: 4 KiB
+constexpr int STAGES = 4;
+constexpr int COPIES = TILE / THREADS;
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Stages sources [j0 + t*TILE, min(j_end, j0 + (t+1)*TILE)) into `stage`.
+__device__ __forceinline__ void load_tile(float4 *stage, const float4 *__restrict__ src, int j0,
+                                          int j_end, int t) {
+    const int base = j0 + t * TILE;
+#pragma unroll
+    for (int r = 0; r < COPIES; ++r) {
+        const int e = threadIdx.x + r * THREADS;
+        if (base + e < j_end) cp_async16(stage + e, src + base + e);
+    }
+}
+
+// Runs f(tile_ptr, count) over the sources [j0, j_end) through the cp.async ring.
+// Every thread of the CTA must call it (it synchronises the CTA).
+template <class F>
+__device__ __forceinline__ void for_each_tile(float4 (*tiles)[TILE], const float4 *__restrict__ src,
+                                              int j0, int j_end, F &&f) {
+    const int ntiles = (j_end - j0 + TILE - 1) / TILE;
+#pragma unroll
+    for (int st = 0; st < STAGES - 1; ++st) {
+        if (st < ntiles) load_tile(tiles[st], src, j0, j_end, st);
+        cp_async_commit();
+    }
+    for (int t = 0; t < ntiles; ++t) {
+        cp_async_wait<STAGES - 2>();
+        __syncthreads();  // tile t visible to all; tile t-1 fully consumed
+        const int nt = t + STAGES - 1;
+        if (nt < ntiles) load_tile(tiles[nt % STAGES], src, j0, j_end, nt);
+        cp_async_commit();
+        f(static_cast<const float4 *>(tiles[t % STAGES]), min(TILE, j_end - (j0 + t * TILE)));
+    }
+    cp_async_wait<0>();
+}
+
+// Knuth two-sum: s + c tracks the running sum with the rounding error of each add.
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float t) {
+    const float sn = s + t;
+    const float bp = sn - s;
+    const float err = (s - (sn - bp)) + (t - bp);
+    s = sn;
+    c += err;
+}
+
+template <int K, bool GUARD>
+__device__ __forceinline__ void interact(const float4 p, const float (&xi)[K], const float (&yi)[K],
+                                         const float (&zi)[K], float (&ax)[K], float (&ay)[K],
+                                         float (&az)[K], float eps2) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const float dx = p.x - xi[k];
+        const float dy = p.y - yi[k];
+        const float dz = p.z - zi[k];
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+        const float inv = rsqrtf(r2);
+        float s = (p.w * inv) * (inv * inv);
+        if (GUARD) s = (r2 > 0.0f) ? s : 0.0f;  // checked && n == 0 contributes d == 0
+        ax[k] = fmaf(dx, s, ax[k]);
+        ay[k] = fmaf(dy, s, ay[k]);
+        az[k] = fmaf(dz, s, az[k]);
+    }
+}
+
+// part (when non-null): [gridDim.y][2][n_aff] float4 = per-slice (sum, compensation).
+template <int K, bool GUARD>
+__global__ void __launch_bounds__(THREADS)
+    bf_fast(const float4 *__restrict__ aff, int n_aff, const float4 *__restrict__ src, int n_src,
+            float eps2, int slice_len, float4 *__restrict__ part, float *__restrict__ out) {
+    __shared__ __align__(16) float4 tiles[STAGES][TILE];
+    const int i0 = blockIdx.x * (THREADS * K);
+    const int j0 = blockIdx.y * slice_len;
+    const int j_end = min(n_src, j0 + slice_len);
+
+    float xi[K], yi[K], zi[K], ax[K], ay[K], az[K], sx[K], sy[K], sz[K], cx[K], cy[K], cz[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int i = i0 + k * THREADS + threadIdx.x;
+        const float4 p = (i < n_aff) ? aff[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        xi[k] = p.x;
+        yi[k] = p.y;
+        zi[k] = p.z;
+        ax[k] = ay[k] = az[k] = 0.f;
+        sx[k] = sy[k] = sz[k] = 0.f;
+        cx[k] = cy[k] = cz[k] = 0.f;
+    }
+
+    for_each_tile(tiles, src, j0, j_end, [&](const float4 *T, int cnt) {
+        if (cnt == TILE) {
+#pragma unroll 8
+            for (int jj = 0; jj < TILE; ++jj) interact<K, GUARD>(T[jj], xi, yi, zi, ax, ay, az, eps2);
+        } else {
+#pragma unroll 1
+            for (int jj = 0; jj < cnt; ++jj) interact<K, GUARD>(T[jj], xi, yi, zi, ax, ay, az, eps2);
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            two_sum_acc(sx[k], cx[k], ax[k]);
+            two_sum_acc(sy[k], cy[k], ay[k]);
+            two_sum_acc(sz[k], cz[k], az[k]);
+            ax[k] = ay[k] = az[k] = 0.f;
+        }
+    });
+
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int i = i0 + k * THREADS + threadIdx.x;
+        if (i >= n_aff) continue;
+        if (part) {
+            float4 *ps = part + size_t(blockIdx.y) * 2 * size_t(n_aff);
+            ps[i] = make_float4(sx[k], sy[k], sz[k], 0.f);
+            ps[size_t(n_aff) + i] = make_float4(cx[k], cy[k], cz[k], 0.f);
+        } else {
+            out[3 * size_t(i) + 0] = sx[k] + cx[k];
+            out[3 * size_t(i) + 1] = sy[k] + cy[k];
+            out[3 * size_t(i) + 2] = sz[k] + cz[k];
+        }
+    }
+}
+
+// Combines the slices' (sum, compensation) pairs in slice order, in double.
+__global__ void bf_fixup(const float4 *__restrict__ part, int n_aff, int slices, float *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_aff) return;
+    double x = 0.0, y = 0.0, z = 0.0;
+    for (int s = 0; s < slices; ++s) {
+        const float4 a = part[size_t(s) * 2 * size_t(n_aff) + i];
+        const float4 c = part[size_t(s) * 2 * size_t(n_aff) + size_t(n_aff) + i];
+        x += double(a.x) + double(c.x);
+        y += double(a.y) + double(c.y);
+        z += double(a.z) + double(c.z);
+    }
+    out[3 * size_t(i) + 0] = float(x);
+    out[3 * size_t(i) + 1] = float(y);
+    out[3 * size_t(i) + 2] = float(z);
+}
+
+// Bit-identical restatement of sequential::BruteForce (sequential.rs:189-193 over
+// gravity/impls/mod.rs:156-165): every operation is an explicitly rounded IEEE op.
+__global__ void __launch_bounds__(THREADS)
+    bf_exact(const float4 *__restrict__ aff, int n_aff, const float4 *__restrict__ src, int n_src,
+             float soft2, int checked, float *__restrict__ out) {
+    __shared__ __align__(16) float4 tiles[STAGES][TILE];
+    const int i = blockIdx.x * THREADS + threadIdx.x;
+    const float4 pi = (i < n_aff) ? aff[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for_each_tile(tiles, src, 0, n_src, [&](const float4 *T, int cnt) {
+#pragma unroll 1
+        for (int jj = 0; jj < cnt; ++jj) {
+            const float4 p = T[jj];
+            const float dx = __fsub_rn(p.x, pi.x);
+            const float dy = __fsub_rn(p.y, pi.y);
+            const float dz = __fsub_rn(p.z, pi.z);
+            const float n = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            float ax, ay, az;
+            if (checked && n == 0.0f) {
+                ax = dx;
+                ay = dy;
+                az = dz;
+            } else {
+                const float ns = __fadd_rn(n, soft2);
+                const float s = __fdiv_rn(p.w, __fmul_rn(ns, __fsqrt_rn(ns)));
+                ax = __fmul_rn(dx, s);
+                ay = __fmul_rn(dy, s);
+                az = __fmul_rn(dz, s);
+            }
+            sx = __fadd_rn(sx, ax);
+            sy = __fadd_rn(sy, ay);
+            sz = __fadd_rn(sz, az);
+        }
+    });
+    if (i < n_aff) {
+        out[3 * size_t(i) + 0] = sx;
+        out[3 * size_t(i) + 1] = sy;
+        out[3 * size_t(i) + 2] = sz;
+    }
+}
+
+// FP64 judge: f32 inputs widened, double arithmetic and accumulation.
+__global__ void __launch_bounds__(THREADS)
+    bf_f64(const float4 *__restrict__ aff, int n_aff, const float4 *__restrict__ src, int n_src,
+           double soft2, int checked, double *__restrict__ out) {
+    __shared__ __align__(16) float4 tiles[STAGES][TILE];
+    const int i = blockIdx.x * THREADS + threadIdx.x;
+    const float4 pi = (i < n_aff) ? aff[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const double xi = pi.x, yi = pi.y, zi = pi.z;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for_each_tile(tiles, src, 0, n_src, [&](const float4 *T, int cnt) {
+#pragma unroll 2
+        for (int jj = 0; jj < cnt; ++jj) {
+            const float4 p = T[jj];
+            const double dx = double(p.x) - xi, dy = double(p.y) - yi, dz = double(p.z) - zi;
+            const double n = dx * dx + dy * dy + dz * dz;
+            if (checked && n == 0.0) continue;
+            const double ns = n + soft2;
+            const double s = double(p.w) / (ns * sqrt(ns));
+            sx += dx * s;
+            sy += dy * s;
+            sz += dz * s;
+        }
+    });
+    if (i < n_aff) {
+        out[3 * size_t(i) + 0] = sx;
+        out[3 * size_t(i) + 1] = sy;
+        out[3 * size_t(i) + 2] = sz;
+    }
+}
+
+using FastKernel = void (*)(const float4 *, int, const float4 *, int, float, int, float4 *, float *);
+
+template <int K>
+FastKernel pick(bool guard) {
+    return guard ? bf_fast<K, true> : bf_fast<K, false>;
+}
+
+FastKernel fast_kernel(int K, bool guard) {
+    switch (K) {
+        case 1: return pick<1>(guard);
+        case 2: return pick<2>(guard);
+        default: return pick<4>(guard);
+    }
+}
+
+struct Plan {
+    int K = 4;
+    int slices = 1;
+    int slice_len = 0;
+    int n_ib = 0;
+};
+
+// Occupancy of the fast kernels, cached per (K, guard).
+static int occupancy(int K, bool guard) {
+    static int cache[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    const int kk = K == 1 ? 0 : (K == 2 ? 1 : 2);
+    int &o = cache[kk][guard ? 1 : 0];
+    if (o == 0) {
+        int v = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, fast_kernel(K, guard), THREADS, 0) != cudaSuccess || v < 1)
+            v = 1;
+        o = v;
+    }
+    return o;
+}
+
+// Picks K and the number of j-slices by a wave model: CTAs of equal cost run in
+// ceil(ctas / slots) waves; minimise waves * per-CTA work, plus the fixup pass.
+static Plan plan(const pt_ctx *ctx, int n_aff, int n_src, bool guard, int force_k, int force_s) {
+    Plan p;
+    p.K = force_k ? force_k : (n_aff >= 16384 ? 4 : (n_aff >= 4096 ? 2 : 1));
+    p.n_ib = (n_aff + THREADS * p.K - 1) / (THREADS * p.K);
+    const int tiles = (n_src + TILE - 1) / TILE;
+    const long long slots = (long long)std::max(1, ctx->sm_count) * occupancy(p.K, guard);
+    int best_s = 1;
+    double best_cost = 1e300;
+    const int max_s = std::max(1, std::min(tiles, 256));
+    for (int s = 1; s <= max_s; ++s) {
+        const int len_tiles = (tiles + s - 1) / s;
+        const int s_eff = (tiles + len_tiles - 1) / len_tiles;
+        if (s_eff != s) continue;
+        const long long ctas = (long long)p.n_ib * s;
+        const long long waves = (ctas + slots - 1) / slots;
+        // per-CTA cost ~ tiles it streams (plus a fixed tile of start-up);
+        // fixup reads 32 B per target per slice.
+        double cost = double(waves) * (len_tiles + 1) * p.K;
+        if (s > 1) cost += 0.02 * s * (double(n_aff) / double(slots * THREADS)) + 1.0;
+        if (cost < best_cost * 0.999) {
+            best_cost = cost;
+            best_s = s;
+        }
+    }
+    if (force_s) best_s = std::max(1, std::min(force_s, std::max(1, tiles)));
+    const int len_tiles = (tiles + best_s - 1) / best_s;
+    p.slice_len = len_tiles * TILE;
+    p.slices = (n_src + p.slice_len - 1) / p.slice_len;
+    return p;
+}
+
+struct Forced {
+    int k = 0, s = 0;
+};
+static thread_local Forced g_forced;
+
+}  // namespace bf
+
+// Launches the fast or exact f32 brute force on device buffers (ctx->stream).
+int bf_launch_f32(pt_ctx *ctx, const float4 *aff, int n_aff, const float4 *src, int n_src,
+                  float softening, int checked, uint32_t flags, float *out) {
+    using namespace bf;
+    cudaStream_t st = ctx->stream;
+    if (n_aff == 0) return PT_OK;
+    if (n_src == 0) {
+        PT_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * 3 * size_t(n_aff), st));
+        return PT_OK;
+    }
+    const float soft2 = softening * softening;
+    if (flags & PT_BF_EXACT) {
+        dim3 grid((n_aff + THREADS - 1) / THREADS);
+        bf_exact<<<grid, THREADS, 0, st>>>(aff, n_aff, src, n_src, soft2, checked, out);
+        return check_launch(ctx, "bf_exact");
+    }
+    const bool guard = checked && soft2 == 0.0f;
+    Plan p = plan(ctx, n_aff, n_src, guard, g_forced.k, g_forced.s);
+    float4 *part = nullptr;
+    if (p.slices > 1) {
+        PT_TRY(ensure(ctx, BUF_PART, sizeof(float4) * 2 * size_t(n_aff) * size_t(p.slices)));
+        part = static_cast<float4 *>(ctx->bufs[BUF_PART].ptr);
+    }
+    dim3 grid(p.n_ib, p.slices);
+    fast_kernel(p.K, guard)<<<grid, THREADS, 0, st>>>(aff, n_aff, src, n_src, soft2, p.slice_len, part, out);
+    PT_TRY(check_launch(ctx, "bf_fast"));
+    if (part) {
+        bf_fixup<<<(n_aff + 255) / 256, 256, 0, st>>>(part, n_aff, p.slices, out);
+        PT_TRY(check_launch(ctx, "bf_fixup"));
+    }
+    return PT_OK;
+}
+
+int bf_launch_f64(pt_ctx *ctx, const float4 *aff, int n_aff, const float4 *src, int n_src,
+                  double softening, int checked, double *out) {
+    using namespace bf;
+    if (n_aff == 0) return PT_OK;
+    if (n_src == 0) {
+        PT_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 3 * size_t(n_aff), ctx->stream));
+        return PT_OK;
+    }
+    dim3 grid((n_aff + THREADS - 1) / THREADS);
+    bf_f64<<<grid, THREADS, 0, ctx->stream>>>(aff, n_aff, src, n_src, softening * softening, checked, out);
+    return check_launch(ctx, "bf_f64");
+}
+
+static int validate_sizes(const char *fn, size_t n_aff, size_t n_src) {
+    const size_t lim = size_t(INT_MAX) / 8;
+    if (n_aff > lim || n_src > lim)
+        return set_error(PT_ERR_INVALID, "%s: n_aff=%zu n_src=%zu exceed the limit %zu", fn, n_aff, n_src, lim);
+    return PT_OK;
+}
+
+}  // namespace pt
+
+extern "C" {
+
+int pt_bf_set_plan(pt_ctx *ctx, int targets_per_thread, int slices) {
+    pt::clear_error();
+    if (!ctx) return pt::set_error(PT_ERR_INVALID, "pt_bf_set_plan: ctx is NULL");
+    if (!(targets_per_thread == 0 || targets_per_thread == 1 || targets_per_thread == 2 ||
+          targets_per_thread == 4) || slices < 0)
+        return pt::set_error(PT_ERR_INVALID, "pt_bf_set_plan: targets_per_thread must be 0, 1, 2 or 4 and slices >= 0");
+    pt::bf::g_forced.k = targets_per_thread;
+    pt::bf::g_forced.s = slices;
+    return PT_OK;
+}
+
+int pt_bf_accel_f32_device(pt_ctx *ctx, const float *d_aff, size_t n_aff, const float *d_src, size_t n_src,
+                           float softening, int checked, uint32_t flags, float *d_out) {
+    pt::clear_error();
+    if (!ctx) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f32_device: ctx is NULL");
+    if (flags & ~PT_BF_EXACT) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f32_device: unknown flags 0x%x", flags);
+    PT_TRY(pt::validate_sizes("pt_bf_accel_f32_device", n_aff, n_src));
+    if (n_aff && (!d_aff || !d_out)) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f32_device: NULL buffer");
+    if (n_src && !d_src) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f32_device: NULL affecting buffer");
+    if ((n_aff && !pt::aligned16(d_aff)) || (n_src && !pt::aligned16(d_src)))
+        return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f32_device: body buffers must be 16-byte aligned");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    return pt::bf_launch_f32(ctx, reinterpret_cast<const float4 *>(d_aff), int(n_aff),
+                             reinterpret_cast<const float4 *>(d_src), int(n_src), softening, checked, flags, d_out);
+}
+
+int pt_bf_accel_f64_device(pt_ctx *ctx, const float *d_aff, size_t n_aff, const float *d_src, size_t n_src,
+                           double softening, int checked, double *d_out) {
+    pt::clear_error();
+    if (!ctx) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f64_device: ctx is NULL");
+    PT_TRY(pt::validate_sizes("pt_bf_accel_f64_device", n_aff, n_src));
+    if (n_aff && (!d_aff || !d_out)) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f64_device: NULL buffer");
+    if (n_src && !d_src) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f64_device: NULL affecting buffer");
+    if ((n_aff && !pt::aligned16(d_aff)) || (n_src && !pt::aligned16(d_src)))
+        return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f64_device: body buffers must be 16-byte aligned");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    return pt::bf_launch_f64(ctx, reinterpret_cast<const float4 *>(d_aff), int(n_aff),
+                             reinterpret_cast<const float4 *>(d_src), int(n_src), softening, checked, d_out);
+}
+
+int pt_bf_accel_f32(pt_ctx *ctx, const float *aff, size_t n_aff, const float *src, size_t n_src, float softening,
+                    int checked, uint32_t flags, float *out) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bf_accel_f32: ctx is NULL");
+    if (flags & ~PT_BF_EXACT) return set_error(PT_ERR_INVALID, "pt_bf_accel_f32: unknown flags 0x%x", flags);
+    PT_TRY(validate_sizes("pt_bf_accel_f32", n_aff, n_src));
+    if (n_aff && (!aff || !out)) return set_error(PT_ERR_INVALID, "pt_bf_accel_f32: NULL buffer");
+    if (n_src && !src) return set_error(PT_ERR_INVALID, "pt_bf_accel_f32: NULL affecting buffer");
+    if (n_aff == 0) return PT_OK;
+    PT_CUDA(cudaSetDevice(ctx->device));
+    const bool same = (aff == src) && (n_aff == n_src);
+    PT_TRY(ensure(ctx, BUF_AFF, 16 * n_aff));
+    if (!same && n_src) PT_TRY(ensure(ctx, BUF_SRC, 16 * n_src));
+    PT_TRY(ensure(ctx, BUF_OUT, 12 * n_aff));
+    float *d_aff = static_cast<float *>(ctx->bufs[BUF_AFF].ptr);
+    float *d_src = same ? d_aff : static_cast<float *>(ctx->bufs[BUF_SRC].ptr);
+    float *d_out = static_cast<float *>(ctx->bufs[BUF_OUT].ptr);
+    cudaStream_t st = ctx->stream;
+    PT_CUDA(cudaMemcpyAsync(d_aff, aff, 16 * n_aff, cudaMemcpyHostToDevice, st));
+    if (!same && n_src) PT_CUDA(cudaMemcpyAsync(d_src, src, 16 * n_src, cudaMemcpyHostToDevice, st));
+    PT_TRY(bf_launch_f32(ctx, reinterpret_cast<const float4 *>(d_aff), int(n_aff),
+                         reinterpret_cast<const float4 *>(d_src), int(n_src), softening, checked, flags, d_out));
+    PT_CUDA(cudaMemcpyAsync(out, d_out, 12 * n_aff, cudaMemcpyDeviceToHost, st));
+    PT_CUDA(cudaStreamSynchronize(st));
+    return PT_OK;
+}
+
+}  // extern "C"

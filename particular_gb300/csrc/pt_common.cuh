@@ -1,0 +1,72 @@
+// Internal helpers shared by the translation units of libparticular_cuda.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+
+#include "particular_cuda.h"
+
+namespace pt {
+
+// Thread-local last-error message (pt_last_error()).
+int set_error(int code, const char *fmt, ...);
+void clear_error();
+
+// Grow-only device buffer owned by a context. Never shrinks; freed with the context.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+};
+
+enum BufSlot : int {
+    BUF_AFF = 0,   // targets, float4
+    BUF_SRC,       // sources, float4
+    BUF_OUT,       // accelerations, float3
+    BUF_PART,      // split-j partial sums
+    BUF_OUT64,     // f64 outputs
+    BUF_COUNT
+};
+
+}  // namespace pt
+
+struct pt_ctx {
+    int device = 0;
+    int sm_count = 0;
+    int max_smem_optin = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    size_t capacity_limit = 0;  // 0 = unlimited
+    size_t bytes_held = 0;
+    unsigned long long launches = 0;
+    pt::DevBuf bufs[pt::BUF_COUNT];
+    // Extra subsystems hang off the context lazily.
+    void *bh = nullptr;
+};
+
+namespace pt {
+
+// Ensures ctx->bufs[slot] holds at least `bytes`; returns PT_OK or an error code.
+int ensure(pt_ctx *ctx, int slot, size_t bytes);
+// Generic grow-only buffer (for subsystems that keep their own DevBufs).
+int ensure_buf(pt_ctx *ctx, DevBuf &b, size_t bytes);
+void free_buf(pt_ctx *ctx, DevBuf &b);
+
+// Checks the launch just made; counts it.
+int check_launch(pt_ctx *ctx, const char *what);
+int check_cuda(cudaError_t e, const char *what);
+
+inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace pt
+
+#define PT_TRY(expr)                    \
+    do {                                \
+        int _pt_rc = (expr);            \
+        if (_pt_rc != PT_OK) return _pt_rc; \
+    } while (0)
+
+#define PT_CUDA(expr) PT_TRY(::pt::check_cuda((expr), #expr))

@@ -1,0 +1,113 @@
+"""The `cuda` compute methods: the GB300 counterpart of particular's `gpu` module.
+
+Mirrors particular/src/gpu/mod.rs:
+* CudaResources      - GpuResources (gpu/mod.rs:84-143): create once, reuse across calls
+* BruteForce         - gpu::BruteForce (gpu/mod.rs:145-208): `compute(storage)`
+* cuda_brute_force   - the GpuCompute::gpu_brute_force sugar (gpu/mod.rs:13-37)
+
+`compute` accepts every storage the reference's methods accept (a particle
+sequence, Ordered, Reordered, Between) and returns the accelerations of the
+affected particles as a float32 (n, 3) array, in the affected order (the
+reference returns a `std::vec::IntoIter` over the same values).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+from .gravity import fields, positions
+from .storage import as_between
+
+
+class CudaResources:
+    """A libparticular_cuda context: device, stream and grow-only device buffers."""
+
+    def __init__(self, device=0):
+        L = N.lib()
+        h = ctypes.c_void_p()
+        N.check(L.pt_ctx_create(ctypes.byref(h), int(device)))
+        self._h = h
+        self.device = int(device)
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise N.CudaError(N.PT_ERR_INVALID, "CudaResources used after close()")
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            N.lib().pt_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def launch_count(self):
+        return int(N.lib().pt_ctx_launch_count(self.handle))
+
+    @property
+    def device_bytes(self):
+        return int(N.lib().pt_ctx_device_bytes(self.handle))
+
+    @property
+    def sm_count(self):
+        return int(N.lib().pt_ctx_sm_count(self.handle))
+
+    def set_capacity_limit(self, nbytes):
+        N.check(N.lib().pt_ctx_set_capacity_limit(self.handle, int(nbytes)))
+
+    def set_stream(self, stream_handle):
+        """Enqueue on a raw cudaStream_t (int handle); None = the context's own stream."""
+        N.check(N.lib().pt_ctx_set_stream(self.handle, stream_handle or None))
+
+    def synchronize(self):
+        N.check(N.lib().pt_ctx_synchronize(self.handle))
+
+
+def _ptr(a):
+    return a.ctypes.data if a.size else None
+
+
+class BruteForce:
+    """cuda::BruteForce: all-pairs accelerations on the GPU.
+
+    `exact=True` selects the bit-identical restatement of sequential::BruteForce
+    (sequential j order, IEEE sqrt and divide); the default is the fast FP32 path
+    with compensated accumulation.
+    """
+
+    def __init__(self, resources, interaction, exact=False):
+        self.resources = resources
+        self.interaction = interaction
+        self.exact = bool(exact)
+
+    def compute(self, storage):
+        b = as_between(storage)
+        aff = positions(b.affected)
+        src = fields(b.affecting)
+        out = np.zeros((aff.shape[0], 3), np.float32)
+        if aff.shape[0] == 0:
+            return out
+        same = b.affected is b.affecting
+        it = self.interaction
+        flags = N.PT_BF_EXACT if self.exact else 0
+        N.check(N.lib().pt_bf_accel_f32(self.resources.handle, _ptr(aff), aff.shape[0],
+                                        _ptr(aff) if same else _ptr(src), src.shape[0],
+                                        it.softening, int(it.is_checked), flags, _ptr(out)))
+        return out
+
+
+def cuda_brute_force(storage, resources, interaction, exact=False):
+    """`storage.cuda_brute_force(resources, interaction)` (CudaCompute sugar)."""
+    return BruteForce(resources, interaction, exact).compute(storage)
