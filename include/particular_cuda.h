@@ -64,8 +64,9 @@ int pt_ctx_create(pt_ctx **ctx, int device);
 void pt_ctx_destroy(pt_ctx *ctx);
 /* Message of the last failed call on this thread ("" if none). */
 const char *pt_last_error(void);
-/* Enqueue subsequent work on `stream` (a cudaStream_t; NULL = the context's own
- * stream). Used to interleave with other CUDA work, e.g. for event timing. */
+/* Enqueue subsequent work on `stream` (a cudaStream_t). NULL selects the
+ * context's own non-blocking stream, not the legacy default stream. Used to
+ * interleave with other CUDA work, e.g. for event timing. */
 int pt_ctx_set_stream(pt_ctx *ctx, void *stream);
 /* Caps the bytes of device memory the context may hold (0 = unlimited). A call
  * that would grow past it fails with PT_ERR_CAPACITY and computes nothing. */
@@ -104,6 +105,11 @@ int pt_bf_accel_f64_device(pt_ctx *ctx, const float *d_affected, size_t n_aff,
  * automatic choice. Tuning and test knob; results do not depend on it beyond
  * FP32 summation order. */
 int pt_bf_set_plan(pt_ctx *ctx, int targets_per_thread, int slices);
+
+/* Measures the device's FP32 FMA-pipe throughput (TFLOP/s, FFMA = 2 flops) with
+ * a dependent-chain FFMA kernel over every SM, at the clock the device runs at
+ * now. Roofline denominator for the FP32-bound kernels; no reference counterpart. */
+int pt_measure_fp32_peak(pt_ctx *ctx, double *tflops);
 
 /* Blocks until all work enqueued by the context has finished; reports any
  * asynchronous kernel error as PT_ERR_CUDA. */

@@ -60,6 +60,7 @@ def _declare(L):
         "pt_bf_accel_f64_device": (ctypes.c_int, [c_ptr, c_ptr, c_size, c_ptr, c_size,
                                                   ctypes.c_double, ctypes.c_int, c_ptr]),
         "pt_bf_set_plan": (ctypes.c_int, [c_ptr, ctypes.c_int, ctypes.c_int]),
+        "pt_measure_fp32_peak": (ctypes.c_int, [c_ptr, ctypes.POINTER(ctypes.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

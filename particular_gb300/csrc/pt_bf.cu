@@ -9,14 +9,14 @@
 //
 // Three kernels:
 //  * bf_fast  : the throughput path. CTAs own an i-block of THREADS*K targets (K
-//               targets per thread) and a j-slice; source tiles of TILE float4
-//               are staged in shared memory by cp.async through a STAGES-deep
-//               ring; every thread reads each tile entry as a warp broadcast and
-//               evaluates K pairs with rsqrt on the MUFU unit and 12 FP32 FMA-pipe
-//               instructions per pair. Sums are plain FP32 inside a tile and
-//               compensated (two-sum) across tiles. j-slices (grid.y) keep all SMs
-//               busy at small N; their partials are combined by bf_fixup in a fixed
-//               order, so the result is deterministic.
+//               targets per thread) and a j-slice; source tiles of TILE bodies, in
+//               structure-of-arrays form (bf_to_soa), are staged in shared memory by
+//               cp.async through a STAGES-deep ring; every thread reads them as warp
+//               broadcasts and evaluates two pairs per packed f32x2 instruction
+//               (12 FMA-pipe lanes-ops and one MUFU rsqrt per pair). Sums are plain
+//               FP32 inside a tile and compensated (two-sum) across tiles. j-slices
+//               (grid.y) keep all SMs busy at small N; their partials are combined by
+//               bf_fixup in a fixed order, so the result is deterministic.
 //  * bf_exact : one thread per target, sequential j order, IEEE sqrt/div and no
 //               contraction: bit-identical to sequential::BruteForce.
 //  * bf_f64   : the same formula in double, the error judge.
@@ -86,36 +86,109 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &c, float t) {
     c += err;
 }
 
-template <int K, bool GUARD>
-__device__ __forceinline__ void interact(const float4 p, const float (&xi)[K], const float (&yi)[K],
-                                         const float (&zi)[K], float (&ax)[K], float (&ay)[K],
-                                         float (&az)[K], float eps2) {
+// ---- packed FP32 (sm_100+ f32x2): one instruction, two lanes of work ------
+// Halves the issue slots the FMA pipe needs, so the pipe, not instruction issue,
+// bounds the inner loop. lo/hi hold two different sources for the same target.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk(f2 v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+// One MUFU.RSQ, no denormal fix-up (n_s >= eps^2 is a normal number whenever eps > 0).
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Two pairs (target i; sources j, j+1) in packed arithmetic: 12 f32x2 FMA-pipe
+// instructions + 2 MUFU. GUARD zeroes the contribution of n == 0 (checked, eps == 0).
+template <bool GUARD>
+__device__ __forceinline__ void interact2(f2 xj, f2 yj, f2 zj, f2 mj, f2 xi, f2 yi, f2 zi, f2 &ax, f2 &ay,
+                                          f2 &az, f2 e2) {
+    const f2 dx = sub2(xj, xi);
+    const f2 dy = sub2(yj, yi);
+    const f2 dz = sub2(zj, zi);
+    const f2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+    float r0, r1;
+    upk(r2, r0, r1);
+    float i0 = rsqrt_ftz(r0), i1 = rsqrt_ftz(r1);
+    if (GUARD) {
+        i0 = (r0 > 0.0f) ? i0 : 0.0f;
+        i1 = (r1 > 0.0f) ? i1 : 0.0f;
+    }
+    const f2 inv = pk(i0, i1);
+    const f2 s = mul2(mul2(mj, inv), mul2(inv, inv));
+    ax = fma2(dx, s, ax);
+    ay = fma2(dy, s, ay);
+    az = fma2(dz, s, az);
+}
+
+template <bool GUARD>
+__device__ __forceinline__ void interact1(float xj, float yj, float zj, float mj, float xi, float yi, float zi,
+                                          float &ax, float &ay, float &az, float eps2) {
+    const float dx = xj - xi, dy = yj - yi, dz = zj - zi;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+    float inv = rsqrt_ftz(r2);
+    if (GUARD) inv = (r2 > 0.0f) ? inv : 0.0f;
+    const float s = (mj * inv) * (inv * inv);
+    ax = fmaf(dx, s, ax);
+    ay = fmaf(dy, s, ay);
+    az = fmaf(dz, s, az);
+}
+
+// Sources in structure-of-arrays form (x[], y[], z[], mu[], each padded to a
+// multiple of TILE) so that one LDS.128 yields two packed source pairs.
+struct SoaTile {
+    float c[4][TILE];
+};
+
+__device__ __forceinline__ void load_tile_soa(SoaTile &stage, const float *__restrict__ soa, int n_pad, int j0,
+                                              int j_end, int t) {
+    const int base = j0 + t * TILE;
+    constexpr int QUADS = TILE / 4;
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const float dx = p.x - xi[k];
-        const float dy = p.y - yi[k];
-        const float dz = p.z - zi[k];
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-        const float inv = rsqrtf(r2);
-        float s = (p.w * inv) * (inv * inv);
-        if (GUARD) s = (r2 > 0.0f) ? s : 0.0f;  // checked && n == 0 contributes d == 0
-        ax[k] = fmaf(dx, s, ax[k]);
-        ay[k] = fmaf(dy, s, ay[k]);
-        az[k] = fmaf(dz, s, az[k]);
+    for (int r = 0; r < (4 * QUADS) / THREADS; ++r) {
+        const int c = threadIdx.x + r * THREADS;
+        const int a = c / QUADS, q = c % QUADS;
+        if (base + 4 * q < j_end) cp_async16(&stage.c[a][4 * q], soa + size_t(a) * n_pad + base + 4 * q);
     }
 }
 
 // part (when non-null): [gridDim.y][2][n_aff] float4 = per-slice (sum, compensation).
 template <int K, bool GUARD>
 __global__ void __launch_bounds__(THREADS)
-    bf_fast(const float4 *__restrict__ aff, int n_aff, const float4 *__restrict__ src, int n_src,
+    bf_fast(const float4 *__restrict__ aff, int n_aff, const float *__restrict__ soa, int n_src, int n_pad,
             float eps2, int slice_len, float4 *__restrict__ part, float *__restrict__ out) {
-    __shared__ __align__(16) float4 tiles[STAGES][TILE];
+    __shared__ __align__(16) SoaTile tiles[STAGES];
     const int i0 = blockIdx.x * (THREADS * K);
     const int j0 = blockIdx.y * slice_len;
     const int j_end = min(n_src, j0 + slice_len);
+    const int ntiles = (j_end - j0 + TILE - 1) / TILE;
 
-    float xi[K], yi[K], zi[K], ax[K], ay[K], az[K], sx[K], sy[K], sz[K], cx[K], cy[K], cz[K];
+    float xi[K], yi[K], zi[K], sx[K], sy[K], sz[K], cx[K], cy[K], cz[K];
+    f2 xi2[K], yi2[K], zi2[K], ax[K], ay[K], az[K];
+    const f2 e2 = pk(eps2, eps2);
+    const f2 zero2 = pk(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const int i = i0 + k * THREADS + threadIdx.x;
@@ -123,27 +196,72 @@ __global__ void __launch_bounds__(THREADS)
         xi[k] = p.x;
         yi[k] = p.y;
         zi[k] = p.z;
-        ax[k] = ay[k] = az[k] = 0.f;
+        xi2[k] = pk(p.x, p.x);
+        yi2[k] = pk(p.y, p.y);
+        zi2[k] = pk(p.z, p.z);
+        ax[k] = ay[k] = az[k] = zero2;
         sx[k] = sy[k] = sz[k] = 0.f;
         cx[k] = cy[k] = cz[k] = 0.f;
     }
 
-    for_each_tile(tiles, src, j0, j_end, [&](const float4 *T, int cnt) {
+#pragma unroll
+    for (int st = 0; st < STAGES - 1; ++st) {
+        if (st < ntiles) load_tile_soa(tiles[st], soa, n_pad, j0, j_end, st);
+        cp_async_commit();
+    }
+    for (int t = 0; t < ntiles; ++t) {
+        cp_async_wait<STAGES - 2>();
+        __syncthreads();
+        const int nt = t + STAGES - 1;
+        if (nt < ntiles) load_tile_soa(tiles[nt % STAGES], soa, n_pad, j0, j_end, nt);
+        cp_async_commit();
+        const SoaTile &T = tiles[t % STAGES];
+        const int cnt = min(TILE, j_end - (j0 + t * TILE));
         if (cnt == TILE) {
-#pragma unroll 8
-            for (int jj = 0; jj < TILE; ++jj) interact<K, GUARD>(T[jj], xi, yi, zi, ax, ay, az, eps2);
+            const float4 *X = reinterpret_cast<const float4 *>(T.c[0]);
+            const float4 *Y = reinterpret_cast<const float4 *>(T.c[1]);
+            const float4 *Z = reinterpret_cast<const float4 *>(T.c[2]);
+            const float4 *M = reinterpret_cast<const float4 *>(T.c[3]);
+#pragma unroll 2
+            for (int q = 0; q < TILE / 4; ++q) {
+                const float4 x = X[q], y = Y[q], z = Z[q], m = M[q];
+                const f2 xa = pk(x.x, x.y), xb = pk(x.z, x.w);
+                const f2 ya = pk(y.x, y.y), yb = pk(y.z, y.w);
+                const f2 za = pk(z.x, z.y), zb = pk(z.z, z.w);
+                const f2 ma = pk(m.x, m.y), mb = pk(m.z, m.w);
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    interact2<GUARD>(xa, ya, za, ma, xi2[k], yi2[k], zi2[k], ax[k], ay[k], az[k], e2);
+                    interact2<GUARD>(xb, yb, zb, mb, xi2[k], yi2[k], zi2[k], ax[k], ay[k], az[k], e2);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                float l, h;
+                upk(ax[k], l, h);
+                two_sum_acc(sx[k], cx[k], l + h);
+                upk(ay[k], l, h);
+                two_sum_acc(sy[k], cy[k], l + h);
+                upk(az[k], l, h);
+                two_sum_acc(sz[k], cz[k], l + h);
+                ax[k] = ay[k] = az[k] = zero2;
+            }
         } else {
 #pragma unroll 1
-            for (int jj = 0; jj < cnt; ++jj) interact<K, GUARD>(T[jj], xi, yi, zi, ax, ay, az, eps2);
-        }
+            for (int jj = 0; jj < cnt; ++jj) {
+                const float xj = T.c[0][jj], yj = T.c[1][jj], zj = T.c[2][jj], mj = T.c[3][jj];
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
-            two_sum_acc(sx[k], cx[k], ax[k]);
-            two_sum_acc(sy[k], cy[k], ay[k]);
-            two_sum_acc(sz[k], cz[k], az[k]);
-            ax[k] = ay[k] = az[k] = 0.f;
+                for (int k = 0; k < K; ++k) {
+                    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+                    interact1<GUARD>(xj, yj, zj, mj, xi[k], yi[k], zi[k], a0, a1, a2, eps2);
+                    two_sum_acc(sx[k], cx[k], a0);
+                    two_sum_acc(sy[k], cy[k], a1);
+                    two_sum_acc(sz[k], cz[k], a2);
+                }
+            }
         }
-    });
+    }
+    cp_async_wait<0>();
 
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -159,6 +277,18 @@ __global__ void __launch_bounds__(THREADS)
             out[3 * size_t(i) + 2] = sz[k] + cz[k];
         }
     }
+}
+
+// Sources (x, y, z, mu) rows -> four padded arrays (tail zero-filled, never read
+// as sources because every loop is bounded by n_src).
+__global__ void bf_to_soa(const float4 *__restrict__ src, int n, int n_pad, float *__restrict__ soa) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    const float4 p = (i < n) ? src[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    soa[i] = p.x;
+    soa[size_t(n_pad) + i] = p.y;
+    soa[2 * size_t(n_pad) + i] = p.z;
+    soa[3 * size_t(n_pad) + i] = p.w;
 }
 
 // Combines the slices' (sum, compensation) pairs in slice order, in double.
@@ -249,7 +379,7 @@ __global__ void __launch_bounds__(THREADS)
     }
 }
 
-using FastKernel = void (*)(const float4 *, int, const float4 *, int, float, int, float4 *, float *);
+using FastKernel = void (*)(const float4 *, int, const float *, int, int, float, int, float4 *, float *);
 
 template <int K>
 FastKernel pick(bool guard) {
@@ -289,7 +419,9 @@ static int occupancy(int K, bool guard) {
 // ceil(ctas / slots) waves; minimise waves * per-CTA work, plus the fixup pass.
 static Plan plan(const pt_ctx *ctx, int n_aff, int n_src, bool guard, int force_k, int force_s) {
     Plan p;
-    p.K = force_k ? force_k : (n_aff >= 16384 ? 4 : (n_aff >= 4096 ? 2 : 1));
+    // K=1 wins below ~2^18 targets: its 56 registers leave room for 9 CTAs per SM,
+    // which hides the MUFU and shared-memory latency better than K=4's ILP.
+    p.K = force_k ? force_k : (n_aff >= (1 << 18) ? 2 : 1);
     p.n_ib = (n_aff + THREADS * p.K - 1) / (THREADS * p.K);
     const int tiles = (n_src + TILE - 1) / TILE;
     const long long slots = (long long)std::max(1, ctx->sm_count) * occupancy(p.K, guard);
@@ -348,8 +480,13 @@ int bf_launch_f32(pt_ctx *ctx, const float4 *aff, int n_aff, const float4 *src, 
         PT_TRY(ensure(ctx, BUF_PART, sizeof(float4) * 2 * size_t(n_aff) * size_t(p.slices)));
         part = static_cast<float4 *>(ctx->bufs[BUF_PART].ptr);
     }
+    const int n_pad = (n_src + TILE - 1) / TILE * TILE;
+    PT_TRY(ensure(ctx, BUF_SOA, sizeof(float) * 4 * size_t(n_pad)));
+    float *soa = static_cast<float *>(ctx->bufs[BUF_SOA].ptr);
+    bf_to_soa<<<(n_pad + 255) / 256, 256, 0, st>>>(src, n_src, n_pad, soa);
+    PT_TRY(check_launch(ctx, "bf_to_soa"));
     dim3 grid(p.n_ib, p.slices);
-    fast_kernel(p.K, guard)<<<grid, THREADS, 0, st>>>(aff, n_aff, src, n_src, soft2, p.slice_len, part, out);
+    fast_kernel(p.K, guard)<<<grid, THREADS, 0, st>>>(aff, n_aff, soa, n_src, n_pad, soft2, p.slice_len, part, out);
     PT_TRY(check_launch(ctx, "bf_fast"));
     if (part) {
         bf_fixup<<<(n_aff + 255) / 256, 256, 0, st>>>(part, n_aff, p.slices, out);

@@ -28,6 +28,7 @@ enum BufSlot : int {
     BUF_OUT,       // accelerations, float3
     BUF_PART,      // split-j partial sums
     BUF_OUT64,     // f64 outputs
+    BUF_SOA,       // sources as padded x[], y[], z[], mu[] arrays
     BUF_COUNT
 };
 

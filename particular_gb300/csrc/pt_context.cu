@@ -154,3 +154,52 @@ int pt_ctx_synchronize(pt_ctx *ctx) {
 }
 
 }  // extern "C"
+
+// ---- FP32 FMA-pipe peak probe --------------------------------------------
+// Measured FP32 pipe throughput at the current clock: every thread runs 8
+// independent FFMA chains; the grid fills every SM. flops = 2 * chains * iters * threads.
+namespace pt {
+__global__ void __launch_bounds__(256) fp32_peak_kernel(float *out, int iters, float a, float b) {
+    float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
+          x6 = x0 + 6, x7 = x0 + 7;
+#pragma unroll 4
+    for (int i = 0; i < iters; ++i) {
+        x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+        x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+    }
+    const float s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == 1.2345f) out[0] = s;  // keeps the chains alive
+}
+}  // namespace pt
+
+extern "C" int pt_measure_fp32_peak(pt_ctx *ctx, double *tflops) {
+    pt::clear_error();
+    if (!ctx || !tflops) return pt::set_error(PT_ERR_INVALID, "pt_measure_fp32_peak: NULL argument");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    PT_TRY(pt::ensure(ctx, pt::BUF_OUT64, 256));
+    float *out = static_cast<float *>(ctx->bufs[pt::BUF_OUT64].ptr);
+    const int iters = 1 << 16;
+    const int blocks = ctx->sm_count * 8;
+    cudaEvent_t e0, e1;
+    PT_CUDA(cudaEventCreate(&e0));
+    PT_CUDA(cudaEventCreate(&e1));
+    pt::fp32_peak_kernel<<<blocks, 256, 0, ctx->stream>>>(out, iters, 0.9999f, 1e-4f);
+    int rc = pt::check_launch(ctx, "fp32_peak_kernel");
+    float best = 1e30f;
+    for (int rep = 0; rep < 3 && rc == PT_OK; ++rep) {
+        cudaEventRecord(e0, ctx->stream);
+        pt::fp32_peak_kernel<<<blocks, 256, 0, ctx->stream>>>(out, iters, 0.9999f, 1e-4f);
+        rc = pt::check_launch(ctx, "fp32_peak_kernel");
+        cudaEventRecord(e1, ctx->stream);
+        if (rc == PT_OK) rc = pt::check_cuda(cudaEventSynchronize(e1), "fp32 peak sync");
+        float ms = 0.f;
+        if (rc == PT_OK) cudaEventElapsedTime(&ms, e0, e1);
+        if (ms > 0.f && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != PT_OK) return rc;
+    const double flops = 2.0 * 8.0 * double(iters) * double(blocks) * 256.0;
+    *tflops = flops / (double(best) * 1e-3) / 1e12;
+    return PT_OK;
+}

@@ -88,7 +88,7 @@ def test_launch_plans_agree(res, oracle, k, slices):
         got = cuda.BruteForce(res, AccelerationSoftened(0.01)).compute(b)
     finally:
         N.check(N.lib().pt_bf_set_plan(res.handle, 0, 0))
-    assert rel(got, ref64).max() < 2e-6
+    assert rel(got, ref64).max() < 5e-6
 
 
 def test_f64_judge_matches_oracle(res, oracle):
