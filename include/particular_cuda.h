@@ -111,6 +111,29 @@ int pt_bf_set_plan(pt_ctx *ctx, int targets_per_thread, int slices);
  * now. Roofline denominator for the FP32-bound kernels; no reference counterpart. */
 int pt_measure_fp32_peak(pt_ctx *ctx, double *tflops);
 
+/* Allocation-free brute force: the same computation as pt_bf_accel_f32_device,
+ * for callers that cannot call cudaMalloc -- host programs that own every byte of
+ * device memory through their own pool or fixed budget, and time-critical loops
+ * where cudaMalloc/cudaFree's implicit device-wide synchronisation is not
+ * acceptable. It needs no context: its scratch is one static device array of
+ * 16 MiB that every device loading the library holds until the process exits,
+ * and no call allocates device memory. The caller passes device inputs and
+ * output (16-byte aligned bodies) and a cudaStream_t (NULL = legacy default
+ * stream); work is enqueued asynchronously.
+ * - n_src above PT_NOALLOC_MAX_SOURCES fails with PT_ERR_CAPACITY.
+ * - The first call on a device, with that device current, looks up the scratch
+ *   array's device address (cudaGetSymbolAddress); make that first call before
+ *   any stream capture.
+ * - All calls share the one array and it keeps the last call's contents: calls
+ *   whose work overlaps on the GPU (other streams, other threads) race, so
+ *   serialise them. Every scratch byte a call reads is written earlier by the
+ *   same call; nothing needs clearing.
+ * This entry point has no counterpart in the reference. */
+#define PT_NOALLOC_MAX_SOURCES 524288
+int pt_bf_accel_f32_noalloc(const float *d_affected, size_t n_aff, const float *d_affecting,
+                            size_t n_src, float softening, int checked, float *d_out_xyz,
+                            void *stream);
+
 /* Blocks until all work enqueued by the context has finished; reports any
  * asynchronous kernel error as PT_ERR_CUDA. */
 int pt_ctx_synchronize(pt_ctx *ctx);

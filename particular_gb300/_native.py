@@ -61,6 +61,8 @@ def _declare(L):
                                                   ctypes.c_double, ctypes.c_int, c_ptr]),
         "pt_bf_set_plan": (ctypes.c_int, [c_ptr, ctypes.c_int, ctypes.c_int]),
         "pt_measure_fp32_peak": (ctypes.c_int, [c_ptr, ctypes.POINTER(ctypes.c_double)]),
+        "pt_bf_accel_f32_noalloc": (ctypes.c_int, [c_ptr, c_size, c_ptr, c_size, ctypes.c_float,
+                                                   ctypes.c_int, c_ptr, c_ptr]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

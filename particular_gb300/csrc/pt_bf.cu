@@ -588,3 +588,114 @@ int pt_bf_accel_f32(pt_ctx *ctx, const float *aff, size_t n_aff, const float *sr
 }
 
 }  // extern "C"
+
+// ---- allocation-free brute force ------------------------------------------
+// pt_bf_accel_f32_noalloc runs the same kernels as pt_bf_accel_f32_device
+// (bf_to_soa -> bf_fast -> bf_fixup) but takes its scratch from one file-scope
+// device array instead of context buffers, so a call never allocates device
+// memory. It serves callers that cannot call cudaMalloc: host programs that own
+// every byte of device memory through their own pool or fixed budget, and
+// time-critical loops where cudaMalloc/cudaFree's implicit device-wide
+// synchronisation is not acceptable.
+#include <mutex>
+
+namespace pt {
+namespace bf {
+
+// Sources as x[], y[], z[], mu[] (16 B per padded source) and the j-slice
+// partials (32 B per target per slice): 16 MiB in total, held by every device
+// that loads this module until the process exits.
+constexpr size_t NOALLOC_SOA_BYTES = size_t(8) << 20;
+constexpr size_t NOALLOC_PART_BYTES = size_t(8) << 20;
+static_assert(size_t(PT_NOALLOC_MAX_SOURCES) * 16 <= NOALLOC_SOA_BYTES, "scratch too small");
+static_assert(PT_NOALLOC_MAX_SOURCES % TILE == 0, "padded sources must fit");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SOA_BYTES + NOALLOC_PART_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 128;
+static std::mutex g_noalloc_mu;
+static unsigned char *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+static int g_noalloc_sms[NOALLOC_MAX_DEVICES];
+
+// Once per device, with that device current: the device address of the scratch
+// array (in host code its name is only a host-side stand-in) and the SM count.
+static int noalloc_setup(int dev, unsigned char **ptr, int *sms) {
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return set_error(PT_ERR_INVALID, "pt_bf_accel_f32_noalloc: device %d unsupported", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        PT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        int sm = 0;
+        PT_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev));
+        g_noalloc_sms[dev] = sm;
+        g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
+    }
+    *ptr = g_noalloc_ptr[dev];
+    *sms = g_noalloc_sms[dev];
+    return PT_OK;
+}
+
+}  // namespace bf
+}  // namespace pt
+
+extern "C" int pt_bf_accel_f32_noalloc(const float *d_aff, size_t n_aff, const float *d_src, size_t n_src,
+                                       float softening, int checked, float *d_out, void *stream) {
+    using namespace pt;
+    using namespace pt::bf;
+    clear_error();
+    PT_TRY(validate_sizes("pt_bf_accel_f32_noalloc", n_aff, n_src));
+    if (n_src > size_t(PT_NOALLOC_MAX_SOURCES))
+        return set_error(PT_ERR_CAPACITY,
+                         "pt_bf_accel_f32_noalloc: n_src=%zu exceeds the static scratch limit of %d sources",
+                         n_src, PT_NOALLOC_MAX_SOURCES);
+    if (n_aff && (!d_aff || !d_out)) return set_error(PT_ERR_INVALID, "pt_bf_accel_f32_noalloc: NULL buffer");
+    if (n_src && !d_src) return set_error(PT_ERR_INVALID, "pt_bf_accel_f32_noalloc: NULL affecting buffer");
+    if ((n_aff && !aligned16(d_aff)) || (n_src && !aligned16(d_src)))
+        return set_error(PT_ERR_INVALID, "pt_bf_accel_f32_noalloc: body buffers must be 16-byte aligned");
+    int dev = 0;
+    PT_CUDA(cudaGetDevice(&dev));
+    unsigned char *scratch = nullptr;
+    int sms = 0;
+    PT_TRY(noalloc_setup(dev, &scratch, &sms));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (n_aff == 0) return PT_OK;
+    if (n_src == 0) {
+        PT_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * 3 * n_aff, st));
+        return PT_OK;
+    }
+    const int na = int(n_aff), ns = int(n_src);
+    const float soft2 = softening * softening;
+    const bool guard = checked && soft2 == 0.0f;
+    pt_ctx shape;  // only carries the SM count into the planner; owns nothing
+    shape.sm_count = sms;
+    Plan p = plan(&shape, na, ns, guard, g_forced.k, g_forced.s);
+    if (p.slices > 1) {
+        // Fit the slice partials into their fixed region; one slice needs none.
+        const size_t per_slice = sizeof(float4) * 2 * size_t(na);
+        const int max_s = int(std::min<size_t>(NOALLOC_PART_BYTES / per_slice, 1 << 20));
+        if (max_s < 2) {
+            p.slices = 1;
+            p.slice_len = (ns + TILE - 1) / TILE * TILE;
+        } else if (p.slices > max_s) {
+            const int tiles = (ns + TILE - 1) / TILE;
+            const int len_tiles = (tiles + max_s - 1) / max_s;
+            p.slice_len = len_tiles * TILE;
+            p.slices = (ns + p.slice_len - 1) / p.slice_len;
+        }
+    }
+    const int n_pad = (ns + TILE - 1) / TILE * TILE;
+    float *soa = reinterpret_cast<float *>(scratch);
+    float4 *part = p.slices > 1 ? reinterpret_cast<float4 *>(scratch + NOALLOC_SOA_BYTES) : nullptr;
+    bf_to_soa<<<(n_pad + 255) / 256, 256, 0, st>>>(reinterpret_cast<const float4 *>(d_src), ns, n_pad, soa);
+    PT_CUDA(cudaGetLastError());
+    dim3 grid(p.n_ib, p.slices);
+    fast_kernel(p.K, guard)<<<grid, THREADS, 0, st>>>(reinterpret_cast<const float4 *>(d_aff), na, soa, ns, n_pad,
+                                                      soft2, p.slice_len, part, d_out);
+    PT_CUDA(cudaGetLastError());
+    if (part) {
+        bf_fixup<<<(na + 255) / 256, 256, 0, st>>>(part, na, p.slices, d_out);
+        PT_CUDA(cudaGetLastError());
+    }
+    return PT_OK;
+}
