@@ -134,6 +134,44 @@ int pt_bf_accel_f32_noalloc(const float *d_affected, size_t n_aff, const float *
                             size_t n_src, float softening, int checked, float *d_out_xyz,
                             void *stream);
 
+/* ---- cuda::BarnesHut { theta } ------------------------------------------------
+ * GPU counterpart of sequential::BarnesHut (particular/src/sequential.rs:456-543):
+ * the tree over the affecting bodies is the reference's orthtree
+ * (tree/mod.rs:91-138: square root box, cells split at their centre, a leaf per
+ * body), built on the device every call; each affected body walks it with the
+ * reference's rule: skip a node whose centre of mass coincides with the body, open
+ * an internal cell when theta^2 d^2 < w^2 (w = cell width), otherwise add the
+ * node's monopole through the per-pair kernel. Because coincident nodes are always
+ * skipped, Acceleration's CHECKED flag has no effect on this method, as in the
+ * reference. Moments are accumulated in FP64 and stored in f32. */
+#define PT_BH_QUADRUPOLE 0x1u /* add the traceless quadrupole of accepted cells */
+#define PT_BH_GROUP 0x2u      /* open a cell for a whole warp of 32 key-adjacent bodies
+                                 when any of them opens it (never less accurate) */
+
+typedef struct pt_bh_stats {
+    uint64_t nodes;        /* cells + leaves of the last tree */
+    uint64_t cells;        /* internal cells */
+    uint64_t leaves;       /* leaves (bodies with distinct keys) */
+    uint64_t interactions; /* accepted nodes summed over bodies, last walk */
+    uint64_t visits;       /* nodes visited, summed over bodies, last walk */
+    uint64_t warps;        /* warps that walked */
+} pt_bh_stats;
+
+/* cuda::BarnesHut over host buffers (synchronous). Layouts as pt_bf_accel_f32. */
+int pt_bh_accel_f32(pt_ctx *ctx, const float *affected, size_t n_aff, const float *affecting,
+                    size_t n_src, float theta, float softening, uint32_t flags, float *out_xyz);
+/* Same on 16-byte aligned device buffers, asynchronous on the context's stream. */
+int pt_bh_accel_f32_device(pt_ctx *ctx, const float *d_affected, size_t n_aff,
+                           const float *d_affecting, size_t n_src, float theta, float softening,
+                           uint32_t flags, float *d_out_xyz);
+/* Counters of the last Barnes-Hut call (synchronises the context's stream). */
+int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out);
+/* Copies the last tree in depth-first preorder (rows >= stats.nodes): per node
+ * com_mass = (x, y, z, mass), links = (width bits, skip index, first body or -1 for
+ * a cell, body count), quad = (Qxx, Qxy, Qxz, Qyy, Qyz, Qzz, 0, 0). NULL skips one.
+ * The tree the reference keeps in RootedOrthtree (particular/src/storage.rs:10-46). */
+int pt_bh_export_tree(pt_ctx *ctx, float *com_mass, int32_t *links, float *quad, size_t rows);
+
 /* Blocks until all work enqueued by the context has finished; reports any
  * asynchronous kernel error as PT_ERR_CUDA. */
 int pt_ctx_synchronize(pt_ctx *ctx);

@@ -6,11 +6,11 @@ this package is the host-side mirror of particular's API around it.
 from .gravity import Acceleration, AccelerationSoftened, GravitationalField, fields, positions
 from .storage import Between, Ordered, Reordered, as_between
 from . import cuda
-from .cuda import CudaResources, cuda_brute_force
+from .cuda import CudaResources, cuda_barnes_hut, cuda_brute_force
 from ._native import CudaError
 
 __all__ = [
     "Acceleration", "AccelerationSoftened", "GravitationalField", "fields", "positions",
     "Between", "Ordered", "Reordered", "as_between", "cuda", "CudaResources",
-    "cuda_brute_force", "CudaError",
+    "cuda_brute_force", "cuda_barnes_hut", "CudaError",
 ]

@@ -19,6 +19,14 @@ PT_ERR_TIMEOUT = -5
 PT_ERR_DEPTH = -6
 
 PT_BF_EXACT = 0x1
+PT_BH_QUADRUPOLE = 0x1
+PT_BH_GROUP = 0x2
+
+
+class BhStats(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_uint64), ("cells", ctypes.c_uint64),
+                ("leaves", ctypes.c_uint64), ("interactions", ctypes.c_uint64),
+                ("visits", ctypes.c_uint64), ("warps", ctypes.c_uint64)]
 
 _NAMES = {PT_ERR_INVALID: "PT_ERR_INVALID", PT_ERR_CUDA: "PT_ERR_CUDA", PT_ERR_OOM: "PT_ERR_OOM",
           PT_ERR_CAPACITY: "PT_ERR_CAPACITY", PT_ERR_TIMEOUT: "PT_ERR_TIMEOUT",
@@ -63,6 +71,13 @@ def _declare(L):
         "pt_measure_fp32_peak": (ctypes.c_int, [c_ptr, ctypes.POINTER(ctypes.c_double)]),
         "pt_bf_accel_f32_noalloc": (ctypes.c_int, [c_ptr, c_size, c_ptr, c_size, ctypes.c_float,
                                                    ctypes.c_int, c_ptr, c_ptr]),
+        "pt_bh_accel_f32": (ctypes.c_int, [c_ptr, c_ptr, c_size, c_ptr, c_size, ctypes.c_float,
+                                           ctypes.c_float, ctypes.c_uint32, c_ptr]),
+        "pt_bh_accel_f32_device": (ctypes.c_int, [c_ptr, c_ptr, c_size, c_ptr, c_size,
+                                                  ctypes.c_float, ctypes.c_float, ctypes.c_uint32,
+                                                  c_ptr]),
+        "pt_bh_last_stats": (ctypes.c_int, [c_ptr, ctypes.POINTER(BhStats)]),
+        "pt_bh_export_tree": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_ptr, c_size]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -1,4 +1,776 @@
-// cuda::BarnesHut (placeholder until the tree path lands).
+// cuda::BarnesHut { theta }: on-device octree build and a warp-synchronous walk.
+//
+// The tree is the reference's orthtree (particular/src/tree/mod.rs:91-138) built in
+// parallel instead of recursively:
+//  1. bbox_*   : the square root box of BoundingBox::square_with
+//                (particular/src/tree/partition.rs:274-292), in the same f32 ops.
+//  2. make_keys: each body replays the reference's subdivision for 21 levels
+//                (centre = (min+max)/2, child bit = pos < centre, tree/mod.rs:116-124,
+//                partition.rs:332-359), giving a 63-bit key whose prefixes are exactly
+//                the reference's cells. The digit stored is 7 - orthant, so ascending
+//                keys follow the reference's LIFO visiting order (children pushed 0..7,
+//                popped 7..0, sequential.rs:489-495).
+//  3. radix sort of (key, body) pairs; bodies gathered into key order.
+//  4. equal keys collapse into one leaf unit (coincident bodies, or bodies closer
+//     than 2^-21 of the root box: deeper than the key resolves).
+//  5. Karras (2012) binary radix tree over the unique keys; a binary node is an
+//     octree cell where its common-prefix level changes. Single-child chains of the
+//     reference tree disappear: accepting a chain cell or its only child adds the
+//     same (COM, M), so the result is unchanged.
+//  6. cells are laid out in depth-first preorder with skip pointers (index after
+//     the subtree), leaves interleaved: the walk needs no stack.
+//  7. moments bottom-up in FP64 (mass, centre of mass, second moment -> traceless
+//     quadrupole) with per-cell arrival counters: the last child to arrive combines
+//     the cell (parallel-axis theorem). No thread ever waits on another.
+// Walk (sequential.rs:466-505): one warp per 32 key-adjacent targets shares a cursor
+// over the preorder array; each lane applies the reference's rule per node (skip
+// when d2 == 0, open an internal cell when theta^2 d2 < w^2, else accept its
+// monopole) and the warp moves to the smallest next index any lane needs. With
+// PT_BH_GROUP a cell is opened for every lane when any lane opens it (more accurate,
+// same visit count); PT_BH_QUADRUPOLE adds the quadrupole term to accepted cells.
 #include "pt_common.cuh"
+#include "pt_prims.cuh"
 
-void pt_bh_state_free(pt_ctx *ctx) { (void)ctx; }
+#include <algorithm>
+#include <climits>
+#include <new>
+
+namespace pt {
+namespace bh {
+
+constexpr int LEVELS = 21;   // 63-bit keys
+constexpr int WALK_THREADS = 128;
+
+struct Moments {  // FP64 cell data used while combining children
+    double m, cx, cy, cz;
+    double sxx, sxy, sxz, syy, syz, szz;  // second moment about the centre of mass
+    double count;
+    double pad;
+};
+
+struct State {
+    PrimScratch prims;
+    DevBuf box_part, box;
+    DevBuf keys, idx, sbody;
+    DevBuf flags, uscan, ukey, ufirst;
+    DevBuf bfirst, blast, bdelta, bparent, lparent, top, oparent, loparent;
+    DevBuf cnt, pscan, pre, nchild, arrive;
+    DevBuf nodeA, nodeB, nodeQ, mom;
+    DevBuf tkeys, tidx, tbody;
+    DevBuf counters;
+    DevBuf out;
+    DevBuf aff_h, src_h;  // staging for the host-pointer entry point
+    int cap_n = 0;
+    int last_n_src = 0;
+};
+
+// ---- 1. root box -----------------------------------------------------------
+__global__ void bbox_partial(const float4 *__restrict__ src, int n, float *__restrict__ part) {
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = src[i];
+        mn[0] = fminf(mn[0], p.x);
+        mn[1] = fminf(mn[1], p.y);
+        mn[2] = fminf(mn[2], p.z);
+        mx[0] = fmaxf(mx[0], p.x);
+        mx[1] = fmaxf(mx[1], p.y);
+        mx[2] = fmaxf(mx[2], p.z);
+    }
+    __shared__ float s[6][256];
+    for (int a = 0; a < 3; ++a) {
+        s[a][threadIdx.x] = mn[a];
+        s[3 + a][threadIdx.x] = mx[a];
+    }
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int a = 0; a < 3; ++a) {
+                s[a][threadIdx.x] = fminf(s[a][threadIdx.x], s[a][threadIdx.x + w]);
+                s[3 + a][threadIdx.x] = fmaxf(s[3 + a][threadIdx.x], s[3 + a][threadIdx.x + w]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) part[blockIdx.x * 6 + threadIdx.x] = s[threadIdx.x][0];
+}
+
+// box = {min x,y,z, max x,y,z} of BoundingBox::square_with: centre = midpoint of the
+// AABB, half = (max extent + 0) / 2 (MidPoint::half), min/max = centre -/+ half.
+__global__ void bbox_final(const float *__restrict__ part, int nb, float *__restrict__ box) {
+    if (threadIdx.x != 0) return;
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int b = 0; b < nb; ++b)
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = fminf(mn[a], part[b * 6 + a]);
+            mx[a] = fmaxf(mx[a], part[b * 6 + 3 + a]);
+        }
+    float half = 0.0f;
+    float c[3];
+    for (int a = 0; a < 3; ++a) {
+        c[a] = __fmul_rn(__fadd_rn(mn[a], mx[a]), 0.5f);
+        half = fmaxf(half, __fsub_rn(mx[a], mn[a]));
+    }
+    half = __fmul_rn(__fadd_rn(half, 0.0f), 0.5f);
+    for (int a = 0; a < 3; ++a) {
+        box[a] = __fsub_rn(c[a], half);
+        box[3 + a] = __fadd_rn(c[a], half);
+    }
+}
+
+// ---- 2. keys ---------------------------------------------------------------
+__device__ __forceinline__ uint64_t key_of(float px, float py, float pz, const float *box) {
+    float mn0 = box[0], mn1 = box[1], mn2 = box[2], mx0 = box[3], mx1 = box[4], mx2 = box[5];
+    uint64_t key = 0;
+#pragma unroll 3
+    for (int l = 0; l < LEVELS; ++l) {
+        const float c0 = __fmul_rn(__fadd_rn(mn0, mx0), 0.5f);
+        const float c1 = __fmul_rn(__fadd_rn(mn1, mx1), 0.5f);
+        const float c2 = __fmul_rn(__fadd_rn(mn2, mx2), 0.5f);
+        const int b0 = px < c0, b1 = py < c1, b2 = pz < c2;
+        if (b0) mx0 = c0; else mn0 = c0;
+        if (b1) mx1 = c1; else mn1 = c1;
+        if (b2) mx2 = c2; else mn2 = c2;
+        const int o = b0 | (b1 << 1) | (b2 << 2);
+        key = (key << 3) | uint64_t(7 - o);
+    }
+    return key;
+}
+
+__global__ void make_keys(const float4 *__restrict__ bodies, int n, const float *__restrict__ box_g,
+                          uint64_t *__restrict__ keys, uint32_t *__restrict__ idx) {
+    __shared__ float box[6];
+    if (threadIdx.x < 6) box[threadIdx.x] = box_g[threadIdx.x];
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = bodies[i];
+    keys[i] = key_of(p.x, p.y, p.z, box);
+    idx[i] = uint32_t(i);
+}
+
+__global__ void gather_bodies(const float4 *__restrict__ src, const uint32_t *__restrict__ idx, int n,
+                              float4 *__restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = src[idx[k]];
+}
+
+// ---- 4. unique keys -> leaf units ------------------------------------------
+__global__ void unit_flags(const uint64_t *__restrict__ keys, int n, uint32_t *__restrict__ flags) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) flags[k] = (k == 0 || keys[k] != keys[k - 1]) ? 1u : 0u;
+}
+
+// counters[0] = M (units)
+__global__ void unit_fill(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ flags,
+                          const uint32_t *__restrict__ uscan, int n, uint64_t *__restrict__ ukey,
+                          uint32_t *__restrict__ ufirst, int *__restrict__ counters) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (flags[k]) {
+        const uint32_t u = uscan[k];
+        ukey[u] = keys[k];
+        ufirst[u] = uint32_t(k);
+    }
+    if (k == 0) {
+        const uint32_t M = uscan[n];
+        ufirst[M] = uint32_t(n);
+        counters[0] = int(M);
+    }
+}
+
+// ---- 5. Karras binary radix tree ---------------------------------------------
+__device__ __forceinline__ int kdelta(const uint64_t *__restrict__ k, int M, int i, int j) {
+    if (j < 0 || j >= M) return -1;
+    return __clzll(k[i] ^ k[j]) - 1;  // bit 63 is always 0: prefix length of the 63-bit keys
+}
+
+__global__ void karras(const uint64_t *__restrict__ ukey, const int *__restrict__ counters, int *__restrict__ bfirst,
+                       int *__restrict__ blast, int *__restrict__ bdelta, int *__restrict__ bparent,
+                       int *__restrict__ lparent) {
+    const int M = counters[0];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M - 1) return;
+    const int d = (kdelta(ukey, M, i, i + 1) - kdelta(ukey, M, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = kdelta(ukey, M, i, i - d);
+    int lmax = 2;
+    while (kdelta(ukey, M, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (kdelta(ukey, M, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = kdelta(ukey, M, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (kdelta(ukey, M, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int gamma = i + s * d + min(d, 0);
+    const int first = min(i, j), last = max(i, j);
+    bfirst[i] = first;
+    blast[i] = last;
+    bdelta[i] = dnode;
+    if (first == gamma) lparent[gamma] = i; else bparent[gamma] = i;
+    if (last == gamma + 1) lparent[gamma + 1] = i; else bparent[gamma + 1] = i;
+    if (i == 0) bparent[0] = -1;
+}
+
+// A binary node is an octree cell iff it is the root or its common-prefix level
+// (delta / 3) exceeds its parent's.
+__global__ void octree_top(const int *__restrict__ counters, const int *__restrict__ bdelta,
+                           const int *__restrict__ bparent, uint8_t *__restrict__ top) {
+    const int M = counters[0];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M - 1) return;
+    top[i] = (i == 0 || bdelta[bparent[i]] / 3 < bdelta[i] / 3) ? 1 : 0;
+}
+
+__device__ __forceinline__ int climb(int p, const uint8_t *__restrict__ top, const int *__restrict__ bparent) {
+    while (!top[p]) p = bparent[p];
+    return p;
+}
+
+// Octree parents, child counts and the count of cells starting at each unit.
+__global__ void octree_links(const int *__restrict__ counters, const int *__restrict__ bfirst,
+                             const int *__restrict__ bparent, const int *__restrict__ lparent,
+                             const uint8_t *__restrict__ top, int *__restrict__ oparent, int *__restrict__ loparent,
+                             uint32_t *__restrict__ cnt, int *__restrict__ nchild) {
+    const int M = counters[0];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < M - 1 && top[k]) {
+        const int op = (k == 0) ? -1 : climb(bparent[k], top, bparent);
+        oparent[k] = op;
+        atomicAdd(&cnt[bfirst[k]], 1u);
+        if (op >= 0) atomicAdd(&nchild[op], 1);
+    }
+    if (k < M) {
+        const int op = (M == 1) ? -1 : climb(lparent[k], top, bparent);
+        loparent[k] = op;
+        if (op >= 0) atomicAdd(&nchild[op], 1);
+    }
+}
+
+// ---- 6. preorder layout ------------------------------------------------------
+// nodeB = {width bits, skip, first body (-1: internal cell), body count}.
+// counters[1] = T (cells + leaves), counters[2] = internal cells.
+__global__ void layout(int *counters, const int *__restrict__ bfirst,
+                       const int *__restrict__ blast, const int *__restrict__ bdelta,
+                       const uint8_t *__restrict__ top, const int *__restrict__ oparent,
+                       const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ pscan,
+                       const uint64_t *__restrict__ ukey, const uint32_t *__restrict__ ufirst,
+                       const float *__restrict__ box, int *__restrict__ pre, int4 *__restrict__ nodeB) {
+    const int M = counters[0];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) {
+        counters[1] = M + int(pscan[M]);
+        counters[2] = int(pscan[M]);
+    }
+    if (k < M - 1 && top[k]) {
+        const int b = bfirst[k];
+        int r = 0;
+        for (int p = oparent[k]; p >= 0 && bfirst[p] == b; p = oparent[p]) ++r;
+        const int pk = b + int(pscan[b]) + r;
+        pre[k] = pk;
+        const int after = blast[k] + 1;
+        const int skip = after + int(pscan[after]);
+        // Cell width at level L along the key's x path: BoundingBox::width() of the
+        // reference cell (partition.rs:322-327), replayed in the same f32 ops.
+        const int L = bdelta[k] / 3;
+        const uint64_t key = ukey[b];
+        float mn = box[0], mx = box[3];
+        for (int l = 0; l < L; ++l) {
+            const int o = 7 - int((key >> (3 * (LEVELS - 1 - l))) & 7u);
+            const float c = __fmul_rn(__fadd_rn(mn, mx), 0.5f);
+            if (o & 1) mx = c; else mn = c;
+        }
+        nodeB[pk] = make_int4(__float_as_int(__fsub_rn(mx, mn)), skip, -1, 0);
+    }
+    if (k < M) {
+        const int pk = k + int(pscan[k]) + int(cnt[k]);
+        const int f = int(ufirst[k]);
+        nodeB[pk] = make_int4(0, pk + 1, f, int(ufirst[k + 1]) - f);
+    }
+}
+
+// ---- 7. moments ------------------------------------------------------------
+__device__ void store_cell(const Moments &m, int pk, Moments *__restrict__ mom, float4 *__restrict__ nodeA,
+                           float4 *__restrict__ nodeQ) {
+    mom[pk] = m;
+    nodeA[pk] = make_float4(float(m.cx), float(m.cy), float(m.cz), float(m.m));
+    const double tr = m.sxx + m.syy + m.szz;
+    nodeQ[2 * pk] = make_float4(float(3 * m.sxx - tr), float(3 * m.sxy), float(3 * m.sxz), float(3 * m.syy - tr));
+    nodeQ[2 * pk + 1] = make_float4(float(3 * m.syz), float(3 * m.szz - tr), 0.f, 0.f);
+}
+
+__device__ __forceinline__ Moments load_moments(const Moments *p) {
+    Moments m;
+    const double *s = reinterpret_cast<const double *>(p);
+    double *d = reinterpret_cast<double *>(&m);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) d[k] = __ldcg(s + k);
+    return m;
+}
+
+__global__ void moments_up(const int *__restrict__ counters, const uint32_t *__restrict__ ufirst,
+                           const float4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
+                           const uint32_t *__restrict__ cnt, const int *__restrict__ loparent,
+                           const int *__restrict__ oparent, const int *__restrict__ pre,
+                           const int *__restrict__ nchild, int *__restrict__ arrive, const int4 *__restrict__ nodeB,
+                           Moments *__restrict__ mom, float4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
+    const int M = counters[0];
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= M) return;
+    // Leaf unit: its bodies (almost always one).
+    {
+        const int f = int(ufirst[u]), e = int(ufirst[u + 1]);
+        Moments m{};
+        double sx = 0, sy = 0, sz = 0;
+        for (int b = f; b < e; ++b) {
+            const float4 p = sbody[b];
+            m.m += p.w;
+            sx += double(p.w) * p.x;
+            sy += double(p.w) * p.y;
+            sz += double(p.w) * p.z;
+        }
+        m.count = e - f;
+        if (m.m != 0.0) {
+            m.cx = sx / m.m;
+            m.cy = sy / m.m;
+            m.cz = sz / m.m;
+        } else {  // massless: plain mean (gravity/impls/mod.rs:127-129)
+            for (int b = f; b < e; ++b) {
+                const float4 p = sbody[b];
+                m.cx += p.x;
+                m.cy += p.y;
+                m.cz += p.z;
+            }
+            m.cx /= m.count;
+            m.cy /= m.count;
+            m.cz /= m.count;
+        }
+        if (e - f == 1) {  // exact body position, as the reference's single-body cell
+            const float4 p = sbody[f];
+            m.cx = p.x;
+            m.cy = p.y;
+            m.cz = p.z;
+        } else {
+            for (int b = f; b < e; ++b) {
+                const float4 p = sbody[b];
+                const double dx = p.x - m.cx, dy = p.y - m.cy, dz = p.z - m.cz;
+                m.sxx += p.w * dx * dx;
+                m.sxy += p.w * dx * dy;
+                m.sxz += p.w * dx * dz;
+                m.syy += p.w * dy * dy;
+                m.syz += p.w * dy * dz;
+                m.szz += p.w * dz * dz;
+            }
+        }
+        const int pk = u + int(pscan[u]) + int(cnt[u]);
+        store_cell(m, pk, mom, nodeA, nodeQ);
+    }
+    // Climb: the last child to arrive at a cell combines it.
+    for (int v = loparent[u]; v >= 0; v = oparent[v]) {
+        __threadfence();
+        if (atomicAdd(&arrive[v], 1) != nchild[v] - 1) return;
+        __threadfence();
+        const int pv = pre[v];
+        const int end = nodeB[pv].y;
+        Moments m{};
+        double sx = 0, sy = 0, sz = 0, ux = 0, uy = 0, uz = 0;
+        for (int c = pv + 1; c < end; c = nodeB[c].y) {
+            const Moments cm = load_moments(mom + c);
+            m.m += cm.m;
+            m.count += cm.count;
+            sx += cm.m * cm.cx;
+            sy += cm.m * cm.cy;
+            sz += cm.m * cm.cz;
+            ux += cm.count * cm.cx;
+            uy += cm.count * cm.cy;
+            uz += cm.count * cm.cz;
+        }
+        if (m.m != 0.0) {
+            m.cx = sx / m.m;
+            m.cy = sy / m.m;
+            m.cz = sz / m.m;
+        } else {
+            m.cx = ux / m.count;
+            m.cy = uy / m.count;
+            m.cz = uz / m.count;
+        }
+        for (int c = pv + 1; c < end; c = nodeB[c].y) {
+            const Moments cm = load_moments(mom + c);
+            const double dx = cm.cx - m.cx, dy = cm.cy - m.cy, dz = cm.cz - m.cz;
+            m.sxx += cm.sxx + cm.m * dx * dx;
+            m.sxy += cm.sxy + cm.m * dx * dy;
+            m.sxz += cm.sxz + cm.m * dx * dz;
+            m.syy += cm.syy + cm.m * dy * dy;
+            m.syz += cm.syz + cm.m * dy * dz;
+            m.szz += cm.szz + cm.m * dz * dz;
+        }
+        store_cell(m, pv, mom, nodeA, nodeQ);
+    }
+}
+
+// ---- walk ------------------------------------------------------------------
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+template <bool GROUP, bool QUAD>
+__global__ void __launch_bounds__(WALK_THREADS)
+    bh_walk(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
+            const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
+            const float4 *__restrict__ sbody, const int *__restrict__ counters, float th2, float eps2,
+            float *__restrict__ out, unsigned long long *__restrict__ stats) {
+    const int lane = threadIdx.x & 31;
+    const int t = blockIdx.x * WALK_THREADS + threadIdx.x;
+    if ((t & ~31) >= n_aff) return;  // whole warp past the end
+    const bool valid = t < n_aff;
+    const int T = counters[1];
+    const float4 p = valid ? tbody[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    int resume = valid ? 0 : T;
+    unsigned nacc = 0, nvisit = 0;
+    int node = 0;
+    while (node < T) {
+        const float4 A = __ldg(nodeA + node);
+        const int4 B = __ldg(nodeB + node);
+        const bool active = node >= resume;
+        float dx = 0.f, dy = 0.f, dz = 0.f, d2 = 0.f;
+        bool open = false, zero = false;
+        if (active) {
+            dx = A.x - p.x;
+            dy = A.y - p.y;
+            dz = A.z - p.z;
+            d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            zero = (d2 == 0.0f);
+            const float w = __int_as_float(B.x);
+            open = !zero && B.z < 0 && th2 * d2 < w * w;
+        }
+        if (GROUP) open = __any_sync(0xffffffffu, open) && B.z < 0;
+        int next = resume;
+        if (active) {
+            ++nvisit;
+            if (zero) {
+                next = resume = B.y;  // the whole node is skipped (sequential.rs:485-487)
+            } else if (open) {
+                next = node + 1;
+            } else {
+                if (B.z >= 0 && B.w > 1) {  // a bucket leaf: its bodies one by one
+                    for (int b = B.z; b < B.z + B.w; ++b) {
+                        const float4 q = __ldg(sbody + b);
+                        const float ex = q.x - p.x, ey = q.y - p.y, ez = q.z - p.z;
+                        const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                        if (e2 == 0.0f) continue;
+                        const float inv = rsqrt_ftz(e2 + eps2);
+                        const float s = (q.w * inv) * (inv * inv);
+                        ax = fmaf(ex, s, ax);
+                        ay = fmaf(ey, s, ay);
+                        az = fmaf(ez, s, az);
+                    }
+                } else {
+                    const float inv = rsqrt_ftz(d2 + eps2);
+                    const float inv2 = inv * inv;
+                    const float s = (A.w * inv) * inv2;
+                    ax = fmaf(dx, s, ax);
+                    ay = fmaf(dy, s, ay);
+                    az = fmaf(dz, s, az);
+                    if (QUAD && B.z < 0) {
+                        const float4 q0 = __ldg(nodeQ + 2 * node);
+                        const float4 q1 = __ldg(nodeQ + 2 * node + 1);
+                        // q0 = (Qxx, Qxy, Qxz, Qyy), q1 = (Qyz, Qzz)
+                        const float qx = fmaf(q0.x, dx, fmaf(q0.y, dy, q0.z * dz));
+                        const float qy = fmaf(q0.y, dx, fmaf(q0.w, dy, q1.x * dz));
+                        const float qz = fmaf(q0.z, dx, fmaf(q1.x, dy, q1.y * dz));
+                        const float dqd = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
+                        const float inv5 = inv2 * inv2 * inv;
+                        const float c7 = 2.5f * dqd * inv5 * inv2;
+                        ax += fmaf(c7, dx, -qx * inv5);
+                        ay += fmaf(c7, dy, -qy * inv5);
+                        az += fmaf(c7, dz, -qz * inv5);
+                    }
+                }
+                ++nacc;
+                next = resume = B.y;
+            }
+        }
+        node = __reduce_min_sync(0xffffffffu, next);
+    }
+    if (valid) {
+        const uint32_t o = tidx[t];
+        out[3 * size_t(o) + 0] = ax;
+        out[3 * size_t(o) + 1] = ay;
+        out[3 * size_t(o) + 2] = az;
+    }
+    if (stats) {
+        unsigned long long a = nacc, v = nvisit;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            v += __shfl_down_sync(0xffffffffu, v, o);
+        }
+        if (lane == 0) {
+            atomicAdd(stats + 0, a);
+            atomicAdd(stats + 1, v);
+            atomicAdd(stats + 2, 1ull);
+        }
+    }
+}
+
+using WalkKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
+                            const float4 *, const int *, float, float, float *, unsigned long long *);
+
+static WalkKernel walk_kernel(bool group, bool quad) {
+    if (group) return quad ? bh_walk<true, true> : bh_walk<true, false>;
+    return quad ? bh_walk<false, true> : bh_walk<false, false>;
+}
+
+static State *state(pt_ctx *ctx) {
+    if (!ctx->bh) ctx->bh = new (std::nothrow) State();
+    return static_cast<State *>(ctx->bh);
+}
+
+template <class T>
+static T *as(DevBuf &b) {
+    return static_cast<T *>(b.ptr);
+}
+
+static inline int blocks(int n, int t = 256) { return (n + t - 1) / t; }
+
+// Builds the tree over d_src (n_src >= 1 bodies) into the context's state.
+static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
+    cudaStream_t st = ctx->stream;
+    const size_t N = size_t(n);
+    PT_TRY(ensure_buf(ctx, S.box_part, sizeof(float) * 6 * 1024));
+    PT_TRY(ensure_buf(ctx, S.box, sizeof(float) * 8));
+    PT_TRY(ensure_buf(ctx, S.keys, sizeof(uint64_t) * N));
+    PT_TRY(ensure_buf(ctx, S.idx, sizeof(uint32_t) * N));
+    PT_TRY(ensure_buf(ctx, S.sbody, sizeof(float4) * N));
+    PT_TRY(ensure_buf(ctx, S.flags, sizeof(uint32_t) * N));
+    PT_TRY(ensure_buf(ctx, S.uscan, sizeof(uint32_t) * (N + 1)));
+    PT_TRY(ensure_buf(ctx, S.ukey, sizeof(uint64_t) * N));
+    PT_TRY(ensure_buf(ctx, S.ufirst, sizeof(uint32_t) * (N + 1)));
+    PT_TRY(ensure_buf(ctx, S.bfirst, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.blast, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.bdelta, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.bparent, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.lparent, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.top, N));
+    PT_TRY(ensure_buf(ctx, S.oparent, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.loparent, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.cnt, sizeof(uint32_t) * (N + 1)));
+    PT_TRY(ensure_buf(ctx, S.pscan, sizeof(uint32_t) * (N + 2)));
+    PT_TRY(ensure_buf(ctx, S.pre, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.nchild, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.arrive, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.nodeA, sizeof(float4) * 2 * N));
+    PT_TRY(ensure_buf(ctx, S.nodeB, sizeof(int4) * 2 * N));
+    PT_TRY(ensure_buf(ctx, S.nodeQ, sizeof(float4) * 4 * N));
+    PT_TRY(ensure_buf(ctx, S.mom, sizeof(Moments) * 2 * N));
+    PT_TRY(ensure_buf(ctx, S.counters, sizeof(unsigned long long) * 8));
+
+    const int nb = std::min(1024, blocks(n));
+    bbox_partial<<<nb, 256, 0, st>>>(d_src, n, as<float>(S.box_part));
+    PT_TRY(check_launch(ctx, "bbox_partial"));
+    bbox_final<<<1, 32, 0, st>>>(as<float>(S.box_part), nb, as<float>(S.box));
+    PT_TRY(check_launch(ctx, "bbox_final"));
+    make_keys<<<blocks(n), 256, 0, st>>>(d_src, n, as<float>(S.box), as<uint64_t>(S.keys), as<uint32_t>(S.idx));
+    PT_TRY(check_launch(ctx, "make_keys"));
+    PT_TRY(radix_sort_u64(ctx, S.prims, as<uint64_t>(S.keys), as<uint32_t>(S.idx), n, 3 * LEVELS));
+    gather_bodies<<<blocks(n), 256, 0, st>>>(d_src, as<uint32_t>(S.idx), n, as<float4>(S.sbody));
+    PT_TRY(check_launch(ctx, "gather_bodies"));
+    unit_flags<<<blocks(n), 256, 0, st>>>(as<uint64_t>(S.keys), n, as<uint32_t>(S.flags));
+    PT_TRY(check_launch(ctx, "unit_flags"));
+    PT_TRY(scan_u32(ctx, S.prims, as<uint32_t>(S.flags), as<uint32_t>(S.uscan), n));
+    int *counters = as<int>(S.counters);
+    unit_fill<<<blocks(n), 256, 0, st>>>(as<uint64_t>(S.keys), as<uint32_t>(S.flags), as<uint32_t>(S.uscan), n,
+                                        as<uint64_t>(S.ukey), as<uint32_t>(S.ufirst), counters);
+    PT_TRY(check_launch(ctx, "unit_fill"));
+    karras<<<blocks(n), 256, 0, st>>>(as<uint64_t>(S.ukey), counters, as<int>(S.bfirst), as<int>(S.blast),
+                                     as<int>(S.bdelta), as<int>(S.bparent), as<int>(S.lparent));
+    PT_TRY(check_launch(ctx, "karras"));
+    octree_top<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<int>(S.bparent), as<uint8_t>(S.top));
+    PT_TRY(check_launch(ctx, "octree_top"));
+    PT_CUDA(cudaMemsetAsync(S.cnt.ptr, 0, sizeof(uint32_t) * (N + 1), st));
+    PT_CUDA(cudaMemsetAsync(S.nchild.ptr, 0, sizeof(int) * N, st));
+    PT_CUDA(cudaMemsetAsync(S.arrive.ptr, 0, sizeof(int) * N, st));
+    octree_links<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.bparent), as<int>(S.lparent),
+                                           as<uint8_t>(S.top), as<int>(S.oparent), as<int>(S.loparent),
+                                           as<uint32_t>(S.cnt), as<int>(S.nchild));
+    PT_TRY(check_launch(ctx, "octree_links"));
+    PT_TRY(scan_u32(ctx, S.prims, as<uint32_t>(S.cnt), as<uint32_t>(S.pscan), n + 1));
+    layout<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.blast), as<int>(S.bdelta),
+                                     as<uint8_t>(S.top), as<int>(S.oparent), as<uint32_t>(S.cnt),
+                                     as<uint32_t>(S.pscan), as<uint64_t>(S.ukey), as<uint32_t>(S.ufirst),
+                                     as<float>(S.box), as<int>(S.pre), as<int4>(S.nodeB));
+    PT_TRY(check_launch(ctx, "layout"));
+    moments_up<<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<float4>(S.sbody),
+                                         as<uint32_t>(S.pscan), as<uint32_t>(S.cnt), as<int>(S.loparent),
+                                         as<int>(S.oparent), as<int>(S.pre), as<int>(S.nchild),
+                                         as<int>(S.arrive), as<int4>(S.nodeB), as<Moments>(S.mom),
+                                         as<float4>(S.nodeA), as<float4>(S.nodeQ));
+    PT_TRY(check_launch(ctx, "moments_up"));
+    S.last_n_src = n;
+    return PT_OK;
+}
+
+// Sorts separate targets along the same keys (same root box) for coherent warps.
+static int sort_targets(pt_ctx *ctx, State &S, const float4 *d_aff, int n) {
+    cudaStream_t st = ctx->stream;
+    PT_TRY(ensure_buf(ctx, S.tkeys, sizeof(uint64_t) * size_t(n)));
+    PT_TRY(ensure_buf(ctx, S.tidx, sizeof(uint32_t) * size_t(n)));
+    PT_TRY(ensure_buf(ctx, S.tbody, sizeof(float4) * size_t(n)));
+    make_keys<<<blocks(n), 256, 0, st>>>(d_aff, n, as<float>(S.box), as<uint64_t>(S.tkeys), as<uint32_t>(S.tidx));
+    PT_TRY(check_launch(ctx, "make_keys(targets)"));
+    PT_TRY(radix_sort_u64(ctx, S.prims, as<uint64_t>(S.tkeys), as<uint32_t>(S.tidx), n, 3 * LEVELS));
+    gather_bodies<<<blocks(n), 256, 0, st>>>(d_aff, as<uint32_t>(S.tidx), n, as<float4>(S.tbody));
+    return check_launch(ctx, "gather_bodies(targets)");
+}
+
+static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src, int n_src, float theta,
+               float softening, uint32_t flags, float *d_out) {
+    cudaStream_t st = ctx->stream;
+    if (n_aff == 0) return PT_OK;
+    if (n_src == 0) {
+        PT_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * 3 * size_t(n_aff), st));
+        return PT_OK;
+    }
+    State *Sp = state(ctx);
+    if (!Sp) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    State &S = *Sp;
+    PT_TRY(build(ctx, S, d_src, n_src));
+    const bool same = (d_aff == d_src) && (n_aff == n_src);
+    const float4 *tbody;
+    const uint32_t *tidx;
+    if (same) {
+        tbody = as<float4>(S.sbody);
+        tidx = as<uint32_t>(S.idx);
+    } else {
+        PT_TRY(sort_targets(ctx, S, d_aff, n_aff));
+        tbody = as<float4>(S.tbody);
+        tidx = as<uint32_t>(S.tidx);
+    }
+    unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 4;
+    PT_CUDA(cudaMemsetAsync(stats, 0, 3 * sizeof(unsigned long long), st));
+    const float th2 = theta * theta;
+    const float eps2 = softening * softening;
+    walk_kernel(flags & PT_BH_GROUP, flags & PT_BH_QUADRUPOLE)<<<blocks(n_aff, WALK_THREADS), WALK_THREADS, 0,
+                                                                st>>>(
+        tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.sbody),
+        as<int>(S.counters), th2, eps2, d_out, stats);
+    return check_launch(ctx, "bh_walk");
+}
+
+static int validate(const char *fn, size_t n_aff, size_t n_src, uint32_t flags) {
+    const size_t lim = size_t(INT_MAX) / 8;
+    if (n_aff > lim || n_src > lim)
+        return set_error(PT_ERR_INVALID, "%s: n_aff=%zu n_src=%zu exceed the limit %zu", fn, n_aff, n_src, lim);
+    if (flags & ~(PT_BH_QUADRUPOLE | PT_BH_GROUP))
+        return set_error(PT_ERR_INVALID, "%s: unknown flags 0x%x", fn, flags);
+    return PT_OK;
+}
+
+}  // namespace bh
+}  // namespace pt
+
+void pt_bh_state_free(pt_ctx *ctx) {
+    using namespace pt;
+    auto *S = static_cast<bh::State *>(ctx->bh);
+    if (!S) return;
+    prim_free(ctx, S->prims);
+    DevBuf *all[] = {&S->box_part, &S->box,    &S->keys,   &S->idx,    &S->sbody,   &S->flags,  &S->uscan,
+                     &S->ukey,     &S->ufirst, &S->bfirst, &S->blast,  &S->bdelta,  &S->bparent, &S->lparent,
+                     &S->top,      &S->oparent, &S->loparent, &S->cnt, &S->pscan,   &S->pre,    &S->nchild,
+                     &S->arrive,   &S->nodeA,  &S->nodeB,  &S->nodeQ,  &S->mom,     &S->tkeys,  &S->tidx,
+                     &S->tbody,    &S->counters, &S->out,  &S->aff_h,  &S->src_h};
+    for (DevBuf *b : all) free_buf(ctx, *b);
+    delete S;
+    ctx->bh = nullptr;
+}
+
+extern "C" {
+
+int pt_bh_accel_f32_device(pt_ctx *ctx, const float *d_aff, size_t n_aff, const float *d_src, size_t n_src,
+                           float theta, float softening, uint32_t flags, float *d_out) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_accel_f32_device: ctx is NULL");
+    PT_TRY(bh::validate("pt_bh_accel_f32_device", n_aff, n_src, flags));
+    if (n_aff && (!d_aff || !d_out)) return set_error(PT_ERR_INVALID, "pt_bh_accel_f32_device: NULL buffer");
+    if (n_src && !d_src) return set_error(PT_ERR_INVALID, "pt_bh_accel_f32_device: NULL affecting buffer");
+    if ((n_aff && !aligned16(d_aff)) || (n_src && !aligned16(d_src)))
+        return set_error(PT_ERR_INVALID, "pt_bh_accel_f32_device: body buffers must be 16-byte aligned");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    return bh::run(ctx, reinterpret_cast<const float4 *>(d_aff), int(n_aff), reinterpret_cast<const float4 *>(d_src),
+                   int(n_src), theta, softening, flags, d_out);
+}
+
+int pt_bh_accel_f32(pt_ctx *ctx, const float *aff, size_t n_aff, const float *src, size_t n_src, float theta,
+                    float softening, uint32_t flags, float *out) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_accel_f32: ctx is NULL");
+    PT_TRY(bh::validate("pt_bh_accel_f32", n_aff, n_src, flags));
+    if (n_aff && (!aff || !out)) return set_error(PT_ERR_INVALID, "pt_bh_accel_f32: NULL buffer");
+    if (n_src && !src) return set_error(PT_ERR_INVALID, "pt_bh_accel_f32: NULL affecting buffer");
+    if (n_aff == 0) return PT_OK;
+    PT_CUDA(cudaSetDevice(ctx->device));
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    const bool same = (aff == src) && (n_aff == n_src);
+    PT_TRY(ensure_buf(ctx, S->aff_h, 16 * n_aff));
+    if (!same && n_src) PT_TRY(ensure_buf(ctx, S->src_h, 16 * n_src));
+    PT_TRY(ensure_buf(ctx, S->out, 12 * n_aff));
+    float *d_aff = static_cast<float *>(S->aff_h.ptr);
+    float *d_src = same ? d_aff : static_cast<float *>(S->src_h.ptr);
+    float *d_out = static_cast<float *>(S->out.ptr);
+    cudaStream_t st = ctx->stream;
+    PT_CUDA(cudaMemcpyAsync(d_aff, aff, 16 * n_aff, cudaMemcpyHostToDevice, st));
+    if (!same && n_src) PT_CUDA(cudaMemcpyAsync(d_src, src, 16 * n_src, cudaMemcpyHostToDevice, st));
+    PT_TRY(bh::run(ctx, reinterpret_cast<const float4 *>(d_aff), int(n_aff), reinterpret_cast<const float4 *>(d_src),
+                   int(n_src), theta, softening, flags, d_out));
+    PT_CUDA(cudaMemcpyAsync(out, d_out, 12 * n_aff, cudaMemcpyDeviceToHost, st));
+    PT_CUDA(cudaStreamSynchronize(st));
+    return PT_OK;
+}
+
+int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out) {
+    using namespace pt;
+    clear_error();
+    if (!ctx || !out) return set_error(PT_ERR_INVALID, "pt_bh_last_stats: NULL argument");
+    auto *S = static_cast<bh::State *>(ctx->bh);
+    if (!S || !S->counters.ptr) return set_error(PT_ERR_INVALID, "pt_bh_last_stats: no Barnes-Hut call yet");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    unsigned long long h[8];
+    PT_CUDA(cudaMemcpyAsync(h, S->counters.ptr, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    PT_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int *hi = reinterpret_cast<const int *>(h);
+    out->leaves = uint64_t(hi[0]);
+    out->nodes = uint64_t(hi[1]);
+    out->cells = uint64_t(hi[2]);
+    out->interactions = h[4];
+    out->visits = h[5];
+    out->warps = h[6];
+    return PT_OK;
+}
+
+// Copies the last tree (preorder) to host arrays of pt_bh_last_stats().nodes rows.
+int pt_bh_export_tree(pt_ctx *ctx, float *com_mass, int32_t *links, float *quad, size_t rows) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_export_tree: ctx is NULL");
+    auto *S = static_cast<bh::State *>(ctx->bh);
+    if (!S || !S->nodeA.ptr) return set_error(PT_ERR_INVALID, "pt_bh_export_tree: no Barnes-Hut call yet");
+    pt_bh_stats st;
+    PT_TRY(pt_bh_last_stats(ctx, &st));
+    if (rows < st.nodes) return set_error(PT_ERR_INVALID, "pt_bh_export_tree: %zu rows < %llu nodes", rows,
+                                          (unsigned long long)st.nodes);
+    cudaStream_t s = ctx->stream;
+    if (com_mass) PT_CUDA(cudaMemcpyAsync(com_mass, S->nodeA.ptr, 16 * st.nodes, cudaMemcpyDeviceToHost, s));
+    if (links) PT_CUDA(cudaMemcpyAsync(links, S->nodeB.ptr, 16 * st.nodes, cudaMemcpyDeviceToHost, s));
+    if (quad) PT_CUDA(cudaMemcpyAsync(quad, S->nodeQ.ptr, 32 * st.nodes, cudaMemcpyDeviceToHost, s));
+    PT_CUDA(cudaStreamSynchronize(s));
+    return PT_OK;
+}
+
+}  // extern "C"

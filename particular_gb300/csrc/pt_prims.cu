@@ -1,0 +1,223 @@
+// Exclusive scan and stable LSD radix sort, written for the Barnes-Hut build.
+//
+// scan_u32: blocks of SCAN_TILE items scan in shared memory and publish their
+// totals; the totals are scanned recursively and added back.
+// radix_sort_u64: 8-bit digits, one histogram pass + one scan + one scatter pass per
+// digit. The scatter ranks keys stably inside a CTA tile with warp match/popc and a
+// per-digit running offset, so equal digits keep their input order.
+#include "pt_prims.cuh"
+
+namespace pt {
+namespace prims {
+
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// Exclusive scan of one tile; writes out[i] and sums[blockIdx.x] = tile total.
+__global__ void __launch_bounds__(SCAN_THREADS)
+    scan_tiles(const uint32_t *__restrict__ in, uint32_t *__restrict__ out, int n, uint32_t *__restrict__ sums) {
+    __shared__ uint32_t tile[SCAN_TILE];
+    __shared__ uint32_t warp_tot[SCAN_THREADS / 32];
+    const size_t base = size_t(blockIdx.x) * SCAN_TILE;
+    for (int k = threadIdx.x; k < SCAN_TILE; k += SCAN_THREADS) {
+        const size_t i = base + k;
+        tile[k] = (i < size_t(n)) ? in[i] : 0u;
+    }
+    __syncthreads();
+    uint32_t local[SCAN_ITEMS];
+    uint32_t acc = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        local[k] = acc;
+        acc += tile[threadIdx.x * SCAN_ITEMS + k];
+    }
+    const uint32_t incl = warp_incl_scan(acc);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = (lane < SCAN_THREADS / 32) ? warp_tot[lane] : 0u;
+        const uint32_t wi = warp_incl_scan(w);
+        if (lane < SCAN_THREADS / 32) warp_tot[lane] = wi - w;
+        if (lane == SCAN_THREADS / 32 - 1) sums[blockIdx.x] = wi;
+    }
+    __syncthreads();
+    const uint32_t off = warp_tot[warp] + incl - acc;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) tile[threadIdx.x * SCAN_ITEMS + k] = off + local[k];
+    __syncthreads();
+    for (int k = threadIdx.x; k < SCAN_TILE; k += SCAN_THREADS) {
+        const size_t i = base + k;
+        if (i < size_t(n)) out[i] = tile[k];
+    }
+}
+
+__global__ void scan_add(uint32_t *__restrict__ out, int n, const uint32_t *__restrict__ offs) {
+    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < size_t(n)) out[i] += offs[i / SCAN_TILE];
+}
+
+__global__ void scan_total(uint32_t *__restrict__ out, int n, const uint32_t *__restrict__ sums) {
+    out[n] = sums[0];
+}
+
+// ---- radix sort ------------------------------------------------------------
+constexpr int RS_THREADS = 256;
+constexpr int RS_ROUNDS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
+constexpr int RS_WARPS = RS_THREADS / 32;
+
+// hist[d * nblocks + b] = count of digit d in tile b.
+__global__ void __launch_bounds__(RS_THREADS)
+    rs_hist(const uint64_t *__restrict__ keys, int n, int shift, uint32_t *__restrict__ hist, int nblocks) {
+    __shared__ uint32_t cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const size_t base = size_t(blockIdx.x) * RS_TILE;
+#pragma unroll 4
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const size_t i = base + size_t(r) * RS_THREADS + threadIdx.x;
+        if (i < size_t(n)) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[size_t(threadIdx.x) * nblocks + blockIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(RS_THREADS)
+    rs_scatter(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin, uint64_t *__restrict__ kout,
+               uint32_t *__restrict__ vout, int n, int shift, const uint32_t *__restrict__ offs, int nblocks) {
+    __shared__ uint32_t warp_cnt[RS_WARPS][256];
+    __shared__ uint32_t warp_off[RS_WARPS][256];
+    __shared__ uint32_t run[256];
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    run[t] = offs[size_t(t) * nblocks + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; ++w) warp_cnt[w][t] = 0;
+    __syncthreads();
+    const uint32_t lt = (1u << lane) - 1u;
+    const size_t base = size_t(blockIdx.x) * RS_TILE;
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const size_t i = base + size_t(r) * RS_THREADS + t;
+        const bool valid = i < size_t(n);
+        const uint64_t key = valid ? kin[i] : 0ull;
+        const uint32_t val = valid ? vin[i] : 0u;
+        const uint32_t d = valid ? uint32_t((key >> shift) & 255u) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t rank = __popc(peers & lt);
+        if (valid && rank == 0) warp_cnt[warp][d] = __popc(peers);
+        __syncthreads();
+        {
+            uint32_t acc = run[t];
+#pragma unroll
+            for (int w = 0; w < RS_WARPS; ++w) {
+                const uint32_t c = warp_cnt[w][t];
+                warp_off[w][t] = acc;
+                warp_cnt[w][t] = 0;
+                acc += c;
+            }
+            run[t] = acc;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t pos = warp_off[warp][d] + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+    }
+}
+
+}  // namespace prims
+
+static int scan_rec(pt_ctx *ctx, uint32_t *tmp, size_t tmp_cap, const uint32_t *in, uint32_t *out, int n) {
+    using namespace prims;
+    cudaStream_t st = ctx->stream;
+    const int nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (size_t(2 * nb) > tmp_cap) return set_error(PT_ERR_INVALID, "scan scratch too small");
+    uint32_t *sums = tmp;
+    uint32_t *sums_scanned = tmp + nb;
+    scan_tiles<<<nb, SCAN_THREADS, 0, st>>>(in, out, n, sums);
+    PT_TRY(check_launch(ctx, "scan_tiles"));
+    if (nb == 1) {
+        scan_total<<<1, 1, 0, st>>>(out, n, sums);
+        return check_launch(ctx, "scan_total");
+    }
+    // sums_scanned gets nb + 1 entries: the scanned totals and the grand total.
+    PT_TRY(scan_rec(ctx, tmp + 2 * nb + 1, tmp_cap - (2 * nb + 1), sums, sums_scanned, nb));
+    scan_add<<<(n + 255) / 256, 256, 0, st>>>(out, n, sums_scanned);
+    PT_TRY(check_launch(ctx, "scan_add"));
+    scan_total<<<1, 1, 0, st>>>(out, n, sums_scanned + nb);
+    return check_launch(ctx, "scan_total");
+}
+
+static size_t scan_scratch_words(int n) {
+    size_t words = 0;
+    int m = n;
+    do {
+        const int nb = (m + prims::SCAN_TILE - 1) / prims::SCAN_TILE;
+        words += 2 * size_t(nb) + 1;
+        m = nb;
+        if (nb == 1) break;
+    } while (true);
+    return words + 16;
+}
+
+int scan_u32(pt_ctx *ctx, PrimScratch &s, const uint32_t *in, uint32_t *out, int n) {
+    if (n <= 0) {
+        PT_CUDA(cudaMemsetAsync(out, 0, sizeof(uint32_t), ctx->stream));
+        return PT_OK;
+    }
+    const size_t words = scan_scratch_words(n);
+    PT_TRY(ensure_buf(ctx, s.scan, words * sizeof(uint32_t)));
+    return scan_rec(ctx, static_cast<uint32_t *>(s.scan.ptr), words, in, out, n);
+}
+
+int radix_sort_u64(pt_ctx *ctx, PrimScratch &s, uint64_t *keys, uint32_t *vals, int n, int bits) {
+    using namespace prims;
+    if (n <= 1) return PT_OK;
+    const int nblocks = (n + RS_TILE - 1) / RS_TILE;
+    const int nhist = 256 * nblocks;
+    PT_TRY(ensure_buf(ctx, s.keys2, sizeof(uint64_t) * size_t(n)));
+    PT_TRY(ensure_buf(ctx, s.vals2, sizeof(uint32_t) * size_t(n)));
+    PT_TRY(ensure_buf(ctx, s.hist, sizeof(uint32_t) * (2 * size_t(nhist) + 1)));
+    uint32_t *hist = static_cast<uint32_t *>(s.hist.ptr);
+    uint32_t *offs = hist + nhist;
+    uint64_t *ka = keys, *kb = static_cast<uint64_t *>(s.keys2.ptr);
+    uint32_t *va = vals, *vb = static_cast<uint32_t *>(s.vals2.ptr);
+    const int passes = (bits + 7) / 8;
+    cudaStream_t st = ctx->stream;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        rs_hist<<<nblocks, RS_THREADS, 0, st>>>(ka, n, shift, hist, nblocks);
+        PT_TRY(check_launch(ctx, "rs_hist"));
+        PT_TRY(scan_u32(ctx, s, hist, offs, nhist));
+        rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, shift, offs, nblocks);
+        PT_TRY(check_launch(ctx, "rs_scatter"));
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    if (ka != keys) {
+        PT_CUDA(cudaMemcpyAsync(keys, ka, sizeof(uint64_t) * size_t(n), cudaMemcpyDeviceToDevice, st));
+        PT_CUDA(cudaMemcpyAsync(vals, va, sizeof(uint32_t) * size_t(n), cudaMemcpyDeviceToDevice, st));
+    }
+    return PT_OK;
+}
+
+void prim_free(pt_ctx *ctx, PrimScratch &s) {
+    free_buf(ctx, s.scan);
+    free_buf(ctx, s.hist);
+    free_buf(ctx, s.keys2);
+    free_buf(ctx, s.vals2);
+}
+
+}  // namespace pt

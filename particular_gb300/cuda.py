@@ -3,7 +3,8 @@
 Mirrors particular/src/gpu/mod.rs:
 * CudaResources      - GpuResources (gpu/mod.rs:84-143): create once, reuse across calls
 * BruteForce         - gpu::BruteForce (gpu/mod.rs:145-208): `compute(storage)`
-* cuda_brute_force   - the GpuCompute::gpu_brute_force sugar (gpu/mod.rs:13-37)
+* BarnesHut          - the GPU counterpart of sequential::BarnesHut (sequential.rs:432-543)
+* cuda_brute_force / cuda_barnes_hut - the GpuCompute::gpu_brute_force sugar (gpu/mod.rs:13-37)
 
 `compute` accepts every storage the reference's methods accept (a particle
 sequence, Ordered, Reordered, Between) and returns the accelerations of the
@@ -111,3 +112,57 @@ class BruteForce:
 def cuda_brute_force(storage, resources, interaction, exact=False):
     """`storage.cuda_brute_force(resources, interaction)` (CudaCompute sugar)."""
     return BruteForce(resources, interaction, exact).compute(storage)
+
+
+class BarnesHut:
+    """cuda::BarnesHut { theta }: the reference's orthtree built on the GPU every call
+    and walked with the reference's opening rule (sequential.rs:466-505).
+
+    quadrupole=True adds the accepted cells' quadrupole terms; group=True opens a
+    cell for a warp of 32 neighbouring bodies whenever one of them opens it. Both
+    only ever reduce the error relative to the reference's monopole walk.
+    """
+
+    def __init__(self, theta, resources, interaction, quadrupole=False, group=False):
+        self.theta = float(np.float32(theta))
+        self.resources = resources
+        self.interaction = interaction
+        self.quadrupole = bool(quadrupole)
+        self.group = bool(group)
+
+    @property
+    def flags(self):
+        return (N.PT_BH_QUADRUPOLE if self.quadrupole else 0) | (N.PT_BH_GROUP if self.group else 0)
+
+    def compute(self, storage):
+        b = as_between(storage)
+        aff = positions(b.affected)
+        src = fields(b.affecting)
+        out = np.zeros((aff.shape[0], 3), np.float32)
+        if aff.shape[0] == 0:
+            return out
+        same = b.affected is b.affecting
+        N.check(N.lib().pt_bh_accel_f32(self.resources.handle, _ptr(aff), aff.shape[0],
+                                        _ptr(aff) if same else _ptr(src), src.shape[0], self.theta,
+                                        self.interaction.softening, self.flags, _ptr(out)))
+        return out
+
+    def stats(self):
+        st = N.BhStats()
+        N.check(N.lib().pt_bh_last_stats(self.resources.handle, ctypes.byref(st)))
+        return {k: int(getattr(st, k)) for k, _ in N.BhStats._fields_}
+
+    def export_tree(self):
+        """The last tree in preorder: com_mass (n, 4), links (n, 4) int32, quad (n, 8)."""
+        st = self.stats()
+        n = st["nodes"]
+        cm = np.zeros((n, 4), np.float32)
+        ln = np.zeros((n, 4), np.int32)
+        q = np.zeros((n, 8), np.float32)
+        N.check(N.lib().pt_bh_export_tree(self.resources.handle, _ptr(cm), _ptr(ln), _ptr(q), n))
+        return {"com_mass": cm, "links": ln, "quad": q, "width": ln[:, 0].view(np.float32)}
+
+
+def cuda_barnes_hut(storage, theta, resources, interaction, **kw):
+    """`storage.cuda_barnes_hut(theta, resources, interaction)` (CudaCompute sugar)."""
+    return BarnesHut(theta, resources, interaction, **kw).compute(storage)

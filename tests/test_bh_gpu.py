@@ -1,0 +1,199 @@
+"""Barnes-Hut parity on the GPU, through the C ABI, against the CPU oracle.
+
+* the device tree is the reference's orthtree: walking the oracle's tree in the
+  reference's pop order (children 7..0, sequential.rs:489-495) with single-child
+  chains collapsed yields the GPU preorder node for node (same widths bit for bit,
+  same leaves, masses and centres of mass to FP32 rounding);
+* the walk accepts the same nodes as sequential::BarnesHut (interaction totals) and
+  gives its accelerations to FP32 rounding, except bodies where a rounding-level
+  change of a centre of mass flips one opening decision;
+* error against the FP64 judge is no worse than the reference's at the same theta;
+  quadrupoles and group opening only reduce it;
+* the reference's known-answer tests run on cuda::BarnesHut.
+"""
+import numpy as np
+import pytest
+
+import kat
+from particular_gb300 import (Acceleration, AccelerationSoftened, Between, Reordered, cuda, ics)
+from particular_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, ref):
+    a = np.asarray(a, np.float64)
+    ref = np.asarray(ref, np.float64)
+    return np.linalg.norm(a - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-30)
+
+
+def oracle_preorder(tree):
+    """Oracle tree nodes in the reference's visiting order, chains collapsed."""
+    e = tree.export()
+    internal, child = e["internal"].astype(bool), e["child"]
+    out = []
+    stack = [0]
+    while stack:
+        k = stack.pop()
+        if internal[k]:
+            kids = [c for c in child[k] if c >= 0]
+            if len(kids) == 1:
+                stack.append(kids[0])  # chain cell: same data as its only child
+                continue
+            out.append(k)
+            stack.extend(kids)  # pushed 0..7, popped 7..0
+        else:
+            out.append(k)
+    return np.array(out), e
+
+
+@pytest.mark.parametrize("kind,n", [("plummer", 3000), ("cube", 2000), ("bulge_disk", 4000)])
+def test_tree_matches_reference_orthtree(res, oracle, kind, n):
+    b = {"plummer": lambda: ics.plummer(n, seed=21)["bodies"],
+         "cube": lambda: ics.uniform_cube(n, 22)["bodies"],
+         "bulge_disk": lambda: ics.bulge_disk(n, seed=23)["bodies"]}[kind]()
+    m = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01))
+    m.compute(b)
+    g = m.export_tree()
+    order, e = oracle_preorder(oracle.Tree(b))
+    assert g["links"].shape[0] == order.size
+    internal = e["internal"][order].astype(bool)
+    g_internal = g["links"][:, 2] < 0
+    assert np.array_equal(internal, g_internal)
+    # widths: same f32 subdivision, bit for bit
+    w_ref = (e["box"][order, 3] - e["box"][order, 0])[internal]
+    assert np.array_equal(g["width"][g_internal], w_ref.astype(np.float32))
+    # leaves: the body itself
+    assert np.array_equal(g["com_mass"][~g_internal], e["data"][order][~internal])
+    # cells: FP64 mass and centre of mass of the oracle cell's bodies, rounded to f32
+    rng, perm = e["range"][order][internal], e["perm"]
+    bp = b[perm].astype(np.float64)
+    cs = np.zeros((bp.shape[0] + 1, 4))
+    cs[1:, 3] = np.cumsum(bp[:, 3])
+    cs[1:, :3] = np.cumsum(bp[:, :3] * bp[:, 3:4], axis=0)
+    lo, hi = rng[:, 0], rng[:, 0] + rng[:, 1]
+    m64 = cs[hi, 3] - cs[lo, 3]
+    c64 = (cs[hi, :3] - cs[lo, :3]) / m64[:, None]
+    cm = g["com_mass"][g_internal].astype(np.float64)
+    np.testing.assert_allclose(cm[:, 3], m64, rtol=1e-6)
+    scale = np.abs(b[:, :3]).max()
+    assert np.abs(cm[:, :3] - c64).max() <= 1e-6 * scale
+    # the reference's own f32 sums drift from those by at most ~count * 2^-24
+    ref_m = e["data"][order][internal][:, 3].astype(np.float64)
+    assert (np.abs(ref_m - m64) <= rng[:, 1] * 2.0 ** -23 * m64 + 1e-12).all()
+
+
+@pytest.mark.parametrize("theta", [0.3, 0.5, 0.8])
+def test_walk_matches_reference(res, oracle, theta):
+    b = ics.plummer(20000, seed=24)["bodies"]
+    m = cuda.BarnesHut(theta, res, AccelerationSoftened(0.01))
+    got = m.compute(b)
+    st = m.stats()
+    ref, acc = oracle.bh_f32(b, b, theta, 0.01, True, accepted=True)
+    r = rel(got, ref)
+    ref64 = oracle.bf_f64(b, b, 0.01, True)
+    e_gpu, e_ref = rel(got, ref64), rel(ref, ref64)
+    print(f"theta={theta} interactions gpu={st['interactions']} ref={int(acc.sum())} "
+          f"rel diff p50={np.median(r):.2e} p99={np.percentile(r, 99):.2e} "
+          f">1e-4: {(r > 1e-4).mean():.4f}; err gpu p50/p95/max="
+          f"{np.median(e_gpu):.2e}/{np.percentile(e_gpu, 95):.2e}/{e_gpu.max():.2e} "
+          f"ref={np.median(e_ref):.2e}/{np.percentile(e_ref, 95):.2e}/{e_ref.max():.2e}")
+    assert abs(st["interactions"] - int(acc.sum())) <= 5e-3 * acc.sum()
+    # centres of mass differ at FP32 rounding (FP64 moments here, f32 sums there)
+    assert np.median(r) < 1e-5
+    assert (r > 1e-4).mean() < 0.02
+    for q in (50, 95):
+        assert np.percentile(e_gpu, q) <= np.percentile(e_ref, q) * 1.02 + 1e-7
+    assert e_gpu.max() <= e_ref.max() * 1.2 + 1e-6
+
+
+@pytest.mark.parametrize("theta", [0.5, 1.0])
+def test_quadrupole_and_group_reduce_error(res, oracle, theta):
+    b = ics.bulge_disk(30000, seed=25)["bodies"]
+    ref64 = oracle.bf_f64(b[::10], b, 0.01, True)
+    errs = {}
+    for quad in (False, True):
+        for group in (False, True):
+            m = cuda.BarnesHut(theta, res, AccelerationSoftened(0.01), quadrupole=quad, group=group)
+            errs[(quad, group)] = np.percentile(rel(m.compute(b)[::10], ref64), 95)
+    assert errs[(True, False)] < 0.6 * errs[(False, False)]
+    assert errs[(False, True)] <= errs[(False, False)] * 1.001
+    assert errs[(True, True)] <= errs[(True, False)] * 1.001
+    print(theta, errs)
+
+
+def test_theta0_is_brute_force(res, oracle):
+    b = ics.plummer(5000, seed=26)["bodies"]
+    got = cuda.BarnesHut(0.0, res, AccelerationSoftened(0.01)).compute(b)
+    ref = oracle.bf_f64(b, b, 0.01, True)
+    r = rel(got, ref)
+    assert np.median(r) < 2e-6 and r.max() < 1e-4
+
+
+@pytest.mark.parametrize("theta,err_eps,orbit_eps", [(0.0, 1e-2, 1e-2), (0.5, 5e-1, 1e-1)])
+def test_kat(res, theta, err_eps, orbit_eps):
+    m = cuda.BarnesHut(theta, res, Acceleration.checked())
+    kat.acceleration_error(m.compute, err_eps)
+    kat.circular_orbit(m.compute, 100, orbit_eps)
+
+
+def test_separate_targets_and_storages(res, oracle):
+    src = ics.plummer(8000, seed=27)["bodies"]
+    aff = ics.uniform_cube(3000, 28)["bodies"]
+    m = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01))
+    got = m.compute(Between(aff, src))
+    ref = oracle.bh_f32(aff, src, 0.5, 0.01, True)
+    r = rel(got, ref)
+    assert np.percentile(r, 99) < 1e-5
+    p = src.copy()
+    p[::5, 3] = 0.0
+    rr = Reordered(p)
+    got = m.compute(rr)
+    ref = oracle.bh_f32(p, rr.affecting(), 0.5, 0.01, True)
+    assert np.percentile(rel(got, ref), 99) < 1e-5
+
+
+def test_edge_cases(res, oracle):
+    m = cuda.BarnesHut(0.5, res, Acceleration.checked())
+    one = np.array([[1, 2, 3, 4]], np.float32)
+    assert not m.compute(one).any()                       # a single body feels nothing
+    b = ics.uniform_cube(100, 29)["bodies"]
+    assert not m.compute(Between(b, np.zeros((0, 4), np.float32))).any()
+    assert m.compute(Between(np.zeros((0, 4), np.float32), b)).shape == (0, 3)
+    same = np.tile(np.array([[0.5, 0.5, 0.5, 1.0]], np.float32), (50, 1))
+    same = np.concatenate([same, b])                      # 50 coincident bodies: one leaf
+    got = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01)).compute(same)
+    assert np.isfinite(got).all()
+    # The reference's f32 centre of mass of the 50 coincident bodies lands a rounding
+    # away from them, so its walk adds a spurious self-pull; this leaf sums its bodies
+    # one by one and skips coincident ones, as the brute force does.
+    ref64 = oracle.bf_f64(same, same, 0.01, True)
+    assert np.percentile(rel(got, ref64), 95) < 2e-2
+    ref = oracle.bh_f32(same[50:], same, 0.5, 0.01, True)
+    assert np.percentile(rel(got[50:], ref), 95) < 1e-4
+    massless = b.copy()
+    massless[:, 3] = 0.0
+    assert not cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01)).compute(massless).any()
+
+
+def test_flags_validated(res):
+    b = ics.uniform_cube(10, 30)["bodies"]
+    out = np.zeros((10, 3), np.float32)
+    rc = N.lib().pt_bh_accel_f32(res.handle, b.ctypes.data, 10, b.ctypes.data, 10, 0.5, 0.0,
+                                 0x80, out.ctypes.data)
+    assert rc == N.PT_ERR_INVALID
+
+
+def test_full_size_sample(res, oracle):
+    """N=1M bulge+disk at theta=0.5: FP64-judged error on a 1024-body sample, no
+    worse than the reference's own walk of the same tree on those bodies."""
+    b = ics.bulge_disk(1 << 20, seed=31)["bodies"]
+    m = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01))
+    got = m.compute(b)
+    idx = np.random.default_rng(1).choice(b.shape[0], 1024, replace=False)
+    ref64 = oracle.bf_f64(b[idx], b, 0.01, True)
+    t = oracle.Tree(b)
+    ref = t.walk(b[idx], 0.5, 0.01, True)
+    e_gpu, e_ref = rel(got[idx], ref64), rel(ref, ref64)
+    assert np.percentile(e_gpu, 95) <= np.percentile(e_ref, 95) * 1.02 + 1e-7
+    assert np.percentile(rel(got[idx], ref), 99) < 1e-4
