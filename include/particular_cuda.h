@@ -145,8 +145,10 @@ int pt_bf_accel_f32_noalloc(const float *d_affected, size_t n_aff, const float *
  * skipped, Acceleration's CHECKED flag has no effect on this method, as in the
  * reference. Moments are accumulated in FP64 and stored in f32. */
 #define PT_BH_QUADRUPOLE 0x1u /* add the traceless quadrupole of accepted cells */
-#define PT_BH_GROUP 0x2u      /* open a cell for a whole warp of 32 key-adjacent bodies
-                                 when any of them opens it (never less accurate) */
+#define PT_BH_GROUP 0x2u      /* walk per warp of 32 key-adjacent bodies: a cell is opened
+                                 for all of them when the per-body rule opens it for any
+                                 (so never less accurate than that rule); accepted nodes
+                                 are evaluated from shared-memory lists */
 
 typedef struct pt_bh_stats {
     uint64_t nodes;        /* cells + leaves of the last tree */
@@ -155,6 +157,10 @@ typedef struct pt_bh_stats {
     uint64_t interactions; /* accepted nodes summed over bodies, last walk */
     uint64_t visits;       /* nodes visited, summed over bodies, last walk */
     uint64_t warps;        /* warps that walked */
+    uint64_t max_stack;    /* deepest shared-memory stack of a PT_BH_GROUP walk */
+    uint64_t overflow;     /* nonzero if a PT_BH_GROUP walk ran out of stack (its
+                              bodies are NaN; the host entry point then fails with
+                              PT_ERR_CAPACITY) */
 } pt_bh_stats;
 
 /* cuda::BarnesHut over host buffers (synchronous). Layouts as pt_bf_accel_f32. */

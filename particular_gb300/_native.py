@@ -26,7 +26,8 @@ PT_BH_GROUP = 0x2
 class BhStats(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_uint64), ("cells", ctypes.c_uint64),
                 ("leaves", ctypes.c_uint64), ("interactions", ctypes.c_uint64),
-                ("visits", ctypes.c_uint64), ("warps", ctypes.c_uint64)]
+                ("visits", ctypes.c_uint64), ("warps", ctypes.c_uint64),
+                ("max_stack", ctypes.c_uint64), ("overflow", ctypes.c_uint64)]
 
 _NAMES = {PT_ERR_INVALID: "PT_ERR_INVALID", PT_ERR_CUDA: "PT_ERR_CUDA", PT_ERR_OOM: "PT_ERR_OOM",
           PT_ERR_CAPACITY: "PT_ERR_CAPACITY", PT_ERR_TIMEOUT: "PT_ERR_TIMEOUT",

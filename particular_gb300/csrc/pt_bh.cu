@@ -20,8 +20,9 @@
 //  6. cells are laid out in depth-first preorder with skip pointers (index after
 //     the subtree), leaves interleaved: the walk needs no stack.
 //  7. moments bottom-up in FP64 (mass, centre of mass, second moment -> traceless
-//     quadrupole) with per-cell arrival counters: the last child to arrive combines
-//     the cell (parallel-axis theorem). No thread ever waits on another.
+//     quadrupole): cells are bucketed by octree level and combined level by level,
+//     deepest first, one thread per cell (parallel-axis theorem). No thread ever
+//     waits on another.
 // Walk (sequential.rs:466-505): one warp per 32 key-adjacent targets shares a cursor
 // over the preorder array; each lane applies the reference's rule per node (skip
 // when d2 == 0, open an internal cell when theta^2 d2 < w^2, else accept its
@@ -54,7 +55,7 @@ struct State {
     DevBuf keys, idx, sbody;
     DevBuf flags, uscan, ukey, ufirst;
     DevBuf bfirst, blast, bdelta, bparent, lparent, top, oparent, loparent;
-    DevBuf cnt, pscan, pre, nchild, arrive;
+    DevBuf cnt, pscan, pre, levels, by_level;
     DevBuf nodeA, nodeB, nodeQ, mom;
     DevBuf tkeys, tidx, tbody;
     DevBuf counters;
@@ -232,19 +233,17 @@ __device__ __forceinline__ int climb(int p, const uint8_t *__restrict__ top, con
 __global__ void octree_links(const int *__restrict__ counters, const int *__restrict__ bfirst,
                              const int *__restrict__ bparent, const int *__restrict__ lparent,
                              const uint8_t *__restrict__ top, int *__restrict__ oparent, int *__restrict__ loparent,
-                             uint32_t *__restrict__ cnt, int *__restrict__ nchild) {
+                             uint32_t *__restrict__ cnt) {
     const int M = counters[0];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < M - 1 && top[k]) {
         const int op = (k == 0) ? -1 : climb(bparent[k], top, bparent);
         oparent[k] = op;
         atomicAdd(&cnt[bfirst[k]], 1u);
-        if (op >= 0) atomicAdd(&nchild[op], 1);
     }
     if (k < M) {
         const int op = (M == 1) ? -1 : climb(lparent[k], top, bparent);
         loparent[k] = op;
-        if (op >= 0) atomicAdd(&nchild[op], 1);
     }
 }
 
@@ -300,83 +299,118 @@ __device__ void store_cell(const Moments &m, int pk, Moments *__restrict__ mom, 
     nodeQ[2 * pk + 1] = make_float4(float(3 * m.syz), float(3 * m.szz - tr), 0.f, 0.f);
 }
 
-__device__ __forceinline__ Moments load_moments(const Moments *p) {
-    Moments m;
-    const double *s = reinterpret_cast<const double *>(p);
-    double *d = reinterpret_cast<double *>(&m);
-#pragma unroll
-    for (int k = 0; k < 12; ++k) d[k] = __ldcg(s + k);
-    return m;
-}
-
-__global__ void moments_up(const int *__restrict__ counters, const uint32_t *__restrict__ ufirst,
-                           const float4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
-                           const uint32_t *__restrict__ cnt, const int *__restrict__ loparent,
-                           const int *__restrict__ oparent, const int *__restrict__ pre,
-                           const int *__restrict__ nchild, int *__restrict__ arrive, const int4 *__restrict__ nodeB,
-                           Moments *__restrict__ mom, float4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
+// Leaves: a single body is its own cell data; several (coincident, or closer than
+// the key resolution) get FP64 moments.
+__global__ void leaf_moments(const int *__restrict__ counters, const uint32_t *__restrict__ ufirst,
+                             const float4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
+                             const uint32_t *__restrict__ cnt, Moments *__restrict__ mom, float4 *__restrict__ nodeA,
+                             float4 *__restrict__ nodeQ) {
     const int M = counters[0];
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= M) return;
-    // Leaf unit: its bodies (almost always one).
-    {
-        const int f = int(ufirst[u]), e = int(ufirst[u + 1]);
-        Moments m{};
-        double sx = 0, sy = 0, sz = 0;
+    const int f = int(ufirst[u]), e = int(ufirst[u + 1]);
+    const int pk = u + int(pscan[u]) + int(cnt[u]);
+    if (e - f == 1) {
+        nodeA[pk] = sbody[f];
+        nodeQ[2 * pk] = make_float4(0.f, 0.f, 0.f, 0.f);
+        nodeQ[2 * pk + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    Moments m{};
+    double sx = 0, sy = 0, sz = 0;
+    for (int b = f; b < e; ++b) {
+        const float4 p = sbody[b];
+        m.m += p.w;
+        sx += double(p.w) * p.x;
+        sy += double(p.w) * p.y;
+        sz += double(p.w) * p.z;
+    }
+    m.count = e - f;
+    if (m.m != 0.0) {
+        m.cx = sx / m.m;
+        m.cy = sy / m.m;
+        m.cz = sz / m.m;
+    } else {  // massless: plain mean (gravity/impls/mod.rs:127-129)
         for (int b = f; b < e; ++b) {
             const float4 p = sbody[b];
-            m.m += p.w;
-            sx += double(p.w) * p.x;
-            sy += double(p.w) * p.y;
-            sz += double(p.w) * p.z;
+            m.cx += p.x;
+            m.cy += p.y;
+            m.cz += p.z;
         }
-        m.count = e - f;
-        if (m.m != 0.0) {
-            m.cx = sx / m.m;
-            m.cy = sy / m.m;
-            m.cz = sz / m.m;
-        } else {  // massless: plain mean (gravity/impls/mod.rs:127-129)
-            for (int b = f; b < e; ++b) {
-                const float4 p = sbody[b];
-                m.cx += p.x;
-                m.cy += p.y;
-                m.cz += p.z;
-            }
-            m.cx /= m.count;
-            m.cy /= m.count;
-            m.cz /= m.count;
-        }
-        if (e - f == 1) {  // exact body position, as the reference's single-body cell
-            const float4 p = sbody[f];
-            m.cx = p.x;
-            m.cy = p.y;
-            m.cz = p.z;
-        } else {
-            for (int b = f; b < e; ++b) {
-                const float4 p = sbody[b];
-                const double dx = p.x - m.cx, dy = p.y - m.cy, dz = p.z - m.cz;
-                m.sxx += p.w * dx * dx;
-                m.sxy += p.w * dx * dy;
-                m.sxz += p.w * dx * dz;
-                m.syy += p.w * dy * dy;
-                m.syz += p.w * dy * dz;
-                m.szz += p.w * dz * dz;
-            }
-        }
-        const int pk = u + int(pscan[u]) + int(cnt[u]);
-        store_cell(m, pk, mom, nodeA, nodeQ);
+        m.cx /= m.count;
+        m.cy /= m.count;
+        m.cz /= m.count;
     }
-    // Climb: the last child to arrive at a cell combines it.
-    for (int v = loparent[u]; v >= 0; v = oparent[v]) {
-        __threadfence();
-        if (atomicAdd(&arrive[v], 1) != nchild[v] - 1) return;
-        __threadfence();
-        const int pv = pre[v];
+    for (int b = f; b < e; ++b) {
+        const float4 p = sbody[b];
+        const double dx = p.x - m.cx, dy = p.y - m.cy, dz = p.z - m.cz;
+        m.sxx += p.w * dx * dx;
+        m.sxy += p.w * dx * dy;
+        m.sxz += p.w * dx * dz;
+        m.syy += p.w * dy * dy;
+        m.syz += p.w * dy * dz;
+        m.szz += p.w * dz * dz;
+    }
+    store_cell(m, pk, mom, nodeA, nodeQ);
+}
+
+// Cells per octree level: lcount[L], then by_level sorted by level (counting sort).
+// levels[0..LEVELS] = counts, levels[LEVELS+1 ..] = offsets, then cursors.
+__global__ void cell_level_count(const int *__restrict__ counters, const int *__restrict__ bdelta,
+                                 const uint8_t *__restrict__ top, int *__restrict__ levels) {
+    const int M = counters[0];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < M - 1 && top[k]) atomicAdd(&levels[bdelta[k] / 3], 1);
+}
+
+__global__ void cell_level_offsets(int *__restrict__ levels) {
+    if (threadIdx.x != 0) return;
+    int acc = 0;
+    for (int L = 0; L < LEVELS; ++L) {
+        levels[LEVELS + 1 + L] = acc;      // offset
+        levels[2 * LEVELS + 2 + L] = acc;  // cursor
+        acc += levels[L];
+    }
+    levels[2 * LEVELS + 1] = acc;
+}
+
+__global__ void cell_level_scatter(const int *__restrict__ counters, const int *__restrict__ bdelta,
+                                   const uint8_t *__restrict__ top, int *__restrict__ levels,
+                                   int *__restrict__ by_level) {
+    const int M = counters[0];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < M - 1 && top[k]) by_level[atomicAdd(&levels[2 * LEVELS + 2 + bdelta[k] / 3], 1)] = k;
+}
+
+// A child's moments: single-body leaves are read straight from nodeA (the body).
+__device__ __forceinline__ Moments load_child(int c, const Moments *__restrict__ mom, const float4 *__restrict__ nodeA,
+                                              const int4 *__restrict__ nodeB) {
+    const int4 b = nodeB[c];
+    if (b.z >= 0 && b.w == 1) {
+        const float4 a = nodeA[c];
+        Moments m{};
+        m.m = a.w;
+        m.cx = a.x;
+        m.cy = a.y;
+        m.cz = a.z;
+        m.count = 1.0;
+        return m;
+    }
+    return mom[c];
+}
+
+// Combines every cell of octree level L from its children (levels > L: done).
+__global__ void cell_moments_level(int L, const int *__restrict__ levels, const int *__restrict__ by_level,
+                                   const int *__restrict__ pre, const int4 *__restrict__ nodeB,
+                                   Moments *__restrict__ mom, float4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
+    const int begin = levels[LEVELS + 1 + L], end_l = begin + levels[L];
+    for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end_l; i += gridDim.x * blockDim.x) {
+        const int pv = pre[by_level[i]];
         const int end = nodeB[pv].y;
         Moments m{};
         double sx = 0, sy = 0, sz = 0, ux = 0, uy = 0, uz = 0;
         for (int c = pv + 1; c < end; c = nodeB[c].y) {
-            const Moments cm = load_moments(mom + c);
+            const Moments cm = load_child(c, mom, nodeA, nodeB);
             m.m += cm.m;
             m.count += cm.count;
             sx += cm.m * cm.cx;
@@ -387,16 +421,17 @@ __global__ void moments_up(const int *__restrict__ counters, const uint32_t *__r
             uz += cm.count * cm.cz;
         }
         if (m.m != 0.0) {
-            m.cx = sx / m.m;
-            m.cy = sy / m.m;
-            m.cz = sz / m.m;
+            const double inv = 1.0 / m.m;
+            m.cx = sx * inv;
+            m.cy = sy * inv;
+            m.cz = sz * inv;
         } else {
             m.cx = ux / m.count;
             m.cy = uy / m.count;
             m.cz = uz / m.count;
         }
         for (int c = pv + 1; c < end; c = nodeB[c].y) {
-            const Moments cm = load_moments(mom + c);
+            const Moments cm = load_child(c, mom, nodeA, nodeB);
             const double dx = cm.cx - m.cx, dy = cm.cy - m.cy, dz = cm.cz - m.cz;
             m.sxx += cm.sxx + cm.m * dx * dx;
             m.sxy += cm.sxy + cm.m * dx * dy;
@@ -416,7 +451,7 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
     return r;
 }
 
-template <bool GROUP, bool QUAD>
+template <bool QUAD>
 __global__ void __launch_bounds__(WALK_THREADS)
     bh_walk(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
             const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
@@ -447,7 +482,6 @@ __global__ void __launch_bounds__(WALK_THREADS)
             const float w = __int_as_float(B.x);
             open = !zero && B.z < 0 && th2 * d2 < w * w;
         }
-        if (GROUP) open = __any_sync(0xffffffffu, open) && B.z < 0;
         int next = resume;
         if (active) {
             ++nvisit;
@@ -475,7 +509,7 @@ __global__ void __launch_bounds__(WALK_THREADS)
                     ax = fmaf(dx, s, ax);
                     ay = fmaf(dy, s, ay);
                     az = fmaf(dz, s, az);
-                    if (QUAD && B.z < 0) {
+                    if (QUAD && B.z < 0) {  // traceless quadrupole of the cell
                         const float4 q0 = __ldg(nodeQ + 2 * node);
                         const float4 q1 = __ldg(nodeQ + 2 * node + 1);
                         // q0 = (Qxx, Qxy, Qxz, Qyy), q1 = (Qyz, Qzz)
@@ -517,12 +551,308 @@ __global__ void __launch_bounds__(WALK_THREADS)
     }
 }
 
+// ---- group walk (PT_BH_GROUP) ----------------------------------------------
+// One warp walks for 32 key-adjacent targets. Each step pops up to 32 nodes from a
+// shared-memory stack of sibling ranges (independent loads, one per lane), opens a
+// cell when the reference's per-body rule opens it for at least one of the 32
+// targets (so never less accurate than that rule), and appends accepted nodes to a
+// shared-memory interaction list. A full list is evaluated densely: every lane runs its target
+// against all entries, two entries per packed f32x2 instruction.
+constexpr int GW_WARPS = 4;
+constexpr int GW_STACK = 1024;  // sibling ranges per warp (~32 per tree level are live)
+
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk2(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk2(f2 v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+template <bool QUAD>
+struct GroupList {
+    static constexpr int CAP = QUAD ? 128 : 256;
+    static constexpr int NF = QUAD ? 10 : 4;  // x, y, z, m [, Qxx, Qxy, Qxz, Qyy, Qyz, Qzz]
+    float f[NF][CAP + 2];
+};
+
+// Evaluates entries [0, cnt) of the list for this lane's target (x, y, z).
+template <bool QUAD, bool GUARD>
+__device__ __forceinline__ void eval_list(GroupList<QUAD> &Lst, int cnt, f2 px, f2 py, f2 pz, f2 e2, f2 &ax,
+                                          f2 &ay, f2 &az) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    if (cnt & 1) {  // pad with a massless entry far away: contributes exactly 0
+        if (lane < GroupList<QUAD>::NF) Lst.f[lane][cnt] = (lane < 3) ? 1e30f : 0.0f;
+        __syncwarp();
+        ++cnt;
+    }
+    const f2 half5 = pk2(2.5f, 2.5f);
+#pragma unroll 2
+    for (int e = 0; e < cnt; e += 2) {
+        const f2 dx = sub2(*reinterpret_cast<const f2 *>(&Lst.f[0][e]), px);
+        const f2 dy = sub2(*reinterpret_cast<const f2 *>(&Lst.f[1][e]), py);
+        const f2 dz = sub2(*reinterpret_cast<const f2 *>(&Lst.f[2][e]), pz);
+        const f2 m = *reinterpret_cast<const f2 *>(&Lst.f[3][e]);
+        const f2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+        float r0, r1;
+        upk2(r2, r0, r1);
+        float i0 = rsqrt_ftz(r0), i1 = rsqrt_ftz(r1);
+        if (GUARD) {
+            i0 = (r0 > 0.0f) ? i0 : 0.0f;
+            i1 = (r1 > 0.0f) ? i1 : 0.0f;
+        }
+        const f2 inv = pk2(i0, i1);
+        const f2 inv2 = mul2(inv, inv);
+        const f2 sc = mul2(mul2(m, inv), inv2);
+        ax = fma2(dx, sc, ax);
+        ay = fma2(dy, sc, ay);
+        az = fma2(dz, sc, az);
+        if constexpr (QUAD) {
+            const f2 qxx = *reinterpret_cast<const f2 *>(&Lst.f[4][e]);
+            const f2 qxy = *reinterpret_cast<const f2 *>(&Lst.f[5][e]);
+            const f2 qxz = *reinterpret_cast<const f2 *>(&Lst.f[6][e]);
+            const f2 qyy = *reinterpret_cast<const f2 *>(&Lst.f[7][e]);
+            const f2 qyz = *reinterpret_cast<const f2 *>(&Lst.f[8][e]);
+            const f2 qzz = *reinterpret_cast<const f2 *>(&Lst.f[9][e]);
+            const f2 qx = fma2(qxx, dx, fma2(qxy, dy, mul2(qxz, dz)));
+            const f2 qy = fma2(qxy, dx, fma2(qyy, dy, mul2(qyz, dz)));
+            const f2 qz = fma2(qxz, dx, fma2(qyz, dy, mul2(qzz, dz)));
+            const f2 dqd = fma2(dx, qx, fma2(dy, qy, mul2(dz, qz)));
+            const f2 inv5 = mul2(mul2(inv2, inv2), inv);
+            const f2 c7 = mul2(mul2(dqd, half5), mul2(inv5, inv2));
+            const f2 ninv5 = sub2(pk2(0.f, 0.f), inv5);
+            ax = fma2(c7, dx, fma2(qx, ninv5, ax));
+            ay = fma2(c7, dy, fma2(qy, ninv5, ay));
+            az = fma2(c7, dz, fma2(qz, ninv5, az));
+        }
+    }
+    __syncwarp();
+}
+
+template <bool QUAD, bool GUARD>
+__global__ void __launch_bounds__(32 * GW_WARPS)
+    bh_walk_group(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
+                  const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
+                  const float4 *__restrict__ sbody, const int *__restrict__ counters,
+                  float th2, float eps2, float *__restrict__ out, unsigned long long *__restrict__ stats,
+                  int *__restrict__ err) {
+    __shared__ int2 s_stack[GW_WARPS][GW_STACK];
+    __shared__ float4 s_tgt[GW_WARPS][32];
+    __shared__ __align__(16) GroupList<QUAD> s_list[GW_WARPS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int group = blockIdx.x * GW_WARPS + warp;
+    if (group * 32 >= n_aff) return;
+    const int t = group * 32 + lane;
+    const bool valid = t < n_aff;
+    const float4 p = tbody[valid ? t : group * 32];
+    const unsigned lt = (1u << lane) - 1u;
+    int2 *stack = s_stack[warp];
+    const int T = counters[1];
+    GroupList<QUAD> &Lst = s_list[warp];
+
+    // the warp's targets, read back as shared-memory broadcasts by the opening test
+    s_tgt[warp][lane] = p;
+    const float4 *tgt = s_tgt[warp];
+    __syncwarp();
+    // and their bounding box: a cell whose centre of mass is far enough from the box
+    // is accepted by every target, which spares the 32-target test
+    float mn0 = p.x, mn1 = p.y, mn2 = p.z, mx0 = p.x, mx1 = p.y, mx2 = p.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn0 = fminf(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
+        mn1 = fminf(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
+        mn2 = fminf(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
+        mx0 = fmaxf(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
+        mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
+        mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
+    }
+
+    const f2 px = pk2(p.x, p.x), py = pk2(p.y, p.y), pz = pk2(p.z, p.z), e2 = pk2(eps2, eps2);
+    f2 ax = pk2(0.f, 0.f), ay = ax, az = ax;
+    // Stack entries are sibling ranges (first, end): `first` is the next node to
+    // visit, its later siblings follow by skip pointers up to `end`. A pop visits one
+    // node and pushes back at most two ranges: its remaining siblings and, for an
+    // opened cell, its children (pre+1, skip). The stack therefore stays within about
+    // 32 ranges per tree level.
+    if (lane == 0) stack[0] = make_int2(0, T);
+    __syncwarp();
+    int S = 1, L = 0, maxS = 1;
+    unsigned long long entries = 0, visits = 0;
+    bool failed = false;
+    while (S > 0) {
+        // each pop pushes at most two ranges: never more than the room left
+        const int k = min(min(32, S), max(1, (GW_STACK - S) / 2));
+        const bool have = lane < k;
+        const int2 range = have ? stack[S - 1 - lane] : make_int2(0, 0);
+        __syncwarp();
+        S -= k;
+        visits += k;
+        const int node = range.x;
+        float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
+        int4 B = make_int4(0, 0, 0, 0);
+        bool open = false;
+        if (have) {
+            A = __ldg(nodeA + node);
+            B = __ldg(nodeB + node);
+        }
+        // Open iff the per-body rule opens for at least one target: the smallest
+        // nonzero d^2 over the warp's targets decides (targets with d^2 == 0 skip the
+        // cell under that rule and do not vote). Cells accepted even from the nearest
+        // point of the targets' box are settled without the per-target loop.
+        bool maybe = false;
+        if (have && B.z < 0) {
+            const float w = __int_as_float(B.x);
+            const float e0 = fmaxf(fmaxf(mn0 - A.x, A.x - mx0), 0.f);
+            const float e1 = fmaxf(fmaxf(mn1 - A.y, A.y - mx1), 0.f);
+            const float e2b = fmaxf(fmaxf(mn2 - A.z, A.z - mx2), 0.f);
+            maybe = th2 * fmaf(e0, e0, fmaf(e1, e1, e2b * e2b)) < w * w;
+        }
+        if (__any_sync(0xffffffffu, maybe)) {
+            float dmin = INFINITY;
+#pragma unroll 8
+            for (int b = 0; b < 32; ++b) {
+                const float4 q = tgt[b];
+                const float dx = A.x - q.x, dy = A.y - q.y, dz = A.z - q.z;
+                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                dmin = (d2 > 0.0f) ? fminf(dmin, d2) : dmin;
+            }
+            const float w = __int_as_float(B.x);
+            open = maybe && th2 * dmin < w * w;
+        }
+        const bool rest = have && B.y < range.y;  // later siblings remain
+        const int np = int(rest) + int(open);
+        int incl = np;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        int w = S + incl - np;
+        if (w + np > GW_STACK) {
+            failed = true;  // never written out of bounds
+        } else {
+            if (rest) stack[w++] = make_int2(B.y, range.y);
+            if (open) stack[w++] = make_int2(node + 1, B.y);  // children on top: popped first
+        }
+        if (__any_sync(0xffffffffu, failed)) {
+            failed = true;
+            break;
+        }
+        S += total;
+        maxS = max(maxS, S);
+        const bool acc = have && !open;
+        const bool bucket = acc && B.z >= 0 && B.w > 1;
+        const bool single = acc && !bucket;
+        const unsigned m1 = __ballot_sync(0xffffffffu, single);
+        const int n1 = __popc(m1);
+        if (L + n1 > GroupList<QUAD>::CAP) {
+            eval_list<QUAD, GUARD>(Lst, L, px, py, pz, e2, ax, ay, az);
+            entries += L;
+            L = 0;
+        }
+        if (single) {
+            const int e = L + __popc(m1 & lt);
+            Lst.f[0][e] = A.x;
+            Lst.f[1][e] = A.y;
+            Lst.f[2][e] = A.z;
+            Lst.f[3][e] = A.w;
+            if constexpr (QUAD) {
+                float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
+                if (B.z < 0) {
+                    q0 = __ldg(nodeQ + 2 * node);
+                    q1 = __ldg(nodeQ + 2 * node + 1);
+                }
+                Lst.f[4][e] = q0.x;
+                Lst.f[5][e] = q0.y;
+                Lst.f[6][e] = q0.z;
+                Lst.f[7][e] = q0.w;
+                Lst.f[8][e] = q1.x;
+                Lst.f[9][e] = q1.y;
+            }
+        }
+        L += n1;
+        unsigned mb = __ballot_sync(0xffffffffu, bucket);
+        while (mb) {  // leaves holding several bodies: one entry per body
+            const int src = __ffs(mb) - 1;
+            mb &= mb - 1;
+            const int f = __shfl_sync(0xffffffffu, B.z, src);
+            const int c = __shfl_sync(0xffffffffu, B.w, src);
+            for (int base = 0; base < c; base += 32) {
+                const int n = min(32, c - base);
+                if (L + n > GroupList<QUAD>::CAP) {
+                    eval_list<QUAD, GUARD>(Lst, L, px, py, pz, e2, ax, ay, az);
+                    entries += L;
+                    L = 0;
+                }
+                if (lane < n) {
+                    const float4 q = __ldg(sbody + f + base + lane);
+                    Lst.f[0][L + lane] = q.x;
+                    Lst.f[1][L + lane] = q.y;
+                    Lst.f[2][L + lane] = q.z;
+                    Lst.f[3][L + lane] = q.w;
+                    if constexpr (QUAD)
+                        for (int j = 4; j < GroupList<QUAD>::NF; ++j) Lst.f[j][L + lane] = 0.f;
+                }
+                L += n;
+            }
+        }
+        __syncwarp();
+    }
+    eval_list<QUAD, GUARD>(Lst, L, px, py, pz, e2, ax, ay, az);
+    entries += L;
+    float x0, x1, y0, y1, z0, z1;
+    upk2(ax, x0, x1);
+    upk2(ay, y0, y1);
+    upk2(az, z0, z1);
+    if (failed) {
+        x0 = y0 = z0 = __int_as_float(0x7fc00000);
+        if (lane == 0) atomicExch(err, 1);
+    }
+    if (valid) {
+        const uint32_t o = tidx[t];
+        out[3 * size_t(o) + 0] = x0 + x1;
+        out[3 * size_t(o) + 1] = y0 + y1;
+        out[3 * size_t(o) + 2] = z0 + z1;
+    }
+    if (stats && lane == 0) {
+        const unsigned long long nvalid = unsigned(min(32, n_aff - group * 32));
+        atomicAdd(stats + 0, entries * nvalid);
+        atomicAdd(stats + 1, visits * nvalid);
+        atomicAdd(stats + 2, 1ull);
+        atomicMax(stats + 3, (unsigned long long)maxS);
+    }
+}
+
 using WalkKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
                             const float4 *, const int *, float, float, float *, unsigned long long *);
+using GroupKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
+                             const float4 *, const int *, float, float, float *,
+                             unsigned long long *, int *);
 
-static WalkKernel walk_kernel(bool group, bool quad) {
-    if (group) return quad ? bh_walk<true, true> : bh_walk<true, false>;
-    return quad ? bh_walk<false, true> : bh_walk<false, false>;
+static WalkKernel walk_kernel(bool quad) { return quad ? bh_walk<true> : bh_walk<false>; }
+
+static GroupKernel group_kernel(bool quad, bool guard) {
+    if (quad) return guard ? bh_walk_group<true, true> : bh_walk_group<true, false>;
+    return guard ? bh_walk_group<false, true> : bh_walk_group<false, false>;
 }
 
 static State *state(pt_ctx *ctx) {
@@ -561,8 +891,8 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
     PT_TRY(ensure_buf(ctx, S.cnt, sizeof(uint32_t) * (N + 1)));
     PT_TRY(ensure_buf(ctx, S.pscan, sizeof(uint32_t) * (N + 2)));
     PT_TRY(ensure_buf(ctx, S.pre, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.nchild, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.arrive, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.levels, sizeof(int) * (3 * LEVELS + 8)));
+    PT_TRY(ensure_buf(ctx, S.by_level, sizeof(int) * N));
     PT_TRY(ensure_buf(ctx, S.nodeA, sizeof(float4) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.nodeB, sizeof(int4) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.nodeQ, sizeof(float4) * 4 * N));
@@ -592,11 +922,10 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
     octree_top<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<int>(S.bparent), as<uint8_t>(S.top));
     PT_TRY(check_launch(ctx, "octree_top"));
     PT_CUDA(cudaMemsetAsync(S.cnt.ptr, 0, sizeof(uint32_t) * (N + 1), st));
-    PT_CUDA(cudaMemsetAsync(S.nchild.ptr, 0, sizeof(int) * N, st));
-    PT_CUDA(cudaMemsetAsync(S.arrive.ptr, 0, sizeof(int) * N, st));
+    PT_CUDA(cudaMemsetAsync(S.levels.ptr, 0, sizeof(int) * (3 * LEVELS + 8), st));
     octree_links<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.bparent), as<int>(S.lparent),
                                            as<uint8_t>(S.top), as<int>(S.oparent), as<int>(S.loparent),
-                                           as<uint32_t>(S.cnt), as<int>(S.nchild));
+                                           as<uint32_t>(S.cnt));
     PT_TRY(check_launch(ctx, "octree_links"));
     PT_TRY(scan_u32(ctx, S.prims, as<uint32_t>(S.cnt), as<uint32_t>(S.pscan), n + 1));
     layout<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.blast), as<int>(S.bdelta),
@@ -604,12 +933,26 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
                                      as<uint32_t>(S.pscan), as<uint64_t>(S.ukey), as<uint32_t>(S.ufirst),
                                      as<float>(S.box), as<int>(S.pre), as<int4>(S.nodeB));
     PT_TRY(check_launch(ctx, "layout"));
-    moments_up<<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<float4>(S.sbody),
-                                         as<uint32_t>(S.pscan), as<uint32_t>(S.cnt), as<int>(S.loparent),
-                                         as<int>(S.oparent), as<int>(S.pre), as<int>(S.nchild),
-                                         as<int>(S.arrive), as<int4>(S.nodeB), as<Moments>(S.mom),
-                                         as<float4>(S.nodeA), as<float4>(S.nodeQ));
-    PT_TRY(check_launch(ctx, "moments_up"));
+
+    int *levels = as<int>(S.levels);
+    cell_level_count<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<uint8_t>(S.top), levels);
+    PT_TRY(check_launch(ctx, "cell_level_count"));
+    cell_level_offsets<<<1, 32, 0, st>>>(levels);
+    PT_TRY(check_launch(ctx, "cell_level_offsets"));
+    cell_level_scatter<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<uint8_t>(S.top), levels,
+                                                 as<int>(S.by_level));
+    PT_TRY(check_launch(ctx, "cell_level_scatter"));
+    leaf_moments<<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<float4>(S.sbody),
+                                           as<uint32_t>(S.pscan), as<uint32_t>(S.cnt), as<Moments>(S.mom),
+                                           as<float4>(S.nodeA), as<float4>(S.nodeQ));
+    PT_TRY(check_launch(ctx, "leaf_moments"));
+    const int lvl_grid = std::max(1, std::min(blocks(n), 8 * ctx->sm_count));
+    for (int L = LEVELS - 1; L >= 0; --L) {
+        cell_moments_level<<<lvl_grid, 256, 0, st>>>(L, levels, as<int>(S.by_level), as<int>(S.pre),
+                                                     as<int4>(S.nodeB), as<Moments>(S.mom), as<float4>(S.nodeA),
+                                                     as<float4>(S.nodeQ));
+        PT_TRY(check_launch(ctx, "cell_moments_level"));
+    }
     S.last_n_src = n;
     return PT_OK;
 }
@@ -650,12 +993,22 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
         tbody = as<float4>(S.tbody);
         tidx = as<uint32_t>(S.tidx);
     }
-    unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 4;
-    PT_CUDA(cudaMemsetAsync(stats, 0, 3 * sizeof(unsigned long long), st));
+    // counters: int[4] = {leaves, nodes, cells, error} then u64[4] = {interactions,
+    // visits, warps, max group stack}
+    unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 2;
+    int *err = as<int>(S.counters) + 3;
+    PT_CUDA(cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), st));
+    PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     const float th2 = theta * theta;
     const float eps2 = softening * softening;
-    walk_kernel(flags & PT_BH_GROUP, flags & PT_BH_QUADRUPOLE)<<<blocks(n_aff, WALK_THREADS), WALK_THREADS, 0,
-                                                                st>>>(
+    const bool quad = flags & PT_BH_QUADRUPOLE;
+    if (flags & PT_BH_GROUP) {
+        const int groups = (n_aff + 31) / 32;
+        group_kernel(quad, eps2 == 0.0f)<<<(groups + GW_WARPS - 1) / GW_WARPS, 32 * GW_WARPS, 0, st>>>(
+            tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.sbody), as<int>(S.counters), th2, eps2, d_out, stats, err);
+        return check_launch(ctx, "bh_walk_group");
+    }
+    walk_kernel(quad)<<<blocks(n_aff, WALK_THREADS), WALK_THREADS, 0, st>>>(
         tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.sbody),
         as<int>(S.counters), th2, eps2, d_out, stats);
     return check_launch(ctx, "bh_walk");
@@ -680,8 +1033,8 @@ void pt_bh_state_free(pt_ctx *ctx) {
     prim_free(ctx, S->prims);
     DevBuf *all[] = {&S->box_part, &S->box,    &S->keys,   &S->idx,    &S->sbody,   &S->flags,  &S->uscan,
                      &S->ukey,     &S->ufirst, &S->bfirst, &S->blast,  &S->bdelta,  &S->bparent, &S->lparent,
-                     &S->top,      &S->oparent, &S->loparent, &S->cnt, &S->pscan,   &S->pre,    &S->nchild,
-                     &S->arrive,   &S->nodeA,  &S->nodeB,  &S->nodeQ,  &S->mom,     &S->tkeys,  &S->tidx,
+                     &S->top,      &S->oparent, &S->loparent, &S->cnt, &S->pscan,   &S->pre,    &S->levels,
+                     &S->by_level,   &S->nodeA,  &S->nodeB,  &S->nodeQ,  &S->mom,     &S->tkeys,  &S->tidx,
                      &S->tbody,    &S->counters, &S->out,  &S->aff_h,  &S->src_h};
     for (DevBuf *b : all) free_buf(ctx, *b);
     delete S;
@@ -730,7 +1083,12 @@ int pt_bh_accel_f32(pt_ctx *ctx, const float *aff, size_t n_aff, const float *sr
     PT_TRY(bh::run(ctx, reinterpret_cast<const float4 *>(d_aff), int(n_aff), reinterpret_cast<const float4 *>(d_src),
                    int(n_src), theta, softening, flags, d_out));
     PT_CUDA(cudaMemcpyAsync(out, d_out, 12 * n_aff, cudaMemcpyDeviceToHost, st));
+    int err = 0;
+    if (n_src) PT_CUDA(cudaMemcpyAsync(&err, static_cast<int *>(S->counters.ptr) + 3, sizeof(int),
+                                       cudaMemcpyDeviceToHost, st));
     PT_CUDA(cudaStreamSynchronize(st));
+    if (err)
+        return set_error(PT_ERR_CAPACITY, "pt_bh_accel_f32: a group walk ran out of stack; its bodies are NaN");
     return PT_OK;
 }
 
@@ -748,9 +1106,11 @@ int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out) {
     out->leaves = uint64_t(hi[0]);
     out->nodes = uint64_t(hi[1]);
     out->cells = uint64_t(hi[2]);
-    out->interactions = h[4];
-    out->visits = h[5];
-    out->warps = h[6];
+    out->overflow = uint64_t(hi[3]);
+    out->interactions = h[2];
+    out->visits = h[3];
+    out->warps = h[4];
+    out->max_stack = h[5];
     return PT_OK;
 }
 

@@ -130,9 +130,10 @@ def test_theta0_is_brute_force(res, oracle):
     assert np.median(r) < 2e-6 and r.max() < 1e-4
 
 
+@pytest.mark.parametrize("group", [False, True])
 @pytest.mark.parametrize("theta,err_eps,orbit_eps", [(0.0, 1e-2, 1e-2), (0.5, 5e-1, 1e-1)])
-def test_kat(res, theta, err_eps, orbit_eps):
-    m = cuda.BarnesHut(theta, res, Acceleration.checked())
+def test_kat(res, theta, err_eps, orbit_eps, group):
+    m = cuda.BarnesHut(theta, res, Acceleration.checked(), group=group)
     kat.acceleration_error(m.compute, err_eps)
     kat.circular_orbit(m.compute, 100, orbit_eps)
 
@@ -197,3 +198,34 @@ def test_full_size_sample(res, oracle):
     e_gpu, e_ref = rel(got[idx], ref64), rel(ref, ref64)
     assert np.percentile(e_gpu, 95) <= np.percentile(e_ref, 95) * 1.02 + 1e-7
     assert np.percentile(rel(got[idx], ref), 99) < 1e-4
+
+
+@pytest.mark.parametrize("kind", ["plummer", "bulge_disk", "cube"])
+@pytest.mark.parametrize("theta", [0.3, 0.7, 1.0])
+def test_group_walk_never_less_accurate(res, oracle, kind, theta):
+    """PT_BH_GROUP opens wherever the per-body rule would: its FP64-judged error is
+    bounded by the reference walk's on every percentile we report."""
+    b = {"plummer": lambda: ics.plummer(20000, seed=41)["bodies"],
+         "bulge_disk": lambda: ics.bulge_disk(20000, seed=42)["bodies"],
+         "cube": lambda: ics.uniform_cube(20000, 43)["bodies"]}[kind]()
+    ref64 = oracle.bf_f64(b, b, 0.01, True)
+    ref = oracle.bh_f32(b, b, theta, 0.01, True)
+    e_ref = rel(ref, ref64)
+    for quad in (False, True):
+        m = cuda.BarnesHut(theta, res, AccelerationSoftened(0.01), quadrupole=quad, group=True)
+        e = rel(m.compute(b), ref64)
+        st = m.stats()
+        assert st["overflow"] == 0 and st["max_stack"] < 1024
+        for q in (50, 95, 99):
+            assert np.percentile(e, q) <= np.percentile(e_ref, q) * 1.01 + 1e-6, (quad, q)
+
+
+def test_group_walk_eps0_and_separate_targets(res, oracle):
+    src = ics.plummer(6000, seed=44)["bodies"]
+    aff = np.concatenate([src[:500], ics.uniform_cube(500, 45)["bodies"]])
+    m = cuda.BarnesHut(0.4, res, Acceleration.checked(), group=True, quadrupole=True)
+    got = m.compute(Between(aff, src))
+    assert np.isfinite(got).all()
+    ref64 = oracle.bf_f64(aff, src, 0.0, True)
+    ref = oracle.bh_f32(aff, src, 0.4, 0.0, True)
+    assert np.percentile(rel(got, ref64), 95) <= np.percentile(rel(ref, ref64), 95) * 1.01 + 1e-6
