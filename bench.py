@@ -35,7 +35,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="bf_plummer_131072")
+    p.add_argument("--workload", default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -177,8 +177,200 @@ class BruteForceWorkload:
     def cpu_sample(self):
         return 8192
 
+    def cpu_reference(self, threads, steps=1):
+        rates = [self.cpu_step(threads, self.cpu_sample()) for _ in range(steps)]
+        return statistics.mean(rates), {"sample": f"{self.cpu_sample()} targets against all "
+                                                  "sources per step"}
 
-WORKLOADS = {BruteForceWorkload.name: BruteForceWorkload}
+    def extra(self):
+        return {}
+
+
+def rel_err(a, ref):
+    a = np.asarray(a, np.float64)
+    ref = np.asarray(ref, np.float64)
+    return np.linalg.norm(a - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-30)
+
+
+def err_stats(e):
+    return {"p50": float(np.median(e)), "p95": float(np.percentile(e, 95)), "max": float(e.max())}
+
+
+class BarnesHutWorkload:
+    """Barnes-Hut accelerations of an N=4,194,304 bulge+disk mixture (70% Plummer bulge
+    a=0.5, 30% exponential disk R_d=2, h=0.05, equal masses summing to 1), softening
+    0.01, full tree rebuild every step. The metric counts bodies/s of the fastest
+    configuration whose p95 relative error against the FP64 brute force (on a seeded
+    2048-body sample) is <= 1e-3; the configurations and their errors are reported."""
+
+    name = "bh_bulge_disk_4194304"
+    metric = "bodies/s at <=1e-3 p95 accel err vs FP64"
+    unit = "bodies/s"
+    bar = 1e-3
+    # (theta, flags) candidates: quadrupole + group opening; the reference's own
+    # monopole per-body walk at theta 0.5 is measured alongside as "plain".
+    ladder = [(0.45, 3), (0.5, 3), (0.55, 3), (0.6, 3)]
+
+    def __init__(self, n=4194304, softening=0.01, sample=2048):
+        from particular_gb300 import ics
+        self.n = n
+        self.softening = softening
+        self.bodies = ics.bulge_disk(n, seed=1810)["bodies"]
+        self.sample = np.random.default_rng(1808).choice(n, sample, replace=False)
+        self.theta, self.flags = 0.5, 3
+        self.table = []
+
+    def config(self):
+        return {"workload": self.name, "n_bodies": self.n, "softening": self.softening,
+                "ic": "70% Plummer bulge a=0.5 + 30% exp. disk Rd=2 h=0.05, equal masses, seeded",
+                "step": "full tree rebuild + accelerations of all bodies",
+                "error_judge": "FP64 brute force on a seeded 2048-body sample",
+                "error_bar_p95": self.bar,
+                "l2": "inputs (64 MiB bodies + ~0.5 GiB tree) exceed L2; also flushed between steps"}
+
+    # ---- GPU arm
+    def setup_gpu(self, res, torch, stream):
+        from particular_gb300 import _native as N
+        self.torch = torch
+        self.res = res
+        L = N.lib()
+        self.d_b = torch.from_numpy(self.bodies).to("cuda")
+        self.d_out = torch.empty((self.n, 3), dtype=torch.float32, device="cuda")
+        self.h_b = torch.from_numpy(self.bodies).pin_memory()
+        self.h_out = torch.empty((self.n, 3), dtype=torch.float32).pin_memory()
+        idx = torch.from_numpy(self.sample).to("cuda")
+        ds = self.d_b[idx].contiguous()
+        ref = torch.empty((self.sample.size, 3), dtype=torch.float64, device="cuda")
+        N.check(L.pt_bf_accel_f64_device(res.handle, ds.data_ptr(), self.sample.size,
+                                         self.d_b.data_ptr(), self.n, self.softening, 1,
+                                         ref.data_ptr()))
+        torch.cuda.synchronize()
+        self.ref64 = ref.cpu().numpy()
+        idx_t = idx
+
+        def measure(theta, flags):
+            for _ in range(2):
+                self._run(theta, flags)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(3):
+                self._run(theta, flags)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / 3
+            e = rel_err(self.d_out[idx_t].cpu().numpy(), self.ref64)
+            return {"theta": theta, "quadrupole": bool(flags & 1), "group": bool(flags & 2),
+                    "ms": ms, "bodies_per_s": self.n / (ms * 1e-3), **err_stats(e)}
+
+        self.plain = measure(0.5, 0)
+        ok = []
+        for theta, flags in self.ladder:
+            row = measure(theta, flags)
+            self.table.append(row)
+            if row["p95"] <= self.bar:
+                ok.append(row)
+        best = max(ok, key=lambda r: r["bodies_per_s"]) if ok else min(self.table, key=lambda r: r["p95"])
+        self.meets_bar = bool(ok)
+        self.theta = best["theta"]
+        self.flags = (1 if best["quadrupole"] else 0) | (2 if best["group"] else 0)
+        self.selected = best
+
+    def _run(self, theta, flags):
+        from particular_gb300 import _native as N
+        N.check(N.lib().pt_bh_accel_f32_device(self.res.handle, self.d_b.data_ptr(), self.n,
+                                               self.d_b.data_ptr(), self.n, theta,
+                                               self.softening, flags, self.d_out.data_ptr()))
+
+    def step_device(self):
+        self._run(self.theta, self.flags)
+
+    def step_e2e(self):
+        from particular_gb300 import _native as N
+        N.check(N.lib().pt_bh_accel_f32(self.res.handle, self.h_b.data_ptr(), self.n,
+                                        self.h_b.data_ptr(), self.n, self.theta, self.softening,
+                                        self.flags, self.h_out.data_ptr()))
+
+    def h2d_d2h_bytes(self):
+        return 16 * self.n, 12 * self.n
+
+    def flops_per_interaction(self):
+        # monopole: 20 (the GPU Gems convention); quadrupole term: 38 more
+        return 20 + (38 if self.flags & 1 else 0)
+
+    def roofline(self, res, step_ms):
+        import ctypes
+        from particular_gb300 import _native as N
+        L = N.lib()
+        N.check(L.pt_ctx_set_timing(res.handle, 1))
+        walk, build = [], []
+        for _ in range(5):
+            self.step_device()
+            t = N.Timing()
+            N.check(L.pt_last_timing(res.handle, ctypes.byref(t)))
+            walk.append(t.walk_ms)
+            build.append(t.build_ms)
+        N.check(L.pt_ctx_set_timing(res.handle, 0))
+        st = N.BhStats()
+        N.check(L.pt_bh_last_stats(res.handle, ctypes.byref(st)))
+        peak = ctypes.c_double(0)
+        N.check(L.pt_measure_fp32_peak(res.handle, ctypes.byref(peak)))
+        walk_ms = statistics.mean(walk)
+        flops = st.interactions * self.flops_per_interaction()
+        achieved = flops / (walk_ms * 1e-3) / 1e12
+        return {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                "frac": achieved / peak.value, "traffic": None,
+                "kernel": "bh_walk_group" if self.flags & 2 else "bh_walk",
+                "walk_ms": walk_ms, "build_ms": statistics.mean(build),
+                "interactions_per_body": st.interactions / self.n,
+                "algorithmic": f"{self.flops_per_interaction()} flop per accepted node per body x "
+                               "interactions counted by the walk",
+                "peak_source": "measured FFMA-chain kernel over all SMs (pt_measure_fp32_peak)"}
+
+    def extra(self):
+        return {"method": {"name": "cuda::BarnesHut", "theta": self.theta,
+                           "quadrupole": bool(self.flags & 1), "group": bool(self.flags & 2)},
+                "selected": self.selected, "meets_bar": self.meets_bar,
+                "calibration": self.table, "plain_reference_rule": self.plain}
+
+    # ---- CPU arm: the reference's parallel::BarnesHut restated (sequential tree
+    # build, walk over all host threads), monopole per-body rule.
+    def cpu_reference(self, threads, steps=1, walk_sample=16384):
+        from oracle import oracle as O
+        sidx = self.sample[:512]
+        ref64 = O.bf_f64(self.bodies[sidx], self.bodies, self.softening, True, threads=threads)
+        t0 = time.perf_counter()
+        tree = O.Tree(self.bodies)
+        t_build = time.perf_counter() - t0
+        cal = []
+        theta = None
+        for th in (0.5, 0.4, 0.35, 0.3, 0.25, 0.2):
+            a = tree.walk(self.bodies[sidx], th, self.softening, True, threads=threads)
+            e = err_stats(rel_err(a, ref64))
+            cal.append({"theta": th, **e})
+            if e["p95"] <= self.bar:
+                theta = th
+                break
+        if theta is None:
+            theta = cal[-1]["theta"]
+        widx = np.linspace(0, self.n - 1, walk_sample).astype(np.int64)
+        rates = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            tree.walk(self.bodies[widx], theta, self.softening, True, threads=threads)
+            t_walk = (time.perf_counter() - t0) * (self.n / walk_sample)
+            rates.append(self.n / (t_build + t_walk))
+        info = {"theta": theta, "build_s": t_build, "calibration": cal,
+                "sample": f"full sequential tree build over {self.n} bodies + walk of "
+                          f"{walk_sample} targets scaled to {self.n}; theta = largest of "
+                          "0.5..0.2 meeting p95<=1e-3 on 512 targets"}
+        return statistics.mean(rates), info
+
+
+WORKLOADS = {BruteForceWorkload.name: BruteForceWorkload,
+             BarnesHutWorkload.name: BarnesHutWorkload}
+DEFAULT_WORKLOAD = BarnesHutWorkload.name
+
 
 
 # --------------------------------------------------------------------------- arms
@@ -188,19 +380,15 @@ def run_reference(args):
         return 0
     from oracle import build as obuild, oracle as O
     obuild.build()
-    wl = WORKLOADS[args.workload]()
+    wl = WORKLOADS[args.workload or DEFAULT_WORKLOAD]()
     threads = O.max_threads()
-    sample = wl.cpu_sample()
-    for _ in range(max(0, min(args.warmup, 1))):
-        wl.cpu_step(threads, max(256, sample // 8))
-    rates = [wl.cpu_step(threads, sample) for _ in range(args.steps)]
-    value = statistics.mean(rates)
+    value, info = wl.cpu_reference(threads, steps=max(1, args.steps))
     line = {"metric": wl.metric, "value": value, "unit": wl.unit, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wl.n / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": wl.config(), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": wl.unit, "cores": threads, "kind": "port",
-                             "sample": f"{sample} targets of the full source set per step"},
+                             **info},
             "e2e": {"value": value, "unit": wl.unit, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -219,7 +407,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     from particular_gb300 import CudaResources, build_native
     build_native.build()
-    wl = WORKLOADS[args.workload]()
+    wl = WORKLOADS[args.workload or DEFAULT_WORKLOAD]()
     res = CudaResources(local)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -279,14 +467,14 @@ def run_ours(args):
             "roofline": roof,
             "e2e": {"value": e2e_value, "unit": wl.unit, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e / args.steps},
-            "gpu_launches": int(launches), "clocks": clk}
+            "gpu_launches": int(launches), "clocks": clk, **wl.extra()}
     if not args.no_cpu_baseline:
         from oracle import build as obuild, oracle as O
         obuild.build()
         threads = O.max_threads()
-        rate = wl.cpu_step(threads, wl.cpu_sample())
+        rate, info = wl.cpu_reference(threads, steps=1)
         line["cpu_baseline"] = {"value": rate, "unit": wl.unit, "cores": threads, "kind": "port",
-                                "sample": f"{wl.cpu_sample()} targets against all sources"}
+                                **info}
     print(json.dumps(line), flush=True)
     res.close()
     return 0

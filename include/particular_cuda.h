@@ -178,6 +178,18 @@ int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out);
  * The tree the reference keeps in RootedOrthtree (particular/src/storage.rs:10-46). */
 int pt_bh_export_tree(pt_ctx *ctx, float *com_mass, int32_t *links, float *quad, size_t rows);
 
+/* Phase timing of the last pt_bf_* / pt_bh_* call, from CUDA events recorded on
+ * the context's stream when enabled: for Barnes-Hut, build = tree construction
+ * and moments, walk = the traversal kernel; for the brute force, build = source
+ * layout conversion, walk = the pair kernel(s). */
+typedef struct pt_timing {
+    float build_ms;
+    float walk_ms;
+} pt_timing;
+int pt_ctx_set_timing(pt_ctx *ctx, int enable);
+/* Waits for the last call's events and reports its phases. */
+int pt_last_timing(pt_ctx *ctx, pt_timing *out);
+
 /* Blocks until all work enqueued by the context has finished; reports any
  * asynchronous kernel error as PT_ERR_CUDA. */
 int pt_ctx_synchronize(pt_ctx *ctx);

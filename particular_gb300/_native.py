@@ -23,6 +23,10 @@ PT_BH_QUADRUPOLE = 0x1
 PT_BH_GROUP = 0x2
 
 
+class Timing(ctypes.Structure):
+    _fields_ = [("build_ms", ctypes.c_float), ("walk_ms", ctypes.c_float)]
+
+
 class BhStats(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_uint64), ("cells", ctypes.c_uint64),
                 ("leaves", ctypes.c_uint64), ("interactions", ctypes.c_uint64),
@@ -79,6 +83,8 @@ def _declare(L):
                                                   c_ptr]),
         "pt_bh_last_stats": (ctypes.c_int, [c_ptr, ctypes.POINTER(BhStats)]),
         "pt_bh_export_tree": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_ptr, c_size]),
+        "pt_ctx_set_timing": (ctypes.c_int, [c_ptr, ctypes.c_int]),
+        "pt_last_timing": (ctypes.c_int, [c_ptr, ctypes.POINTER(Timing)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

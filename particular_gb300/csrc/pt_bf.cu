@@ -483,8 +483,10 @@ int bf_launch_f32(pt_ctx *ctx, const float4 *aff, int n_aff, const float4 *src, 
     const int n_pad = (n_src + TILE - 1) / TILE * TILE;
     PT_TRY(ensure(ctx, BUF_SOA, sizeof(float) * 4 * size_t(n_pad)));
     float *soa = static_cast<float *>(ctx->bufs[BUF_SOA].ptr);
+    mark(ctx, 0);
     bf_to_soa<<<(n_pad + 255) / 256, 256, 0, st>>>(src, n_src, n_pad, soa);
     PT_TRY(check_launch(ctx, "bf_to_soa"));
+    mark(ctx, 1);
     dim3 grid(p.n_ib, p.slices);
     fast_kernel(p.K, guard)<<<grid, THREADS, 0, st>>>(aff, n_aff, soa, n_src, n_pad, soft2, p.slice_len, part, out);
     PT_TRY(check_launch(ctx, "bf_fast"));
@@ -492,6 +494,7 @@ int bf_launch_f32(pt_ctx *ctx, const float4 *aff, int n_aff, const float4 *src, 
         bf_fixup<<<(n_aff + 255) / 256, 256, 0, st>>>(part, n_aff, p.slices, out);
         PT_TRY(check_launch(ctx, "bf_fixup"));
     }
+    mark(ctx, 2);
     return PT_OK;
 }
 

@@ -981,6 +981,7 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
     State *Sp = state(ctx);
     if (!Sp) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
     State &S = *Sp;
+    mark(ctx, 0);
     PT_TRY(build(ctx, S, d_src, n_src));
     const bool same = (d_aff == d_src) && (n_aff == n_src);
     const float4 *tbody;
@@ -1002,16 +1003,22 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
     const float th2 = theta * theta;
     const float eps2 = softening * softening;
     const bool quad = flags & PT_BH_QUADRUPOLE;
+    mark(ctx, 1);
     if (flags & PT_BH_GROUP) {
         const int groups = (n_aff + 31) / 32;
         group_kernel(quad, eps2 == 0.0f)<<<(groups + GW_WARPS - 1) / GW_WARPS, 32 * GW_WARPS, 0, st>>>(
-            tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.sbody), as<int>(S.counters), th2, eps2, d_out, stats, err);
-        return check_launch(ctx, "bh_walk_group");
+            tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.sbody),
+            as<int>(S.counters), th2, eps2, d_out, stats, err);
+        PT_TRY(check_launch(ctx, "bh_walk_group"));
+        mark(ctx, 2);
+        return PT_OK;
     }
     walk_kernel(quad)<<<blocks(n_aff, WALK_THREADS), WALK_THREADS, 0, st>>>(
         tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.sbody),
         as<int>(S.counters), th2, eps2, d_out, stats);
-    return check_launch(ctx, "bh_walk");
+    PT_TRY(check_launch(ctx, "bh_walk"));
+    mark(ctx, 2);
+    return PT_OK;
 }
 
 static int validate(const char *fn, size_t n_aff, size_t n_src, uint32_t flags) {

@@ -46,6 +46,9 @@ struct pt_ctx {
     pt::DevBuf bufs[pt::BUF_COUNT];
     // Extra subsystems hang off the context lazily.
     void *bh = nullptr;
+    // Optional phase timing: events recorded at phase boundaries of the last call.
+    bool timing = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 };
 
 namespace pt {
@@ -59,6 +62,11 @@ void free_buf(pt_ctx *ctx, DevBuf &b);
 // Checks the launch just made; counts it.
 int check_launch(pt_ctx *ctx, const char *what);
 int check_cuda(cudaError_t e, const char *what);
+
+// Records phase boundary k (0 = start, 1 = build done, 2 = walk done) when enabled.
+inline void mark(pt_ctx *ctx, int k) {
+    if (ctx->timing) cudaEventRecord(ctx->ev[k], ctx->stream);
+}
 
 inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 

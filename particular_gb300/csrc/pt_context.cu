@@ -121,6 +121,8 @@ void pt_ctx_destroy(pt_ctx *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     pt_bh_state_free(ctx);
     for (auto &b : ctx->bufs) pt::free_buf(ctx, b);
+    for (auto &e : ctx->ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -144,6 +146,28 @@ size_t pt_ctx_device_bytes(const pt_ctx *ctx) { return ctx ? ctx->bytes_held : 0
 uint64_t pt_ctx_launch_count(const pt_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
 int pt_ctx_sm_count(const pt_ctx *ctx) { return ctx ? ctx->sm_count : 0; }
+
+int pt_ctx_set_timing(pt_ctx *ctx, int enable) {
+    pt::clear_error();
+    if (!ctx) return pt::set_error(PT_ERR_INVALID, "pt_ctx_set_timing: ctx is NULL");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    if (enable)
+        for (auto &e : ctx->ev)
+            if (!e) PT_CUDA(cudaEventCreate(&e));
+    ctx->timing = enable != 0;
+    return PT_OK;
+}
+
+int pt_last_timing(pt_ctx *ctx, pt_timing *out) {
+    pt::clear_error();
+    if (!ctx || !out) return pt::set_error(PT_ERR_INVALID, "pt_last_timing: NULL argument");
+    if (!ctx->timing) return pt::set_error(PT_ERR_INVALID, "pt_last_timing: timing is not enabled");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    PT_CUDA(cudaEventSynchronize(ctx->ev[2]));
+    PT_CUDA(cudaEventElapsedTime(&out->build_ms, ctx->ev[0], ctx->ev[1]));
+    PT_CUDA(cudaEventElapsedTime(&out->walk_ms, ctx->ev[1], ctx->ev[2]));
+    return PT_OK;
+}
 
 int pt_ctx_synchronize(pt_ctx *ctx) {
     pt::clear_error();
