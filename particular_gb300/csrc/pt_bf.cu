@@ -349,16 +349,20 @@ __global__ void __launch_bounds__(THREADS)
     }
 }
 
-// FP64 judge: f32 inputs widened, double arithmetic and accumulation.
+// FP64 judge: f32 inputs widened, double arithmetic and accumulation. grid.y splits
+// the sources into slices whose partial sums (part, [slices][3 * n_aff]) are added
+// in slice order by bf_f64_fixup; with one slice the kernel writes out directly.
 __global__ void __launch_bounds__(THREADS)
     bf_f64(const float4 *__restrict__ aff, int n_aff, const float4 *__restrict__ src, int n_src,
-           double soft2, int checked, double *__restrict__ out) {
+           double soft2, int checked, int slice_len, double *__restrict__ part, double *__restrict__ out) {
     __shared__ __align__(16) float4 tiles[STAGES][TILE];
     const int i = blockIdx.x * THREADS + threadIdx.x;
+    const int j0 = blockIdx.y * slice_len;
+    const int j_end = min(n_src, j0 + slice_len);
     const float4 pi = (i < n_aff) ? aff[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const double xi = pi.x, yi = pi.y, zi = pi.z;
     double sx = 0.0, sy = 0.0, sz = 0.0;
-    for_each_tile(tiles, src, 0, n_src, [&](const float4 *T, int cnt) {
+    for_each_tile(tiles, src, j0, j_end, [&](const float4 *T, int cnt) {
 #pragma unroll 2
         for (int jj = 0; jj < cnt; ++jj) {
             const float4 p = T[jj];
@@ -373,10 +377,19 @@ __global__ void __launch_bounds__(THREADS)
         }
     });
     if (i < n_aff) {
-        out[3 * size_t(i) + 0] = sx;
-        out[3 * size_t(i) + 1] = sy;
-        out[3 * size_t(i) + 2] = sz;
+        double *o = part ? part + size_t(blockIdx.y) * 3 * size_t(n_aff) : out;
+        o[3 * size_t(i) + 0] = sx;
+        o[3 * size_t(i) + 1] = sy;
+        o[3 * size_t(i) + 2] = sz;
     }
+}
+
+__global__ void bf_f64_fixup(const double *__restrict__ part, int n_aff, int slices, double *__restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 3 * n_aff) return;
+    double acc = 0.0;
+    for (int s = 0; s < slices; ++s) acc += part[size_t(s) * 3 * size_t(n_aff) + k];
+    out[k] = acc;
 }
 
 using FastKernel = void (*)(const float4 *, int, const float *, int, int, float, int, float4 *, float *);
@@ -506,9 +519,25 @@ int bf_launch_f64(pt_ctx *ctx, const float4 *aff, int n_aff, const float4 *src, 
         PT_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 3 * size_t(n_aff), ctx->stream));
         return PT_OK;
     }
-    dim3 grid((n_aff + THREADS - 1) / THREADS);
-    bf_f64<<<grid, THREADS, 0, ctx->stream>>>(aff, n_aff, src, n_src, softening * softening, checked, out);
-    return check_launch(ctx, "bf_f64");
+    const int n_ib = (n_aff + THREADS - 1) / THREADS;
+    const int tiles = (n_src + TILE - 1) / TILE;
+    int slices = std::max(1, std::min(tiles, (4 * ctx->sm_count + n_ib - 1) / n_ib));
+    const int slice_len = (tiles + slices - 1) / slices * TILE;
+    slices = (n_src + slice_len - 1) / slice_len;
+    double *part = nullptr;
+    if (slices > 1) {
+        PT_TRY(ensure(ctx, BUF_PART, sizeof(double) * 3 * size_t(n_aff) * size_t(slices)));
+        part = static_cast<double *>(ctx->bufs[BUF_PART].ptr);
+    }
+    dim3 grid(n_ib, slices);
+    bf_f64<<<grid, THREADS, 0, ctx->stream>>>(aff, n_aff, src, n_src, softening * softening, checked, slice_len,
+                                             part, out);
+    PT_TRY(check_launch(ctx, "bf_f64"));
+    if (part) {
+        bf_f64_fixup<<<(3 * n_aff + 255) / 256, 256, 0, ctx->stream>>>(part, n_aff, slices, out);
+        PT_TRY(check_launch(ctx, "bf_f64_fixup"));
+    }
+    return PT_OK;
 }
 
 static int validate_sizes(const char *fn, size_t n_aff, size_t n_src) {

@@ -358,9 +358,14 @@ __global__ void leaf_moments(const int *__restrict__ counters, const uint32_t *_
 // levels[0..LEVELS] = counts, levels[LEVELS+1 ..] = offsets, then cursors.
 __global__ void cell_level_count(const int *__restrict__ counters, const int *__restrict__ bdelta,
                                  const uint8_t *__restrict__ top, int *__restrict__ levels) {
+    __shared__ int h[LEVELS];
+    if (threadIdx.x < LEVELS) h[threadIdx.x] = 0;
+    __syncthreads();
     const int M = counters[0];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < M - 1 && top[k]) atomicAdd(&levels[bdelta[k] / 3], 1);
+    if (k < M - 1 && top[k]) atomicAdd(&h[bdelta[k] / 3], 1);
+    __syncthreads();
+    if (threadIdx.x < LEVELS && h[threadIdx.x]) atomicAdd(&levels[threadIdx.x], h[threadIdx.x]);
 }
 
 __global__ void cell_level_offsets(int *__restrict__ levels) {
@@ -374,12 +379,23 @@ __global__ void cell_level_offsets(int *__restrict__ levels) {
     levels[2 * LEVELS + 1] = acc;
 }
 
+// Each block reserves one range per level with a single global atomic.
 __global__ void cell_level_scatter(const int *__restrict__ counters, const int *__restrict__ bdelta,
                                    const uint8_t *__restrict__ top, int *__restrict__ levels,
                                    int *__restrict__ by_level) {
+    __shared__ int h[LEVELS], base[LEVELS];
+    if (threadIdx.x < LEVELS) h[threadIdx.x] = 0;
+    __syncthreads();
     const int M = counters[0];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < M - 1 && top[k]) by_level[atomicAdd(&levels[2 * LEVELS + 2 + bdelta[k] / 3], 1)] = k;
+    const bool cell = k < M - 1 && top[k];
+    const int L = cell ? bdelta[k] / 3 : 0;
+    const int local = cell ? atomicAdd(&h[L], 1) : 0;
+    __syncthreads();
+    if (threadIdx.x < LEVELS && h[threadIdx.x])
+        base[threadIdx.x] = atomicAdd(&levels[2 * LEVELS + 2 + threadIdx.x], h[threadIdx.x]);
+    __syncthreads();
+    if (cell) by_level[base[L] + local] = k;
 }
 
 // A child's moments: single-body leaves are read straight from nodeA (the body).
@@ -559,7 +575,7 @@ __global__ void __launch_bounds__(WALK_THREADS)
 // shared-memory interaction list. A full list is evaluated densely: every lane runs its target
 // against all entries, two entries per packed f32x2 instruction.
 constexpr int GW_WARPS = 4;
-constexpr int GW_STACK = 1024;  // sibling ranges per warp (~32 per tree level are live)
+constexpr int GW_STACK = 768;  // sibling ranges per warp (~32 per tree level are live)
 
 typedef unsigned long long f2;
 __device__ __forceinline__ f2 pk2(float lo, float hi) {
@@ -586,21 +602,23 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
     return r;
 }
 
-template <bool QUAD>
-struct GroupList {
-    static constexpr int CAP = QUAD ? 128 : 256;
-    static constexpr int NF = QUAD ? 10 : 4;  // x, y, z, m [, Qxx, Qxy, Qxz, Qyy, Qyz, Qzz]
+// Interaction lists in structure-of-arrays form. Cells carry their quadrupole
+// when QUAD; single bodies never need one.
+template <int NF, int CAP_>
+struct IList {
+    static constexpr int CAP = CAP_;
     float f[NF][CAP + 2];
 };
 
-// Evaluates entries [0, cnt) of the list for this lane's target (x, y, z).
-template <bool QUAD, bool GUARD>
-__device__ __forceinline__ void eval_list(GroupList<QUAD> &Lst, int cnt, f2 px, f2 py, f2 pz, f2 e2, f2 &ax,
-                                          f2 &ay, f2 &az) {
+// Evaluates entries [0, cnt) of a list for this lane's target (px, py, pz): NF = 4 is
+// the monopole (x, y, z, m), NF = 10 adds the traceless quadrupole of cells.
+template <int NF, int CAP, bool GUARD>
+__device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, f2 px, f2 py, f2 pz, f2 e2, f2 &ax, f2 &ay,
+                                          f2 &az) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
     if (cnt & 1) {  // pad with a massless entry far away: contributes exactly 0
-        if (lane < GroupList<QUAD>::NF) Lst.f[lane][cnt] = (lane < 3) ? 1e30f : 0.0f;
+        if (lane < NF) Lst.f[lane][cnt] = (lane < 3) ? 1e30f : 0.0f;
         __syncwarp();
         ++cnt;
     }
@@ -625,7 +643,7 @@ __device__ __forceinline__ void eval_list(GroupList<QUAD> &Lst, int cnt, f2 px, 
         ax = fma2(dx, sc, ax);
         ay = fma2(dy, sc, ay);
         az = fma2(dz, sc, az);
-        if constexpr (QUAD) {
+        if constexpr (NF == 10) {
             const f2 qxx = *reinterpret_cast<const f2 *>(&Lst.f[4][e]);
             const f2 qxy = *reinterpret_cast<const f2 *>(&Lst.f[5][e]);
             const f2 qxz = *reinterpret_cast<const f2 *>(&Lst.f[6][e]);
@@ -654,9 +672,13 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
                   const float4 *__restrict__ sbody, const int *__restrict__ counters,
                   float th2, float eps2, float *__restrict__ out, unsigned long long *__restrict__ stats,
                   int *__restrict__ err) {
+    constexpr int NFC = QUAD ? 10 : 4;
+    using CellList = IList<NFC, 96>;
+    using BodyList = IList<4, 128>;
     __shared__ int2 s_stack[GW_WARPS][GW_STACK];
     __shared__ float4 s_tgt[GW_WARPS][32];
-    __shared__ __align__(16) GroupList<QUAD> s_list[GW_WARPS];
+    __shared__ __align__(16) CellList s_cells[GW_WARPS];
+    __shared__ __align__(16) BodyList s_bodies[GW_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int group = blockIdx.x * GW_WARPS + warp;
     if (group * 32 >= n_aff) return;
@@ -666,7 +688,8 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     const unsigned lt = (1u << lane) - 1u;
     int2 *stack = s_stack[warp];
     const int T = counters[1];
-    GroupList<QUAD> &Lst = s_list[warp];
+    CellList &Lc = s_cells[warp];
+    BodyList &Lb = s_bodies[warp];
 
     // the warp's targets, read back as shared-memory broadcasts by the opening test
     s_tgt[warp][lane] = p;
@@ -694,7 +717,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     // 32 ranges per tree level.
     if (lane == 0) stack[0] = make_int2(0, T);
     __syncwarp();
-    int S = 1, L = 0, maxS = 1;
+    int S = 1, Nc = 0, Nb = 0, maxS = 1;
     unsigned long long entries = 0, visits = 0;
     bool failed = false;
     while (S > 0) {
@@ -761,35 +784,50 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
         maxS = max(maxS, S);
         const bool acc = have && !open;
         const bool bucket = acc && B.z >= 0 && B.w > 1;
-        const bool single = acc && !bucket;
-        const unsigned m1 = __ballot_sync(0xffffffffu, single);
-        const int n1 = __popc(m1);
-        if (L + n1 > GroupList<QUAD>::CAP) {
-            eval_list<QUAD, GUARD>(Lst, L, px, py, pz, e2, ax, ay, az);
-            entries += L;
-            L = 0;
+        const bool cellacc = acc && B.z < 0;
+        const bool bodyacc = acc && B.z >= 0 && B.w == 1;
+        // accepted cells -> the cell list (with their quadrupoles)
+        const unsigned mc = __ballot_sync(0xffffffffu, cellacc);
+        const int nc1 = __popc(mc);
+        if (Nc + nc1 > CellList::CAP) {
+            eval_list<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
+            entries += Nc;
+            Nc = 0;
         }
-        if (single) {
-            const int e = L + __popc(m1 & lt);
-            Lst.f[0][e] = A.x;
-            Lst.f[1][e] = A.y;
-            Lst.f[2][e] = A.z;
-            Lst.f[3][e] = A.w;
+        if (cellacc) {
+            const int e = Nc + __popc(mc & lt);
+            Lc.f[0][e] = A.x;
+            Lc.f[1][e] = A.y;
+            Lc.f[2][e] = A.z;
+            Lc.f[3][e] = A.w;
             if constexpr (QUAD) {
-                float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
-                if (B.z < 0) {
-                    q0 = __ldg(nodeQ + 2 * node);
-                    q1 = __ldg(nodeQ + 2 * node + 1);
-                }
-                Lst.f[4][e] = q0.x;
-                Lst.f[5][e] = q0.y;
-                Lst.f[6][e] = q0.z;
-                Lst.f[7][e] = q0.w;
-                Lst.f[8][e] = q1.x;
-                Lst.f[9][e] = q1.y;
+                const float4 q0 = __ldg(nodeQ + 2 * node);
+                const float4 q1 = __ldg(nodeQ + 2 * node + 1);
+                Lc.f[4][e] = q0.x;
+                Lc.f[5][e] = q0.y;
+                Lc.f[6][e] = q0.z;
+                Lc.f[7][e] = q0.w;
+                Lc.f[8][e] = q1.x;
+                Lc.f[9][e] = q1.y;
             }
         }
-        L += n1;
+        Nc += nc1;
+        // accepted single-body leaves -> the body list (monopole only)
+        const unsigned mb1 = __ballot_sync(0xffffffffu, bodyacc);
+        const int nb1 = __popc(mb1);
+        if (Nb + nb1 > BodyList::CAP) {
+            eval_list<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+            entries += Nb;
+            Nb = 0;
+        }
+        if (bodyacc) {
+            const int e = Nb + __popc(mb1 & lt);
+            Lb.f[0][e] = A.x;
+            Lb.f[1][e] = A.y;
+            Lb.f[2][e] = A.z;
+            Lb.f[3][e] = A.w;
+        }
+        Nb += nb1;
         unsigned mb = __ballot_sync(0xffffffffu, bucket);
         while (mb) {  // leaves holding several bodies: one entry per body
             const int src = __ffs(mb) - 1;
@@ -798,27 +836,26 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
             const int c = __shfl_sync(0xffffffffu, B.w, src);
             for (int base = 0; base < c; base += 32) {
                 const int n = min(32, c - base);
-                if (L + n > GroupList<QUAD>::CAP) {
-                    eval_list<QUAD, GUARD>(Lst, L, px, py, pz, e2, ax, ay, az);
-                    entries += L;
-                    L = 0;
+                if (Nb + n > BodyList::CAP) {
+                    eval_list<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+                    entries += Nb;
+                    Nb = 0;
                 }
                 if (lane < n) {
                     const float4 q = __ldg(sbody + f + base + lane);
-                    Lst.f[0][L + lane] = q.x;
-                    Lst.f[1][L + lane] = q.y;
-                    Lst.f[2][L + lane] = q.z;
-                    Lst.f[3][L + lane] = q.w;
-                    if constexpr (QUAD)
-                        for (int j = 4; j < GroupList<QUAD>::NF; ++j) Lst.f[j][L + lane] = 0.f;
+                    Lb.f[0][Nb + lane] = q.x;
+                    Lb.f[1][Nb + lane] = q.y;
+                    Lb.f[2][Nb + lane] = q.z;
+                    Lb.f[3][Nb + lane] = q.w;
                 }
-                L += n;
+                Nb += n;
             }
         }
         __syncwarp();
     }
-    eval_list<QUAD, GUARD>(Lst, L, px, py, pz, e2, ax, ay, az);
-    entries += L;
+    eval_list<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
+    eval_list<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+    entries += Nc + Nb;
     float x0, x1, y0, y1, z0, z1;
     upk2(ax, x0, x1);
     upk2(ay, y0, y1);
