@@ -178,6 +178,55 @@ int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out);
  * The tree the reference keeps in RootedOrthtree (particular/src/storage.rs:10-46). */
 int pt_bh_export_tree(pt_ctx *ctx, float *com_mass, int32_t *links, float *quad, size_t rows);
 
+/* ---- time integration ------------------------------------------------------
+ * Kick-drift-kick leapfrog on device-resident state, around either method:
+ *   v += a dt/2; x += v dt; a = accel(x); v += a dt/2      (per step)
+ * with the closing half kick of a step fused into the next step's opening kick.
+ * The reference integrates with semi-implicit Euler around its methods in its
+ * benchmark and tests (particular/benches/benchmark.rs:81,
+ * gravity/newtonian/mod.rs:318-330); this driver has no reference counterpart. */
+#define PT_METHOD_BRUTE_FORCE 0
+#define PT_METHOD_BARNES_HUT 1
+/* Host state: bodies float[4] (x, y, z, mu) and velocities float[4] (vx, vy, vz,
+ * unused) per body, updated in place after `steps` steps (synchronous). `flags` are
+ * the method's flags (PT_BF_* or PT_BH_*); theta is used by Barnes-Hut only. */
+int pt_leapfrog(pt_ctx *ctx, float *bodies, float *vel, size_t n, float dt, int steps, int method,
+                float theta, float softening, uint32_t flags);
+/* Device state (16-byte aligned bodies and velocities; acc = float[3] per body
+ * holding the accelerations of the current positions, updated to the final ones).
+ * use_graph != 0 captures the whole `steps`-step sequence into a CUDA graph on first
+ * use for this (pointers, n, steps, method, dt, theta, softening, flags, stream) and
+ * replays it afterwards; that first call also recomputes `acc` from the positions
+ * before capturing, so every buffer is sized outside the capture. */
+int pt_leapfrog_device(pt_ctx *ctx, float *d_bodies, float *d_vel, float *d_acc, size_t n, float dt,
+                       int steps, int method, float theta, float softening, uint32_t flags,
+                       int use_graph);
+
+/* ---- batched ensembles -------------------------------------------------------
+ * n_sys independent systems in one device array: system k is bodies
+ * [offsets[k], offsets[k+1]) (host array, offsets[0] == 0). Each evolves by the
+ * leapfrog above with brute-force accelerations inside the system only, for `steps`
+ * steps, all steps in ONE persistent cooperative kernel (work queue over (system,
+ * target tile) items, largest first; grid barriers between phases). With use_graph
+ * the launch is captured once per (pointers, steps, dt, softening) and replayed.
+ * Synchronous. A grid barrier that exceeds its spin limit makes the call fail with
+ * PT_ERR_TIMEOUT (the state is then partially advanced); the context stays usable.
+ * The reference evaluates one system per call; ensembles have no counterpart. */
+int pt_ensemble_run(pt_ctx *ctx, const uint32_t *offsets, uint32_t n_sys, float *d_bodies,
+                    float *d_vel, float dt, int steps, float softening, int use_graph);
+/* Autotuner: times 1, 2 and 4 targets per thread (the item's block shape) for each
+ * system-size class present (class c: 64*2^c <= n < 64*2^(c+1), c = 0..7, the ends
+ * open) and keeps the fastest per class for later runs; table_out (8 ints, may be
+ * NULL) receives the choice. */
+int pt_ensemble_tune(pt_ctx *ctx, const uint32_t *offsets, uint32_t n_sys, const float *d_bodies,
+                     float softening, int *table_out);
+/* Sets the per-class table directly (8 ints: 0 = default, else 1, 2 or 4). */
+int pt_ensemble_set_table(pt_ctx *ctx, const int *table);
+/* Barrier spin limit (iterations of ~64 ns sleeps; default 2^22). stall != 0 makes
+ * every barrier wait for one block more than the grid has: a wait nothing ends, to
+ * test the timeout path without faulting the GPU. */
+int pt_ensemble_set_barrier(pt_ctx *ctx, long long spin_limit, int stall);
+
 /* Phase timing of the last pt_bf_* / pt_bh_* call, from CUDA events recorded on
  * the context's stream when enabled: for Barnes-Hut, build = tree construction
  * and moments, walk = the traversal kernel; for the brute force, build = source

@@ -1,0 +1,309 @@
+// particular_cuda.hpp -- C++17 host mirror of particular's API over the C ABI.
+//
+// The reference is a Rust crate; this header restates, for C++ callers, the part of
+// its API the cuda compute methods plug into, with the same names and meaning:
+//
+//   Between<S1, S2>               particular/src/lib.rs:296-300
+//   Ordered<P>, Reordered<P, F>   particular/src/storage.rs:48-205
+//   GravitationalField<V, S>      particular/src/gravity/mod.rs:12-35
+//   Position / Mass               particular/src/gravity/mod.rs:40-148 (a type with a
+//                                 `position` member and a `mu` or `mass` member, plus an
+//                                 optional `static constexpr G`, as #[derive(Position,
+//                                 Mass)] requires, particular_derive/src/gravity.rs)
+//   Acceleration<CHECKED>         particular/src/gravity/newtonian/acceleration.rs:17-44
+//   AccelerationSoftened<S, C>    particular/src/gravity/newtonian/acceleration_softened.rs:17-49
+//   cuda::CudaResources           gpu::GpuResources, particular/src/gpu/mod.rs:84-143
+//   cuda::BruteForce<T>           gpu::BruteForce, particular/src/gpu/mod.rs:145-208
+//   cuda::BarnesHut<S, T>         sequential::BarnesHut, particular/src/sequential.rs:432-543
+//   cuda_brute_force(...) etc.    GpuCompute, particular/src/gpu/mod.rs:13-37
+//
+// `compute(storage)` accepts a slice (Slice<P>, std::vector<P>), an Ordered, a
+// Reordered or a Between, as the storage blanket impls (storage.rs:207-241) do, and
+// returns the affected bodies' accelerations in order. A failed call throws
+// particular::cuda::Error (the reference panics).
+#pragma once
+
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "particular_cuda.h"
+
+namespace particular {
+
+struct Vec3 {
+    float x = 0.f, y = 0.f, z = 0.f;
+    Vec3() = default;
+    Vec3(float x_, float y_, float z_) : x(x_), y(y_), z(z_) {}
+    static Vec3 splat(float v) { return {v, v, v}; }
+    Vec3 operator+(const Vec3 &o) const { return {x + o.x, y + o.y, z + o.z}; }
+    Vec3 operator-(const Vec3 &o) const { return {x - o.x, y - o.y, z - o.z}; }
+    Vec3 operator*(float s) const { return {x * s, y * s, z * s}; }
+    Vec3 &operator+=(const Vec3 &o) {
+        x += o.x;
+        y += o.y;
+        z += o.z;
+        return *this;
+    }
+    float length_squared() const { return x * x + y * y + z * z; }
+};
+
+// A view of contiguous particles (the role of `&[P]`).
+template <class P>
+struct Slice {
+    const P *ptr = nullptr;
+    size_t len = 0;
+    Slice() = default;
+    Slice(const P *p, size_t n) : ptr(p), len(n) {}
+    Slice(const std::vector<P> &v) : ptr(v.data()), len(v.size()) {}
+    const P &operator[](size_t i) const { return ptr[i]; }
+    size_t size() const { return len; }
+};
+
+template <class S1, class S2>
+struct Between {
+    S1 affected;
+    S2 affecting;
+};
+template <class S1, class S2>
+Between<S1, S2> between(S1 a, S2 b) {
+    return Between<S1, S2>{a, b};
+}
+
+template <class V, class S>
+struct GravitationalField {
+    V position;
+    S m;
+    bool is_affecting() const { return m != S(0); }
+};
+
+// ---- Position + Mass detection (the derive's contract) ---------------------
+namespace detail {
+template <class, class = void>
+struct has_mu : std::false_type {};
+template <class P>
+struct has_mu<P, std::void_t<decltype(std::declval<const P &>().mu)>> : std::true_type {};
+template <class, class = void>
+struct has_m : std::false_type {};
+template <class P>
+struct has_m<P, std::void_t<decltype(std::declval<const P &>().m)>> : std::true_type {};
+template <class, class = void>
+struct has_G : std::false_type {};
+template <class P>
+struct has_G<P, std::void_t<decltype(P::G)>> : std::true_type {};
+}  // namespace detail
+
+template <class P>
+inline Vec3 position_of(const P &p) {
+    return Vec3(float(p.position.x), float(p.position.y), float(p.position.z));
+}
+template <class P>
+inline float mu_of(const P &p) {
+    if constexpr (detail::has_mu<P>::value) {
+        return float(p.mu);
+    } else if constexpr (detail::has_m<P>::value) {
+        return float(p.m);
+    } else if constexpr (detail::has_G<P>::value) {
+        return float(P::G * p.mass);
+    } else {
+        return float(p.mass);
+    }
+}
+
+// ---- interactions ---------------------------------------------------------
+template <bool CHECKED>
+struct Acceleration {
+    static constexpr bool checked = CHECKED;
+    float softening() const { return 0.f; }
+};
+inline Acceleration<true> acceleration_checked() { return {}; }
+inline Acceleration<false> acceleration_unchecked() { return {}; }
+
+template <class S, bool CHECKED>
+struct AccelerationSoftened {
+    S softening_;
+    static constexpr bool checked = CHECKED;
+    float softening() const { return float(softening_); }
+};
+template <class S>
+AccelerationSoftened<S, true> softened_checked(S s) {
+    return {s};
+}
+
+// ---- storages ---------------------------------------------------------------
+template <class P>
+struct DefaultIsAffecting {
+    bool operator()(const P &p) const { return mu_of(p) != 0.f; }
+};
+
+template <class P>
+class Ordered {
+  public:
+    template <class F = DefaultIsAffecting<P>>
+    static Ordered create(Slice<P> unordered, F is_affecting = F()) {
+        Ordered o;
+        for (size_t i = 0; i < unordered.size(); ++i)
+            if (is_affecting(unordered[i])) o.particles_.push_back(unordered[i]);
+        o.affecting_len_ = o.particles_.size();
+        for (size_t i = 0; i < unordered.size(); ++i)
+            if (!is_affecting(unordered[i])) o.particles_.push_back(unordered[i]);
+        return o;
+    }
+    size_t affecting_len() const { return affecting_len_; }
+    Slice<P> affecting() const { return Slice<P>(particles_.data(), affecting_len_); }
+    Slice<P> non_affecting() const {
+        return Slice<P>(particles_.data() + affecting_len_, particles_.size() - affecting_len_);
+    }
+    Slice<P> particles() const { return Slice<P>(particles_); }
+
+  private:
+    std::vector<P> particles_;
+    size_t affecting_len_ = 0;
+};
+
+template <class P, class F = DefaultIsAffecting<P>>
+class Reordered {
+  public:
+    Reordered(Slice<P> unordered, F is_affecting = F())
+        : unordered(unordered), ordered_(Ordered<P>::create(unordered, is_affecting)) {}
+    Slice<P> unordered;
+    const Ordered<P> &ordered() const { return ordered_; }
+    Slice<P> affecting() const { return ordered_.affecting(); }
+    size_t affecting_len() const { return ordered_.affecting_len(); }
+
+  private:
+    Ordered<P> ordered_;
+};
+
+// storage -> Between(affected, affecting) (storage.rs:207-241)
+template <class P>
+Between<Slice<P>, Slice<P>> as_between(Slice<P> s) {
+    return {s, s};
+}
+template <class P>
+Between<Slice<P>, Slice<P>> as_between(const std::vector<P> &v) {
+    return {Slice<P>(v), Slice<P>(v)};
+}
+template <class P>
+Between<Slice<P>, Slice<P>> as_between(const Ordered<P> &o) {
+    return {o.particles(), o.affecting()};
+}
+template <class P, class F>
+Between<Slice<P>, Slice<P>> as_between(const Reordered<P, F> &r) {
+    return {r.unordered, r.affecting()};
+}
+template <class P1, class P2>
+Between<Slice<P1>, Slice<P2>> as_between(Between<Slice<P1>, Slice<P2>> b) {
+    return b;
+}
+
+namespace cuda {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+inline void check(int rc) {
+    if (rc != PT_OK) throw Error(rc, std::string("particular cuda: ") + pt_last_error());
+}
+
+// One context per device; create once and reuse (gpu/mod.rs:150-151).
+class CudaResources {
+  public:
+    explicit CudaResources(int device = 0) { check(pt_ctx_create(&ctx_, device)); }
+    ~CudaResources() { pt_ctx_destroy(ctx_); }
+    CudaResources(const CudaResources &) = delete;
+    CudaResources &operator=(const CudaResources &) = delete;
+    pt_ctx *get() const { return ctx_; }
+
+  private:
+    pt_ctx *ctx_ = nullptr;
+};
+
+namespace detail {
+template <class P>
+std::vector<float> pack_fields(Slice<P> s) {
+    std::vector<float> out(4 * s.size());
+    for (size_t i = 0; i < s.size(); ++i) {
+        const Vec3 p = position_of(s[i]);
+        out[4 * i] = p.x;
+        out[4 * i + 1] = p.y;
+        out[4 * i + 2] = p.z;
+        out[4 * i + 3] = mu_of(s[i]);
+    }
+    return out;
+}
+inline std::vector<Vec3> unpack(const std::vector<float> &o) {
+    std::vector<Vec3> r(o.size() / 3);
+    for (size_t i = 0; i < r.size(); ++i) r[i] = Vec3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
+    return r;
+}
+}  // namespace detail
+
+template <class T>
+struct BruteForce {
+    CudaResources &resources;
+    T interaction;
+    bool exact = false;  // bit-identical to sequential::BruteForce
+
+    template <class Storage>
+    std::vector<Vec3> compute(const Storage &storage) {
+        auto b = as_between(storage);
+        const auto aff = detail::pack_fields(b.affected);
+        const bool same = static_cast<const void *>(b.affected.ptr) ==
+                              static_cast<const void *>(b.affecting.ptr) &&
+                          b.affected.size() == b.affecting.size();
+        const auto src = same ? std::vector<float>() : detail::pack_fields(b.affecting);
+        std::vector<float> out(3 * b.affected.size());
+        if (out.empty()) return {};
+        check(pt_bf_accel_f32(resources.get(), aff.data(), b.affected.size(),
+                              same ? aff.data() : src.data(), b.affecting.size(),
+                              interaction.softening(), T::checked ? 1 : 0, exact ? PT_BF_EXACT : 0u,
+                              out.data()));
+        return detail::unpack(out);
+    }
+};
+
+template <class S, class T>
+struct BarnesHut {
+    S theta;
+    CudaResources &resources;
+    T interaction;
+    uint32_t flags = 0;  // PT_BH_QUADRUPOLE | PT_BH_GROUP
+
+    template <class Storage>
+    std::vector<Vec3> compute(const Storage &storage) {
+        auto b = as_between(storage);
+        const auto aff = detail::pack_fields(b.affected);
+        const bool same = static_cast<const void *>(b.affected.ptr) ==
+                              static_cast<const void *>(b.affecting.ptr) &&
+                          b.affected.size() == b.affecting.size();
+        const auto src = same ? std::vector<float>() : detail::pack_fields(b.affecting);
+        std::vector<float> out(3 * b.affected.size());
+        if (out.empty()) return {};
+        check(pt_bh_accel_f32(resources.get(), aff.data(), b.affected.size(),
+                              same ? aff.data() : src.data(), b.affecting.size(), float(theta),
+                              interaction.softening(), flags, out.data()));
+        return detail::unpack(out);
+    }
+};
+
+// GpuCompute-style sugar: storage.cuda_brute_force(resources, interaction).
+template <class Storage, class T>
+std::vector<Vec3> cuda_brute_force(const Storage &storage, CudaResources &res, T interaction) {
+    return BruteForce<T>{res, interaction}.compute(storage);
+}
+template <class Storage, class S, class T>
+std::vector<Vec3> cuda_barnes_hut(const Storage &storage, S theta, CudaResources &res, T interaction,
+                                  uint32_t flags = 0) {
+    return BarnesHut<S, T>{theta, res, interaction, flags}.compute(storage);
+}
+
+}  // namespace cuda
+}  // namespace particular

@@ -21,6 +21,8 @@ PT_ERR_DEPTH = -6
 PT_BF_EXACT = 0x1
 PT_BH_QUADRUPOLE = 0x1
 PT_BH_GROUP = 0x2
+PT_METHOD_BRUTE_FORCE = 0
+PT_METHOD_BARNES_HUT = 1
 
 
 class Timing(ctypes.Structure):
@@ -84,6 +86,19 @@ def _declare(L):
         "pt_bh_last_stats": (ctypes.c_int, [c_ptr, ctypes.POINTER(BhStats)]),
         "pt_bh_export_tree": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_ptr, c_size]),
         "pt_ctx_set_timing": (ctypes.c_int, [c_ptr, ctypes.c_int]),
+        "pt_ensemble_run": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_uint32, c_ptr, c_ptr,
+                                           ctypes.c_float, ctypes.c_int, ctypes.c_float,
+                                           ctypes.c_int]),
+        "pt_ensemble_tune": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_uint32, c_ptr, ctypes.c_float,
+                                            c_ptr]),
+        "pt_ensemble_set_table": (ctypes.c_int, [c_ptr, c_ptr]),
+        "pt_ensemble_set_barrier": (ctypes.c_int, [c_ptr, ctypes.c_longlong, ctypes.c_int]),
+        "pt_leapfrog": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_size, ctypes.c_float, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                       ctypes.c_uint32]),
+        "pt_leapfrog_device": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_ptr, c_size, ctypes.c_float,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                              ctypes.c_float, ctypes.c_uint32, ctypes.c_int]),
         "pt_last_timing": (ctypes.c_int, [c_ptr, ctypes.POINTER(Timing)]),
     }
     for name, (res, args) in sig.items():

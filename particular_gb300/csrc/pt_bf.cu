@@ -21,6 +21,7 @@
 //               contraction: bit-identical to sequential::BruteForce.
 //  * bf_f64   : the same formula in double, the error judge.
 #include "pt_common.cuh"
+#include "pt_f32x2.cuh"
 
 #include <algorithm>
 #include <climits>
@@ -77,85 +78,6 @@ __device__ __forceinline__ void for_each_tile(float4 (*tiles)[TILE], const float
     cp_async_wait<0>();
 }
 
-// Knuth two-sum: s + c tracks the running sum with the rounding error of each add.
-__device__ __forceinline__ void two_sum_acc(float &s, float &c, float t) {
-    const float sn = s + t;
-    const float bp = sn - s;
-    const float err = (s - (sn - bp)) + (t - bp);
-    s = sn;
-    c += err;
-}
-
-// ---- packed FP32 (sm_100+ f32x2): one instruction, two lanes of work ------
-// Halves the issue slots the FMA pipe needs, so the pipe, not instruction issue,
-// bounds the inner loop. lo/hi hold two different sources for the same target.
-typedef unsigned long long f2;
-__device__ __forceinline__ f2 pk(float lo, float hi) {
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void upk(f2 v, float &lo, float &hi) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
-    f2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
-    f2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
-    f2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-// One MUFU.RSQ, no denormal fix-up (n_s >= eps^2 is a normal number whenever eps > 0).
-__device__ __forceinline__ float rsqrt_ftz(float x) {
-    float r;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
-// Two pairs (target i; sources j, j+1) in packed arithmetic: 12 f32x2 FMA-pipe
-// instructions + 2 MUFU. GUARD zeroes the contribution of n == 0 (checked, eps == 0).
-template <bool GUARD>
-__device__ __forceinline__ void interact2(f2 xj, f2 yj, f2 zj, f2 mj, f2 xi, f2 yi, f2 zi, f2 &ax, f2 &ay,
-                                          f2 &az, f2 e2) {
-    const f2 dx = sub2(xj, xi);
-    const f2 dy = sub2(yj, yi);
-    const f2 dz = sub2(zj, zi);
-    const f2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-    float r0, r1;
-    upk(r2, r0, r1);
-    float i0 = rsqrt_ftz(r0), i1 = rsqrt_ftz(r1);
-    if (GUARD) {
-        i0 = (r0 > 0.0f) ? i0 : 0.0f;
-        i1 = (r1 > 0.0f) ? i1 : 0.0f;
-    }
-    const f2 inv = pk(i0, i1);
-    const f2 s = mul2(mul2(mj, inv), mul2(inv, inv));
-    ax = fma2(dx, s, ax);
-    ay = fma2(dy, s, ay);
-    az = fma2(dz, s, az);
-}
-
-template <bool GUARD>
-__device__ __forceinline__ void interact1(float xj, float yj, float zj, float mj, float xi, float yi, float zi,
-                                          float &ax, float &ay, float &az, float eps2) {
-    const float dx = xj - xi, dy = yj - yi, dz = zj - zi;
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-    float inv = rsqrt_ftz(r2);
-    if (GUARD) inv = (r2 > 0.0f) ? inv : 0.0f;
-    const float s = (mj * inv) * (inv * inv);
-    ax = fmaf(dx, s, ax);
-    ay = fmaf(dy, s, ay);
-    az = fmaf(dz, s, az);
-}
-
 // Sources in structure-of-arrays form (x[], y[], z[], mu[], each padded to a
 // multiple of TILE) so that one LDS.128 yields two packed source pairs.
 struct SoaTile {
@@ -187,8 +109,8 @@ __global__ void __launch_bounds__(THREADS)
 
     float xi[K], yi[K], zi[K], sx[K], sy[K], sz[K], cx[K], cy[K], cz[K];
     f2 xi2[K], yi2[K], zi2[K], ax[K], ay[K], az[K];
-    const f2 e2 = pk(eps2, eps2);
-    const f2 zero2 = pk(0.f, 0.f);
+    const f2 e2 = pk2(eps2, eps2);
+    const f2 zero2 = pk2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const int i = i0 + k * THREADS + threadIdx.x;
@@ -196,9 +118,9 @@ __global__ void __launch_bounds__(THREADS)
         xi[k] = p.x;
         yi[k] = p.y;
         zi[k] = p.z;
-        xi2[k] = pk(p.x, p.x);
-        yi2[k] = pk(p.y, p.y);
-        zi2[k] = pk(p.z, p.z);
+        xi2[k] = pk2(p.x, p.x);
+        yi2[k] = pk2(p.y, p.y);
+        zi2[k] = pk2(p.z, p.z);
         ax[k] = ay[k] = az[k] = zero2;
         sx[k] = sy[k] = sz[k] = 0.f;
         cx[k] = cy[k] = cz[k] = 0.f;
@@ -225,10 +147,10 @@ __global__ void __launch_bounds__(THREADS)
 #pragma unroll 2
             for (int q = 0; q < TILE / 4; ++q) {
                 const float4 x = X[q], y = Y[q], z = Z[q], m = M[q];
-                const f2 xa = pk(x.x, x.y), xb = pk(x.z, x.w);
-                const f2 ya = pk(y.x, y.y), yb = pk(y.z, y.w);
-                const f2 za = pk(z.x, z.y), zb = pk(z.z, z.w);
-                const f2 ma = pk(m.x, m.y), mb = pk(m.z, m.w);
+                const f2 xa = pk2(x.x, x.y), xb = pk2(x.z, x.w);
+                const f2 ya = pk2(y.x, y.y), yb = pk2(y.z, y.w);
+                const f2 za = pk2(z.x, z.y), zb = pk2(z.z, z.w);
+                const f2 ma = pk2(m.x, m.y), mb = pk2(m.z, m.w);
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
                     interact2<GUARD>(xa, ya, za, ma, xi2[k], yi2[k], zi2[k], ax[k], ay[k], az[k], e2);
@@ -238,11 +160,11 @@ __global__ void __launch_bounds__(THREADS)
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 float l, h;
-                upk(ax[k], l, h);
+                upk2(ax[k], l, h);
                 two_sum_acc(sx[k], cx[k], l + h);
-                upk(ay[k], l, h);
+                upk2(ay[k], l, h);
                 two_sum_acc(sy[k], cy[k], l + h);
-                upk(az[k], l, h);
+                upk2(az[k], l, h);
                 two_sum_acc(sz[k], cz[k], l + h);
                 ax[k] = ay[k] = az[k] = zero2;
             }

@@ -31,6 +31,7 @@
 // same visit count); PT_BH_QUADRUPOLE adds the quadrupole term to accepted cells.
 #include "pt_common.cuh"
 #include "pt_prims.cuh"
+#include "pt_f32x2.cuh"
 
 #include <algorithm>
 #include <climits>
@@ -461,11 +462,6 @@ __global__ void cell_moments_level(int L, const int *__restrict__ levels, const 
 }
 
 // ---- walk ------------------------------------------------------------------
-__device__ __forceinline__ float rsqrt_ftz(float x) {
-    float r;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
 
 template <bool QUAD>
 __global__ void __launch_bounds__(WALK_THREADS)
@@ -576,31 +572,6 @@ __global__ void __launch_bounds__(WALK_THREADS)
 // against all entries, two entries per packed f32x2 instruction.
 constexpr int GW_WARPS = 4;
 constexpr int GW_STACK = 768;  // sibling ranges per warp (~32 per tree level are live)
-
-typedef unsigned long long f2;
-__device__ __forceinline__ f2 pk2(float lo, float hi) {
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void upk2(f2 v, float &lo, float &hi) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
-    f2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
-    f2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
-    f2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
 
 // Interaction lists in structure-of-arrays form. Cells carry their quadrupole
 // when QUAD; single bodies never need one.

@@ -29,6 +29,9 @@ enum BufSlot : int {
     BUF_PART,      // split-j partial sums
     BUF_OUT64,     // f64 outputs
     BUF_SOA,       // sources as padded x[], y[], z[], mu[] arrays
+    BUF_LF_BODY,   // leapfrog state for the host entry point
+    BUF_LF_VEL,
+    BUF_LF_ACC,
     BUF_COUNT
 };
 
@@ -46,6 +49,10 @@ struct pt_ctx {
     pt::DevBuf bufs[pt::BUF_COUNT];
     // Extra subsystems hang off the context lazily.
     void *bh = nullptr;
+    void *lf = nullptr;
+    void *ens = nullptr;
+    // True while a CUDA graph is being captured on `stream`: buffers must not grow.
+    bool capturing = false;
     // Optional phase timing: events recorded at phase boundaries of the last call.
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};

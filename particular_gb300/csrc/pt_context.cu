@@ -38,6 +38,8 @@ int check_launch(pt_ctx *ctx, const char *what) {
 
 int ensure_buf(pt_ctx *ctx, DevBuf &b, size_t bytes) {
     if (bytes <= b.cap) return PT_OK;
+    if (ctx->capturing)
+        return set_error(PT_ERR_INVALID, "a buffer would grow during CUDA graph capture (%zu bytes)", bytes);
     // Grow by 1/8 extra so slowly growing sizes do not reallocate every call.
     size_t want = bytes + bytes / 8;
     want = (want + 255) & ~size_t(255);
@@ -82,8 +84,10 @@ int ensure(pt_ctx *ctx, int slot, size_t bytes) { return ensure_buf(ctx, ctx->bu
 
 }  // namespace pt
 
-// Defined by the Barnes-Hut translation unit.
+// Defined by the Barnes-Hut, leapfrog and ensemble translation units.
 void pt_bh_state_free(pt_ctx *ctx);
+void pt_lf_state_free(pt_ctx *ctx);
+void pt_ens_state_free(pt_ctx *ctx);
 
 extern "C" {
 
@@ -119,6 +123,8 @@ void pt_ctx_destroy(pt_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    pt_lf_state_free(ctx);
+    pt_ens_state_free(ctx);
     pt_bh_state_free(ctx);
     for (auto &b : ctx->bufs) pt::free_buf(ctx, b);
     for (auto &e : ctx->ev)

@@ -166,3 +166,33 @@ class BarnesHut:
 def cuda_barnes_hut(storage, theta, resources, interaction, **kw):
     """`storage.cuda_barnes_hut(theta, resources, interaction)` (CudaCompute sugar)."""
     return BarnesHut(theta, resources, interaction, **kw).compute(storage)
+
+
+class Leapfrog:
+    """Kick-drift-kick leapfrog around a cuda method (the driver the reference's tests
+    and benchmark write by hand around their methods; particular/benches/benchmark.rs:81).
+
+    `method` is a BruteForce or BarnesHut instance; `run` advances host state in place.
+    """
+
+    def __init__(self, method, dt):
+        self.method = method
+        self.dt = float(np.float32(dt))
+
+    def _args(self):
+        m = self.method
+        if isinstance(m, BarnesHut):
+            return N.PT_METHOD_BARNES_HUT, m.theta, m.interaction.softening, m.flags
+        return (N.PT_METHOD_BRUTE_FORCE, 0.0, m.interaction.softening,
+                N.PT_BF_EXACT if m.exact else 0)
+
+    def run(self, bodies, vel, steps):
+        """bodies: (n, 4) float32 (x, y, z, mu); vel: (n, 3) or (n, 4) float32.
+        Returns the advanced (bodies, vel) as new arrays."""
+        b = np.ascontiguousarray(bodies, np.float32).copy()
+        v4 = np.zeros((b.shape[0], 4), np.float32)
+        v4[:, :3] = np.asarray(vel, np.float32)[:, :3]
+        method, theta, soft, flags = self._args()
+        N.check(N.lib().pt_leapfrog(self.method.resources.handle, _ptr(b), _ptr(v4), b.shape[0],
+                                    self.dt, int(steps), method, theta, soft, flags))
+        return b, v4[:, :3].copy()

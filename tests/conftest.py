@@ -34,3 +34,13 @@ def res(native_lib):
     r = CudaResources(0)
     yield r
     r.close()
+
+
+def load_cpp_build():
+    """tests/cpp/build.py, loaded by path (it builds the C++ KAT program)."""
+    import importlib.util
+    path = os.path.join(ROOT, "tests", "cpp", "build.py")
+    spec = importlib.util.spec_from_file_location("pt_cpp_kat_build", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod

@@ -1,0 +1,106 @@
+// The reference's known-answer tests, on the cuda methods, through the C++ host
+// mirror (include/particular_cuda.hpp):
+//   acceleration_error!  particular/src/gravity/newtonian/mod.rs:228-277
+//   circular_orbit!      particular/src/gravity/newtonian/mod.rs:281-347
+// run like tests_algorithms_gpu! (mod.rs:474-521): 100 orbits, tolerances 1e-2
+// (Barnes-Hut theta 0.5: 5e-1 and 1e-1, mod.rs:415-420).
+// Exit status 0 when every case passes; one line per case on stdout.
+#include <cmath>
+#include <cstdio>
+#include <functional>
+#include <vector>
+
+#include "particular_cuda.hpp"
+
+using namespace particular;
+
+struct Body {  // what #[derive(Position, Mass)] would accept
+    Vec3 position;
+    float mu;
+};
+
+using Compute = std::function<std::vector<Vec3>(const Reordered<Body> &)>;
+using ComputeSlice = std::function<std::vector<Vec3>(const std::vector<Body> &)>;
+
+static bool acceleration_error(const Compute &compute, float epsilon, const char *name) {
+    const std::vector<Body> massive = {{Vec3::splat(0.f), 20.f}, {Vec3::splat(1.f), 30.f}, {Vec3::splat(-3.f), 40.f}};
+    const std::vector<Body> particles = {{Vec3::splat(10.f), 0.f}, massive[0], massive[1], massive[2],
+                                         {Vec3::splat(30.f), 0.f}, {Vec3::splat(-45.f), 0.f}};
+    Reordered<Body> reordered{Slice<Body>(particles)};
+    const auto computed = compute(reordered);
+    bool ok = computed.size() == particles.size();
+    float worst = 0.f;
+    for (size_t k = 0; ok && k < particles.size(); ++k) {
+        Vec3 acc;
+        for (const auto &m2 : massive) {
+            const Vec3 dir = m2.position - particles[k].position;
+            const float mag2 = dir.length_squared();
+            if (mag2 != 0.f) acc += dir * m2.mu * std::sqrt(1.f / mag2) * (1.f / mag2);
+        }
+        const Vec3 c = computed[k];
+        const float ex = 1.f - c.x / acc.x, ey = 1.f - c.y / acc.y, ez = 1.f - c.z / acc.z;
+        const float err = std::sqrt(ex * ex + ey * ey + ez * ez);
+        worst = std::fmax(worst, err);
+        ok = ok && err <= epsilon;
+    }
+    std::printf("%-40s acceleration_error max %.3e (<= %.1e) %s\n", name, worst, epsilon, ok ? "ok" : "FAIL");
+    return ok;
+}
+
+static bool circular_orbit(const ComputeSlice &compute, int orbit_count, float epsilon, const char *name) {
+    const float DT = 1.0f / 60.0f;
+    std::vector<Body> particles = {{Vec3(0.f, 0.f, 0.f), 1e6f}, {Vec3(100.f, 0.f, 0.f), 0.f}};
+    std::vector<Vec3> velocities = {Vec3(), Vec3(0.f, 100.f, 0.f)};
+    auto dist = [&] { return std::sqrt((particles[0].position - particles[1].position).length_squared()); };
+    auto energy = [&](float r) { return -(particles[0].mu + particles[1].mu) / (r + r); };
+    const float d0 = dist(), e0 = energy(d0);
+    const float period = 6.2831853f * std::sqrt((d0 * d0 * d0) / particles[0].mu);
+    const int steps = int(std::lround(period / DT));
+    for (int s = 0; s < steps * orbit_count; ++s) {
+        const auto acc = compute(particles);
+        for (size_t i = 0; i < particles.size(); ++i) velocities[i] += acc[i] * DT;
+        for (size_t i = 0; i < particles.size(); ++i) particles[i].position += velocities[i] * DT;
+    }
+    const float d1 = dist(), e1 = energy(d1);
+    const float ed = std::fabs(1.f - d0 / d1), ee = std::fabs(1.f - e0 / e1);
+    const bool ok = ed < epsilon && ee < epsilon;
+    std::printf("%-40s circular_orbit distance %.3e energy %.3e (< %.1e) %s\n", name, ed, ee, epsilon,
+                ok ? "ok" : "FAIL");
+    return ok;
+}
+
+int main() {
+    cuda::CudaResources res(0);
+    bool ok = true;
+    for (bool exact : {false, true}) {
+        cuda::BruteForce<Acceleration<true>> bf{res, acceleration_checked(), exact};
+        const char *name = exact ? "cuda::BruteForce (exact)" : "cuda::BruteForce";
+        ok &= acceleration_error([&](const Reordered<Body> &r) { return bf.compute(r); }, 1e-2f, name);
+        ok &= circular_orbit([&](const std::vector<Body> &p) { return bf.compute(p); }, 100, 1e-2f, name);
+    }
+    struct Case {
+        float theta;
+        uint32_t flags;
+        float err, orbit;
+        const char *name;
+    };
+    const Case cases[] = {{0.f, 0, 1e-2f, 1e-2f, "cuda::BarnesHut(0.0)"},
+                          {0.5f, 0, 5e-1f, 1e-1f, "cuda::BarnesHut(0.5)"},
+                          {0.5f, PT_BH_GROUP | PT_BH_QUADRUPOLE, 5e-1f, 1e-1f, "cuda::BarnesHut(0.5, quad+group)"}};
+    for (const auto &c : cases) {
+        cuda::BarnesHut<float, Acceleration<true>> bh{c.theta, res, acceleration_checked(), c.flags};
+        ok &= acceleration_error([&](const Reordered<Body> &r) { return bh.compute(r); }, c.err, c.name);
+        ok &= circular_orbit([&](const std::vector<Body> &p) { return bh.compute(p); }, 100, c.orbit, c.name);
+    }
+    // the sugar and the Between storage
+    std::vector<Body> few = {{Vec3(0, 0, 0), 1.f}, {Vec3(1, 0, 0), 2.f}, {Vec3(0, 2, 0), 3.f}};
+    const auto a1 = cuda::cuda_brute_force(few, res, softened_checked(0.01f));
+    const auto a2 = cuda::BruteForce<AccelerationSoftened<float, true>>{res, softened_checked(0.01f)}.compute(
+        between(Slice<Body>(few), Slice<Body>(few)));
+    bool same = a1.size() == 3;
+    for (size_t i = 0; same && i < 3; ++i) same = a1[i].x == a2[i].x && a1[i].y == a2[i].y && a1[i].z == a2[i].z;
+    std::printf("%-40s %s\n", "cuda_brute_force == BruteForce(Between)", same ? "ok" : "FAIL");
+    ok &= same;
+    std::printf("%s\n", ok ? "ALL OK" : "SOME FAILED");
+    return ok ? 0 : 1;
+}

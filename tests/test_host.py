@@ -117,3 +117,10 @@ def test_plummer_is_in_virial_equilibrium():
     b, v = d["bodies"].astype(np.float64), d["vel"].astype(np.float64)
     K = 0.5 * (b[:, 3] * (v ** 2).sum(1)).sum()
     assert abs(K - 3 * np.pi / 64) / (3 * np.pi / 64) < 0.05
+
+
+def test_cpp_host_mirror_compiles(native_lib):
+    """The C++ mirror of the reference API and its KAT program build (no GPU needed)."""
+    import os
+    from conftest import load_cpp_build
+    assert os.path.exists(load_cpp_build().build())
