@@ -149,6 +149,10 @@ int pt_bf_accel_f32_noalloc(const float *d_affected, size_t n_aff, const float *
                                  for all of them when the per-body rule opens it for any
                                  (so never less accurate than that rule); accepted nodes
                                  are evaluated from shared-memory lists */
+#define PT_BH_LEARNED 0x4u    /* with PT_BH_GROUP: add the learned far-field correction
+                                 (pt_mlp_*) of every cell accepted at theta that the
+                                 model's inner angle would have opened, evaluated once
+                                 per warp at the warp's centre */
 
 typedef struct pt_bh_stats {
     uint64_t nodes;        /* cells + leaves of the last tree */
@@ -161,6 +165,7 @@ typedef struct pt_bh_stats {
     uint64_t overflow;     /* nonzero if a PT_BH_GROUP walk ran out of stack (its
                               bodies are NaN; the host entry point then fails with
                               PT_ERR_CAPACITY) */
+    uint64_t learned;      /* learned corrections evaluated (per warp and cell) */
 } pt_bh_stats;
 
 /* cuda::BarnesHut over host buffers (synchronous). Layouts as pt_bf_accel_f32. */
@@ -226,6 +231,34 @@ int pt_ensemble_set_table(pt_ctx *ctx, const int *table);
  * every barrier wait for one block more than the grid has: a wait nothing ends, to
  * test the timeout path without faulting the GPU. */
 int pt_ensemble_set_barrier(pt_ctx *ctx, long long spin_limit, int stall);
+
+/* ---- learned far-field correction ------------------------------------------
+ * A 12 -> 64 -> 64 -> 3 MLP (GELU, BF16 weights, FP32 accumulation) predicting the
+ * residual between a Barnes-Hut cell's exact field and its monopole + quadrupole, for
+ * cells accepted at theta that theta_inner would have opened. Trained on the GPU by
+ * this library's kernels from residuals the brute-force pair kernel computes; the
+ * reference has no learned part. Parameters: PT_MLP_NPARAM floats (BF16 values). */
+#define PT_MLP_NPARAM 5188
+/* Random initialisation (seeded). */
+int pt_mlp_init(pt_ctx *ctx, uint64_t seed);
+/* Loads / reads parameters (host arrays of PT_MLP_NPARAM floats). */
+int pt_mlp_set_params(pt_ctx *ctx, const float *params, size_t n, float theta_inner);
+int pt_mlp_get_params(pt_ctx *ctx, float *params, size_t n);
+/* Builds the tree of one snapshot (device bodies) and appends the samples of
+ * n_targets evenly spaced bodies to the dataset (capacity samples at most, kept on
+ * the device); *total receives the dataset size. */
+int pt_mlp_generate(pt_ctx *ctx, const float *d_bodies, size_t n, int n_targets, float theta_outer,
+                    float theta_inner, float softening, size_t capacity, size_t *total);
+int pt_mlp_reset_dataset(pt_ctx *ctx);
+int pt_mlp_export_dataset(pt_ctx *ctx, float *features, float *targets, size_t n);
+/* Adam training for `steps` steps of `batch` random samples; loss_out = mean loss
+ * over the last 10% of steps (targets scaled by their RMS). */
+int pt_mlp_train(pt_ctx *ctx, int steps, int batch, float lr, uint64_t seed, float *loss_out);
+/* Loss and gradient (PT_MLP_NPARAM floats) for host samples: the training kernel's check. */
+int pt_mlp_loss_grad(pt_ctx *ctx, const float *features, const float *targets, int batch, float *grad,
+                     double *loss_out);
+/* Predictions (n x 3) for host features (n x 12). */
+int pt_mlp_predict(pt_ctx *ctx, const float *features, int n, float *out);
 
 /* Phase timing of the last pt_bf_* / pt_bh_* call, from CUDA events recorded on
  * the context's stream when enabled: for Barnes-Hut, build = tree construction

@@ -21,6 +21,8 @@ PT_ERR_DEPTH = -6
 PT_BF_EXACT = 0x1
 PT_BH_QUADRUPOLE = 0x1
 PT_BH_GROUP = 0x2
+PT_BH_LEARNED = 0x4
+PT_MLP_NPARAM = 5188
 PT_METHOD_BRUTE_FORCE = 0
 PT_METHOD_BARNES_HUT = 1
 
@@ -33,7 +35,8 @@ class BhStats(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_uint64), ("cells", ctypes.c_uint64),
                 ("leaves", ctypes.c_uint64), ("interactions", ctypes.c_uint64),
                 ("visits", ctypes.c_uint64), ("warps", ctypes.c_uint64),
-                ("max_stack", ctypes.c_uint64), ("overflow", ctypes.c_uint64)]
+                ("max_stack", ctypes.c_uint64), ("overflow", ctypes.c_uint64),
+                ("learned", ctypes.c_uint64)]
 
 _NAMES = {PT_ERR_INVALID: "PT_ERR_INVALID", PT_ERR_CUDA: "PT_ERR_CUDA", PT_ERR_OOM: "PT_ERR_OOM",
           PT_ERR_CAPACITY: "PT_ERR_CAPACITY", PT_ERR_TIMEOUT: "PT_ERR_TIMEOUT",
@@ -86,6 +89,19 @@ def _declare(L):
         "pt_bh_last_stats": (ctypes.c_int, [c_ptr, ctypes.POINTER(BhStats)]),
         "pt_bh_export_tree": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_ptr, c_size]),
         "pt_ctx_set_timing": (ctypes.c_int, [c_ptr, ctypes.c_int]),
+        "pt_mlp_init": (ctypes.c_int, [c_ptr, ctypes.c_uint64]),
+        "pt_mlp_set_params": (ctypes.c_int, [c_ptr, c_ptr, c_size, ctypes.c_float]),
+        "pt_mlp_get_params": (ctypes.c_int, [c_ptr, c_ptr, c_size]),
+        "pt_mlp_generate": (ctypes.c_int, [c_ptr, c_ptr, c_size, ctypes.c_int, ctypes.c_float,
+                                           ctypes.c_float, ctypes.c_float, c_size,
+                                           ctypes.POINTER(c_size)]),
+        "pt_mlp_reset_dataset": (ctypes.c_int, [c_ptr]),
+        "pt_mlp_export_dataset": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_size]),
+        "pt_mlp_train": (ctypes.c_int, [c_ptr, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                        ctypes.c_uint64, ctypes.POINTER(ctypes.c_float)]),
+        "pt_mlp_loss_grad": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, ctypes.c_int, c_ptr,
+                                            ctypes.POINTER(ctypes.c_double)]),
+        "pt_mlp_predict": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_int, c_ptr]),
         "pt_ensemble_run": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_uint32, c_ptr, c_ptr,
                                            ctypes.c_float, ctypes.c_int, ctypes.c_float,
                                            ctypes.c_int]),

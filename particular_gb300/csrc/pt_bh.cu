@@ -32,6 +32,7 @@
 #include "pt_common.cuh"
 #include "pt_prims.cuh"
 #include "pt_f32x2.cuh"
+#include "pt_mlp.cuh"
 
 #include <algorithm>
 #include <climits>
@@ -57,11 +58,13 @@ struct State {
     DevBuf flags, uscan, ukey, ufirst;
     DevBuf bfirst, blast, bdelta, bparent, lparent, top, oparent, loparent;
     DevBuf cnt, pscan, pre, levels, by_level;
-    DevBuf nodeA, nodeB, nodeQ, mom;
+    DevBuf nodeA, nodeB, nodeQ, nodeG, nodeR, mom;
     DevBuf tkeys, tidx, tbody;
     DevBuf counters;
     DevBuf out;
     DevBuf aff_h, src_h;  // staging for the host-pointer entry point
+    const float *mlp = nullptr;  // learned-correction parameters (owned by the MLP state)
+    float theta_inner = 0.5f;
     int cap_n = 0;
     int last_n_src = 0;
 };
@@ -256,7 +259,8 @@ __global__ void layout(int *counters, const int *__restrict__ bfirst,
                        const uint8_t *__restrict__ top, const int *__restrict__ oparent,
                        const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ pscan,
                        const uint64_t *__restrict__ ukey, const uint32_t *__restrict__ ufirst,
-                       const float *__restrict__ box, int *__restrict__ pre, int4 *__restrict__ nodeB) {
+                       const float *__restrict__ box, int *__restrict__ pre, int4 *__restrict__ nodeB,
+                       float4 *__restrict__ nodeG, int2 *__restrict__ nodeR) {
     const int M = counters[0];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0) {
@@ -271,22 +275,32 @@ __global__ void layout(int *counters, const int *__restrict__ bfirst,
         pre[k] = pk;
         const int after = blast[k] + 1;
         const int skip = after + int(pscan[after]);
-        // Cell width at level L along the key's x path: BoundingBox::width() of the
-        // reference cell (partition.rs:322-327), replayed in the same f32 ops.
+        // Cell box at level L along the key's path: BoundingBox::width() of the
+        // reference cell (partition.rs:322-327) and its centre, replayed in the same
+        // f32 ops.
         const int L = bdelta[k] / 3;
         const uint64_t key = ukey[b];
-        float mn = box[0], mx = box[3];
+        float mn0 = box[0], mn1 = box[1], mn2 = box[2], mx0 = box[3], mx1 = box[4], mx2 = box[5];
         for (int l = 0; l < L; ++l) {
             const int o = 7 - int((key >> (3 * (LEVELS - 1 - l))) & 7u);
-            const float c = __fmul_rn(__fadd_rn(mn, mx), 0.5f);
-            if (o & 1) mx = c; else mn = c;
+            const float c0 = __fmul_rn(__fadd_rn(mn0, mx0), 0.5f);
+            const float c1 = __fmul_rn(__fadd_rn(mn1, mx1), 0.5f);
+            const float c2 = __fmul_rn(__fadd_rn(mn2, mx2), 0.5f);
+            if (o & 1) mx0 = c0; else mn0 = c0;
+            if (o & 2) mx1 = c1; else mn1 = c1;
+            if (o & 4) mx2 = c2; else mn2 = c2;
         }
-        nodeB[pk] = make_int4(__float_as_int(__fsub_rn(mx, mn)), skip, -1, 0);
+        const float w = __fsub_rn(mx0, mn0);
+        nodeB[pk] = make_int4(__float_as_int(w), skip, -1, 0);
+        nodeG[pk] = make_float4(0.5f * (mn0 + mx0), 0.5f * (mn1 + mx1), 0.5f * (mn2 + mx2), w);
+        nodeR[pk] = make_int2(int(ufirst[b]), int(ufirst[blast[k] + 1]));
     }
     if (k < M) {
         const int pk = k + int(pscan[k]) + int(cnt[k]);
         const int f = int(ufirst[k]);
         nodeB[pk] = make_int4(0, pk + 1, f, int(ufirst[k + 1]) - f);
+        nodeG[pk] = make_float4(0.f, 0.f, 0.f, 0.f);
+        nodeR[pk] = make_int2(f, int(ufirst[k + 1]));
     }
 }
 
@@ -636,13 +650,62 @@ __device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, f2 px, f
     __syncwarp();
 }
 
-template <bool QUAD, bool GUARD>
+// Parameters read as warp-uniform loads (every lane reads the same weight at the
+// same time: one broadcast per instruction).
+struct UniformParams {
+    const float *__restrict__ p;
+    __device__ __forceinline__ float operator[](int i) const { return __ldg(p + i); }
+};
+
+// Learned correction of up to 32 marginal cells (one per lane) at the group centre:
+// returns the sum over the cells of the predicted residual accelerations.
+// Cells whose size/distance ratio at the group centre lies outside the range the
+// model was trained on ([theta_inner, theta]) get no correction.
+__device__ __forceinline__ void eval_learned(const float *__restrict__ M, int cnt, float gx, float gy, float gz,
+                                             const float *__restrict__ params, float lo, float hi, float &cx,
+                                             float &cy, float &cz) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    float rx = 0.f, ry = 0.f, rz = 0.f;
+    float f[mlp::IN];
+    float r2 = 0.f;
+    bool use = false;
+    float4 com;
+    if (lane < cnt) {
+        const float *e = M + lane * 14;
+        com = make_float4(e[0], e[1], e[2], e[3]);
+        const float q[6] = {e[4], e[5], e[6], e[7], e[8], e[9]};
+        const float4 g = make_float4(e[10], e[11], e[12], e[13]);
+        r2 = mlp::features(gx, gy, gz, com, q, g, f);
+        use = f[3] >= lo && f[3] <= hi;
+    }
+    if (use) {
+        float o[mlp::OUT];
+        mlp::forward<true>(UniformParams{params}, f, o);
+        const float a = com.w / r2;  // M / |r|^2
+        rx = o[0] * a;
+        ry = o[1] * a;
+        rz = o[2] * a;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        rx += __shfl_xor_sync(0xffffffffu, rx, off);
+        ry += __shfl_xor_sync(0xffffffffu, ry, off);
+        rz += __shfl_xor_sync(0xffffffffu, rz, off);
+    }
+    cx += rx;
+    cy += ry;
+    cz += rz;
+    __syncwarp();
+}
+
+template <bool QUAD, bool GUARD, bool LEARNED>
 __global__ void __launch_bounds__(32 * GW_WARPS)
     bh_walk_group(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
                   const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
-                  const float4 *__restrict__ sbody, const int *__restrict__ counters,
-                  float th2, float eps2, float *__restrict__ out, unsigned long long *__restrict__ stats,
-                  int *__restrict__ err) {
+                  const float4 *__restrict__ nodeG, const float4 *__restrict__ sbody, const int *__restrict__ counters,
+                  float th2, float th_in2, const float *__restrict__ mlp_params, float eps2, float *__restrict__ out,
+                  unsigned long long *__restrict__ stats, int *__restrict__ err) {
     constexpr int NFC = QUAD ? 10 : 4;
     using CellList = IList<NFC, 96>;
     using BodyList = IList<4, 128>;
@@ -650,6 +713,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     __shared__ float4 s_tgt[GW_WARPS][32];
     __shared__ __align__(16) CellList s_cells[GW_WARPS];
     __shared__ __align__(16) BodyList s_bodies[GW_WARPS];
+    __shared__ float s_learn[GW_WARPS][LEARNED ? 32 * 14 : 1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int group = blockIdx.x * GW_WARPS + warp;
     if (group * 32 >= n_aff) return;
@@ -678,6 +742,24 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
         mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
         mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
     }
+    // the group centre, where learned corrections are evaluated
+    float gcx = valid ? p.x : 0.f, gcy = valid ? p.y : 0.f, gcz = valid ? p.z : 0.f;
+    if (LEARNED) {
+        const float nv = float(min(32, n_aff - group * 32));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            gcx += __shfl_xor_sync(0xffffffffu, gcx, o);
+            gcy += __shfl_xor_sync(0xffffffffu, gcy, o);
+            gcz += __shfl_xor_sync(0xffffffffu, gcz, o);
+        }
+        gcx /= nv;
+        gcy /= nv;
+        gcz /= nv;
+    }
+    float lx = 0.f, ly = 0.f, lz = 0.f;  // learned corrections (same in every lane)
+    const float th_in = sqrtf(th_in2), th_out = sqrtf(th2);
+    int Nm = 0;
+    unsigned long long learned = 0;
 
     const f2 px = pk2(p.x, p.x), py = pk2(p.y, p.y), pz = pk2(p.z, p.z), e2 = pk2(eps2, eps2);
     f2 ax = pk2(0.f, 0.f), ay = ax, az = ax;
@@ -717,8 +799,9 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
             const float e0 = fmaxf(fmaxf(mn0 - A.x, A.x - mx0), 0.f);
             const float e1 = fmaxf(fmaxf(mn1 - A.y, A.y - mx1), 0.f);
             const float e2b = fmaxf(fmaxf(mn2 - A.z, A.z - mx2), 0.f);
-            maybe = th2 * fmaf(e0, e0, fmaf(e1, e1, e2b * e2b)) < w * w;
+            maybe = (LEARNED ? th_in2 : th2) * fmaf(e0, e0, fmaf(e1, e1, e2b * e2b)) < w * w;
         }
+        bool marginal = false;
         if (__any_sync(0xffffffffu, maybe)) {
             float dmin = INFINITY;
 #pragma unroll 8
@@ -730,6 +813,26 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
             }
             const float w = __int_as_float(B.x);
             open = maybe && th2 * dmin < w * w;
+            // accepted by every target, but opened by one at theta_inner
+            if (LEARNED) marginal = maybe && !open && th_in2 * dmin < w * w && A.w > 0.0f;
+        }
+        if (LEARNED) {
+            const unsigned mm = __ballot_sync(0xffffffffu, marginal);
+            const int nm = __popc(mm);
+            if (Nm + nm > 32) {
+                eval_learned(s_learn[warp], Nm, gcx, gcy, gcz, mlp_params, th_in, th_out, lx, ly, lz);
+                learned += Nm;
+                Nm = 0;
+            }
+            if (marginal) {
+                float *e = s_learn[warp] + (Nm + __popc(mm & lt)) * 14;
+                const float4 q0 = __ldg(nodeQ + 2 * node), q1 = __ldg(nodeQ + 2 * node + 1);
+                const float4 g = __ldg(nodeG + node);
+                e[0] = A.x; e[1] = A.y; e[2] = A.z; e[3] = A.w;
+                e[4] = q0.x; e[5] = q0.y; e[6] = q0.z; e[7] = q0.w; e[8] = q1.x; e[9] = q1.y;
+                e[10] = g.x; e[11] = g.y; e[12] = g.z; e[13] = g.w;
+            }
+            Nm += nm;
         }
         const bool rest = have && B.y < range.y;  // later siblings remain
         const int np = int(rest) + int(open);
@@ -827,6 +930,10 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     eval_list<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
     eval_list<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
     entries += Nc + Nb;
+    if (LEARNED && Nm > 0) {
+        eval_learned(s_learn[warp], Nm, gcx, gcy, gcz, mlp_params, th_in, th_out, lx, ly, lz);
+        learned += Nm;
+    }
     float x0, x1, y0, y1, z0, z1;
     upk2(ax, x0, x1);
     upk2(ay, y0, y1);
@@ -837,14 +944,15 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     }
     if (valid) {
         const uint32_t o = tidx[t];
-        out[3 * size_t(o) + 0] = x0 + x1;
-        out[3 * size_t(o) + 1] = y0 + y1;
-        out[3 * size_t(o) + 2] = z0 + z1;
+        out[3 * size_t(o) + 0] = (x0 + x1) + lx;
+        out[3 * size_t(o) + 1] = (y0 + y1) + ly;
+        out[3 * size_t(o) + 2] = (z0 + z1) + lz;
     }
     if (stats && lane == 0) {
         const unsigned long long nvalid = unsigned(min(32, n_aff - group * 32));
         atomicAdd(stats + 0, entries * nvalid);
         atomicAdd(stats + 1, visits * nvalid);
+        if (LEARNED) atomicAdd(stats + 4, learned);
         atomicAdd(stats + 2, 1ull);
         atomicMax(stats + 3, (unsigned long long)maxS);
     }
@@ -853,14 +961,18 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
 using WalkKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
                             const float4 *, const int *, float, float, float *, unsigned long long *);
 using GroupKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
-                             const float4 *, const int *, float, float, float *,
-                             unsigned long long *, int *);
+                             const float4 *, const float4 *, const int *, float, float, const float *, float,
+                             float *, unsigned long long *, int *);
 
 static WalkKernel walk_kernel(bool quad) { return quad ? bh_walk<true> : bh_walk<false>; }
 
-static GroupKernel group_kernel(bool quad, bool guard) {
-    if (quad) return guard ? bh_walk_group<true, true> : bh_walk_group<true, false>;
-    return guard ? bh_walk_group<false, true> : bh_walk_group<false, false>;
+static GroupKernel group_kernel(bool quad, bool guard, bool learned) {
+    if (learned) {
+        if (quad) return guard ? bh_walk_group<true, true, true> : bh_walk_group<true, false, true>;
+        return guard ? bh_walk_group<false, true, true> : bh_walk_group<false, false, true>;
+    }
+    if (quad) return guard ? bh_walk_group<true, true, false> : bh_walk_group<true, false, false>;
+    return guard ? bh_walk_group<false, true, false> : bh_walk_group<false, false, false>;
 }
 
 static State *state(pt_ctx *ctx) {
@@ -904,6 +1016,8 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
     PT_TRY(ensure_buf(ctx, S.nodeA, sizeof(float4) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.nodeB, sizeof(int4) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.nodeQ, sizeof(float4) * 4 * N));
+    PT_TRY(ensure_buf(ctx, S.nodeG, sizeof(float4) * 2 * N));
+    PT_TRY(ensure_buf(ctx, S.nodeR, sizeof(int2) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.mom, sizeof(Moments) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.counters, sizeof(unsigned long long) * 8));
 
@@ -939,7 +1053,8 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
     layout<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.blast), as<int>(S.bdelta),
                                      as<uint8_t>(S.top), as<int>(S.oparent), as<uint32_t>(S.cnt),
                                      as<uint32_t>(S.pscan), as<uint64_t>(S.ukey), as<uint32_t>(S.ufirst),
-                                     as<float>(S.box), as<int>(S.pre), as<int4>(S.nodeB));
+                                     as<float>(S.box), as<int>(S.pre), as<int4>(S.nodeB), as<float4>(S.nodeG),
+                                     as<int2>(S.nodeR));
     PT_TRY(check_launch(ctx, "layout"));
 
     int *levels = as<int>(S.levels);
@@ -1006,7 +1121,7 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
     // visits, warps, max group stack}
     unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 2;
     int *err = as<int>(S.counters) + 3;
-    PT_CUDA(cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), st));
+    PT_CUDA(cudaMemsetAsync(stats, 0, 5 * sizeof(unsigned long long), st));
     PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     const float th2 = theta * theta;
     const float eps2 = softening * softening;
@@ -1014,9 +1129,12 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
     mark(ctx, 1);
     if (flags & PT_BH_GROUP) {
         const int groups = (n_aff + 31) / 32;
-        group_kernel(quad, eps2 == 0.0f)<<<(groups + GW_WARPS - 1) / GW_WARPS, 32 * GW_WARPS, 0, st>>>(
-            tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.sbody),
-            as<int>(S.counters), th2, eps2, d_out, stats, err);
+        const bool learned = flags & PT_BH_LEARNED;
+        if (learned && !S.mlp) return set_error(PT_ERR_INVALID, "PT_BH_LEARNED needs a model (pt_mlp_*)");
+        group_kernel(quad, eps2 == 0.0f, learned)<<<(groups + GW_WARPS - 1) / GW_WARPS, 32 * GW_WARPS, 0, st>>>(
+            tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.nodeG),
+            as<float4>(S.sbody), as<int>(S.counters), th2, S.theta_inner * S.theta_inner, S.mlp, eps2, d_out, stats,
+            err);
         PT_TRY(check_launch(ctx, "bh_walk_group"));
         mark(ctx, 2);
         return PT_OK;
@@ -1033,12 +1151,46 @@ static int validate(const char *fn, size_t n_aff, size_t n_src, uint32_t flags) 
     const size_t lim = size_t(INT_MAX) / 8;
     if (n_aff > lim || n_src > lim)
         return set_error(PT_ERR_INVALID, "%s: n_aff=%zu n_src=%zu exceed the limit %zu", fn, n_aff, n_src, lim);
-    if (flags & ~(PT_BH_QUADRUPOLE | PT_BH_GROUP))
+    if (flags & ~(PT_BH_QUADRUPOLE | PT_BH_GROUP | PT_BH_LEARNED))
         return set_error(PT_ERR_INVALID, "%s: unknown flags 0x%x", fn, flags);
+    if ((flags & PT_BH_LEARNED) && !(flags & PT_BH_GROUP))
+        return set_error(PT_ERR_INVALID, "%s: PT_BH_LEARNED requires PT_BH_GROUP", fn);
     return PT_OK;
 }
 
 }  // namespace bh
+}  // namespace pt
+
+namespace pt {
+
+int bh_build_only(pt_ctx *ctx, const float4 *d_src, int n) {
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    return bh::build(ctx, *S, d_src, n);
+}
+
+int bh_tree_view(pt_ctx *ctx, TreeView *out) {
+    auto *S = static_cast<bh::State *>(ctx->bh);
+    if (!S || !S->nodeA.ptr) return set_error(PT_ERR_INVALID, "no Barnes-Hut tree built yet");
+    out->nodeA = static_cast<const float4 *>(S->nodeA.ptr);
+    out->nodeB = static_cast<const int4 *>(S->nodeB.ptr);
+    out->nodeQ = static_cast<const float4 *>(S->nodeQ.ptr);
+    out->nodeG = static_cast<const float4 *>(S->nodeG.ptr);
+    out->nodeR = static_cast<const int2 *>(S->nodeR.ptr);
+    out->sbody = static_cast<const float4 *>(S->sbody.ptr);
+    out->counters = static_cast<const int *>(S->counters.ptr);
+    out->n_src = S->last_n_src;
+    return PT_OK;
+}
+
+int bh_set_mlp(pt_ctx *ctx, const float *d_params, float theta_inner) {
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    S->mlp = d_params;
+    S->theta_inner = theta_inner;
+    return PT_OK;
+}
+
 }  // namespace pt
 
 void pt_bh_state_free(pt_ctx *ctx) {
@@ -1049,7 +1201,7 @@ void pt_bh_state_free(pt_ctx *ctx) {
     DevBuf *all[] = {&S->box_part, &S->box,    &S->keys,   &S->idx,    &S->sbody,   &S->flags,  &S->uscan,
                      &S->ukey,     &S->ufirst, &S->bfirst, &S->blast,  &S->bdelta,  &S->bparent, &S->lparent,
                      &S->top,      &S->oparent, &S->loparent, &S->cnt, &S->pscan,   &S->pre,    &S->levels,
-                     &S->by_level,   &S->nodeA,  &S->nodeB,  &S->nodeQ,  &S->mom,     &S->tkeys,  &S->tidx,
+                     &S->by_level,   &S->nodeA,  &S->nodeB,  &S->nodeQ,  &S->nodeG, &S->nodeR, &S->mom,     &S->tkeys,  &S->tidx,
                      &S->tbody,    &S->counters, &S->out,  &S->aff_h,  &S->src_h};
     for (DevBuf *b : all) free_buf(ctx, *b);
     delete S;
@@ -1126,6 +1278,7 @@ int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out) {
     out->visits = h[3];
     out->warps = h[4];
     out->max_stack = h[5];
+    out->learned = h[6];
     return PT_OK;
 }
 

@@ -51,6 +51,7 @@ struct pt_ctx {
     void *bh = nullptr;
     void *lf = nullptr;
     void *ens = nullptr;
+    void *mlp = nullptr;
     // True while a CUDA graph is being captured on `stream`: buffers must not grow.
     bool capturing = false;
     // Optional phase timing: events recorded at phase boundaries of the last call.

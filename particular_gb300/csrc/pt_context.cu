@@ -88,6 +88,7 @@ int ensure(pt_ctx *ctx, int slot, size_t bytes) { return ensure_buf(ctx, ctx->bu
 void pt_bh_state_free(pt_ctx *ctx);
 void pt_lf_state_free(pt_ctx *ctx);
 void pt_ens_state_free(pt_ctx *ctx);
+void pt_mlp_state_free(pt_ctx *ctx);
 
 extern "C" {
 
@@ -126,6 +127,7 @@ void pt_ctx_destroy(pt_ctx *ctx) {
     pt_lf_state_free(ctx);
     pt_ens_state_free(ctx);
     pt_bh_state_free(ctx);
+    pt_mlp_state_free(ctx);
     for (auto &b : ctx->bufs) pt::free_buf(ctx, b);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);

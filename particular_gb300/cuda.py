@@ -123,16 +123,19 @@ class BarnesHut:
     only ever reduce the error relative to the reference's monopole walk.
     """
 
-    def __init__(self, theta, resources, interaction, quadrupole=False, group=False):
+    def __init__(self, theta, resources, interaction, quadrupole=False, group=False,
+                 learned=False):
         self.theta = float(np.float32(theta))
         self.resources = resources
         self.interaction = interaction
         self.quadrupole = bool(quadrupole)
         self.group = bool(group)
+        self.learned = bool(learned)  # needs a model (particular_gb300.learned) and group
 
     @property
     def flags(self):
-        return (N.PT_BH_QUADRUPOLE if self.quadrupole else 0) | (N.PT_BH_GROUP if self.group else 0)
+        return ((N.PT_BH_QUADRUPOLE if self.quadrupole else 0) | (N.PT_BH_GROUP if self.group else 0)
+                | (N.PT_BH_LEARNED if self.learned else 0))
 
     def compute(self, storage):
         b = as_between(storage)

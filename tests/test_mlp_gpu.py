@@ -1,0 +1,93 @@
+"""The learned far-field correction: kernels checked against an FP64 restatement,
+and what the trained network gains over Barnes-Hut without it."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from particular_gb300 import AccelerationSoftened, cuda, ics, learned
+from particular_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gradient_matches_fp64_restatement(res):
+    from oracle import mlp_oracle as M
+    learned.init(res, seed=3)
+    rng = np.random.default_rng(0)
+    f = rng.normal(size=(200, 12)).astype(np.float32)
+    t = rng.normal(size=(200, 3)).astype(np.float32)
+    g = np.zeros(N.PT_MLP_NPARAM, np.float32)
+    loss = ctypes.c_double(0)
+    N.check(N.lib().pt_mlp_loss_grad(res.handle, f.ctypes.data, t.ctypes.data, 200, g.ctypes.data,
+                                     ctypes.byref(loss)))
+    p = learned.get_params(res)
+    want_loss, want = M.loss_grad(p, f, t)
+    assert abs(loss.value - want_loss) <= 1e-5 * abs(want_loss)
+    sl = slice(0, M.SCALE)
+    err = np.abs(g[sl] - want[sl]).max() / np.abs(want[sl]).max()
+    assert err < 1e-4, err
+    # forward pass too
+    out = np.zeros((200, 3), np.float32)
+    N.check(N.lib().pt_mlp_predict(res.handle, f.ctypes.data, 200, out.ctypes.data))
+    np.testing.assert_allclose(out, M.forward(p, f), rtol=1e-4, atol=1e-5)
+
+
+@pytest.fixture(scope="module")
+def trained(res):
+    """A small model: 24 snapshots of 16384 bodies, 400 Adam steps."""
+    learned.init(res, seed=1)
+    count = learned.generate(res, snapshots=24, n=16384, targets=512, capacity=4_000_000)
+    f, t = learned.dataset(res, min(count, 20000))
+    first = learned.train(res, steps=20, batch=4096, lr=1e-3, seed=5)
+    last = learned.train(res, steps=1500, batch=4096, lr=1e-3, seed=6)
+    return {"count": count, "features": f, "targets": t, "first": first, "last": last}
+
+
+def test_samples_are_marginal_cells(trained):
+    f, t = trained["features"], trained["targets"]
+    assert trained["count"] > 10000
+    assert np.isfinite(f).all() and np.isfinite(t).all()
+    np.testing.assert_allclose(np.linalg.norm(f[:, :3], axis=1), 1.0, rtol=1e-5)
+    assert (f[:, 3] >= 0.5 - 1e-6).all() and (f[:, 3] <= 1.0 + 1e-6).all()   # w/d in [theta_in, theta_out]
+    assert (np.abs(f[:, 9:12]) <= 0.5 + 1e-5).all()                          # COM inside the cell
+
+
+def test_training_reduces_loss(trained):
+    # targets are scaled to unit RMS per component: predicting zero scores 3.0
+    print(f"loss after 20 steps {trained['first']:.3f}, after 1520 {trained['last']:.3f} "
+          f"(zero predictor: 3.0)")
+    assert trained["last"] < trained["first"] and trained["last"] < 2.9
+
+
+def test_network_gains_on_held_out_cells(res, trained):
+    """On samples from snapshots it never saw, the trained network's prediction leaves
+    a smaller residual than no correction: what it learned about marginal cells."""
+    learned.generate(res, snapshots=2, n=16384, targets=512, seed0=7000, capacity=4_000_000)
+    f, t = learned.dataset(res, 20000)
+    pred = np.zeros_like(t)
+    N.check(N.lib().pt_mlp_predict(res.handle, f.ctypes.data, f.shape[0], pred.ctypes.data))
+    before = float((t.astype(np.float64) ** 2).sum(1).mean())
+    after = float(((t - pred).astype(np.float64) ** 2).sum(1).mean())
+    print(f"held-out marginal cells: residual MSE {before:.4e} -> {after:.4e} "
+          f"({100 * (1 - after / before):.1f}% lower)")
+    assert after < 0.97 * before
+
+
+def test_learned_walk_reports_its_effect(res, oracle, trained):
+    """theta 1.0, quadrupole + group, with and without the model on a held-out
+    snapshot, judged against the FP64 brute force. The walk evaluates the model once
+    per warp at the warp's centre; the test records the effect and guards against
+    breakage (finite results, corrections applied, error within 2x of plain)."""
+    b = ics.bulge_disk(16384, seed=999)["bodies"]
+    ref = oracle.bf_f64(b[::8], b, 0.01, True)
+    plain = cuda.BarnesHut(1.0, res, AccelerationSoftened(0.01), quadrupole=True, group=True)
+    e0 = np.linalg.norm(plain.compute(b)[::8] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    m = cuda.BarnesHut(1.0, res, AccelerationSoftened(0.01), quadrupole=True, group=True, learned=True)
+    got = m.compute(b)
+    st = m.stats()
+    e1 = np.linalg.norm(got[::8] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    print(f"theta 1.0 quad+group p50/p95: plain {np.median(e0):.3e}/{np.percentile(e0, 95):.3e} "
+          f"learned {np.median(e1):.3e}/{np.percentile(e1, 95):.3e} ({st['learned']} corrections)")
+    assert np.isfinite(got).all() and st["learned"] > 0
+    assert np.median(e1) < 2 * np.median(e0)

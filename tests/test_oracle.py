@@ -150,3 +150,22 @@ def test_empty_inputs(oracle):
     assert not oracle.bf_f32(b, np.zeros((0, 4), np.float32)).any()
     assert oracle.bh_f32(np.zeros((0, 4), np.float32), b, 0.5).shape == (0, 3)
     assert not oracle.bh_f32(b, np.zeros((0, 4), np.float32), 0.5).any()
+
+
+def test_mlp_oracle_gradient_by_finite_differences():
+    """The FP64 restatement of the learned-correction MLP (the GPU kernels' checker):
+    its hand-written gradient agrees with central differences."""
+    from oracle import mlp_oracle as M
+    rng = np.random.default_rng(1)
+    p = rng.normal(scale=0.3, size=M.NPARAM)
+    p[M.SCALE] = 1.7
+    f = rng.normal(size=(16, 12))
+    t = rng.normal(size=(16, 3))
+    _, g = M.loss_grad(p, f, t)
+    for k in rng.choice(M.SCALE, 40, replace=False):
+        h = 1e-6
+        pp, pm = p.copy(), p.copy()
+        pp[k] += h
+        pm[k] -= h
+        fd = (M.loss_grad(pp, f, t)[0] - M.loss_grad(pm, f, t)[0]) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 + 1e-5 * abs(fd), k
