@@ -261,9 +261,23 @@ class BarnesHutWorkload:
             ms = e0.elapsed_time(e1) / 3
             e = rel_err(self.d_out[idx_t].cpu().numpy(), self.ref64)
             return {"theta": theta, "quadrupole": bool(flags & 1), "group": bool(flags & 2),
-                    "ms": ms, "bodies_per_s": self.n / (ms * 1e-3), **err_stats(e)}
+                    "learned": bool(flags & 4), "ms": ms, "bodies_per_s": self.n / (ms * 1e-3),
+                    **err_stats(e)}
 
         self.plain = measure(0.5, 0)
+        # the learned correction at theta 1.0 (model trained by `python -m
+        # particular_gb300.learned`, shipped in particular_gb300/data)
+        self.learned_row = None
+        model = os.path.join(ROOT, "particular_gb300", "data", "mlp_bulge_disk.npz")
+        if os.path.exists(model):
+            from particular_gb300 import learned as LM
+            meta = LM.load(res, model)
+            row = measure(1.0, 7)
+            row["learned"] = True
+            row["model_samples"] = int(meta["samples"])
+            row["model_loss_vs_zero_predictor"] = [float(meta["loss_last"]), 3.0]
+            self.learned_row = row
+            self.plain_theta1 = measure(1.0, 3)
         ok = []
         for theta, flags in self.ladder:
             row = measure(theta, flags)
@@ -331,7 +345,9 @@ class BarnesHutWorkload:
         return {"method": {"name": "cuda::BarnesHut", "theta": self.theta,
                            "quadrupole": bool(self.flags & 1), "group": bool(self.flags & 2)},
                 "selected": self.selected, "meets_bar": self.meets_bar,
-                "calibration": self.table, "plain_reference_rule": self.plain}
+                "calibration": self.table, "plain_reference_rule": self.plain,
+                "learned_theta1": self.learned_row,
+                "plain_theta1": getattr(self, "plain_theta1", None)}
 
     # ---- CPU arm: the reference's parallel::BarnesHut restated (sequential tree
     # build, walk over all host threads), monopole per-body rule.

@@ -51,6 +51,12 @@ extern "C" {
  * ascending order, IEEE sqrt and divide, no contraction. Slower; it is the
  * drop-in for callers that need the reference's exact f32 result. */
 #define PT_BF_EXACT 0x1u
+/* With PT_BF_EXACT: glam Vec3A / Vec4's operand order, a = (d * mu) / (n_s sqrt(n_s))
+ * per component (particular/src/gravity/impls/glam.rs:260-275), for callers whose
+ * particles use those types. Other 3D f32 vectors (glam Vec3, nalgebra Vector3,
+ * ultraviolet Vec3) share the default order; 2D bodies pass z = 0, which gives their
+ * 2D results bit for bit (the squared norm adds an exact +0). */
+#define PT_BF_VEC3A 0x2u
 
 /* Opaque context: device, stream and grow-only device buffers. It plays the role
  * of gpu::GpuResources (particular/src/gpu/mod.rs:84-143): create it once and

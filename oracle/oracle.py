@@ -27,6 +27,8 @@ def lib():
         L = ctypes.CDLL(path)
         L.oracle_bf_f32.argtypes = [_f32p, ctypes.c_size_t, _f32p, ctypes.c_size_t,
                                     ctypes.c_float, ctypes.c_int, _f32p, ctypes.c_int]
+        L.oracle_bf_f32_vec3a.argtypes = [_f32p, ctypes.c_size_t, _f32p, ctypes.c_size_t,
+                                          ctypes.c_float, ctypes.c_int, _f32p, ctypes.c_int]
         L.oracle_bf_f64.argtypes = [_f32p, ctypes.c_size_t, _f32p, ctypes.c_size_t,
                                     ctypes.c_double, ctypes.c_int, _f64p, ctypes.c_int]
         L.oracle_bh_build.argtypes = [_f32p, ctypes.c_size_t, ctypes.c_int]
@@ -73,6 +75,17 @@ def bf_f32(targets, sources, softening=0.0, checked=True, threads=0):
     rc = lib().oracle_bf_f32(t, t.shape[0], s, s.shape[0], softening, int(checked), out, threads)
     if rc:
         raise RuntimeError(f"oracle_bf_f32 failed: {rc}")
+    return out
+
+
+def bf_f32_vec3a(targets, sources, softening=0.0, checked=True, threads=0):
+    """sequential::BruteForce with glam Vec3A/Vec4's operand order (d * m / ...)."""
+    t, s = _targets(targets), _sources(sources)
+    out = np.zeros((t.shape[0], 3), np.float32)
+    rc = lib().oracle_bf_f32_vec3a(t, t.shape[0], s, s.shape[0], softening, int(checked), out,
+                                   threads)
+    if rc:
+        raise RuntimeError(f"oracle_bf_f32_vec3a failed: {rc}")
     return out
 
 

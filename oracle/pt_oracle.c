@@ -115,6 +115,50 @@ int oracle_bf_f32(const float *aff, size_t n_aff, const float *src, size_t n_src
     return OR_OK;
 }
 
+/* The glam Vec3A / Vec4 local kernel (particular/src/gravity/impls/glam.rs:260-275):
+ * same as pair_f32 but a = (d * m) / (n_s * sqrt(n_s)) per component. */
+static inline void pair_f32_vec3a(float xi, float yi, float zi, const float *p2, float softening,
+                                  int checked, float *ax, float *ay, float *az) {
+    float dx = p2[0] - xi;
+    float dy = p2[1] - yi;
+    float dz = p2[2] - zi;
+    float norm = dx * dx + dy * dy + dz * dz;
+    if (checked && norm == 0.0f) {
+        *ax = dx;
+        *ay = dy;
+        *az = dz;
+        return;
+    }
+    float norm_s = norm + softening * softening;
+    float den = norm_s * sqrtf(norm_s);
+    *ax = (dx * p2[3]) / den;
+    *ay = (dy * p2[3]) / den;
+    *az = (dz * p2[3]) / den;
+}
+
+int oracle_bf_f32_vec3a(const float *aff, size_t n_aff, const float *src, size_t n_src,
+                        float softening, int checked, float *out, int threads) {
+    if ((n_aff && (!aff || !out)) || (n_src && !src)) return OR_ERR_INVALID;
+    set_threads(threads);
+    long long n = (long long)n_aff;
+#pragma omp parallel for schedule(dynamic, 16) if (threads != 1)
+    for (long long i = 0; i < n; ++i) {
+        float xi = aff[4 * i + 0], yi = aff[4 * i + 1], zi = aff[4 * i + 2];
+        float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+        for (size_t j = 0; j < n_src; ++j) {
+            float ax, ay, az;
+            pair_f32_vec3a(xi, yi, zi, src + 4 * j, softening, checked, &ax, &ay, &az);
+            sx = sx + ax;
+            sy = sy + ay;
+            sz = sz + az;
+        }
+        out[3 * i + 0] = sx;
+        out[3 * i + 1] = sy;
+        out[3 * i + 2] = sz;
+    }
+    return OR_OK;
+}
+
 /* FP64 judge: the same formula in double, inputs widened from f32. */
 int oracle_bf_f64(const float *aff, size_t n_aff, const float *src, size_t n_src,
                   double softening, int checked, double *out, int threads) {

@@ -19,6 +19,7 @@ PT_ERR_TIMEOUT = -5
 PT_ERR_DEPTH = -6
 
 PT_BF_EXACT = 0x1
+PT_BF_VEC3A = 0x2
 PT_BH_QUADRUPOLE = 0x1
 PT_BH_GROUP = 0x2
 PT_BH_LEARNED = 0x4

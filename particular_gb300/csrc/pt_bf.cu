@@ -232,6 +232,9 @@ __global__ void bf_fixup(const float4 *__restrict__ part, int n_aff, int slices,
 
 // Bit-identical restatement of sequential::BruteForce (sequential.rs:189-193 over
 // gravity/impls/mod.rs:156-165): every operation is an explicitly rounded IEEE op.
+// VEC3A: glam Vec3A / Vec4's own kernel, a = (d * m) / (n_s sqrt(n_s)) per component
+// (particular/src/gravity/impls/glam.rs:260-275), instead of d * (m / ...).
+template <bool VEC3A>
 __global__ void __launch_bounds__(THREADS)
     bf_exact(const float4 *__restrict__ aff, int n_aff, const float4 *__restrict__ src, int n_src,
              float soft2, int checked, float *__restrict__ out) {
@@ -254,10 +257,17 @@ __global__ void __launch_bounds__(THREADS)
                 az = dz;
             } else {
                 const float ns = __fadd_rn(n, soft2);
-                const float s = __fdiv_rn(p.w, __fmul_rn(ns, __fsqrt_rn(ns)));
-                ax = __fmul_rn(dx, s);
-                ay = __fmul_rn(dy, s);
-                az = __fmul_rn(dz, s);
+                const float den = __fmul_rn(ns, __fsqrt_rn(ns));
+                if (VEC3A) {
+                    ax = __fdiv_rn(__fmul_rn(dx, p.w), den);
+                    ay = __fdiv_rn(__fmul_rn(dy, p.w), den);
+                    az = __fdiv_rn(__fmul_rn(dz, p.w), den);
+                } else {
+                    const float s = __fdiv_rn(p.w, den);
+                    ax = __fmul_rn(dx, s);
+                    ay = __fmul_rn(dy, s);
+                    az = __fmul_rn(dz, s);
+                }
             }
             sx = __fadd_rn(sx, ax);
             sy = __fadd_rn(sy, ay);
@@ -405,7 +415,8 @@ int bf_launch_f32(pt_ctx *ctx, const float4 *aff, int n_aff, const float4 *src, 
     const float soft2 = softening * softening;
     if (flags & PT_BF_EXACT) {
         dim3 grid((n_aff + THREADS - 1) / THREADS);
-        bf_exact<<<grid, THREADS, 0, st>>>(aff, n_aff, src, n_src, soft2, checked, out);
+        if (flags & PT_BF_VEC3A) bf_exact<true><<<grid, THREADS, 0, st>>>(aff, n_aff, src, n_src, soft2, checked, out);
+        else bf_exact<false><<<grid, THREADS, 0, st>>>(aff, n_aff, src, n_src, soft2, checked, out);
         return check_launch(ctx, "bf_exact");
     }
     const bool guard = checked && soft2 == 0.0f;
@@ -488,7 +499,7 @@ int pt_bf_accel_f32_device(pt_ctx *ctx, const float *d_aff, size_t n_aff, const 
                            float softening, int checked, uint32_t flags, float *d_out) {
     pt::clear_error();
     if (!ctx) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f32_device: ctx is NULL");
-    if (flags & ~PT_BF_EXACT) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f32_device: unknown flags 0x%x", flags);
+    if (flags & ~(PT_BF_EXACT | PT_BF_VEC3A)) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f32_device: unknown flags 0x%x", flags);
     PT_TRY(pt::validate_sizes("pt_bf_accel_f32_device", n_aff, n_src));
     if (n_aff && (!d_aff || !d_out)) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f32_device: NULL buffer");
     if (n_src && !d_src) return pt::set_error(PT_ERR_INVALID, "pt_bf_accel_f32_device: NULL affecting buffer");
@@ -518,7 +529,7 @@ int pt_bf_accel_f32(pt_ctx *ctx, const float *aff, size_t n_aff, const float *sr
     using namespace pt;
     clear_error();
     if (!ctx) return set_error(PT_ERR_INVALID, "pt_bf_accel_f32: ctx is NULL");
-    if (flags & ~PT_BF_EXACT) return set_error(PT_ERR_INVALID, "pt_bf_accel_f32: unknown flags 0x%x", flags);
+    if (flags & ~(PT_BF_EXACT | PT_BF_VEC3A)) return set_error(PT_ERR_INVALID, "pt_bf_accel_f32: unknown flags 0x%x", flags);
     PT_TRY(validate_sizes("pt_bf_accel_f32", n_aff, n_src));
     if (n_aff && (!aff || !out)) return set_error(PT_ERR_INVALID, "pt_bf_accel_f32: NULL buffer");
     if (n_src && !src) return set_error(PT_ERR_INVALID, "pt_bf_accel_f32: NULL affecting buffer");

@@ -88,10 +88,11 @@ class BruteForce:
     with compensated accumulation.
     """
 
-    def __init__(self, resources, interaction, exact=False):
+    def __init__(self, resources, interaction, exact=False, vec3a=False):
         self.resources = resources
         self.interaction = interaction
         self.exact = bool(exact)
+        self.vec3a = bool(vec3a)  # glam Vec3A/Vec4 operand order (exact path)
 
     def compute(self, storage):
         b = as_between(storage)
@@ -102,7 +103,7 @@ class BruteForce:
             return out
         same = b.affected is b.affecting
         it = self.interaction
-        flags = N.PT_BF_EXACT if self.exact else 0
+        flags = (N.PT_BF_EXACT if self.exact else 0) | (N.PT_BF_VEC3A if self.vec3a else 0)
         N.check(N.lib().pt_bf_accel_f32(self.resources.handle, _ptr(aff), aff.shape[0],
                                         _ptr(aff) if same else _ptr(src), src.shape[0],
                                         it.softening, int(it.is_checked), flags, _ptr(out)))

@@ -185,3 +185,37 @@ def test_full_size_properties(res, oracle):
     ref = oracle.bf_f64(b[idx], b, 0.01, True)
     e = rel(a[idx], ref)
     assert np.percentile(e, 95) < 1e-6 and e.max() < 1e-5
+
+
+@pytest.mark.parametrize("softening,checked", [(0.0, True), (1e-3, True)])
+def test_exact_vec3a_operand_order(res, oracle, softening, checked):
+    """glam Vec3A/Vec4's kernel (d * m / ...): bit-identical to its restatement, and
+    not the same bits as the default order (so the flag does something)."""
+    b = mixed(3000, 71)
+    it = AccelerationSoftened(softening, checked)
+    got = cuda.BruteForce(res, it, exact=True, vec3a=True).compute(b)
+    want = oracle.bf_f32_vec3a(b, b, softening, checked)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    other = oracle.bf_f32(b, b, softening, checked)
+    assert not np.array_equal(got.view(np.uint32), other.view(np.uint32))
+
+
+def test_two_dimensional_bodies_through_z0(res, oracle):
+    """2D particles (glam Vec2) as z = 0: the 2D reference sum (x*x + y*y) is what the
+    3D path computes bit for bit, with a zero z acceleration."""
+    b = ics.uniform_cube(2000, 72)["bodies"].copy()
+    b[:, 2] = 0.0
+    got = cuda.BruteForce(res, AccelerationSoftened(1e-3), exact=True).compute(b)
+    s = np.float32
+    x, y, m = b[:, 0], b[:, 1], b[:, 3]
+    acc = np.zeros((2000, 2), np.float32)
+    for j in range(2000):  # the 2D restatement, vectorised over targets
+        dx, dy = x[j] - x, y[j] - y
+        n = dx * dx + dy * dy
+        ns = n + s(1e-3) * s(1e-3)
+        q = m[j] / (ns * np.sqrt(ns))
+        a = np.stack([dx * q, dy * q], 1)
+        a = np.where((n == 0)[:, None], np.stack([dx, dy], 1), a)
+        acc = acc + a
+    assert np.array_equal(got[:, :2].view(np.uint32), acc.view(np.uint32))
+    assert not got[:, 2].any()
