@@ -265,6 +265,10 @@ int pt_mlp_loss_grad(pt_ctx *ctx, const float *features, const float *targets, i
                      double *loss_out);
 /* Predictions (n x 3) for host features (n x 12). */
 int pt_mlp_predict(pt_ctx *ctx, const float *features, int n, float *out);
+/* The same predictions through the Barnes-Hut walk's inference path: BF16 tensor-core
+ * MMAs (mma.sync m16n8k16) with features and activations rounded to BF16, FP32
+ * accumulation. */
+int pt_mlp_predict_tc(pt_ctx *ctx, const float *features, int n, float *out);
 
 /* Phase timing of the last pt_bf_* / pt_bh_* call, from CUDA events recorded on
  * the context's stream when enabled: for Barnes-Hut, build = tree construction

@@ -38,6 +38,22 @@ def forward(p, f):
     return (h2 @ w3.T + b3) * scale
 
 
+def bf16(x):
+    """Round to the nearest BF16 value (ties to even), returned as float64."""
+    b = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    b = (b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000
+    return b.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def forward_bf16(p, f):
+    """The tensor-core inference path: features and both hidden layers' activations
+    rounded to BF16 before each product, everything else exact."""
+    w1, b1, w2, b2, w3, b3, scale = unpack(p)
+    h1, _ = gelu(bf16(f) @ w1.T + b1)
+    h2, _ = gelu(bf16(h1) @ w2.T + b2)
+    return (bf16(h2) @ w3.T + b3) * scale
+
+
 def loss_grad(p, f, t):
     """Loss and gradient of the training kernel for features f (b, 12), raw targets t."""
     w1, b1, w2, b2, w3, b3, scale = unpack(p)

@@ -103,6 +103,7 @@ def _declare(L):
         "pt_mlp_loss_grad": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, ctypes.c_int, c_ptr,
                                             ctypes.POINTER(ctypes.c_double)]),
         "pt_mlp_predict": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_int, c_ptr]),
+        "pt_mlp_predict_tc": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_int, c_ptr]),
         "pt_ensemble_run": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_uint32, c_ptr, c_ptr,
                                            ctypes.c_float, ctypes.c_int, ctypes.c_float,
                                            ctypes.c_int]),

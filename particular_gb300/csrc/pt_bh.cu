@@ -63,7 +63,10 @@ struct State {
     DevBuf counters;
     DevBuf out;
     DevBuf aff_h, src_h;  // staging for the host-pointer entry point
-    const float *mlp = nullptr;  // learned-correction parameters (owned by the MLP state)
+    DevBuf lrec, lgroup, lnext, lpart, lhead, lcentre, lused;  // learned-correction records
+    int lcap = 0;                     // record chunks allocated
+    const uint32_t *mlp_w = nullptr;  // learned correction: packed BF16 weights (owned by the MLP state)
+    const float *mlp_b = nullptr;     // and its bias block
     float theta_inner = 0.5f;
     int cap_n = 0;
     int last_n_src = 0;
@@ -650,53 +653,102 @@ __device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, f2 px, f
     __syncwarp();
 }
 
-// Parameters read as warp-uniform loads (every lane reads the same weight at the
-// same time: one broadcast per instruction).
-struct UniformParams {
-    const float *__restrict__ p;
-    __device__ __forceinline__ float operator[](int i) const { return __ldg(p + i); }
+// ---- learned correction: records of marginal cells ---------------------------
+// The walk (PT_BH_LEARNED) does not evaluate the network itself: it records the
+// node index of every marginal cell (accepted at theta, opened at theta_inner) in
+// chunks of LCHUNK entries that each belong to one warp (one group of 32 targets),
+// chained per group in walk order, and the group's centre. A tensor-core kernel then
+// evaluates all records (bh_learned_eval) and bh_learned_apply adds each group's
+// sum, chunk by chunk in chain order, so results do not depend on scheduling.
+constexpr int LCHUNK = 128;
+
+struct LearnedRecords {
+    int *rec;        // [cap][LCHUNK] node indices, -1 = padding
+    int *chunk_group;  // [cap]
+    int *next;       // [cap] next chunk of the same group, -1 = last
+    int *head;       // [groups] first chunk of the group, -1 = none
+    float4 *centre;  // [groups] mean position of the group's targets
+    float4 *part;    // [cap] the chunk's summed correction
+    int *used;       // chunks handed out (may exceed cap: then nothing past cap is written)
+    int cap;
 };
 
-// Learned correction of up to 32 marginal cells (one per lane) at the group centre:
-// returns the sum over the cells of the predicted residual accelerations.
+// One warp per chunk (grid-stride): features of the 128 recorded cells at the group
+// centre, four 32-row tensor-core batches, the chunk's sum into part[chunk].
 // Cells whose size/distance ratio at the group centre lies outside the range the
-// model was trained on ([theta_inner, theta]) get no correction.
-__device__ __forceinline__ void eval_learned(const float *__restrict__ M, int cnt, float gx, float gy, float gz,
-                                             const float *__restrict__ params, float lo, float hi, float &cx,
-                                             float &cy, float &cz) {
-    const int lane = threadIdx.x & 31;
-    __syncwarp();
-    float rx = 0.f, ry = 0.f, rz = 0.f;
-    float f[mlp::IN];
-    float r2 = 0.f;
-    bool use = false;
-    float4 com;
-    if (lane < cnt) {
-        const float *e = M + lane * 14;
-        com = make_float4(e[0], e[1], e[2], e[3]);
-        const float q[6] = {e[4], e[5], e[6], e[7], e[8], e[9]};
-        const float4 g = make_float4(e[10], e[11], e[12], e[13]);
-        r2 = mlp::features(gx, gy, gz, com, q, g, f);
-        use = f[3] >= lo && f[3] <= hi;
-    }
-    if (use) {
-        float o[mlp::OUT];
-        mlp::forward<true>(UniformParams{params}, f, o);
-        const float a = com.w / r2;  // M / |r|^2
-        rx = o[0] * a;
-        ry = o[1] * a;
-        rz = o[2] * a;
-    }
+// model was trained on ([lo, hi]) get no correction.
+__global__ void __launch_bounds__(128) bh_learned_eval(LearnedRecords L, const float4 *__restrict__ nodeA,
+                                                      const float4 *__restrict__ nodeQ,
+                                                      const float4 *__restrict__ nodeG,
+                                                      const uint32_t *__restrict__ W, const float *__restrict__ bias,
+                                                      float lo, float hi) {
+    __shared__ float X[4][32 * mlp::TC_XS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const int used = min(*L.used, L.cap);
+    const float sc = __ldg(bias + mlp::TC_SCALE);
+    float *Xw = X[warp];
+    for (int c = blockIdx.x * 4 + warp; c < used; c += gridDim.x * 4) {
+        const float4 gc = L.centre[L.chunk_group[c]];
+        float rx = 0.f, ry = 0.f, rz = 0.f;
+        for (int b = 0; b < LCHUNK / 32; ++b) {
+            const int node = L.rec[size_t(c) * LCHUNK + b * 32 + lane];
+            if (__ballot_sync(0xffffffffu, node >= 0) == 0u) break;  // padding fills the chunk's tail
+            float f[mlp::IN];
+            float a = 0.f;  // M / |r|^2 of this row's cell, 0 = no correction
+            if (node >= 0) {
+                const float4 A = __ldg(nodeA + node);
+                const float4 q0 = __ldg(nodeQ + 2 * node), q1 = __ldg(nodeQ + 2 * node + 1);
+                const float q[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+                const float r2 = mlp::features(gc.x, gc.y, gc.z, A, q, __ldg(nodeG + node), f);
+                if (f[3] >= lo && f[3] <= hi) a = A.w / r2;
+            }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        rx += __shfl_xor_sync(0xffffffffu, rx, off);
-        ry += __shfl_xor_sync(0xffffffffu, ry, off);
-        rz += __shfl_xor_sync(0xffffffffu, rz, off);
+            for (int i = 0; i < 16; ++i) Xw[lane * mlp::TC_XS + i] = (i < mlp::IN && a != 0.f) ? f[i] : 0.f;
+            __syncwarp();
+            float y[2][4];
+            mlp::tc_batch(Xw, W, bias, y);
+            __syncwarp();
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float s = __shfl_sync(0xffffffffu, a, 16 * mt + 8 * h + g);
+                    if (t == 0) {
+                        rx = fmaf(y[mt][2 * h], s, rx);
+                        ry = fmaf(y[mt][2 * h + 1], s, ry);
+                    } else if (t == 1) {
+                        rz = fmaf(y[mt][2 * h], s, rz);
+                    }
+                }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            rx += __shfl_xor_sync(0xffffffffu, rx, off);
+            ry += __shfl_xor_sync(0xffffffffu, ry, off);
+            rz += __shfl_xor_sync(0xffffffffu, rz, off);
+        }
+        if (lane == 0) L.part[c] = make_float4(rx * sc, ry * sc, rz * sc, 0.f);
     }
-    cx += rx;
-    cy += ry;
-    cz += rz;
-    __syncwarp();
+}
+
+// out[target] += the sum of its group's chunk corrections, in chain order.
+__global__ void bh_learned_apply(LearnedRecords L, const uint32_t *__restrict__ tidx, int n_aff,
+                                 float *__restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_aff) return;
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    // chunk indices grow along a chain (each is taken after its predecessor)
+    for (int c = L.head[t >> 5], prev = -1; c > prev && c < L.cap; prev = c, c = L.next[c]) {
+        const float4 v = L.part[c];
+        cx += v.x;
+        cy += v.y;
+        cz += v.z;
+    }
+    const uint32_t o = tidx[t];
+    out[3 * size_t(o) + 0] += cx;
+    out[3 * size_t(o) + 1] += cy;
+    out[3 * size_t(o) + 2] += cz;
 }
 
 template <bool QUAD, bool GUARD, bool LEARNED>
@@ -704,7 +756,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     bh_walk_group(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
                   const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
                   const float4 *__restrict__ nodeG, const float4 *__restrict__ sbody, const int *__restrict__ counters,
-                  float th2, float th_in2, const float *__restrict__ mlp_params, float eps2, float *__restrict__ out,
+                  float th2, float th_in2, LearnedRecords LR, float eps2, float *__restrict__ out,
                   unsigned long long *__restrict__ stats, int *__restrict__ err) {
     constexpr int NFC = QUAD ? 10 : 4;
     using CellList = IList<NFC, 96>;
@@ -713,7 +765,6 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     __shared__ float4 s_tgt[GW_WARPS][32];
     __shared__ __align__(16) CellList s_cells[GW_WARPS];
     __shared__ __align__(16) BodyList s_bodies[GW_WARPS];
-    __shared__ float s_learn[GW_WARPS][LEARNED ? 32 * 14 : 1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int group = blockIdx.x * GW_WARPS + warp;
     if (group * 32 >= n_aff) return;
@@ -756,9 +807,9 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
         gcy /= nv;
         gcz /= nv;
     }
-    float lx = 0.f, ly = 0.f, lz = 0.f;  // learned corrections (same in every lane)
-    const float th_in = sqrtf(th_in2), th_out = sqrtf(th2);
-    int Nm = 0;
+    // learned: the warp's current record chunk and its fill; the previous chunk links to
+    // the next one (head of the group's chain first)
+    int chunk = -1, fill = LCHUNK;
     unsigned long long learned = 0;
 
     const f2 px = pk2(p.x, p.x), py = pk2(p.y, p.y), pz = pk2(p.z, p.z), e2 = pk2(eps2, eps2);
@@ -819,20 +870,29 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
         if (LEARNED) {
             const unsigned mm = __ballot_sync(0xffffffffu, marginal);
             const int nm = __popc(mm);
-            if (Nm + nm > 32) {
-                eval_learned(s_learn[warp], Nm, gcx, gcy, gcz, mlp_params, th_in, th_out, lx, ly, lz);
-                learned += Nm;
-                Nm = 0;
+            if (nm && fill + nm > LCHUNK) {
+                // pad the current chunk's tail, take the next chunk and link it
+                if (chunk >= 0 && chunk < LR.cap)
+                    for (int i = fill + lane; i < LCHUNK; i += 32) LR.rec[size_t(chunk) * LCHUNK + i] = -1;
+                int nc = 0;
+                if (lane == 0) nc = atomicAdd(LR.used, 1);
+                nc = __shfl_sync(0xffffffffu, nc, 0);
+                if (lane == 0) {
+                    if (nc < LR.cap) {
+                        LR.chunk_group[nc] = group;
+                        LR.next[nc] = -1;
+                    } else {
+                        atomicOr(err, 2);
+                    }
+                    if (chunk < 0) LR.head[group] = nc;
+                    else if (chunk < LR.cap) LR.next[chunk] = nc;
+                }
+                chunk = nc;
+                fill = 0;
             }
-            if (marginal) {
-                float *e = s_learn[warp] + (Nm + __popc(mm & lt)) * 14;
-                const float4 q0 = __ldg(nodeQ + 2 * node), q1 = __ldg(nodeQ + 2 * node + 1);
-                const float4 g = __ldg(nodeG + node);
-                e[0] = A.x; e[1] = A.y; e[2] = A.z; e[3] = A.w;
-                e[4] = q0.x; e[5] = q0.y; e[6] = q0.z; e[7] = q0.w; e[8] = q1.x; e[9] = q1.y;
-                e[10] = g.x; e[11] = g.y; e[12] = g.z; e[13] = g.w;
-            }
-            Nm += nm;
+            if (marginal && chunk < LR.cap) LR.rec[size_t(chunk) * LCHUNK + fill + __popc(mm & lt)] = node;
+            fill += nm;
+            learned += nm;
         }
         const bool rest = have && B.y < range.y;  // later siblings remain
         const int np = int(rest) + int(open);
@@ -930,9 +990,13 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     eval_list<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
     eval_list<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
     entries += Nc + Nb;
-    if (LEARNED && Nm > 0) {
-        eval_learned(s_learn[warp], Nm, gcx, gcy, gcz, mlp_params, th_in, th_out, lx, ly, lz);
-        learned += Nm;
+    if (LEARNED) {
+        if (chunk >= 0 && chunk < LR.cap)
+            for (int i = fill + lane; i < LCHUNK; i += 32) LR.rec[size_t(chunk) * LCHUNK + i] = -1;
+        if (lane == 0) {
+            if (chunk < 0) LR.head[group] = -1;
+            LR.centre[group] = make_float4(gcx, gcy, gcz, 0.f);
+        }
     }
     float x0, x1, y0, y1, z0, z1;
     upk2(ax, x0, x1);
@@ -940,13 +1004,13 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     upk2(az, z0, z1);
     if (failed) {
         x0 = y0 = z0 = __int_as_float(0x7fc00000);
-        if (lane == 0) atomicExch(err, 1);
+        if (lane == 0) atomicOr(err, 1);
     }
     if (valid) {
         const uint32_t o = tidx[t];
-        out[3 * size_t(o) + 0] = (x0 + x1) + lx;
-        out[3 * size_t(o) + 1] = (y0 + y1) + ly;
-        out[3 * size_t(o) + 2] = (z0 + z1) + lz;
+        out[3 * size_t(o) + 0] = x0 + x1;
+        out[3 * size_t(o) + 1] = y0 + y1;
+        out[3 * size_t(o) + 2] = z0 + z1;
     }
     if (stats && lane == 0) {
         const unsigned long long nvalid = unsigned(min(32, n_aff - group * 32));
@@ -961,7 +1025,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
 using WalkKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
                             const float4 *, const int *, float, float, float *, unsigned long long *);
 using GroupKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
-                             const float4 *, const float4 *, const int *, float, float, const float *, float,
+                             const float4 *, const float4 *, const int *, float, float, LearnedRecords, float,
                              float *, unsigned long long *, int *);
 
 static WalkKernel walk_kernel(bool quad) { return quad ? bh_walk<true> : bh_walk<false>; }
@@ -1130,11 +1194,48 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
     if (flags & PT_BH_GROUP) {
         const int groups = (n_aff + 31) / 32;
         const bool learned = flags & PT_BH_LEARNED;
-        if (learned && !S.mlp) return set_error(PT_ERR_INVALID, "PT_BH_LEARNED needs a model (pt_mlp_*)");
-        group_kernel(quad, eps2 == 0.0f, learned)<<<(groups + GW_WARPS - 1) / GW_WARPS, 32 * GW_WARPS, 0, st>>>(
-            tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.nodeG),
-            as<float4>(S.sbody), as<int>(S.counters), th2, S.theta_inner * S.theta_inner, S.mlp, eps2, d_out, stats,
-            err);
+        if (learned && !S.mlp_w) return set_error(PT_ERR_INVALID, "PT_BH_LEARNED needs a model (pt_mlp_*)");
+        LearnedRecords LR{};
+        if (learned) {
+            PT_TRY(ensure_buf(ctx, S.lhead, sizeof(int) * size_t(groups)));
+            PT_TRY(ensure_buf(ctx, S.lcentre, sizeof(float4) * size_t(groups)));
+            PT_TRY(ensure_buf(ctx, S.lused, sizeof(int)));
+            if (S.lcap == 0) S.lcap = std::max(1024, 2 * groups);
+        }
+        for (int attempt = 0;; ++attempt) {
+            if (learned) {
+                PT_TRY(ensure_buf(ctx, S.lrec, sizeof(int) * size_t(S.lcap) * LCHUNK));
+                PT_TRY(ensure_buf(ctx, S.lgroup, sizeof(int) * size_t(S.lcap)));
+                PT_TRY(ensure_buf(ctx, S.lnext, sizeof(int) * size_t(S.lcap)));
+                PT_TRY(ensure_buf(ctx, S.lpart, sizeof(float4) * size_t(S.lcap)));
+                LR = LearnedRecords{as<int>(S.lrec),   as<int>(S.lgroup),   as<int>(S.lnext), as<int>(S.lhead),
+                                    as<float4>(S.lcentre), as<float4>(S.lpart), as<int>(S.lused), S.lcap};
+                PT_CUDA(cudaMemsetAsync(LR.used, 0, sizeof(int), st));
+            }
+            group_kernel(quad, eps2 == 0.0f, learned)<<<(groups + GW_WARPS - 1) / GW_WARPS, 32 * GW_WARPS, 0, st>>>(
+                tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.nodeG),
+                as<float4>(S.sbody), as<int>(S.counters), th2, S.theta_inner * S.theta_inner, LR, eps2, d_out, stats,
+                err);
+            PT_TRY(check_launch(ctx, "bh_walk_group"));
+            // Outside stream capture the record count is checked and the walk rerun
+            // with room for all records; inside, an overflow sets error bit 2.
+            if (!learned || ctx->capturing || attempt > 0) break;
+            int used = 0;
+            PT_CUDA(cudaMemcpyAsync(&used, LR.used, sizeof(int), cudaMemcpyDeviceToHost, st));
+            PT_CUDA(cudaStreamSynchronize(st));
+            if (used <= S.lcap) break;
+            S.lcap = used + used / 4;
+            PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+            PT_CUDA(cudaMemsetAsync(stats, 0, 5 * sizeof(unsigned long long), st));
+        }
+        if (learned) {
+            bh_learned_eval<<<ctx->sm_count * 4, 128, 0, st>>>(LR, as<float4>(S.nodeA), as<float4>(S.nodeQ),
+                                                               as<float4>(S.nodeG), S.mlp_w, S.mlp_b,
+                                                               S.theta_inner, theta);
+            PT_TRY(check_launch(ctx, "bh_learned_eval"));
+            bh_learned_apply<<<blocks(n_aff), 256, 0, st>>>(LR, tidx, n_aff, d_out);
+            PT_TRY(check_launch(ctx, "bh_learned_apply"));
+        }
         PT_TRY(check_launch(ctx, "bh_walk_group"));
         mark(ctx, 2);
         return PT_OK;
@@ -1183,10 +1284,11 @@ int bh_tree_view(pt_ctx *ctx, TreeView *out) {
     return PT_OK;
 }
 
-int bh_set_mlp(pt_ctx *ctx, const float *d_params, float theta_inner) {
+int bh_set_mlp(pt_ctx *ctx, const uint32_t *d_tc_weights, const float *d_tc_bias, float theta_inner) {
     bh::State *S = bh::state(ctx);
     if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
-    S->mlp = d_params;
+    S->mlp_w = d_tc_weights;
+    S->mlp_b = d_tc_bias;
     S->theta_inner = theta_inner;
     return PT_OK;
 }
@@ -1202,7 +1304,8 @@ void pt_bh_state_free(pt_ctx *ctx) {
                      &S->ukey,     &S->ufirst, &S->bfirst, &S->blast,  &S->bdelta,  &S->bparent, &S->lparent,
                      &S->top,      &S->oparent, &S->loparent, &S->cnt, &S->pscan,   &S->pre,    &S->levels,
                      &S->by_level,   &S->nodeA,  &S->nodeB,  &S->nodeQ,  &S->nodeG, &S->nodeR, &S->mom,     &S->tkeys,  &S->tidx,
-                     &S->tbody,    &S->counters, &S->out,  &S->aff_h,  &S->src_h};
+                     &S->tbody,    &S->counters, &S->out,  &S->aff_h,  &S->src_h, &S->lrec, &S->lgroup,
+                     &S->lnext,    &S->lpart,  &S->lhead, &S->lcentre, &S->lused};
     for (DevBuf *b : all) free_buf(ctx, *b);
     delete S;
     ctx->bh = nullptr;
@@ -1254,8 +1357,10 @@ int pt_bh_accel_f32(pt_ctx *ctx, const float *aff, size_t n_aff, const float *sr
     if (n_src) PT_CUDA(cudaMemcpyAsync(&err, static_cast<int *>(S->counters.ptr) + 3, sizeof(int),
                                        cudaMemcpyDeviceToHost, st));
     PT_CUDA(cudaStreamSynchronize(st));
-    if (err)
+    if (err & 1)
         return set_error(PT_ERR_CAPACITY, "pt_bh_accel_f32: a group walk ran out of stack; its bodies are NaN");
+    if (err & 2)
+        return set_error(PT_ERR_CAPACITY, "pt_bh_accel_f32: learned-correction records overflowed");
     return PT_OK;
 }
 

@@ -255,8 +255,62 @@ __global__ void mlp_predict(const float *__restrict__ P, const float *__restrict
     for (int c = 0; c < OUT; ++c) out[size_t(s) * 3 + c] = o[c];
 }
 
+// FP32 parameters (BF16 values) -> BF16 pairs in B-fragment order + bias block.
+__global__ void mlp_pack_tc(const float *__restrict__ P, uint32_t *__restrict__ W, float *__restrict__ bias) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < TC_WORDS) {
+        int layer, n, p;
+        tc_word_source(k, layer, n, p);
+        float lo = 0.f, hi = 0.f;
+        if (layer == 1) {
+            lo = 2 * p < IN ? P[W1 + n * IN + 2 * p] : 0.f;
+            hi = 2 * p + 1 < IN ? P[W1 + n * IN + 2 * p + 1] : 0.f;
+        } else if (layer == 2) {
+            lo = P[W2 + n * H + 2 * p];
+            hi = P[W2 + n * H + 2 * p + 1];
+        } else if (n < OUT) {
+            lo = P[W3 + n * H + 2 * p];
+            hi = P[W3 + n * H + 2 * p + 1];
+        }
+        W[k] = pack_bf16(lo, hi);
+    }
+    if (k < 64) {
+        bias[k] = P[B1 + k];
+        bias[64 + k] = P[B2 + k];
+    }
+    if (k < 8) bias[128 + k] = k < OUT ? P[B3 + k] : 0.f;
+    if (k == 0) bias[TC_SCALE] = P[SCALE];
+}
+
+// Tensor-core predictions per cell (the walk's inference path), 32 rows per warp.
+__global__ void mlp_predict_tc(const uint32_t *__restrict__ W, const float *__restrict__ bias,
+                               const float *__restrict__ feat, int n, float *__restrict__ out) {
+    __shared__ float X[4][32 * TC_XS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row0 = (blockIdx.x * 4 + warp) * 32;
+    if (row0 >= n) return;
+    const int r = row0 + lane;
+    for (int i = 0; i < 16; ++i) X[warp][lane * TC_XS + i] = (r < n && i < IN) ? feat[size_t(r) * IN + i] : 0.f;
+    __syncwarp();
+    float y[2][4];
+    tc_batch(X[warp], W, bias, y);
+    const int g = lane >> 2, t = lane & 3;
+    const float sc = bias[TC_SCALE];
+    for (int mt = 0; mt < 2; ++mt)
+        for (int h = 0; h < 2; ++h) {
+            const int row = row0 + 16 * mt + g + 8 * h;
+            for (int c = 0; c < 2; ++c) {
+                const int col = 2 * t + c;
+                if (row < n && col < OUT) out[size_t(row) * 3 + col] = y[mt][2 * h + c] * sc;
+            }
+        }
+}
+
+struct State;
+static int install(pt_ctx *ctx, State &S);
+
 struct State {
-    DevBuf master, params, grad, m1, m2, loss, feat, targ, count, power, scratch;
+    DevBuf master, params, grad, m1, m2, loss, feat, targ, count, power, scratch, tcw, tcb;
     unsigned cap = 0;
     long long adam_t = 0;
     float theta_inner = 0.5f;
@@ -292,7 +346,19 @@ static int upload(pt_ctx *ctx, State &S, const std::vector<float> &host) {
     PT_CUDA(cudaStreamSynchronize(st));
     S.adam_t = 0;
     S.initialised = true;
-    return bh_set_mlp(ctx, static_cast<const float *>(S.params.ptr), S.theta_inner);
+    return install(ctx, S);
+}
+
+// Packs the current parameters for the tensor-core path and hands them to the walk.
+static int install(pt_ctx *ctx, State &S) {
+    PT_TRY(ensure_buf(ctx, S.tcw, sizeof(uint32_t) * TC_WORDS));
+    PT_TRY(ensure_buf(ctx, S.tcb, sizeof(float) * TC_BIAS));
+    mlp_pack_tc<<<(TC_WORDS + 255) / 256, 256, 0, ctx->stream>>>(static_cast<const float *>(S.params.ptr),
+                                                                 static_cast<uint32_t *>(S.tcw.ptr),
+                                                                 static_cast<float *>(S.tcb.ptr));
+    PT_TRY(check_launch(ctx, "mlp_pack_tc"));
+    return bh_set_mlp(ctx, static_cast<const uint32_t *>(S.tcw.ptr), static_cast<const float *>(S.tcb.ptr),
+                      S.theta_inner);
 }
 
 }  // namespace mlp
@@ -306,7 +372,7 @@ void pt_mlp_state_free(pt_ctx *ctx) {
     auto *S = static_cast<pt::mlp::State *>(ctx->mlp);
     if (!S) return;
     pt::DevBuf *all[] = {&S->master, &S->params, &S->grad, &S->m1, &S->m2, &S->loss,
-                         &S->feat, &S->targ, &S->count, &S->power, &S->scratch};
+                         &S->feat, &S->targ, &S->count, &S->power, &S->scratch, &S->tcw, &S->tcb};
     for (auto *b : all) pt::free_buf(ctx, *b);
     delete S;
     ctx->mlp = nullptr;
@@ -488,7 +554,7 @@ int pt_mlp_train(pt_ctx *ctx, int steps, int batch, float lr, uint64_t seed, flo
     }
     PT_CUDA(cudaStreamSynchronize(st));
     if (loss_out) *loss_out = float(loss_sum / std::max(1, loss_n));
-    return bh_set_mlp(ctx, static_cast<const float *>(S->params.ptr), S->theta_inner);
+    return mlp::install(ctx, *S);
 }
 
 // Loss and its gradient for host samples (features b x 12, targets b x 3) at the
@@ -528,6 +594,27 @@ int pt_mlp_loss_grad(pt_ctx *ctx, const float *features, const float *targets, i
     PT_CUDA(cudaMemcpyAsync(grad, S->grad.ptr, sizeof(float) * mlp::NPARAM, cudaMemcpyDeviceToHost, st));
     PT_CUDA(cudaMemcpyAsync(loss_out, S->loss.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
     PT_CUDA(cudaMemsetAsync(S->grad.ptr, 0, sizeof(float) * mlp::NPARAM, st));
+    PT_CUDA(cudaStreamSynchronize(st));
+    return PT_OK;
+}
+
+// The same predictions through the walk's tensor-core path (BF16 activations).
+int pt_mlp_predict_tc(pt_ctx *ctx, const float *features, int n, float *out) {
+    using namespace pt;
+    clear_error();
+    auto *S = ctx ? static_cast<mlp::State *>(ctx->mlp) : nullptr;
+    if (!S || !S->initialised || !S->tcw.ptr || !features || !out || n <= 0)
+        return set_error(PT_ERR_INVALID, "pt_mlp_predict_tc: bad arguments");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    PT_TRY(ensure_buf(ctx, S->scratch, sizeof(float) * size_t(n) * (mlp::IN + 3)));
+    float *f = static_cast<float *>(S->scratch.ptr);
+    float *o = f + size_t(n) * mlp::IN;
+    PT_CUDA(cudaMemcpyAsync(f, features, sizeof(float) * size_t(n) * mlp::IN, cudaMemcpyHostToDevice, st));
+    mlp::mlp_predict_tc<<<(n + 127) / 128, 128, 0, st>>>(static_cast<const uint32_t *>(S->tcw.ptr),
+                                                         static_cast<const float *>(S->tcb.ptr), f, n, o);
+    PT_TRY(check_launch(ctx, "mlp_predict_tc"));
+    PT_CUDA(cudaMemcpyAsync(out, o, sizeof(float) * size_t(n) * 3, cudaMemcpyDeviceToHost, st));
     PT_CUDA(cudaStreamSynchronize(st));
     return PT_OK;
 }

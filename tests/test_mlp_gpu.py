@@ -33,6 +33,33 @@ def test_gradient_matches_fp64_restatement(res):
     np.testing.assert_allclose(out, M.forward(p, f), rtol=1e-4, atol=1e-5)
 
 
+def test_tensor_core_inference_matches_bf16_restatement(res):
+    """pt_mlp_predict_tc (the walk's mma.sync path) against the FP64 forward pass
+    with the same BF16 roundings of features and activations. What remains is FP32
+    accumulation order and the hardware tanh approximation, whose error can move an
+    activation by one BF16 step; relative RMS difference bound 2e-3, and the plain
+    FP64 forward within 2e-2 (the BF16 roundings themselves)."""
+    from oracle import mlp_oracle as M
+    learned.init(res, seed=4)
+    p = learned.get_params(res)
+    rng = np.random.default_rng(1)
+    # trained-model-like weights: the initial output layer is zero, so draw one
+    p[M.W3:M.B3] = M.bf16(rng.normal(scale=0.2, size=M.B3 - M.W3))
+    p[M.B3:M.SCALE] = [0.01, -0.02, 0.03]
+    learned.set_params(res, p.astype(np.float32))
+    p = learned.get_params(res)
+    f = rng.normal(size=(1000, 12)).astype(np.float32)   # 1000: ragged last batch of 32
+    out = np.zeros((1000, 3), np.float32)
+    N.check(N.lib().pt_mlp_predict_tc(res.handle, f.ctypes.data, 1000, out.ctypes.data))
+    want = M.forward_bf16(p, f)
+    rms = np.sqrt((want ** 2).mean())
+    err = np.sqrt(((out - want) ** 2).mean()) / rms
+    err64 = np.sqrt(((out - M.forward(p, f)) ** 2).mean()) / rms
+    print(f"tensor-core inference: rel RMS vs BF16 restatement {err:.2e}, vs FP64 {err64:.2e}")
+    assert np.isfinite(out).all()
+    assert err < 2e-3 and err64 < 2e-2
+
+
 @pytest.fixture(scope="module")
 def trained(res):
     """A small model: 24 snapshots of 16384 bodies, 400 Adam steps."""
@@ -91,3 +118,5 @@ def test_learned_walk_reports_its_effect(res, oracle, trained):
           f"learned {np.median(e1):.3e}/{np.percentile(e1, 95):.3e} ({st['learned']} corrections)")
     assert np.isfinite(got).all() and st["learned"] > 0
     assert np.median(e1) < 2 * np.median(e0)
+    # corrections are summed per group in walk order: the result is reproducible
+    np.testing.assert_array_equal(m.compute(b), got)
