@@ -308,9 +308,12 @@ class BarnesHutWorkload:
     def h2d_d2h_bytes(self):
         return 16 * self.n, 12 * self.n
 
-    def flops_per_interaction(self):
-        # monopole: 20 (the GPU Gems convention); quadrupole term: 38 more
-        return 20 + (38 if self.flags & 1 else 0)
+    QUAD_FLOPS = 38  # the quadrupole term's extra flops per accepted cell
+
+    def walk_flops(self, st):
+        # monopole: 20 per accepted node (the GPU Gems convention); the quadrupole
+        # term adds 38 per accepted cell (single bodies carry none)
+        return 20 * st.interactions + (self.QUAD_FLOPS * st.cell_interactions if self.flags & 1 else 0)
 
     def roofline(self, res, step_ms):
         import ctypes
@@ -330,15 +333,16 @@ class BarnesHutWorkload:
         peak = ctypes.c_double(0)
         N.check(L.pt_measure_fp32_peak(res.handle, ctypes.byref(peak)))
         walk_ms = statistics.mean(walk)
-        flops = st.interactions * self.flops_per_interaction()
+        flops = self.walk_flops(st)
         achieved = flops / (walk_ms * 1e-3) / 1e12
         return {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                 "frac": achieved / peak.value, "traffic": None,
                 "kernel": "bh_walk_group" if self.flags & 2 else "bh_walk",
                 "walk_ms": walk_ms, "build_ms": statistics.mean(build),
                 "interactions_per_body": st.interactions / self.n,
-                "algorithmic": f"{self.flops_per_interaction()} flop per accepted node per body x "
-                               "interactions counted by the walk",
+                "cell_interactions_per_body": st.cell_interactions / self.n,
+                "algorithmic": "20 flop per accepted node per body (+38 per accepted cell with "
+                               "the quadrupole) x the walk's own counts",
                 "peak_source": "measured FFMA-chain kernel over all SMs (pt_measure_fp32_peak)"}
 
     def extra(self):

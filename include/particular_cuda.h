@@ -168,10 +168,13 @@ typedef struct pt_bh_stats {
     uint64_t visits;       /* nodes visited, summed over bodies, last walk */
     uint64_t warps;        /* warps that walked */
     uint64_t max_stack;    /* deepest shared-memory stack of a PT_BH_GROUP walk */
-    uint64_t overflow;     /* nonzero if a PT_BH_GROUP walk ran out of stack (its
-                              bodies are NaN; the host entry point then fails with
-                              PT_ERR_CAPACITY) */
+    uint64_t overflow;     /* warps of a PT_BH_GROUP walk whose shared-memory stack
+                              ran out; they took the per-body walk instead (same
+                              rule as without PT_BH_GROUP, no error) */
     uint64_t learned;      /* learned corrections evaluated (per warp and cell) */
+    uint64_t cell_interactions; /* the accepted nodes of `interactions` that are cells
+                                   (the ones a PT_BH_QUADRUPOLE walk adds the
+                                   quadrupole term to) */
 } pt_bh_stats;
 
 /* cuda::BarnesHut over host buffers (synchronous). Layouts as pt_bf_accel_f32. */
@@ -181,6 +184,10 @@ int pt_bh_accel_f32(pt_ctx *ctx, const float *affected, size_t n_aff, const floa
 int pt_bh_accel_f32_device(pt_ctx *ctx, const float *d_affected, size_t n_aff,
                            const float *d_affecting, size_t n_src, float theta, float softening,
                            uint32_t flags, float *d_out_xyz);
+/* Caps the PT_BH_GROUP walk's shared-memory stack at `ranges` entries per warp (2 to
+ * the compiled capacity; 0 restores the capacity). A warp that runs out takes the
+ * per-body walk instead (counted in pt_bh_stats.overflow): a tuning and test hook. */
+int pt_bh_set_stack_limit(pt_ctx *ctx, int ranges);
 /* Counters of the last Barnes-Hut call (synchronises the context's stream). */
 int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out);
 /* Copies the last tree in depth-first preorder (rows >= stats.nodes): per node

@@ -37,7 +37,7 @@ class BhStats(ctypes.Structure):
                 ("leaves", ctypes.c_uint64), ("interactions", ctypes.c_uint64),
                 ("visits", ctypes.c_uint64), ("warps", ctypes.c_uint64),
                 ("max_stack", ctypes.c_uint64), ("overflow", ctypes.c_uint64),
-                ("learned", ctypes.c_uint64)]
+                ("learned", ctypes.c_uint64), ("cell_interactions", ctypes.c_uint64)]
 
 _NAMES = {PT_ERR_INVALID: "PT_ERR_INVALID", PT_ERR_CUDA: "PT_ERR_CUDA", PT_ERR_OOM: "PT_ERR_OOM",
           PT_ERR_CAPACITY: "PT_ERR_CAPACITY", PT_ERR_TIMEOUT: "PT_ERR_TIMEOUT",
@@ -88,6 +88,7 @@ def _declare(L):
                                                   ctypes.c_float, ctypes.c_float, ctypes.c_uint32,
                                                   c_ptr]),
         "pt_bh_last_stats": (ctypes.c_int, [c_ptr, ctypes.POINTER(BhStats)]),
+        "pt_bh_set_stack_limit": (ctypes.c_int, [c_ptr, ctypes.c_int]),
         "pt_bh_export_tree": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_ptr, c_size]),
         "pt_ctx_set_timing": (ctypes.c_int, [c_ptr, ctypes.c_int]),
         "pt_mlp_init": (ctypes.c_int, [c_ptr, ctypes.c_uint64]),

@@ -65,6 +65,7 @@ struct State {
     DevBuf aff_h, src_h;  // staging for the host-pointer entry point
     DevBuf lrec, lgroup, lnext, lpart, lhead, lcentre, lused;  // learned-correction records
     int lcap = 0;                     // record chunks allocated
+    int stack_cap = 0;                // group-walk stack ranges per warp in use (0 = all)
     const uint32_t *mlp_w = nullptr;  // learned correction: packed BF16 weights (owned by the MLP state)
     const float *mlp_b = nullptr;     // and its bias block
     float theta_inner = 0.5f;
@@ -480,21 +481,16 @@ __global__ void cell_moments_level(int L, const int *__restrict__ levels, const 
 
 // ---- walk ------------------------------------------------------------------
 
+// The reference's per-body walk (sequential.rs) for this lane's target p, the cursor
+// being the warp minimum of the lanes' next nodes: all 32 lanes take part. Adds the
+// accepted nodes' accelerations to (ax, ay, az) and counts them.
 template <bool QUAD>
-__global__ void __launch_bounds__(WALK_THREADS)
-    bh_walk(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
-            const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
-            const float4 *__restrict__ sbody, const int *__restrict__ counters, float th2, float eps2,
-            float *__restrict__ out, unsigned long long *__restrict__ stats) {
-    const int lane = threadIdx.x & 31;
-    const int t = blockIdx.x * WALK_THREADS + threadIdx.x;
-    if ((t & ~31) >= n_aff) return;  // whole warp past the end
-    const bool valid = t < n_aff;
-    const int T = counters[1];
-    const float4 p = valid ? tbody[t] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float ax = 0.f, ay = 0.f, az = 0.f;
+__device__ __forceinline__ void lane_walk(float4 p, bool valid, int T, const float4 *__restrict__ nodeA,
+                                          const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
+                                          const float4 *__restrict__ sbody, float th2, float eps2, float &ax,
+                                          float &ay, float &az, unsigned &nacc, unsigned &nvisit,
+                                          unsigned &ncell) {
     int resume = valid ? 0 : T;
-    unsigned nacc = 0, nvisit = 0;
     int node = 0;
     while (node < T) {
         const float4 A = __ldg(nodeA + node);
@@ -554,11 +550,29 @@ __global__ void __launch_bounds__(WALK_THREADS)
                     }
                 }
                 ++nacc;
+                ncell += B.z < 0;
                 next = resume = B.y;
             }
         }
         node = __reduce_min_sync(0xffffffffu, next);
     }
+}
+
+template <bool QUAD>
+__global__ void __launch_bounds__(WALK_THREADS)
+    bh_walk(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
+            const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
+            const float4 *__restrict__ sbody, const int *__restrict__ counters, float th2, float eps2,
+            float *__restrict__ out, unsigned long long *__restrict__ stats) {
+    const int lane = threadIdx.x & 31;
+    const int t = blockIdx.x * WALK_THREADS + threadIdx.x;
+    if ((t & ~31) >= n_aff) return;  // whole warp past the end
+    const bool valid = t < n_aff;
+    const int T = counters[1];
+    const float4 p = valid ? tbody[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    unsigned nacc = 0, nvisit = 0, ncell = 0;
+    lane_walk<QUAD>(p, valid, T, nodeA, nodeB, nodeQ, sbody, th2, eps2, ax, ay, az, nacc, nvisit, ncell);
     if (valid) {
         const uint32_t o = tidx[t];
         out[3 * size_t(o) + 0] = ax;
@@ -566,16 +580,18 @@ __global__ void __launch_bounds__(WALK_THREADS)
         out[3 * size_t(o) + 2] = az;
     }
     if (stats) {
-        unsigned long long a = nacc, v = nvisit;
+        unsigned long long a = nacc, v = nvisit, c = ncell;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             a += __shfl_down_sync(0xffffffffu, a, o);
             v += __shfl_down_sync(0xffffffffu, v, o);
+            c += __shfl_down_sync(0xffffffffu, c, o);
         }
         if (lane == 0) {
             atomicAdd(stats + 0, a);
             atomicAdd(stats + 1, v);
             atomicAdd(stats + 2, 1ull);
+            atomicAdd(stats + 5, c);
         }
     }
 }
@@ -588,7 +604,14 @@ __global__ void __launch_bounds__(WALK_THREADS)
 // shared-memory interaction list. A full list is evaluated densely: every lane runs its target
 // against all entries, two entries per packed f32x2 instruction.
 constexpr int GW_WARPS = 4;
-constexpr int GW_STACK = 768;  // sibling ranges per warp (~32 per tree level are live)
+// Sibling ranges per warp. A pop takes fewer nodes when the stack is nearly full, and
+// a warp that still runs out takes the per-body walk (counted, not an error). At
+// N = 4M bulge+disk the deepest stack seen is 239 ranges at theta 0.5 and 379 at 0.3.
+// 384 ranges with 80 registers keep 6 CTAs (24 warps) resident per SM.
+#ifndef PT_GW_STACK
+#define PT_GW_STACK 384
+#endif
+constexpr int GW_STACK = PT_GW_STACK;
 
 // Interaction lists in structure-of-arrays form. Cells carry their quadrupole
 // when QUAD; single bodies never need one.
@@ -610,7 +633,7 @@ __device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, f2 px, f
         __syncwarp();
         ++cnt;
     }
-    const f2 half5 = pk2(2.5f, 2.5f);
+    const f2 mhalf5 = pk2(-2.5f, -2.5f);
 #pragma unroll 2
     for (int e = 0; e < cnt; e += 2) {
         const f2 dx = sub2(*reinterpret_cast<const f2 *>(&Lst.f[0][e]), px);
@@ -628,26 +651,30 @@ __device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, f2 px, f
         const f2 inv = pk2(i0, i1);
         const f2 inv2 = mul2(inv, inv);
         const f2 sc = mul2(mul2(m, inv), inv2);
-        ax = fma2(dx, sc, ax);
-        ay = fma2(dy, sc, ay);
-        az = fma2(dz, sc, az);
         if constexpr (NF == 10) {
-            const f2 qxx = *reinterpret_cast<const f2 *>(&Lst.f[4][e]);
-            const f2 qxy = *reinterpret_cast<const f2 *>(&Lst.f[5][e]);
-            const f2 qxz = *reinterpret_cast<const f2 *>(&Lst.f[6][e]);
-            const f2 qyy = *reinterpret_cast<const f2 *>(&Lst.f[7][e]);
-            const f2 qyz = *reinterpret_cast<const f2 *>(&Lst.f[8][e]);
-            const f2 qzz = *reinterpret_cast<const f2 *>(&Lst.f[9][e]);
-            const f2 qx = fma2(qxx, dx, fma2(qxy, dy, mul2(qxz, dz)));
-            const f2 qy = fma2(qxy, dx, fma2(qyy, dy, mul2(qyz, dz)));
-            const f2 qz = fma2(qxz, dx, fma2(qyz, dy, mul2(qzz, dz)));
-            const f2 dqd = fma2(dx, qx, fma2(dy, qy, mul2(dz, qz)));
+            // entries hold the negated quadrupole N = -Q: with u = N d and c = d.u,
+            // a += d (m / r^3 + 2.5 (d.Q.d) / r^7) - (Q d) / r^5
+            //    = d (sc - 2.5 c / r^7) + u / r^5
+            const f2 nxx = *reinterpret_cast<const f2 *>(&Lst.f[4][e]);
+            const f2 nxy = *reinterpret_cast<const f2 *>(&Lst.f[5][e]);
+            const f2 nxz = *reinterpret_cast<const f2 *>(&Lst.f[6][e]);
+            const f2 nyy = *reinterpret_cast<const f2 *>(&Lst.f[7][e]);
+            const f2 nyz = *reinterpret_cast<const f2 *>(&Lst.f[8][e]);
+            const f2 nzz = *reinterpret_cast<const f2 *>(&Lst.f[9][e]);
+            const f2 ux = fma2(nxx, dx, fma2(nxy, dy, mul2(nxz, dz)));
+            const f2 uy = fma2(nxy, dx, fma2(nyy, dy, mul2(nyz, dz)));
+            const f2 uz = fma2(nxz, dx, fma2(nyz, dy, mul2(nzz, dz)));
+            const f2 c = fma2(dx, ux, fma2(dy, uy, mul2(dz, uz)));
             const f2 inv5 = mul2(mul2(inv2, inv2), inv);
-            const f2 c7 = mul2(mul2(dqd, half5), mul2(inv5, inv2));
-            const f2 ninv5 = sub2(pk2(0.f, 0.f), inv5);
-            ax = fma2(c7, dx, fma2(qx, ninv5, ax));
-            ay = fma2(c7, dy, fma2(qy, ninv5, ay));
-            az = fma2(c7, dz, fma2(qz, ninv5, az));
+            const f2 k = mul2(c, mul2(inv2, mhalf5));
+            const f2 s2 = fma2(inv5, k, sc);
+            ax = fma2(dx, s2, fma2(inv5, ux, ax));
+            ay = fma2(dy, s2, fma2(inv5, uy, ay));
+            az = fma2(dz, s2, fma2(inv5, uz, az));
+        } else {
+            ax = fma2(dx, sc, ax);
+            ay = fma2(dy, sc, ay);
+            az = fma2(dz, sc, az);
         }
     }
     __syncwarp();
@@ -751,18 +778,20 @@ __global__ void bh_learned_apply(LearnedRecords L, const uint32_t *__restrict__ 
     out[3 * size_t(o) + 2] += cz;
 }
 
+#ifndef PT_GW_MINB
+#define PT_GW_MINB 6  // CTAs per SM the register budget is set for
+#endif
 template <bool QUAD, bool GUARD, bool LEARNED>
-__global__ void __launch_bounds__(32 * GW_WARPS)
+__global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
     bh_walk_group(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
                   const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
                   const float4 *__restrict__ nodeG, const float4 *__restrict__ sbody, const int *__restrict__ counters,
                   float th2, float th_in2, LearnedRecords LR, float eps2, float *__restrict__ out,
-                  unsigned long long *__restrict__ stats, int *__restrict__ err) {
+                  unsigned long long *__restrict__ stats, int *__restrict__ err, int stack_cap) {
     constexpr int NFC = QUAD ? 10 : 4;
     using CellList = IList<NFC, 96>;
     using BodyList = IList<4, 128>;
     __shared__ int2 s_stack[GW_WARPS][GW_STACK];
-    __shared__ float4 s_tgt[GW_WARPS][32];
     __shared__ __align__(16) CellList s_cells[GW_WARPS];
     __shared__ __align__(16) BodyList s_bodies[GW_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -777,12 +806,8 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     CellList &Lc = s_cells[warp];
     BodyList &Lb = s_bodies[warp];
 
-    // the warp's targets, read back as shared-memory broadcasts by the opening test
-    s_tgt[warp][lane] = p;
-    const float4 *tgt = s_tgt[warp];
-    __syncwarp();
-    // and their bounding box: a cell whose centre of mass is far enough from the box
-    // is accepted by every target, which spares the 32-target test
+    // the bounding box of the warp's targets: it settles most opening decisions
+    // without the per-target vote
     float mn0 = p.x, mn1 = p.y, mn2 = p.z, mx0 = p.x, mx1 = p.y, mx2 = p.z;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -822,11 +847,11 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     if (lane == 0) stack[0] = make_int2(0, T);
     __syncwarp();
     int S = 1, Nc = 0, Nb = 0, maxS = 1;
-    unsigned long long entries = 0, visits = 0;
+    unsigned long long entries = 0, visits = 0, centries = 0;
     bool failed = false;
     while (S > 0) {
         // each pop pushes at most two ranges: never more than the room left
-        const int k = min(min(32, S), max(1, (GW_STACK - S) / 2));
+        const int k = min(min(32, S), max(1, (stack_cap - S) / 2));
         const bool have = lane < k;
         const int2 range = have ? stack[S - 1 - lane] : make_int2(0, 0);
         __syncwarp();
@@ -840,32 +865,46 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
             A = __ldg(nodeA + node);
             B = __ldg(nodeB + node);
         }
-        // Open iff the per-body rule opens for at least one target: the smallest
-        // nonzero d^2 over the warp's targets decides (targets with d^2 == 0 skip the
-        // cell under that rule and do not vote). Cells accepted even from the nearest
-        // point of the targets' box are settled without the per-target loop.
-        bool maybe = false;
+        // Open iff the per-body rule opens for at least one target: some target with
+        // nonzero d^2 (targets with d^2 == 0 skip the cell under that rule and do not
+        // vote) and theta^2 d^2 < w^2. Settled without a vote: cells accepted even from
+        // the nearest point of the targets' box (maybe false) and cells opened even
+        // from its farthest corner (sure). Rounding is monotone, so these box bounds
+        // never contradict the per-target values. The remaining cells are voted on one
+        // at a time: each lane tests its own target, a ballot collects the votes.
+        bool maybe = false, sure = false;
+        float w = 0.f;
         if (have && B.z < 0) {
-            const float w = __int_as_float(B.x);
+            w = __int_as_float(B.x);
             const float e0 = fmaxf(fmaxf(mn0 - A.x, A.x - mx0), 0.f);
             const float e1 = fmaxf(fmaxf(mn1 - A.y, A.y - mx1), 0.f);
             const float e2b = fmaxf(fmaxf(mn2 - A.z, A.z - mx2), 0.f);
             maybe = (LEARNED ? th_in2 : th2) * fmaf(e0, e0, fmaf(e1, e1, e2b * e2b)) < w * w;
+            const float f0 = fmaxf(A.x - mn0, mx0 - A.x);
+            const float f1 = fmaxf(A.y - mn1, mx1 - A.y);
+            const float f2b = fmaxf(A.z - mn2, mx2 - A.z);
+            const float dmax2 = fmaf(f0, f0, fmaf(f1, f1, f2b * f2b));
+            sure = dmax2 > 0.0f && th2 * dmax2 < w * w;  // dmax2 > 0: some target is off the centre of mass
         }
+        open = sure;
         bool marginal = false;
-        if (__any_sync(0xffffffffu, maybe)) {
-            float dmin = INFINITY;
-#pragma unroll 8
-            for (int b = 0; b < 32; ++b) {
-                const float4 q = tgt[b];
-                const float dx = A.x - q.x, dy = A.y - q.y, dz = A.z - q.z;
-                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                dmin = (d2 > 0.0f) ? fminf(dmin, d2) : dmin;
+        unsigned amb = __ballot_sync(0xffffffffu, maybe && !sure);
+        while (amb) {
+            const int j = __ffs(amb) - 1;
+            amb &= amb - 1;
+            const float cx = __shfl_sync(0xffffffffu, A.x, j);
+            const float cy = __shfl_sync(0xffffffffu, A.y, j);
+            const float cz = __shfl_sync(0xffffffffu, A.z, j);
+            const float cw = __shfl_sync(0xffffffffu, w, j);
+            const float dx = cx - p.x, dy = cy - p.y, dz = cz - p.z;
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const unsigned vo = __ballot_sync(0xffffffffu, d2 > 0.0f && th2 * d2 < cw * cw);
+            if (lane == j) open = vo != 0u;
+            if (LEARNED) {
+                // accepted by every target, but opened by one at theta_inner
+                const unsigned vi = __ballot_sync(0xffffffffu, d2 > 0.0f && th_in2 * d2 < cw * cw);
+                if (lane == j) marginal = vo == 0u && vi != 0u && A.w > 0.0f;
             }
-            const float w = __int_as_float(B.x);
-            open = maybe && th2 * dmin < w * w;
-            // accepted by every target, but opened by one at theta_inner
-            if (LEARNED) marginal = maybe && !open && th_in2 * dmin < w * w && A.w > 0.0f;
         }
         if (LEARNED) {
             const unsigned mm = __ballot_sync(0xffffffffu, marginal);
@@ -903,12 +942,12 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
             if (lane >= o) incl += v;
         }
         const int total = __shfl_sync(0xffffffffu, incl, 31);
-        int w = S + incl - np;
-        if (w + np > GW_STACK) {
+        int slot = S + incl - np;
+        if (slot + np > stack_cap) {
             failed = true;  // never written out of bounds
         } else {
-            if (rest) stack[w++] = make_int2(B.y, range.y);
-            if (open) stack[w++] = make_int2(node + 1, B.y);  // children on top: popped first
+            if (rest) stack[slot++] = make_int2(B.y, range.y);
+            if (open) stack[slot++] = make_int2(node + 1, B.y);  // children on top: popped first
         }
         if (__any_sync(0xffffffffu, failed)) {
             failed = true;
@@ -926,6 +965,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
         if (Nc + nc1 > CellList::CAP) {
             eval_list<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
             entries += Nc;
+            centries += Nc;
             Nc = 0;
         }
         if (cellacc) {
@@ -934,15 +974,15 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
             Lc.f[1][e] = A.y;
             Lc.f[2][e] = A.z;
             Lc.f[3][e] = A.w;
-            if constexpr (QUAD) {
+            if constexpr (QUAD) {  // negated: the list evaluation's form
                 const float4 q0 = __ldg(nodeQ + 2 * node);
                 const float4 q1 = __ldg(nodeQ + 2 * node + 1);
-                Lc.f[4][e] = q0.x;
-                Lc.f[5][e] = q0.y;
-                Lc.f[6][e] = q0.z;
-                Lc.f[7][e] = q0.w;
-                Lc.f[8][e] = q1.x;
-                Lc.f[9][e] = q1.y;
+                Lc.f[4][e] = -q0.x;
+                Lc.f[5][e] = -q0.y;
+                Lc.f[6][e] = -q0.z;
+                Lc.f[7][e] = -q0.w;
+                Lc.f[8][e] = -q1.x;
+                Lc.f[9][e] = -q1.y;
             }
         }
         Nc += nc1;
@@ -990,35 +1030,53 @@ __global__ void __launch_bounds__(32 * GW_WARPS)
     eval_list<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
     eval_list<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
     entries += Nc + Nb;
-    if (LEARNED) {
-        if (chunk >= 0 && chunk < LR.cap)
-            for (int i = fill + lane; i < LCHUNK; i += 32) LR.rec[size_t(chunk) * LCHUNK + i] = -1;
-        if (lane == 0) {
-            if (chunk < 0) LR.head[group] = -1;
-            LR.centre[group] = make_float4(gcx, gcy, gcz, 0.f);
-        }
-    }
+    centries += Nc;
     float x0, x1, y0, y1, z0, z1;
     upk2(ax, x0, x1);
     upk2(ay, y0, y1);
     upk2(az, z0, z1);
+    float rx = x0 + x1, ry = y0 + y1, rz = z0 + z1;
+    const unsigned long long nvalid = unsigned(min(32, n_aff - group * 32));
+    unsigned long long s_acc = entries * nvalid, s_vis = visits * nvalid, s_cell = centries * nvalid;
     if (failed) {
-        x0 = y0 = z0 = __int_as_float(0x7fc00000);
-        if (lane == 0) atomicOr(err, 1);
+        // The stack ran out (failed is warp-uniform): this warp's targets take the
+        // reference's per-body walk instead, which needs no stack.
+        rx = ry = rz = 0.f;
+        unsigned na = 0, nv = 0, nc = 0;
+        lane_walk<QUAD>(p, valid, T, nodeA, nodeB, nodeQ, sbody, th2, eps2, rx, ry, rz, na, nv, nc);
+        unsigned long long a = na, v = nv, c = nc;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            v += __shfl_xor_sync(0xffffffffu, v, o);
+            c += __shfl_xor_sync(0xffffffffu, c, o);
+        }
+        s_acc = a;
+        s_vis = v;
+        s_cell = c;
+    }
+    if (LEARNED) {
+        if (chunk >= 0 && chunk < LR.cap)
+            for (int i = fill + lane; i < LCHUNK; i += 32) LR.rec[size_t(chunk) * LCHUNK + i] = -1;
+        if (lane == 0) {
+            if (chunk < 0 || failed) LR.head[group] = -1;  // a fallback warp keeps the plain result
+            LR.centre[group] = make_float4(gcx, gcy, gcz, 0.f);
+        }
     }
     if (valid) {
         const uint32_t o = tidx[t];
-        out[3 * size_t(o) + 0] = x0 + x1;
-        out[3 * size_t(o) + 1] = y0 + y1;
-        out[3 * size_t(o) + 2] = z0 + z1;
+        out[3 * size_t(o) + 0] = rx;
+        out[3 * size_t(o) + 1] = ry;
+        out[3 * size_t(o) + 2] = rz;
     }
     if (stats && lane == 0) {
-        const unsigned long long nvalid = unsigned(min(32, n_aff - group * 32));
-        atomicAdd(stats + 0, entries * nvalid);
-        atomicAdd(stats + 1, visits * nvalid);
+        atomicAdd(stats + 0, s_acc);
+        atomicAdd(stats + 1, s_vis);
         if (LEARNED) atomicAdd(stats + 4, learned);
+        atomicAdd(stats + 5, s_cell);
         atomicAdd(stats + 2, 1ull);
         atomicMax(stats + 3, (unsigned long long)maxS);
+        if (failed) atomicAdd(stats + 6, 1ull);
     }
 }
 
@@ -1026,7 +1084,7 @@ using WalkKernel = void (*)(const float4 *, const uint32_t *, int, const float4 
                             const float4 *, const int *, float, float, float *, unsigned long long *);
 using GroupKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
                              const float4 *, const float4 *, const int *, float, float, LearnedRecords, float,
-                             float *, unsigned long long *, int *);
+                             float *, unsigned long long *, int *, int);
 
 static WalkKernel walk_kernel(bool quad) { return quad ? bh_walk<true> : bh_walk<false>; }
 
@@ -1083,7 +1141,7 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
     PT_TRY(ensure_buf(ctx, S.nodeG, sizeof(float4) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.nodeR, sizeof(int2) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.mom, sizeof(Moments) * 2 * N));
-    PT_TRY(ensure_buf(ctx, S.counters, sizeof(unsigned long long) * 8));
+    PT_TRY(ensure_buf(ctx, S.counters, sizeof(unsigned long long) * 16));
 
     const int nb = std::min(1024, blocks(n));
     bbox_partial<<<nb, 256, 0, st>>>(d_src, n, as<float>(S.box_part));
@@ -1181,11 +1239,12 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
         tbody = as<float4>(S.tbody);
         tidx = as<uint32_t>(S.tidx);
     }
-    // counters: int[4] = {leaves, nodes, cells, error} then u64[4] = {interactions,
-    // visits, warps, max group stack}
+    // counters: int[4] = {leaves, nodes, cells, error} then u64[7] = {interactions,
+    // visits, warps, max group stack, learned records, cell interactions, warps that
+    // fell back to the per-body walk}
     unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 2;
     int *err = as<int>(S.counters) + 3;
-    PT_CUDA(cudaMemsetAsync(stats, 0, 5 * sizeof(unsigned long long), st));
+    PT_CUDA(cudaMemsetAsync(stats, 0, 7 * sizeof(unsigned long long), st));
     PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     const float th2 = theta * theta;
     const float eps2 = softening * softening;
@@ -1215,7 +1274,7 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
             group_kernel(quad, eps2 == 0.0f, learned)<<<(groups + GW_WARPS - 1) / GW_WARPS, 32 * GW_WARPS, 0, st>>>(
                 tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.nodeG),
                 as<float4>(S.sbody), as<int>(S.counters), th2, S.theta_inner * S.theta_inner, LR, eps2, d_out, stats,
-                err);
+                err, S.stack_cap > 0 ? S.stack_cap : GW_STACK);
             PT_TRY(check_launch(ctx, "bh_walk_group"));
             // Outside stream capture the record count is checked and the walk rerun
             // with room for all records; inside, an overflow sets error bit 2.
@@ -1226,7 +1285,7 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
             if (used <= S.lcap) break;
             S.lcap = used + used / 4;
             PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-            PT_CUDA(cudaMemsetAsync(stats, 0, 5 * sizeof(unsigned long long), st));
+            PT_CUDA(cudaMemsetAsync(stats, 0, 7 * sizeof(unsigned long long), st));
         }
         if (learned) {
             bh_learned_eval<<<ctx->sm_count * 4, 128, 0, st>>>(LR, as<float4>(S.nodeA), as<float4>(S.nodeQ),
@@ -1357,10 +1416,21 @@ int pt_bh_accel_f32(pt_ctx *ctx, const float *aff, size_t n_aff, const float *sr
     if (n_src) PT_CUDA(cudaMemcpyAsync(&err, static_cast<int *>(S->counters.ptr) + 3, sizeof(int),
                                        cudaMemcpyDeviceToHost, st));
     PT_CUDA(cudaStreamSynchronize(st));
-    if (err & 1)
-        return set_error(PT_ERR_CAPACITY, "pt_bh_accel_f32: a group walk ran out of stack; its bodies are NaN");
     if (err & 2)
         return set_error(PT_ERR_CAPACITY, "pt_bh_accel_f32: learned-correction records overflowed");
+    return PT_OK;
+}
+
+int pt_bh_set_stack_limit(pt_ctx *ctx, int ranges) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_set_stack_limit: ctx is NULL");
+    if (ranges > bh::GW_STACK || (ranges > 0 && ranges < 2))
+        return set_error(PT_ERR_INVALID, "pt_bh_set_stack_limit: %d outside [2, %d] (0 = %d)", ranges,
+                         bh::GW_STACK, bh::GW_STACK);
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    S->stack_cap = ranges;
     return PT_OK;
 }
 
@@ -1371,19 +1441,20 @@ int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out) {
     auto *S = static_cast<bh::State *>(ctx->bh);
     if (!S || !S->counters.ptr) return set_error(PT_ERR_INVALID, "pt_bh_last_stats: no Barnes-Hut call yet");
     PT_CUDA(cudaSetDevice(ctx->device));
-    unsigned long long h[8];
+    unsigned long long h[9];
     PT_CUDA(cudaMemcpyAsync(h, S->counters.ptr, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
     PT_CUDA(cudaStreamSynchronize(ctx->stream));
     const int *hi = reinterpret_cast<const int *>(h);
     out->leaves = uint64_t(hi[0]);
     out->nodes = uint64_t(hi[1]);
     out->cells = uint64_t(hi[2]);
-    out->overflow = uint64_t(hi[3]);
+    out->overflow = h[8];
     out->interactions = h[2];
     out->visits = h[3];
     out->warps = h[4];
     out->max_stack = h[5];
     out->learned = h[6];
+    out->cell_interactions = h[7];
     return PT_OK;
 }
 

@@ -124,10 +124,32 @@ def test_quadrupole_and_group_reduce_error(res, oracle, theta):
 
 def test_theta0_is_brute_force(res, oracle):
     b = ics.plummer(5000, seed=26)["bodies"]
-    got = cuda.BarnesHut(0.0, res, AccelerationSoftened(0.01)).compute(b)
+    m = cuda.BarnesHut(0.0, res, AccelerationSoftened(0.01))
+    got = m.compute(b)
     ref = oracle.bf_f64(b, b, 0.01, True)
     r = rel(got, ref)
     assert np.median(r) < 2e-6 and r.max() < 1e-4
+    assert m.stats()["cell_interactions"] == 0   # every cell opened
+
+
+@pytest.mark.parametrize("group", [False, True])
+def test_cell_interaction_counts(res, group):
+    """Accepted cells are a part of the accepted nodes, grow as theta loosens, and
+    do not depend on whether the quadrupole term is evaluated."""
+    b = ics.plummer(20000, seed=27)["bodies"]
+    prev = 0
+    for theta in (0.3, 0.6, 1.0):
+        st = {}
+        for quad in (False, True):
+            m = cuda.BarnesHut(theta, res, AccelerationSoftened(0.01), quadrupole=quad, group=group)
+            m.compute(b)
+            st[quad] = m.stats()
+        assert st[False]["cell_interactions"] == st[True]["cell_interactions"]
+        assert st[False]["interactions"] == st[True]["interactions"]
+        c, a = st[True]["cell_interactions"], st[True]["interactions"]
+        assert 0 < c < a
+        assert c / a > prev
+        prev = c / a
 
 
 @pytest.mark.parametrize("group", [False, True])
@@ -229,3 +251,39 @@ def test_group_walk_eps0_and_separate_targets(res, oracle):
     ref64 = oracle.bf_f64(aff, src, 0.0, True)
     ref = oracle.bh_f32(aff, src, 0.4, 0.0, True)
     assert np.percentile(rel(got, ref64), 95) <= np.percentile(rel(ref, ref64), 95) * 1.01 + 1e-6
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_group_walk_stack_fallback(res, oracle, learned):
+    """A warp whose shared-memory stack runs out takes the per-body walk. With room
+    for 2 ranges every warp does: the result is the per-body walk's, bit for bit (and
+    the learned correction is dropped for those warps). With room for 48 some warps
+    do, and the error stays within the per-body walk's."""
+    from particular_gb300 import learned as LM
+    b = ics.plummer(20000, seed=46)["bodies"]
+    ref64 = oracle.bf_f64(b[::4], b, 0.01, True)
+    lane = cuda.BarnesHut(0.6, res, AccelerationSoftened(0.01), quadrupole=True).compute(b)
+    if learned:
+        LM.init(res, seed=2)
+    m = cuda.BarnesHut(0.6, res, AccelerationSoftened(0.01), quadrupole=True, group=True, learned=learned)
+    L = N.lib()
+    try:
+        N.check(L.pt_bh_set_stack_limit(res.handle, 2))
+        got = m.compute(b)
+        st = m.stats()
+        assert st["overflow"] == st["warps"] == (20000 + 31) // 32
+        np.testing.assert_array_equal(got, lane)
+        N.check(L.pt_bh_set_stack_limit(res.handle, 48))
+        got = m.compute(b)
+        st = m.stats()
+        assert 0 < st["overflow"] < st["warps"], st
+        assert np.isfinite(got).all()
+        e, e_lane = rel(got[::4], ref64), rel(lane[::4], ref64)
+        for q in (50, 95):
+            assert np.percentile(e, q) <= np.percentile(e_lane, q) * 1.01 + 1e-6
+        with pytest.raises(N.CudaError):
+            N.check(L.pt_bh_set_stack_limit(res.handle, 1 << 20))
+    finally:
+        N.check(L.pt_bh_set_stack_limit(res.handle, 0))
+    m.compute(b)
+    assert m.stats()["overflow"] == 0
