@@ -209,7 +209,7 @@ class BarnesHutWorkload:
     bar = 1e-3
     # (theta, flags) candidates: quadrupole + group opening; the reference's own
     # monopole per-body walk at theta 0.5 is measured alongside as "plain".
-    ladder = [(0.45, 3), (0.5, 3), (0.55, 3), (0.6, 3)]
+    ladder = [(0.45, 3), (0.5, 3), (0.52, 3), (0.55, 3), (0.6, 3)]
 
     def __init__(self, n=4194304, softening=0.01, sample=2048):
         from particular_gb300 import ics
