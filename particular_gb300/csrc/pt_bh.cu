@@ -417,63 +417,70 @@ __global__ void cell_level_scatter(const int *__restrict__ counters, const int *
     if (cell) by_level[base[L] + local] = k;
 }
 
-// A child's moments: single-body leaves are read straight from nodeA (the body).
-__device__ __forceinline__ Moments load_child(int c, const Moments *__restrict__ mom, const float4 *__restrict__ nodeA,
-                                              const int4 *__restrict__ nodeB) {
-    const int4 b = nodeB[c];
-    if (b.z >= 0 && b.w == 1) {
-        const float4 a = nodeA[c];
-        Moments m{};
-        m.m = a.w;
-        m.cx = a.x;
-        m.cy = a.y;
-        m.cz = a.z;
-        m.count = 1.0;
-        return m;
-    }
-    return mom[c];
-}
-
-// Combines every cell of octree level L from its children (levels > L: done).
+// Combines every cell of octree level L from its children (levels > L: done), in one
+// pass over the children: sums about the cell's geometric centre G (offsets within
+// a cell width, no cancellation), then moved to the centre of mass C by the
+// parallel-axis rule S_C = S_G - P P^T / M with P = sum m (c - G) = M (C - G).
 __global__ void cell_moments_level(int L, const int *__restrict__ levels, const int *__restrict__ by_level,
                                    const int *__restrict__ pre, const int4 *__restrict__ nodeB,
-                                   Moments *__restrict__ mom, float4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
+                                   const float4 *__restrict__ nodeG, Moments *__restrict__ mom,
+                                   float4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
     const int begin = levels[LEVELS + 1 + L], end_l = begin + levels[L];
     for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end_l; i += gridDim.x * blockDim.x) {
         const int pv = pre[by_level[i]];
         const int end = nodeB[pv].y;
+        const float4 g = nodeG[pv];
+        const double gx = g.x, gy = g.y, gz = g.z;
         Moments m{};
-        double sx = 0, sy = 0, sz = 0, ux = 0, uy = 0, uz = 0;
-        for (int c = pv + 1; c < end; c = nodeB[c].y) {
-            const Moments cm = load_child(c, mom, nodeA, nodeB);
+        double px = 0, py = 0, pz = 0, ux = 0, uy = 0, uz = 0;
+        for (int c = pv + 1; c < end;) {
+            const int4 cb = nodeB[c];
+            Moments cm;
+            if (cb.z >= 0 && cb.w == 1) {  // a single body: read from nodeA
+                const float4 a = nodeA[c];
+                cm = Moments{};
+                cm.m = a.w;
+                cm.cx = a.x;
+                cm.cy = a.y;
+                cm.cz = a.z;
+                cm.count = 1.0;
+            } else {
+                cm = mom[c];
+            }
+            const double dx = cm.cx - gx, dy = cm.cy - gy, dz = cm.cz - gz;
             m.m += cm.m;
             m.count += cm.count;
-            sx += cm.m * cm.cx;
-            sy += cm.m * cm.cy;
-            sz += cm.m * cm.cz;
-            ux += cm.count * cm.cx;
-            uy += cm.count * cm.cy;
-            uz += cm.count * cm.cz;
+            const double mx = cm.m * dx, my = cm.m * dy, mz = cm.m * dz;
+            px += mx;
+            py += my;
+            pz += mz;
+            ux += cm.count * dx;
+            uy += cm.count * dy;
+            uz += cm.count * dz;
+            m.sxx += cm.sxx + mx * dx;
+            m.sxy += cm.sxy + mx * dy;
+            m.sxz += cm.sxz + mx * dz;
+            m.syy += cm.syy + my * dy;
+            m.syz += cm.syz + my * dz;
+            m.szz += cm.szz + mz * dz;
+            c = cb.y;
         }
         if (m.m != 0.0) {
             const double inv = 1.0 / m.m;
-            m.cx = sx * inv;
-            m.cy = sy * inv;
-            m.cz = sz * inv;
-        } else {
-            m.cx = ux / m.count;
-            m.cy = uy / m.count;
-            m.cz = uz / m.count;
-        }
-        for (int c = pv + 1; c < end; c = nodeB[c].y) {
-            const Moments cm = load_child(c, mom, nodeA, nodeB);
-            const double dx = cm.cx - m.cx, dy = cm.cy - m.cy, dz = cm.cz - m.cz;
-            m.sxx += cm.sxx + cm.m * dx * dx;
-            m.sxy += cm.sxy + cm.m * dx * dy;
-            m.sxz += cm.sxz + cm.m * dx * dz;
-            m.syy += cm.syy + cm.m * dy * dy;
-            m.syz += cm.syz + cm.m * dy * dz;
-            m.szz += cm.szz + cm.m * dz * dz;
+            const double ox = px * inv, oy = py * inv, oz = pz * inv;  // C - G
+            m.cx = gx + ox;
+            m.cy = gy + oy;
+            m.cz = gz + oz;
+            m.sxx -= px * ox;
+            m.sxy -= px * oy;
+            m.sxz -= px * oz;
+            m.syy -= py * oy;
+            m.syz -= py * oz;
+            m.szz -= pz * oz;
+        } else {  // massless: plain mean of the bodies (gravity/impls/mod.rs:127-129)
+            m.cx = gx + ux / m.count;
+            m.cy = gy + uy / m.count;
+            m.cz = gz + uz / m.count;
         }
         store_cell(m, pv, mom, nodeA, nodeQ);
     }
@@ -1253,8 +1260,8 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
     const int lvl_grid = std::max(1, std::min(blocks(n), 8 * ctx->sm_count));
     for (int L = LEVELS - 1; L >= 0; --L) {
         cell_moments_level<<<lvl_grid, 256, 0, st>>>(L, levels, as<int>(S.by_level), as<int>(S.pre),
-                                                     as<int4>(S.nodeB), as<Moments>(S.mom), as<float4>(S.nodeA),
-                                                     as<float4>(S.nodeQ));
+                                                     as<int4>(S.nodeB), as<float4>(S.nodeG), as<Moments>(S.mom),
+                                                     as<float4>(S.nodeA), as<float4>(S.nodeQ));
         PT_TRY(check_launch(ctx, "cell_moments_level"));
     }
     S.last_n_src = n;

@@ -47,6 +47,33 @@ def oracle_preorder(tree):
     return np.array(out), e
 
 
+@pytest.mark.parametrize("kind,n", [("plummer", 3000), ("bulge_disk", 4000)])
+def test_cell_quadrupoles_match_fp64(res, oracle, kind, n):
+    """Every cell's traceless quadrupole (about its centre of mass) against FP64 sums
+    over the cell's bodies; the tolerance is relative to the cell's M w^2."""
+    b = {"plummer": lambda: ics.plummer(n, seed=28)["bodies"],
+         "bulge_disk": lambda: ics.bulge_disk(n, seed=29)["bodies"]}[kind]()
+    m = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=True)
+    m.compute(b)
+    g = m.export_tree()
+    order, e = oracle_preorder(oracle.Tree(b))
+    internal = e["internal"][order].astype(bool)
+    rng, perm = e["range"][order][internal], e["perm"]
+    q = g["quad"][g["links"][:, 2] < 0].astype(np.float64)
+    w = g["width"][g["links"][:, 2] < 0].astype(np.float64)
+    bp = b[perm].astype(np.float64)
+    worst = 0.0
+    for j, (lo, cnt) in enumerate(rng):
+        x = bp[lo:lo + cnt]
+        M = x[:, 3].sum()
+        d = x[:, :3] - (x[:, :3] * x[:, 3:4]).sum(0) / M
+        r2 = (d * d).sum(1)
+        Q = 3 * np.einsum("n,ni,nj->ij", x[:, 3], d, d) - np.eye(3) * (x[:, 3] * r2).sum()
+        want = np.array([Q[0, 0], Q[0, 1], Q[0, 2], Q[1, 1], Q[1, 2], Q[2, 2]])
+        worst = max(worst, np.abs(q[j, :6] - want).max() / (M * w[j] ** 2))
+    assert worst < 1e-5, worst
+
+
 @pytest.mark.parametrize("kind,n", [("plummer", 3000), ("cube", 2000), ("bulge_disk", 4000)])
 def test_tree_matches_reference_orthtree(res, oracle, kind, n):
     b = {"plummer": lambda: ics.plummer(n, seed=21)["bodies"],
