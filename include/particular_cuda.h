@@ -99,6 +99,19 @@ int pt_bf_accel_f32_device(pt_ctx *ctx, const float *d_affected, size_t n_aff,
                            const float *d_affecting, size_t n_src, float softening, int checked,
                            uint32_t flags, float *d_out_xyz);
 
+/* cuda::BruteForce over glam DVec3 bodies: double[4] (x, y, z, mu) in, double[3] out.
+ * Replaces the f64 instantiation of the per-pair kernel (impl_acceleration_cpu_scalar!
+ * (DVec3, f64), particular/src/gravity/impls/glam.rs:234 over gravity/impls/mod.rs:
+ * 150-166) folded as sequential::BruteForce (sequential.rs:189-193): every operation
+ * IEEE-rounded in the reference's order, so results equal the reference's bit for bit.
+ * Synchronous, host buffers. */
+int pt_bf_accel_dvec3(pt_ctx *ctx, const double *affected, size_t n_aff, const double *affecting,
+                      size_t n_src, double softening, int checked, double *out_xyz);
+/* Same on device buffers (8-byte aligned), asynchronous on the context's stream. */
+int pt_bf_accel_dvec3_device(pt_ctx *ctx, const double *d_affected, size_t n_aff,
+                             const double *d_affecting, size_t n_src, double softening, int checked,
+                             double *d_out_xyz);
+
 /* FP64 brute force of the same formula on device buffers (f32 inputs widened to
  * f64, double accumulation): the error judge for the FP32 methods. It has no
  * counterpart in the reference, which reports no accuracy figures. */

@@ -31,6 +31,10 @@ def lib():
                                           ctypes.c_float, ctypes.c_int, _f32p, ctypes.c_int]
         L.oracle_bf_f64.argtypes = [_f32p, ctypes.c_size_t, _f32p, ctypes.c_size_t,
                                     ctypes.c_double, ctypes.c_int, _f64p, ctypes.c_int]
+        L.oracle_bf_dvec3.argtypes = [_f64p, ctypes.c_size_t, _f64p, ctypes.c_size_t,
+                                      ctypes.c_double, ctypes.c_int, _f64p, ctypes.c_int]
+        L.oracle_bf_pairs_f32.argtypes = [_f32p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_float, _f32p]
+        L.oracle_bf_pairs_f64.argtypes = [_f64p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_double, _f64p]
         L.oracle_bh_build.argtypes = [_f32p, ctypes.c_size_t, ctypes.c_int]
         L.oracle_bh_build.restype = ctypes.c_void_p
         L.oracle_tree_free.argtypes = [ctypes.c_void_p]
@@ -96,6 +100,37 @@ def bf_f64(targets, sources, softening=0.0, checked=True, threads=0):
     rc = lib().oracle_bf_f64(t, t.shape[0], s, s.shape[0], softening, int(checked), out, threads)
     if rc:
         raise RuntimeError(f"oracle_bf_f64 failed: {rc}")
+    return out
+
+
+def bf_dvec3(targets, sources, softening=0.0, checked=True, threads=0):
+    """sequential::BruteForce over glam DVec3 bodies: double (n, 4) in, double (n, 3) out."""
+    t = np.ascontiguousarray(np.asarray(targets, np.float64))
+    if t.shape[1] == 3:
+        t = np.ascontiguousarray(np.concatenate([t, np.zeros((t.shape[0], 1))], axis=1))
+    s = np.ascontiguousarray(np.asarray(sources, np.float64))
+    out = np.zeros((t.shape[0], 3), np.float64)
+    rc = lib().oracle_bf_dvec3(t, t.shape[0], s, s.shape[0], softening, int(checked), out, threads)
+    if rc:
+        raise RuntimeError(f"oracle_bf_dvec3 failed: {rc}")
+    return out
+
+
+def bf_pairs(bodies, restrict_len=None, softening=0.0):
+    """BruteForcePairs / RestrictedBruteForce over one slice (f32 or f64 by dtype):
+    every body is affected, the first `restrict_len` (default all) are affecting."""
+    b = np.ascontiguousarray(bodies)
+    n = b.shape[0]
+    r = n if restrict_len is None else int(restrict_len)
+    if b.dtype == np.float64:
+        out = np.zeros((n, 3), np.float64)
+        rc = lib().oracle_bf_pairs_f64(b, n, r, softening, out)
+    else:
+        b = np.ascontiguousarray(b, np.float32)
+        out = np.zeros((n, 3), np.float32)
+        rc = lib().oracle_bf_pairs_f32(b, n, r, softening, out)
+    if rc:
+        raise RuntimeError(f"oracle_bf_pairs failed: {rc}")
     return out
 
 

@@ -24,7 +24,9 @@
  *                        skip d2 == 0, open when theta^2 d2 < w^2)
  *   BH distance          particular/src/gravity/newtonian/acceleration.rs:121-126
  *
- * plus an FP64 brute force of the same formula, used as the error judge.
+ * plus an FP64 brute force of the same formula, used as the error judge, the
+ * same kernel and fold for glam DVec3 bodies in double (gravity/impls/glam.rs:234),
+ * and BruteForcePairs' pairwise fold (sequential.rs:232-304, impls/mod.rs:175-207).
  *
  * Vector arithmetic follows glam's scalar Vec3: component-wise sub/add/mul
  * and length_squared = (x*x + y*y) + z*z evaluated left to right. glam's
@@ -184,6 +186,104 @@ int oracle_bf_f64(const float *aff, size_t n_aff, const float *src, size_t n_src
         out[3 * i + 0] = sx;
         out[3 * i + 1] = sy;
         out[3 * i + 2] = sz;
+    }
+    return OR_OK;
+}
+
+/* ---- f3: glam DVec3 bodies (impl_acceleration_cpu_scalar!(DVec3, f64) at
+ * particular/src/gravity/impls/glam.rs:234, the macro at gravity/impls/mod.rs:137-171):
+ * the a1 kernel and the a2 fold in double. Bodies are double[4] (x, y, z, mu). */
+static inline void pair_f64(double xi, double yi, double zi, const double *p2, double softening,
+                            int checked, double *ax, double *ay, double *az) {
+    double dx = p2[0] - xi;
+    double dy = p2[1] - yi;
+    double dz = p2[2] - zi;
+    double norm = dx * dx + dy * dy + dz * dz;
+    if (checked && norm == 0.0) {
+        *ax = dx;
+        *ay = dy;
+        *az = dz;
+        return;
+    }
+    double norm_s = norm + softening * softening;
+    double s = p2[3] / (norm_s * sqrt(norm_s));
+    *ax = dx * s;
+    *ay = dy * s;
+    *az = dz * s;
+}
+
+int oracle_bf_dvec3(const double *aff, size_t n_aff, const double *src, size_t n_src,
+                    double softening, int checked, double *out, int threads) {
+    if ((n_aff && (!aff || !out)) || (n_src && !src)) return OR_ERR_INVALID;
+    set_threads(threads);
+    long long n = (long long)n_aff;
+#pragma omp parallel for schedule(dynamic, 16) if (threads != 1)
+    for (long long i = 0; i < n; ++i) {
+        double xi = aff[4 * i + 0], yi = aff[4 * i + 1], zi = aff[4 * i + 2];
+        double sx = 0.0, sy = 0.0, sz = 0.0;
+        for (size_t j = 0; j < n_src; ++j) {
+            double ax, ay, az;
+            pair_f64(xi, yi, zi, src + 4 * j, softening, checked, &ax, &ay, &az);
+            sx = sx + ax;
+            sy = sy + ay;
+            sz = sz + az;
+        }
+        out[3 * i + 0] = sx;
+        out[3 * i + 1] = sy;
+        out[3 * i + 2] = sz;
+    }
+    return OR_OK;
+}
+
+/* ---- f4: BruteForcePairs (particular/src/sequential.rs:232-304: RestrictedBruteForce
+ * over restrict_len = affecting_len for Ordered storage, the whole slice for a plain
+ * one) with the paired kernel of gravity/impls/mod.rs:175-207: for i < restrict_len
+ * and j > i, dir = d / (n_s sqrt(n_s)) with d = x_j - x_i (unchecked, mu = 1);
+ * out_i gets dir * m_j (summed from zero over j, then added to out[i]) and out[j]
+ * gets -dir * m_i as i advances. Bodies are float[4] / double[4]. */
+int oracle_bf_pairs_f32(const float *b, size_t n, size_t restrict_len, float softening, float *out) {
+    if ((n && (!b || !out)) || restrict_len > n) return OR_ERR_INVALID;
+    memset(out, 0, sizeof(float) * 3 * n);
+    const float one = 1.0f;
+    for (size_t i = 0; i < restrict_len; ++i) {
+        float oi[3] = {0.0f, 0.0f, 0.0f};
+        for (size_t j = i + 1; j < n; ++j) {
+            const float pj[4] = {b[4 * j + 0], b[4 * j + 1], b[4 * j + 2], one};
+            float dx, dy, dz;
+            pair_f32(b[4 * i + 0], b[4 * i + 1], b[4 * i + 2], pj, softening, 0, &dx, &dy, &dz);
+            oi[0] = oi[0] + dx * b[4 * j + 3];
+            oi[1] = oi[1] + dy * b[4 * j + 3];
+            oi[2] = oi[2] + dz * b[4 * j + 3];
+            out[3 * j + 0] = out[3 * j + 0] + (-dx) * b[4 * i + 3];
+            out[3 * j + 1] = out[3 * j + 1] + (-dy) * b[4 * i + 3];
+            out[3 * j + 2] = out[3 * j + 2] + (-dz) * b[4 * i + 3];
+        }
+        out[3 * i + 0] = out[3 * i + 0] + oi[0];
+        out[3 * i + 1] = out[3 * i + 1] + oi[1];
+        out[3 * i + 2] = out[3 * i + 2] + oi[2];
+    }
+    return OR_OK;
+}
+
+int oracle_bf_pairs_f64(const double *b, size_t n, size_t restrict_len, double softening, double *out) {
+    if ((n && (!b || !out)) || restrict_len > n) return OR_ERR_INVALID;
+    memset(out, 0, sizeof(double) * 3 * n);
+    for (size_t i = 0; i < restrict_len; ++i) {
+        double oi[3] = {0.0, 0.0, 0.0};
+        for (size_t j = i + 1; j < n; ++j) {
+            const double pj[4] = {b[4 * j + 0], b[4 * j + 1], b[4 * j + 2], 1.0};
+            double dx, dy, dz;
+            pair_f64(b[4 * i + 0], b[4 * i + 1], b[4 * i + 2], pj, softening, 0, &dx, &dy, &dz);
+            oi[0] = oi[0] + dx * b[4 * j + 3];
+            oi[1] = oi[1] + dy * b[4 * j + 3];
+            oi[2] = oi[2] + dz * b[4 * j + 3];
+            out[3 * j + 0] = out[3 * j + 0] + (-dx) * b[4 * i + 3];
+            out[3 * j + 1] = out[3 * j + 1] + (-dy) * b[4 * i + 3];
+            out[3 * j + 2] = out[3 * j + 2] + (-dz) * b[4 * i + 3];
+        }
+        out[3 * i + 0] = out[3 * i + 0] + oi[0];
+        out[3 * i + 1] = out[3 * i + 1] + oi[1];
+        out[3 * i + 2] = out[3 * i + 2] + oi[2];
     }
     return OR_OK;
 }

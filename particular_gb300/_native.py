@@ -76,6 +76,10 @@ def _declare(L):
         "pt_bf_accel_f32_device": (ctypes.c_int, [c_ptr, c_ptr, c_size, c_ptr, c_size,
                                                   ctypes.c_float, ctypes.c_int, ctypes.c_uint32,
                                                   c_ptr]),
+        "pt_bf_accel_dvec3": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr, ctypes.c_size_t,
+                                             ctypes.c_double, ctypes.c_int, c_ptr]),
+        "pt_bf_accel_dvec3_device": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr, ctypes.c_size_t,
+                                                    ctypes.c_double, ctypes.c_int, c_ptr]),
         "pt_bf_accel_f64_device": (ctypes.c_int, [c_ptr, c_ptr, c_size, c_ptr, c_size,
                                                   ctypes.c_double, ctypes.c_int, c_ptr]),
         "pt_bf_set_plan": (ctypes.c_int, [c_ptr, ctypes.c_int, ctypes.c_int]),

@@ -324,6 +324,59 @@ __global__ void bf_f64_fixup(const double *__restrict__ part, int n_aff, int sli
     out[k] = acc;
 }
 
+// glam DVec3 bodies (impl_acceleration_cpu_scalar!(DVec3, f64) at
+// particular/src/gravity/impls/glam.rs:234 over gravity/impls/mod.rs:150-166, folded
+// as sequential.rs:189-193): the exact kernel in double. Every operation is an
+// explicitly rounded IEEE op and j runs in order, so the result is the reference's
+// bit for bit. Bodies are double[4] (x, y, z, mu); a tile of 256 sources is staged
+// in shared memory per step.
+__global__ void __launch_bounds__(THREADS)
+    bf_dvec3(const double *__restrict__ aff, int n_aff, const double *__restrict__ src, int n_src, double soft2,
+             int checked, double *__restrict__ out) {
+    __shared__ __align__(16) double tile[TILE][4];
+    const int i = blockIdx.x * THREADS + threadIdx.x;
+    double xi = 0.0, yi = 0.0, zi = 0.0;
+    if (i < n_aff) {
+        xi = aff[4 * size_t(i) + 0];
+        yi = aff[4 * size_t(i) + 1];
+        zi = aff[4 * size_t(i) + 2];
+    }
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int j0 = 0; j0 < n_src; j0 += TILE) {
+        const int cnt = min(TILE, n_src - j0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < 4 * cnt; k += THREADS) (&tile[0][0])[k] = src[4 * size_t(j0) + k];
+        __syncthreads();
+#pragma unroll 1
+        for (int jj = 0; jj < cnt; ++jj) {
+            const double dx = __dsub_rn(tile[jj][0], xi);
+            const double dy = __dsub_rn(tile[jj][1], yi);
+            const double dz = __dsub_rn(tile[jj][2], zi);
+            const double n = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            double ax, ay, az;
+            if (checked && n == 0.0) {
+                ax = dx;
+                ay = dy;
+                az = dz;
+            } else {
+                const double ns = __dadd_rn(n, soft2);
+                const double s = __ddiv_rn(tile[jj][3], __dmul_rn(ns, __dsqrt_rn(ns)));
+                ax = __dmul_rn(dx, s);
+                ay = __dmul_rn(dy, s);
+                az = __dmul_rn(dz, s);
+            }
+            sx = __dadd_rn(sx, ax);
+            sy = __dadd_rn(sy, ay);
+            sz = __dadd_rn(sz, az);
+        }
+    }
+    if (i < n_aff) {
+        out[3 * size_t(i) + 0] = sx;
+        out[3 * size_t(i) + 1] = sy;
+        out[3 * size_t(i) + 2] = sz;
+    }
+}
+
 using FastKernel = void (*)(const float4 *, int, const float *, int, int, float, int, float4 *, float *);
 
 template <int K>
@@ -473,6 +526,22 @@ int bf_launch_f64(pt_ctx *ctx, const float4 *aff, int n_aff, const float4 *src, 
     return PT_OK;
 }
 
+int bf_launch_dvec3(pt_ctx *ctx, const double *aff, int n_aff, const double *src, int n_src, double softening,
+                    int checked, double *out) {
+    using namespace bf;
+    if (n_aff == 0) return PT_OK;
+    if (n_src == 0) {
+        PT_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 3 * size_t(n_aff), ctx->stream));
+        return PT_OK;
+    }
+    mark(ctx, 1);
+    bf_dvec3<<<(n_aff + THREADS - 1) / THREADS, THREADS, 0, ctx->stream>>>(aff, n_aff, src, n_src,
+                                                                          softening * softening, checked, out);
+    PT_TRY(check_launch(ctx, "bf_dvec3"));
+    mark(ctx, 2);
+    return PT_OK;
+}
+
 static int validate_sizes(const char *fn, size_t n_aff, size_t n_src) {
     const size_t lim = size_t(INT_MAX) / 8;
     if (n_aff > lim || n_src > lim)
@@ -548,6 +617,46 @@ int pt_bf_accel_f32(pt_ctx *ctx, const float *aff, size_t n_aff, const float *sr
     PT_TRY(bf_launch_f32(ctx, reinterpret_cast<const float4 *>(d_aff), int(n_aff),
                          reinterpret_cast<const float4 *>(d_src), int(n_src), softening, checked, flags, d_out));
     PT_CUDA(cudaMemcpyAsync(out, d_out, 12 * n_aff, cudaMemcpyDeviceToHost, st));
+    PT_CUDA(cudaStreamSynchronize(st));
+    return PT_OK;
+}
+
+int pt_bf_accel_dvec3_device(pt_ctx *ctx, const double *d_aff, size_t n_aff, const double *d_src, size_t n_src,
+                             double softening, int checked, double *d_out) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bf_accel_dvec3_device: ctx is NULL");
+    PT_TRY(validate_sizes("pt_bf_accel_dvec3_device", n_aff, n_src));
+    if (n_aff && (!d_aff || !d_out)) return set_error(PT_ERR_INVALID, "pt_bf_accel_dvec3_device: NULL buffer");
+    if (n_src && !d_src) return set_error(PT_ERR_INVALID, "pt_bf_accel_dvec3_device: NULL affecting buffer");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    mark(ctx, 0);
+    return bf_launch_dvec3(ctx, d_aff, int(n_aff), d_src, int(n_src), softening, checked, d_out);
+}
+
+int pt_bf_accel_dvec3(pt_ctx *ctx, const double *aff, size_t n_aff, const double *src, size_t n_src,
+                      double softening, int checked, double *out) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bf_accel_dvec3: ctx is NULL");
+    PT_TRY(validate_sizes("pt_bf_accel_dvec3", n_aff, n_src));
+    if (n_aff && (!aff || !out)) return set_error(PT_ERR_INVALID, "pt_bf_accel_dvec3: NULL buffer");
+    if (n_src && !src) return set_error(PT_ERR_INVALID, "pt_bf_accel_dvec3: NULL affecting buffer");
+    if (n_aff == 0) return PT_OK;
+    PT_CUDA(cudaSetDevice(ctx->device));
+    const bool same = (aff == src) && (n_aff == n_src);
+    PT_TRY(ensure(ctx, BUF_AFF, 32 * n_aff));
+    if (!same && n_src) PT_TRY(ensure(ctx, BUF_SRC, 32 * n_src));
+    PT_TRY(ensure(ctx, BUF_OUT64, 24 * n_aff));
+    double *d_aff = static_cast<double *>(ctx->bufs[BUF_AFF].ptr);
+    double *d_src = same ? d_aff : static_cast<double *>(ctx->bufs[BUF_SRC].ptr);
+    double *d_out = static_cast<double *>(ctx->bufs[BUF_OUT64].ptr);
+    cudaStream_t st = ctx->stream;
+    mark(ctx, 0);
+    PT_CUDA(cudaMemcpyAsync(d_aff, aff, 32 * n_aff, cudaMemcpyHostToDevice, st));
+    if (!same && n_src) PT_CUDA(cudaMemcpyAsync(d_src, src, 32 * n_src, cudaMemcpyHostToDevice, st));
+    PT_TRY(bf_launch_dvec3(ctx, d_aff, int(n_aff), d_src, int(n_src), softening, checked, d_out));
+    PT_CUDA(cudaMemcpyAsync(out, d_out, 24 * n_aff, cudaMemcpyDeviceToHost, st));
     PT_CUDA(cudaStreamSynchronize(st));
     return PT_OK;
 }

@@ -85,17 +85,33 @@ class BruteForce:
 
     `exact=True` selects the bit-identical restatement of sequential::BruteForce
     (sequential j order, IEEE sqrt and divide); the default is the fast FP32 path
-    with compensated accumulation.
+    with compensated accumulation. `dvec3=True` computes over glam DVec3 bodies:
+    float64 in and out, the reference's f64 kernel bit for bit (storages built with
+    dtype=np.float64 keep their float64 values).
     """
 
-    def __init__(self, resources, interaction, exact=False, vec3a=False):
+    def __init__(self, resources, interaction, exact=False, vec3a=False, dvec3=False):
         self.resources = resources
         self.interaction = interaction
         self.exact = bool(exact)
         self.vec3a = bool(vec3a)  # glam Vec3A/Vec4 operand order (exact path)
+        self.dvec3 = bool(dvec3)
 
     def compute(self, storage):
         b = as_between(storage)
+        if self.dvec3:
+            aff = positions(b.affected, np.float64)
+            src = fields(b.affecting, np.float64)
+            out = np.zeros((aff.shape[0], 3), np.float64)
+            if aff.shape[0] == 0:
+                return out
+            same = b.affected is b.affecting
+            it = self.interaction
+            eps = getattr(it, "softening64", it.softening)
+            N.check(N.lib().pt_bf_accel_dvec3(self.resources.handle, _ptr(aff), aff.shape[0],
+                                              _ptr(aff) if same else _ptr(src), src.shape[0],
+                                              eps, int(it.is_checked), _ptr(out)))
+            return out
         aff = positions(b.affected)
         src = fields(b.affecting)
         out = np.zeros((aff.shape[0], 3), np.float32)

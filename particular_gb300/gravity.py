@@ -51,8 +51,9 @@ def _position_of(p):
     return pos() if callable(pos) else pos
 
 
-def fields(particles):
-    """Packs particles into a C-contiguous float32 (n, 4) array of (x, y, z, mu).
+def fields(particles, dtype=np.float32):
+    """Packs particles into a C-contiguous (n, 4) array of (x, y, z, mu), float32 by
+    default (GravitationalField<Vec3, f32>) or float64 (glam DVec3 bodies).
 
     Accepts an (n, 4) array (already packed), a (positions (n, 3), mu (n,)) pair, a
     structured array with `position` and `mu`/`mass` fields, or a sequence of objects
@@ -62,42 +63,42 @@ def fields(particles):
         a = np.asarray(particles)
         if a.ndim != 2 or a.shape[1] != 4:
             raise ValueError("a packed particle array must have shape (n, 4): x, y, z, mu")
-        return np.ascontiguousarray(a, dtype=np.float32)
+        return np.ascontiguousarray(a, dtype=dtype)
     if isinstance(particles, np.ndarray):
         names = particles.dtype.names
         mu = particles["mu"] if "mu" in names else particles["mass"]
         pos = particles["position"]
-        return _pack(pos, mu)
+        return _pack(pos, mu, dtype)
     if isinstance(particles, tuple) and len(particles) == 2 and isinstance(particles[0], np.ndarray):
-        return _pack(particles[0], particles[1])
+        return _pack(particles[0], particles[1], dtype)
     items = list(particles)
     if not items:
-        return np.zeros((0, 4), np.float32)
+        return np.zeros((0, 4), dtype)
     if isinstance(items[0], tuple) and len(items[0]) == 2:
         pos = [it[0] for it in items]
         mu = [it[1] for it in items]
     else:
         pos = [_position_of(it) for it in items]
         mu = [_mu_of(it) for it in items]
-    return _pack(np.asarray(pos, np.float32), np.asarray(mu, np.float32))
+    return _pack(np.asarray(pos, dtype), np.asarray(mu, dtype), dtype)
 
 
-def positions(particles):
-    """Packs the positions of affected particles as float32 (n, 4) (w unused)."""
+def positions(particles, dtype=np.float32):
+    """Packs the positions of affected particles as (n, 4) rows (w unused)."""
     if isinstance(particles, np.ndarray) and particles.dtype.names is None and particles.ndim == 2 \
             and particles.shape[1] == 3:
-        out = np.zeros((particles.shape[0], 4), np.float32)
+        out = np.zeros((particles.shape[0], 4), dtype)
         out[:, :3] = particles
         return out
-    return fields(particles)
+    return fields(particles, dtype)
 
 
-def _pack(pos, mu):
-    pos = np.asarray(pos, np.float32).reshape(-1, 3)
-    mu = np.asarray(mu, np.float32).reshape(-1)
+def _pack(pos, mu, dtype=np.float32):
+    pos = np.asarray(pos, dtype).reshape(-1, 3)
+    mu = np.asarray(mu, dtype).reshape(-1)
     if pos.shape[0] != mu.shape[0]:
         raise ValueError("positions and mu differ in length")
-    out = np.empty((pos.shape[0], 4), np.float32)
+    out = np.empty((pos.shape[0], 4), dtype)
     out[:, :3] = pos
     out[:, 3] = mu
     return out
@@ -132,7 +133,8 @@ class AccelerationSoftened:
     (gravity/newtonian/acceleration_softened.rs:17-49)."""
 
     def __init__(self, softening, checked=True):
-        self.softening = float(np.float32(softening))
+        self.softening = float(np.float32(softening))  # the f32 value the f32 methods use
+        self.softening64 = float(softening)            # and the f64 one (DVec3 bodies)
         self.is_checked = bool(checked)
 
     @classmethod

@@ -52,16 +52,16 @@ class Ordered:
         self._affecting_len = int(affecting_len)
 
     @classmethod
-    def new(cls, unordered, is_affecting_fn=None):
-        packed = fields(unordered)
+    def new(cls, unordered, is_affecting_fn=None, dtype=np.float32):
+        packed = fields(unordered, dtype)
         m = _mask(unordered, packed, is_affecting_fn)
         return cls(np.ascontiguousarray(np.concatenate([packed[m], packed[~m]])), int(m.sum()))
 
     @classmethod
-    def with_groups(cls, affecting, non_affecting, is_affecting_fn=None):
+    def with_groups(cls, affecting, non_affecting, is_affecting_fn=None, dtype=np.float32):
         """Ordered::with (storage.rs:61-80): affecting_len is the first non-affecting
         position of the concatenation."""
-        packed = np.concatenate([fields(affecting), fields(non_affecting)])
+        packed = np.concatenate([fields(affecting, dtype), fields(non_affecting, dtype)])
         m = _mask(None, packed, is_affecting_fn)
         first = np.flatnonzero(~m)
         return cls(np.ascontiguousarray(packed), int(first[0]) if first.size else packed.shape[0])
@@ -85,10 +85,10 @@ class Ordered:
 class Reordered:
     """The original particles plus an Ordered copy (storage.rs:140-205)."""
 
-    def __init__(self, unordered, is_affecting_fn=None):
+    def __init__(self, unordered, is_affecting_fn=None, dtype=np.float32):
         self.unordered = unordered
-        self._unordered_packed = fields(unordered)
-        self._ordered = Ordered.new(unordered, is_affecting_fn)
+        self._unordered_packed = fields(unordered, dtype)
+        self._ordered = Ordered.new(unordered, is_affecting_fn, dtype)
 
     def ordered(self):
         return self._ordered

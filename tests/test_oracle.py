@@ -74,6 +74,52 @@ def test_bf_bit_identical_to_numpy_restatement(oracle, softening, checked):
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
 
 
+def numpy_bf_dvec3(aff, src, softening, checked):
+    """The same restatement in float64 (glam DVec3 bodies)."""
+    x = aff[:, :3]
+    acc = np.zeros_like(x)
+    e2 = softening * softening
+    with np.errstate(all="ignore"):
+        for j in range(src.shape[0]):
+            d = src[j, :3][None, :] - x
+            n = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+            ns = n + e2
+            a = d * (src[j, 3] / (ns * np.sqrt(ns)))[:, None]
+            if checked:
+                a = np.where((n == 0)[:, None], d, a)
+            acc = acc + a
+    return acc
+
+
+@pytest.mark.parametrize("softening,checked", [(0.0, True), (1e-3, True), (0.05, False)])
+def test_dvec3_bit_identical_to_numpy_restatement(oracle, softening, checked):
+    b = mixed_bodies(300, 10).astype(np.float64)
+    b[:, :3] += np.random.default_rng(1).normal(scale=1e-9, size=(300, 3))  # bits below f32
+    if not checked:
+        b = ics.uniform_cube(300, 11)["bodies"].astype(np.float64)
+    got = oracle.bf_dvec3(b, b, softening, checked, threads=1)
+    want = numpy_bf_dvec3(b, b, softening, checked)
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+
+
+def test_pairs_restatement_agrees_with_brute_force(oracle):
+    """BruteForcePairs sums each pair once (a_i += dir m_j, a_j -= dir m_i): the same
+    accelerations as BruteForce up to summation order; on Ordered storage only the
+    affecting prefix acts (restrict_len)."""
+    b = ics.uniform_cube(500, 12)["bodies"].copy()
+    bf = oracle.bf_f64(b, b, 1e-3, True)
+    p32 = oracle.bf_pairs(b, softening=1e-3)
+    p64 = oracle.bf_pairs(b.astype(np.float64), softening=1e-3)
+    scale = np.abs(bf).max()
+    assert np.abs(p64 - bf).max() < 1e-12 * scale
+    assert np.abs(p32 - bf).max() < 1e-5 * scale
+    # Ordered: 200 massive first, then 300 massless
+    b[200:, 3] = 0.0
+    p = oracle.bf_pairs(b.astype(np.float64), restrict_len=200, softening=1e-3)
+    want = oracle.bf_f64(b, b[:200], 1e-3, True)
+    assert np.abs(p - want).max() < 1e-12 * np.abs(want).max()
+
+
 def test_parallel_bf_bit_identical_to_sequential(oracle):
     b = mixed_bodies(2000, 9)
     one = oracle.bf_f32(b, b, 1e-3, True, threads=1)
