@@ -37,6 +37,9 @@ def parse_args():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--leapfrog-steps", type=int, default=0,
+                   help="leapfrog steps per call for the leapfrog/ensemble workloads "
+                        "(default: the workload's own; fewer make short profiling runs)")
     return p.parse_args()
 
 
@@ -567,6 +570,13 @@ WORKLOADS = {BruteForceWorkload.name: BruteForceWorkload,
 DEFAULT_WORKLOAD = BarnesHutWorkload.name
 
 
+def make_workload(args):
+    wl = WORKLOADS[args.workload or DEFAULT_WORKLOAD]()
+    if args.leapfrog_steps > 0 and hasattr(wl, "steps_per_call"):
+        wl.steps_per_call = args.leapfrog_steps
+    return wl
+
+
 
 # --------------------------------------------------------------------------- arms
 def run_reference(args):
@@ -575,7 +585,7 @@ def run_reference(args):
         return 0
     from oracle import build as obuild, oracle as O
     obuild.build()
-    wl = WORKLOADS[args.workload or DEFAULT_WORKLOAD]()
+    wl = make_workload(args)
     threads = O.max_threads()
     value, info = wl.cpu_reference(threads, steps=max(1, args.steps))
     work = wl.work_per_step() if hasattr(wl, "work_per_step") else wl.n
@@ -603,7 +613,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     from particular_gb300 import CudaResources, build_native
     build_native.build()
-    wl = WORKLOADS[args.workload or DEFAULT_WORKLOAD]()
+    wl = make_workload(args)
     res = CudaResources(local)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
