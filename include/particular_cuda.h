@@ -197,6 +197,24 @@ int pt_bh_accel_f32(pt_ctx *ctx, const float *affected, size_t n_aff, const floa
 int pt_bh_accel_f32_device(pt_ctx *ctx, const float *d_affected, size_t n_aff,
                            const float *d_affecting, size_t n_src, float theta, float softening,
                            uint32_t flags, float *d_out_xyz);
+/* Tree reuse: the GPU counterpart of computing with Between(affected, &tree) over a
+ * RootedOrthtree built once (particular/src/lib.rs:186-199, sequential.rs:508-522,
+ * storage.rs:20-33). pt_bh_build_device builds the reference's orthtree over the
+ * affecting bodies (device buffer, asynchronous) and keeps it in the context;
+ * *generation (may be NULL) receives its number. pt_bh_walk_device walks the
+ * context's current tree for any affected bodies with the same theta rule and flags
+ * as pt_bh_accel_f32_device, which gives the same results as one combined call. Every
+ * Barnes-Hut call on the context (pt_bh_accel_*, the learned-sample generation)
+ * replaces the current tree; pt_bh_tree_generation reports which one is current. */
+int pt_bh_build_device(pt_ctx *ctx, const float *d_affecting, size_t n_src, uint64_t *generation);
+int pt_bh_walk_device(pt_ctx *ctx, const float *d_affected, size_t n_aff, float theta, float softening,
+                      uint32_t flags, float *d_out_xyz);
+int pt_bh_tree_generation(pt_ctx *ctx, uint64_t *generation);
+/* The same over host buffers (synchronous): the bodies are staged in context buffers;
+ * the tree keeps its own copy, so `affecting` may change after pt_bh_build returns. */
+int pt_bh_build(pt_ctx *ctx, const float *affecting, size_t n_src, uint64_t *generation);
+int pt_bh_walk(pt_ctx *ctx, const float *affected, size_t n_aff, float theta, float softening,
+               uint32_t flags, float *out_xyz);
 /* Caps the PT_BH_GROUP walk's shared-memory stack at `ranges` entries per warp (2 to
  * the compiled capacity; 0 restores the capacity). A warp that runs out takes the
  * per-body walk instead (counted in pt_bh_stats.overflow): a tuning and test hook. */

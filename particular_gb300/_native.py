@@ -93,6 +93,13 @@ def _declare(L):
                                                   c_ptr]),
         "pt_bh_last_stats": (ctypes.c_int, [c_ptr, ctypes.POINTER(BhStats)]),
         "pt_bh_set_stack_limit": (ctypes.c_int, [c_ptr, ctypes.c_int]),
+        "pt_bh_build_device": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr]),
+        "pt_bh_walk_device": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, ctypes.c_float, ctypes.c_float,
+                                             ctypes.c_uint32, c_ptr]),
+        "pt_bh_tree_generation": (ctypes.c_int, [c_ptr, c_ptr]),
+        "pt_bh_build": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr]),
+        "pt_bh_walk": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_uint32, c_ptr]),
         "pt_bh_export_tree": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_ptr, c_size]),
         "pt_ctx_set_timing": (ctypes.c_int, [c_ptr, ctypes.c_int]),
         "pt_mlp_init": (ctypes.c_int, [c_ptr, ctypes.c_uint64]),

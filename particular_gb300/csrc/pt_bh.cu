@@ -66,6 +66,7 @@ struct State {
     DevBuf lrec, lgroup, lnext, lpart, lhead, lcentre, lused;  // learned-correction records
     int lcap = 0;                     // record chunks allocated
     int stack_cap = 0;                // group-walk stack ranges per warp in use (0 = all)
+    uint64_t generation = 0;          // trees built so far (0 = none)
     const uint32_t *mlp_w = nullptr;  // learned correction: packed BF16 weights (owned by the MLP state)
     const float *mlp_b = nullptr;     // and its bias block
     float theta_inner = 0.5f;
@@ -1265,6 +1266,7 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
         PT_TRY(check_launch(ctx, "cell_moments_level"));
     }
     S.last_n_src = n;
+    ++S.generation;
     return PT_OK;
 }
 
@@ -1280,6 +1282,9 @@ static int sort_targets(pt_ctx *ctx, State &S, const float4 *d_aff, int n) {
     gather_bodies<<<blocks(n), 256, 0, st>>>(d_aff, as<uint32_t>(S.tidx), n, as<float4>(S.tbody));
     return check_launch(ctx, "gather_bodies(targets)");
 }
+
+static int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n_aff, float theta,
+                float softening, uint32_t flags, float *d_out);
 
 static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src, int n_src, float theta,
                float softening, uint32_t flags, float *d_out) {
@@ -1305,6 +1310,14 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
         tbody = as<float4>(S.tbody);
         tidx = as<uint32_t>(S.tidx);
     }
+    return walk(ctx, S, tbody, tidx, n_aff, theta, softening, flags, d_out);
+}
+
+// Walks the context's current tree for targets tbody (key-sorted; tidx maps them back
+// to the caller's order) and writes accelerations to d_out.
+static int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n_aff, float theta,
+                float softening, uint32_t flags, float *d_out) {
+    cudaStream_t st = ctx->stream;
     // counters: int[4] = {leaves, nodes, cells, error} then u64[7] = {interactions,
     // visits, warps, max group stack, learned records, cell interactions, warps that
     // fell back to the per-body walk}
@@ -1484,6 +1497,108 @@ int pt_bh_accel_f32(pt_ctx *ctx, const float *aff, size_t n_aff, const float *sr
     PT_CUDA(cudaStreamSynchronize(st));
     if (err & 2)
         return set_error(PT_ERR_CAPACITY, "pt_bh_accel_f32: learned-correction records overflowed");
+    return PT_OK;
+}
+
+int pt_bh_build_device(pt_ctx *ctx, const float *d_src, size_t n_src, uint64_t *generation) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_build_device: ctx is NULL");
+    PT_TRY(bh::validate("pt_bh_build_device", 0, n_src, 0));
+    if (n_src && !d_src) return set_error(PT_ERR_INVALID, "pt_bh_build_device: NULL affecting buffer");
+    if (n_src && !aligned16(d_src))
+        return set_error(PT_ERR_INVALID, "pt_bh_build_device: body buffer must be 16-byte aligned");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    if (n_src == 0) {
+        S->last_n_src = 0;
+        ++S->generation;
+    } else {
+        mark(ctx, 0);
+        PT_TRY(bh::build(ctx, *S, reinterpret_cast<const float4 *>(d_src), int(n_src)));
+    }
+    if (generation) *generation = S->generation;
+    return PT_OK;
+}
+
+int pt_bh_walk_device(pt_ctx *ctx, const float *d_aff, size_t n_aff, float theta, float softening, uint32_t flags,
+                      float *d_out) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_walk_device: ctx is NULL");
+    PT_TRY(bh::validate("pt_bh_walk_device", n_aff, 0, flags));
+    if (n_aff && (!d_aff || !d_out)) return set_error(PT_ERR_INVALID, "pt_bh_walk_device: NULL buffer");
+    if (n_aff && !aligned16(d_aff))
+        return set_error(PT_ERR_INVALID, "pt_bh_walk_device: body buffer must be 16-byte aligned");
+    auto *S = static_cast<bh::State *>(ctx->bh);
+    if (!S || S->generation == 0)
+        return set_error(PT_ERR_INVALID, "pt_bh_walk_device: no tree (call pt_bh_build_device first)");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    if (n_aff == 0) return PT_OK;
+    if (S->last_n_src == 0) {
+        PT_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * 3 * n_aff, ctx->stream));
+        return PT_OK;
+    }
+    mark(ctx, 0);
+    PT_TRY(bh::sort_targets(ctx, *S, reinterpret_cast<const float4 *>(d_aff), int(n_aff)));
+    return bh::walk(ctx, *S, bh::as<float4>(S->tbody), bh::as<uint32_t>(S->tidx), int(n_aff), theta, softening,
+                    flags, d_out);
+}
+
+int pt_bh_build(pt_ctx *ctx, const float *src, size_t n_src, uint64_t *generation) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_build: ctx is NULL");
+    PT_TRY(bh::validate("pt_bh_build", 0, n_src, 0));
+    if (n_src && !src) return set_error(PT_ERR_INVALID, "pt_bh_build: NULL affecting buffer");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    float *d_src = nullptr;
+    if (n_src) {
+        PT_TRY(ensure_buf(ctx, S->src_h, 16 * n_src));
+        d_src = static_cast<float *>(S->src_h.ptr);
+        PT_CUDA(cudaMemcpyAsync(d_src, src, 16 * n_src, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    PT_TRY(pt_bh_build_device(ctx, d_src, n_src, generation));
+    PT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_bh_walk(pt_ctx *ctx, const float *aff, size_t n_aff, float theta, float softening, uint32_t flags,
+               float *out) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_walk: ctx is NULL");
+    PT_TRY(bh::validate("pt_bh_walk", n_aff, 0, flags));
+    if (n_aff && (!aff || !out)) return set_error(PT_ERR_INVALID, "pt_bh_walk: NULL buffer");
+    if (n_aff == 0) return PT_OK;
+    PT_CUDA(cudaSetDevice(ctx->device));
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    PT_TRY(ensure_buf(ctx, S->aff_h, 16 * n_aff));
+    PT_TRY(ensure_buf(ctx, S->out, 12 * n_aff));
+    float *d_aff = static_cast<float *>(S->aff_h.ptr);
+    float *d_out = static_cast<float *>(S->out.ptr);
+    cudaStream_t st = ctx->stream;
+    PT_CUDA(cudaMemcpyAsync(d_aff, aff, 16 * n_aff, cudaMemcpyHostToDevice, st));
+    PT_TRY(pt_bh_walk_device(ctx, d_aff, n_aff, theta, softening, flags, d_out));
+    PT_CUDA(cudaMemcpyAsync(out, d_out, 12 * n_aff, cudaMemcpyDeviceToHost, st));
+    int err = 0;
+    PT_CUDA(cudaMemcpyAsync(&err, static_cast<int *>(S->counters.ptr) + 3, sizeof(int), cudaMemcpyDeviceToHost,
+                            st));
+    PT_CUDA(cudaStreamSynchronize(st));
+    if (err & 2) return set_error(PT_ERR_CAPACITY, "pt_bh_walk: learned-correction records overflowed");
+    return PT_OK;
+}
+
+int pt_bh_tree_generation(pt_ctx *ctx, uint64_t *generation) {
+    using namespace pt;
+    clear_error();
+    if (!ctx || !generation) return set_error(PT_ERR_INVALID, "pt_bh_tree_generation: NULL argument");
+    auto *S = static_cast<bh::State *>(ctx->bh);
+    *generation = S ? S->generation : 0;
     return PT_OK;
 }
 

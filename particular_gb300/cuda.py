@@ -131,6 +131,23 @@ def cuda_brute_force(storage, resources, interaction, exact=False):
     return BruteForce(resources, interaction, exact).compute(storage)
 
 
+class DeviceTree:
+    """A Barnes-Hut tree kept on the device (the counterpart of a RootedOrthtree built
+    once and reused through Between(affected, &tree): particular/src/lib.rs:186-199).
+    It stays valid until the next Barnes-Hut call on the same CudaResources replaces
+    the context's tree; using it afterwards raises."""
+
+    def __init__(self, resources, n_affecting, generation):
+        self.resources = resources
+        self.n_affecting = int(n_affecting)
+        self.generation = int(generation)
+
+    def is_current(self):
+        g = ctypes.c_uint64(0)
+        N.check(N.lib().pt_bh_tree_generation(self.resources.handle, ctypes.byref(g)))
+        return g.value == self.generation
+
+
 class BarnesHut:
     """cuda::BarnesHut { theta }: the reference's orthtree built on the GPU every call
     and walked with the reference's opening rule (sequential.rs:466-505).
@@ -154,8 +171,28 @@ class BarnesHut:
         return ((N.PT_BH_QUADRUPOLE if self.quadrupole else 0) | (N.PT_BH_GROUP if self.group else 0)
                 | (N.PT_BH_LEARNED if self.learned else 0))
 
+    def build(self, affecting):
+        """Builds the tree over `affecting` (any storage of particles) once; pass the
+        returned DeviceTree as the affecting side of Between to walk it."""
+        src = fields(affecting)
+        g = ctypes.c_uint64(0)
+        N.check(N.lib().pt_bh_build(self.resources.handle, _ptr(src), src.shape[0], ctypes.byref(g)))
+        return DeviceTree(self.resources, src.shape[0], g.value)
+
     def compute(self, storage):
         b = as_between(storage)
+        if isinstance(b.affecting, DeviceTree):
+            tree = b.affecting
+            if tree.resources is not self.resources:
+                raise ValueError("the tree belongs to another CudaResources")
+            if not tree.is_current():
+                raise N.CudaError(N.PT_ERR_INVALID, "the tree was replaced by a later Barnes-Hut call")
+            aff = positions(b.affected)
+            out = np.zeros((aff.shape[0], 3), np.float32)
+            if aff.shape[0]:
+                N.check(N.lib().pt_bh_walk(self.resources.handle, _ptr(aff), aff.shape[0], self.theta,
+                                           self.interaction.softening, self.flags, _ptr(out)))
+            return out
         aff = positions(b.affected)
         src = fields(b.affecting)
         out = np.zeros((aff.shape[0], 3), np.float32)

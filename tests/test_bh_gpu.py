@@ -314,3 +314,53 @@ def test_group_walk_stack_fallback(res, oracle, learned):
         N.check(L.pt_bh_set_stack_limit(res.handle, 0))
     m.compute(b)
     assert m.stats()["overflow"] == 0
+
+
+@pytest.mark.parametrize("quad,group", [(False, False), (True, True)])
+def test_tree_reuse(res, quad, group):
+    """Build once, walk many (Between(affected, &tree) in the reference): the same
+    accelerations as one combined call per target set; a later Barnes-Hut call
+    replaces the context's tree and the stale handle is refused."""
+    src = ics.plummer(20000, seed=47)["bodies"]
+    t1 = ics.uniform_cube(3000, 48)["bodies"]
+    t2 = ics.plummer(5000, seed=49)["bodies"]
+    m = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=quad, group=group)
+    tree = m.build(src)
+    assert tree.is_current() and tree.n_affecting == 20000
+    a1 = m.compute(Between(t1, tree))
+    a2 = m.compute(Between(t2, tree))
+    a_self = m.compute(Between(src, tree))
+    assert tree.is_current()
+    np.testing.assert_array_equal(a1, m.compute(Between(t1, src)))
+    np.testing.assert_array_equal(a2, m.compute(Between(t2, src)))
+    np.testing.assert_array_equal(a_self, m.compute(src))
+    assert not tree.is_current()
+    with pytest.raises(N.CudaError):
+        m.compute(Between(t1, tree))
+    # empty tree and empty targets
+    empty = m.build(np.zeros((0, 4), np.float32))
+    assert np.array_equal(m.compute(Between(t1, empty)), np.zeros_like(t1[:, :3]))
+    tree = m.build(src)
+    assert m.compute(Between(np.zeros((0, 4), np.float32), tree)).shape == (0, 3)
+
+
+def test_tree_reuse_device_entry_points(res):
+    import ctypes
+    import torch
+    src = ics.bulge_disk(30000, seed=50)["bodies"]
+    tgt = ics.uniform_cube(4000, 51)["bodies"]
+    d_s, d_t = torch.from_numpy(src).cuda(), torch.from_numpy(tgt).cuda()
+    d_o = torch.empty((4000, 3), dtype=torch.float32, device="cuda")
+    L = N.lib()
+    g = ctypes.c_uint64(0)
+    N.check(L.pt_bh_build_device(res.handle, d_s.data_ptr(), 30000, ctypes.byref(g)))
+    N.check(L.pt_bh_walk_device(res.handle, d_t.data_ptr(), 4000, 0.6, 0.01, N.PT_BH_QUADRUPOLE | N.PT_BH_GROUP,
+                                d_o.data_ptr()))
+    res.synchronize()
+    got = d_o.cpu().numpy()
+    want = cuda.BarnesHut(0.6, res, AccelerationSoftened(0.01), quadrupole=True, group=True).compute(
+        Between(tgt, src))
+    np.testing.assert_array_equal(got, want)
+    g2 = ctypes.c_uint64(0)
+    N.check(L.pt_bh_tree_generation(res.handle, ctypes.byref(g2)))
+    assert g2.value > g.value > 0
