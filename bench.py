@@ -48,6 +48,23 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(values, dist, device):
+    """Element-wise maximum of a list of floats over all ranks (the slowest replica
+    sets the job's time); identity without a process group."""
+    if dist is None:
+        return list(values)
+    import torch
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def job_throughput(world, work_per_step, total_ms, steps):
+    """Whole-job units/s: every replica processes work_per_step per step, and the job
+    takes the slowest rank's time."""
+    return world * work_per_step / (total_ms / steps * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
 
@@ -655,14 +672,11 @@ def run_ours(args):
     barrier()
     t_e2e = timed(wl.step_e2e, args.steps)
     barrier()
-    if dist:
-        tt = torch.tensor([t_ms, t_e2e], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ms, t_e2e = tt.tolist()
+    t_ms, t_e2e = max_over_ranks([t_ms, t_e2e], dist, "cuda")
     step_ms = t_ms / args.steps
     work = wl.work_per_step() if hasattr(wl, "work_per_step") else wl.n
-    value = world * work / (step_ms * 1e-3)
-    e2e_value = world * work / (t_e2e / args.steps * 1e-3)
+    value = job_throughput(world, work, t_ms, args.steps)
+    e2e_value = job_throughput(world, work, t_e2e, args.steps)
     h2d, d2h = wl.h2d_d2h_bytes()
     roof = wl.roofline(res, step_ms)
     if rank != 0:

@@ -1,0 +1,62 @@
+"""The N > 1 path of bench.py on CPU: two gloo ranks, replicas only (each rank runs its
+own copy of the workload), the job's time is the slowest rank's and the value is the
+work of all replicas over that time; the reference arm runs on rank 0 alone."""
+import os
+import subprocess
+import sys
+
+import pytest
+import torch.multiprocessing as mp
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _rank(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
+    sys.path.insert(0, ROOT)
+    import torch.distributed as dist
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    assert bench.dist_env() == (rank, world, rank)
+    # per-rank timed totals (ms over 4 steps): rank 1 is the slow replica
+    local = [40.0 + 20.0 * rank, 50.0 + 10.0 * rank]
+    t_ms, t_e2e = bench.max_over_ranks(local, dist, "cpu")
+    value = bench.job_throughput(world, 1000, t_ms, 4)
+    q.put((rank, t_ms, t_e2e, value))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_take_the_slowest_replica():
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    got = sorted(q.get(timeout=5) for _ in range(2))
+    for rank, t_ms, t_e2e, value in got:
+        assert (t_ms, t_e2e) == (60.0, 60.0)
+        # 2 replicas x 1000 units per step, 15 ms per step
+        assert value == pytest.approx(2 * 1000 / 15e-3)
+
+
+def test_reference_arm_non_zero_rank_exits_quietly():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--steps", "1", "--warmup", "0"], env=env, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_single_process_identity():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.max_over_ranks([1.0, 2.0], None, "cpu") == [1.0, 2.0]
+    assert bench.job_throughput(1, 500, 100.0, 10) == pytest.approx(500 / 10e-3)
