@@ -53,9 +53,28 @@ struct Vec3 {
     float length_squared() const { return x * x + y * y + z * z; }
 };
 
+// glam DVec3: particles whose position is made of doubles take the f64 path.
+struct DVec3 {
+    double x = 0.0, y = 0.0, z = 0.0;
+    DVec3() = default;
+    DVec3(double x_, double y_, double z_) : x(x_), y(y_), z(z_) {}
+    static DVec3 splat(double v) { return {v, v, v}; }
+    DVec3 operator+(const DVec3 &o) const { return {x + o.x, y + o.y, z + o.z}; }
+    DVec3 operator-(const DVec3 &o) const { return {x - o.x, y - o.y, z - o.z}; }
+    DVec3 operator*(double s) const { return {x * s, y * s, z * s}; }
+    DVec3 &operator+=(const DVec3 &o) {
+        x += o.x;
+        y += o.y;
+        z += o.z;
+        return *this;
+    }
+    double length_squared() const { return x * x + y * y + z * z; }
+};
+
 // A view of contiguous particles (the role of `&[P]`).
 template <class P>
 struct Slice {
+    using value_type = P;
     const P *ptr = nullptr;
     size_t len = 0;
     Slice() = default;
@@ -103,6 +122,18 @@ inline Vec3 position_of(const P &p) {
     return Vec3(float(p.position.x), float(p.position.y), float(p.position.z));
 }
 template <class P>
+inline double mu64_of(const P &p) {
+    if constexpr (detail::has_mu<P>::value) {
+        return double(p.mu);
+    } else if constexpr (detail::has_m<P>::value) {
+        return double(p.m);
+    } else if constexpr (detail::has_G<P>::value) {
+        return double(P::G * p.mass);
+    } else {
+        return double(p.mass);
+    }
+}
+template <class P>
 inline float mu_of(const P &p) {
     if constexpr (detail::has_mu<P>::value) {
         return float(p.mu);
@@ -114,12 +145,19 @@ inline float mu_of(const P &p) {
         return float(p.mass);
     }
 }
+namespace detail {
+// particles whose position components are doubles (glam DVec3 and the like)
+template <class P>
+struct is_f64_position
+    : std::is_same<std::decay_t<decltype(std::declval<const P &>().position.x)>, double> {};
+}  // namespace detail
 
 // ---- interactions ---------------------------------------------------------
 template <bool CHECKED>
 struct Acceleration {
     static constexpr bool checked = CHECKED;
     float softening() const { return 0.f; }
+    double softening64() const { return 0.0; }
 };
 inline Acceleration<true> acceleration_checked() { return {}; }
 inline Acceleration<false> acceleration_unchecked() { return {}; }
@@ -129,6 +167,7 @@ struct AccelerationSoftened {
     S softening_;
     static constexpr bool checked = CHECKED;
     float softening() const { return float(softening_); }
+    double softening64() const { return double(softening_); }
 };
 template <class S>
 AccelerationSoftened<S, true> softened_checked(S s) {
@@ -239,6 +278,22 @@ std::vector<float> pack_fields(Slice<P> s) {
     }
     return out;
 }
+template <class P>
+std::vector<double> pack_fields64(Slice<P> s) {
+    std::vector<double> out(4 * s.size());
+    for (size_t i = 0; i < s.size(); ++i) {
+        out[4 * i] = double(s[i].position.x);
+        out[4 * i + 1] = double(s[i].position.y);
+        out[4 * i + 2] = double(s[i].position.z);
+        out[4 * i + 3] = mu64_of(s[i]);
+    }
+    return out;
+}
+inline std::vector<DVec3> unpack64(const std::vector<double> &o) {
+    std::vector<DVec3> r(o.size() / 3);
+    for (size_t i = 0; i < r.size(); ++i) r[i] = DVec3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
+    return r;
+}
 inline std::vector<Vec3> unpack(const std::vector<float> &o) {
     std::vector<Vec3> r(o.size() / 3);
     for (size_t i = 0; i < r.size(); ++i) r[i] = Vec3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
@@ -252,21 +307,50 @@ struct BruteForce {
     T interaction;
     bool exact = false;  // bit-identical to sequential::BruteForce
 
+    // Accelerations of the affected particles: std::vector<Vec3> for f32 particles,
+    // std::vector<DVec3> (the reference's f64 result bit for bit) for DVec3 ones.
     template <class Storage>
-    std::vector<Vec3> compute(const Storage &storage) {
+    auto compute(const Storage &storage) {
         auto b = as_between(storage);
-        const auto aff = detail::pack_fields(b.affected);
+        using P1 = typename decltype(b.affected)::value_type;
         const bool same = static_cast<const void *>(b.affected.ptr) ==
                               static_cast<const void *>(b.affecting.ptr) &&
                           b.affected.size() == b.affecting.size();
-        const auto src = same ? std::vector<float>() : detail::pack_fields(b.affecting);
-        std::vector<float> out(3 * b.affected.size());
-        if (out.empty()) return {};
-        check(pt_bf_accel_f32(resources.get(), aff.data(), b.affected.size(),
-                              same ? aff.data() : src.data(), b.affecting.size(),
-                              interaction.softening(), T::checked ? 1 : 0, exact ? PT_BF_EXACT : 0u,
-                              out.data()));
-        return detail::unpack(out);
+        if constexpr (particular::detail::is_f64_position<P1>::value) {
+            const auto aff = detail::pack_fields64(b.affected);
+            const auto src = same ? std::vector<double>() : detail::pack_fields64(b.affecting);
+            std::vector<double> out(3 * b.affected.size());
+            if (out.empty()) return std::vector<DVec3>();
+            check(pt_bf_accel_dvec3(resources.get(), aff.data(), b.affected.size(),
+                                    same ? aff.data() : src.data(), b.affecting.size(),
+                                    interaction.softening64(), T::checked ? 1 : 0, out.data()));
+            return detail::unpack64(out);
+        } else {
+            const auto aff = detail::pack_fields(b.affected);
+            const auto src = same ? std::vector<float>() : detail::pack_fields(b.affecting);
+            std::vector<float> out(3 * b.affected.size());
+            if (out.empty()) return std::vector<Vec3>();
+            check(pt_bf_accel_f32(resources.get(), aff.data(), b.affected.size(),
+                                  same ? aff.data() : src.data(), b.affecting.size(),
+                                  interaction.softening(), T::checked ? 1 : 0, exact ? PT_BF_EXACT : 0u,
+                                  out.data()));
+            return detail::unpack(out);
+        }
+    }
+};
+
+// A Barnes-Hut tree kept on the device: built once by BarnesHut::build and walked
+// through Between(affected, tree), the counterpart of Between(&affected[..], &tree)
+// over a RootedOrthtree (lib.rs:186-199). Valid until the next Barnes-Hut call on the
+// same resources replaces the context's tree.
+struct CudaTree {
+    CudaResources *resources = nullptr;
+    size_t n_affecting = 0;
+    uint64_t generation = 0;
+    bool is_current() const {
+        uint64_t g = 0;
+        check(pt_bh_tree_generation(resources->get(), &g));
+        return g == generation;
     }
 };
 
@@ -276,6 +360,30 @@ struct BarnesHut {
     CudaResources &resources;
     T interaction;
     uint32_t flags = 0;  // PT_BH_QUADRUPOLE | PT_BH_GROUP
+
+    // Builds the tree over the affecting particles of `storage` once.
+    template <class Storage>
+    CudaTree build(const Storage &storage) {
+        auto b = as_between(storage);
+        const auto src = detail::pack_fields(b.affecting);
+        CudaTree t{&resources, b.affecting.size(), 0};
+        check(pt_bh_build(resources.get(), src.data(), b.affecting.size(), &t.generation));
+        return t;
+    }
+
+    // Walks a tree built by `build` for the affected particles.
+    template <class P>
+    std::vector<Vec3> compute(const Between<Slice<P>, CudaTree> &b) {
+        if (b.affecting.resources != &resources) throw Error(PT_ERR_INVALID, "particular cuda: tree of other resources");
+        if (!b.affecting.is_current())
+            throw Error(PT_ERR_INVALID, "particular cuda: the tree was replaced by a later Barnes-Hut call");
+        const auto aff = detail::pack_fields(b.affected);
+        std::vector<float> out(3 * b.affected.size());
+        if (out.empty()) return {};
+        check(pt_bh_walk(resources.get(), aff.data(), b.affected.size(), float(theta), interaction.softening(), flags,
+                         out.data()));
+        return detail::unpack(out);
+    }
 
     template <class Storage>
     std::vector<Vec3> compute(const Storage &storage) {
@@ -296,7 +404,7 @@ struct BarnesHut {
 
 // GpuCompute-style sugar: storage.cuda_brute_force(resources, interaction).
 template <class Storage, class T>
-std::vector<Vec3> cuda_brute_force(const Storage &storage, CudaResources &res, T interaction) {
+auto cuda_brute_force(const Storage &storage, CudaResources &res, T interaction) {
     return BruteForce<T>{res, interaction}.compute(storage);
 }
 template <class Storage, class S, class T>

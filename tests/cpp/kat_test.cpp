@@ -101,6 +101,72 @@ int main() {
     for (size_t i = 0; same && i < 3; ++i) same = a1[i].x == a2[i].x && a1[i].y == a2[i].y && a1[i].z == a2[i].z;
     std::printf("%-40s %s\n", "cuda_brute_force == BruteForce(Between)", same ? "ok" : "FAIL");
     ok &= same;
+
+    // DVec3 bodies: the f64 path, equal to the reference's scalar f64 kernel and fold
+    // (gravity/impls/mod.rs:150-166, sequential.rs:189-193) evaluated here in double
+    struct Body64 {
+        DVec3 position;
+        double mu;
+    };
+    std::vector<Body64> b64;
+    for (int i = 0; i < 257; ++i)
+        b64.push_back({DVec3(std::sin(1.1 * i), std::cos(0.7 * i) * 2.0, 1e-3 * i), 0.5 + (i % 7) * 0.25});
+    b64[5].position = b64[3].position;  // a coincident pair (checked: zero)
+    const auto g64 = cuda::cuda_brute_force(b64, res, softened_checked(1e-3));
+    bool exact64 = g64.size() == b64.size();
+    for (size_t i = 0; exact64 && i < b64.size(); ++i) {
+        volatile double sx = 0.0, sy = 0.0, sz = 0.0;  // kept in double, no contraction
+        for (size_t j = 0; j < b64.size(); ++j) {
+            volatile double dx = b64[j].position.x - b64[i].position.x;
+            volatile double dy = b64[j].position.y - b64[i].position.y;
+            volatile double dz = b64[j].position.z - b64[i].position.z;
+            volatile double dxx = dx * dx, dyy = dy * dy, dzz = dz * dz;
+            volatile double n2 = dxx + dyy;
+            volatile double n = n2 + dzz;
+            if (n == 0.0) {
+                sx = sx + dx;
+                sy = sy + dy;
+                sz = sz + dz;
+                continue;
+            }
+            volatile double ns = n + 1e-3 * 1e-3;
+            volatile double den = ns * std::sqrt(double(ns));
+            volatile double q = b64[j].mu / den;
+            volatile double ax = dx * q, ay = dy * q, az = dz * q;
+            sx = sx + ax;
+            sy = sy + ay;
+            sz = sz + az;
+        }
+        exact64 = g64[i].x == sx && g64[i].y == sy && g64[i].z == sz;
+    }
+    std::printf("%-40s %s\n", "cuda::BruteForce over DVec3 (bit-exact)", exact64 ? "ok" : "FAIL");
+    ok &= exact64;
+
+    // tree reuse: build once, walk two target sets; equal to the combined calls
+    std::vector<Body> srcs, t1, t2;
+    for (int i = 0; i < 5000; ++i)
+        srcs.push_back({Vec3(std::sin(0.37f * i) * 3.f, std::cos(0.91f * i) * 3.f, std::sin(0.13f * i)), 1.f / 5000});
+    for (int i = 0; i < 700; ++i) t1.push_back({Vec3(std::cos(0.5f * i) * 4.f, std::sin(0.3f * i), 0.2f), 0.f});
+    for (int i = 0; i < 900; ++i) t2.push_back({Vec3(0.01f * i - 4.f, 0.5f, -0.3f), 0.f});
+    cuda::BarnesHut<float, AccelerationSoftened<float, true>> bhq{0.5f, res, softened_checked(0.01f),
+                                                                  PT_BH_QUADRUPOLE | PT_BH_GROUP};
+    const cuda::CudaTree tree = bhq.build(srcs);
+    const auto w1 = bhq.compute(between(Slice<Body>(t1), tree));
+    const auto w2 = bhq.compute(between(Slice<Body>(t2), tree));
+    const bool current = tree.is_current();
+    const auto c1 = bhq.compute(between(Slice<Body>(t1), Slice<Body>(srcs)));
+    const auto c2 = bhq.compute(between(Slice<Body>(t2), Slice<Body>(srcs)));
+    bool reuse = current && !tree.is_current() && w1.size() == t1.size() && w2.size() == t2.size();
+    for (size_t i = 0; reuse && i < t1.size(); ++i) reuse = w1[i].x == c1[i].x && w1[i].y == c1[i].y && w1[i].z == c1[i].z;
+    for (size_t i = 0; reuse && i < t2.size(); ++i) reuse = w2[i].x == c2[i].x && w2[i].y == c2[i].y && w2[i].z == c2[i].z;
+    bool refused = false;
+    try {
+        bhq.compute(between(Slice<Body>(t1), tree));
+    } catch (const cuda::Error &) {
+        refused = true;
+    }
+    std::printf("%-40s %s\n", "BarnesHut tree reuse (build once, walk)", reuse && refused ? "ok" : "FAIL");
+    ok &= reuse && refused;
     std::printf("%s\n", ok ? "ALL OK" : "SOME FAILED");
     return ok ? 0 : 1;
 }
