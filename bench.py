@@ -48,6 +48,15 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def measured_hbm_gbs():
+    """The measured HBM copy bandwidth of this GPU pool (MEASURED_PEAKS.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return None
+
+
 def max_over_ranks(values, dist, device):
     """Element-wise maximum of a list of floats over all ranks (the slowest replica
     sets the job's time); identity without a process group."""
@@ -355,8 +364,22 @@ class BarnesHutWorkload:
         walk_ms = statistics.mean(walk)
         flops = self.walk_flops(st)
         achieved = flops / (walk_ms * 1e-3) / 1e12
+        build_ms = statistics.mean(build)
+        n, T, C = self.n, st.nodes, st.cells
+        M = T - C
+        # algorithmic bytes of one tree build (each pass's reads + writes of its
+        # arrays): bbox 16N; keys 16N + 12N; 8 radix passes x (8N histogram + 24N
+        # scatter); gather 36N; unique keys 24N; Karras + links 44M; layout 44T;
+        # leaf moments 16N + 56M + 8M; cell moments (children read + cell written)
+        # 32M + 256C
+        build_bytes = (16 + 28 + 8 * 32 + 36 + 24 + 16) * n + (24 + 20 + 56 + 8 + 32) * M + 44 * T + 256 * C
+        hbm = measured_hbm_gbs()
+        build_gbs = build_bytes / (build_ms * 1e-3) / 1e9
         return {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                 "frac": achieved / peak.value, "traffic": None,
+                "build": {"bound": "hbm", "achieved": build_gbs, "peak": hbm, "unit": "GB/s",
+                          "frac": build_gbs / hbm if hbm else None, "bytes": build_bytes,
+                          "ms": build_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy)"},
                 "kernel": "bh_walk_group" if self.flags & 2 else "bh_walk",
                 "walk_ms": walk_ms, "build_ms": statistics.mean(build),
                 "interactions_per_body": st.interactions / self.n,

@@ -105,13 +105,33 @@ __global__ void bbox_partial(const float4 *__restrict__ src, int n, float *__res
 
 // box = {min x,y,z, max x,y,z} of BoundingBox::square_with: centre = midpoint of the
 // AABB, half = (max extent + 0) / 2 (MidPoint::half), min/max = centre -/+ half.
+// One block of 256 threads folds the per-block extents (min/max: exact in any
+// order), then thread 0 forms the reference's square root box.
 __global__ void bbox_final(const float *__restrict__ part, int nb, float *__restrict__ box) {
-    if (threadIdx.x != 0) return;
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int b = 0; b < nb; ++b)
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
         for (int a = 0; a < 3; ++a) {
             mn[a] = fminf(mn[a], part[b * 6 + a]);
             mx[a] = fmaxf(mx[a], part[b * 6 + 3 + a]);
+        }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+        }
+    __shared__ float s[6][8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+        for (int a = 0; a < 3; ++a) {
+            s[a][warp] = mn[a];
+            s[3 + a][warp] = mx[a];
+        }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int w = 1; w < int(blockDim.x >> 5); ++w)
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = fminf(mn[a], s[a][w]);
+            mx[a] = fmaxf(mx[a], s[3 + a][w]);
         }
     float half = 0.0f;
     float c[3];
@@ -1213,7 +1233,7 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
     const int nb = std::min(1024, blocks(n));
     bbox_partial<<<nb, 256, 0, st>>>(d_src, n, as<float>(S.box_part));
     PT_TRY(check_launch(ctx, "bbox_partial"));
-    bbox_final<<<1, 32, 0, st>>>(as<float>(S.box_part), nb, as<float>(S.box));
+    bbox_final<<<1, 256, 0, st>>>(as<float>(S.box_part), nb, as<float>(S.box));
     PT_TRY(check_launch(ctx, "bbox_final"));
     make_keys<<<blocks(n), 256, 0, st>>>(d_src, n, as<float>(S.box), as<uint64_t>(S.keys), as<uint32_t>(S.idx));
     PT_TRY(check_launch(ctx, "make_keys"));
