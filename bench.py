@@ -238,7 +238,8 @@ class BarnesHutWorkload:
     bar = 1e-3
     # (theta, flags) candidates: quadrupole + group opening; the reference's own
     # monopole per-body walk at theta 0.5 is measured alongside as "plain".
-    ladder = [(0.45, 3), (0.5, 3), (0.52, 3), (0.55, 3), (0.6, 3)]
+    # flags: 1 quadrupole, 2 group, 8 local expansion of far nodes
+    ladder = [(0.45, 3), (0.5, 3), (0.52, 3), (0.55, 3), (0.6, 3), (0.48, 11), (0.5, 11), (0.52, 11), (0.55, 11)]
 
     def __init__(self, n=4194304, softening=0.01, sample=2048):
         from particular_gb300 import ics
@@ -290,7 +291,7 @@ class BarnesHutWorkload:
             ms = e0.elapsed_time(e1) / 3
             e = rel_err(self.d_out[idx_t].cpu().numpy(), self.ref64)
             return {"theta": theta, "quadrupole": bool(flags & 1), "group": bool(flags & 2),
-                    "learned": bool(flags & 4), "ms": ms, "bodies_per_s": self.n / (ms * 1e-3),
+                    "learned": bool(flags & 4), "local": bool(flags & 8), "ms": ms, "bodies_per_s": self.n / (ms * 1e-3),
                     **err_stats(e)}
 
         self.plain = measure(0.5, 0)
@@ -316,7 +317,8 @@ class BarnesHutWorkload:
         best = max(ok, key=lambda r: r["bodies_per_s"]) if ok else min(self.table, key=lambda r: r["p95"])
         self.meets_bar = bool(ok)
         self.theta = best["theta"]
-        self.flags = (1 if best["quadrupole"] else 0) | (2 if best["group"] else 0)
+        self.flags = ((1 if best["quadrupole"] else 0) | (2 if best["group"] else 0)
+                      | (8 if best.get("local") else 0))
         self.selected = best
 
     def _run(self, theta, flags):
@@ -339,10 +341,15 @@ class BarnesHutWorkload:
 
     QUAD_FLOPS = 38  # the quadrupole term's extra flops per accepted cell
 
+    LOCAL_FLOPS = (85, 180)  # one far node into a group's local expansion: monopole, + quadrupole
+
     def walk_flops(self, st):
         # monopole: 20 per accepted node (the GPU Gems convention); the quadrupole
-        # term adds 38 per accepted cell (single bodies carry none)
-        return 20 * st.interactions + (self.QUAD_FLOPS * st.cell_interactions if self.flags & 1 else 0)
+        # term adds 38 per accepted cell (single bodies carry none); a far node taken
+        # by the local expansion costs its lane 85 flops (180 with the quadrupole)
+        quad = bool(self.flags & 1)
+        return (20 * st.interactions + (self.QUAD_FLOPS * st.cell_interactions if quad else 0)
+                + self.LOCAL_FLOPS[quad] * st.local_nodes)
 
     def roofline(self, res, step_ms):
         import ctypes
@@ -384,13 +391,16 @@ class BarnesHutWorkload:
                 "walk_ms": walk_ms, "build_ms": statistics.mean(build),
                 "interactions_per_body": st.interactions / self.n,
                 "cell_interactions_per_body": st.cell_interactions / self.n,
+                "local_nodes_per_body": st.local_nodes / self.n,
                 "algorithmic": "20 flop per accepted node per body (+38 per accepted cell with "
-                               "the quadrupole) x the walk's own counts",
+                               "the quadrupole) + 85 (180 with the quadrupole) per far node taken "
+                               "by a group's local expansion, x the walk's own counts",
                 "peak_source": "measured FFMA-chain kernel over all SMs (pt_measure_fp32_peak)"}
 
     def extra(self):
         return {"method": {"name": "cuda::BarnesHut", "theta": self.theta,
-                           "quadrupole": bool(self.flags & 1), "group": bool(self.flags & 2)},
+                           "quadrupole": bool(self.flags & 1), "group": bool(self.flags & 2),
+                           "local": bool(self.flags & 8)},
                 "selected": self.selected, "meets_bar": self.meets_bar,
                 "calibration": self.table, "plain_reference_rule": self.plain,
                 "learned_theta1": self.learned_row,

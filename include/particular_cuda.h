@@ -164,10 +164,15 @@ int pt_bf_accel_f32_noalloc(const float *d_affected, size_t n_aff, const float *
  * skipped, Acceleration's CHECKED flag has no effect on this method, as in the
  * reference. Moments are accumulated in FP64 and stored in f32. */
 #define PT_BH_QUADRUPOLE 0x1u /* add the traceless quadrupole of accepted cells */
-#define PT_BH_GROUP 0x2u      /* walk per warp of 32 key-adjacent bodies: a cell is opened
-                                 for all of them when the per-body rule opens it for any
-                                 (so never less accurate than that rule); accepted nodes
-                                 are evaluated from shared-memory lists */
+#define PT_BH_GROUP 0x2u      /* walk per warp of 64 key-adjacent bodies (two per lane):
+                                 a cell is opened for all of them when the per-body rule
+                                 opens it for any (so never less accurate than that
+                                 rule); accepted nodes are evaluated from shared-memory
+                                 lists */
+#define PT_BH_LOCAL 0x8u      /* with PT_BH_GROUP: far nodes (group radius < ratio x
+                                 distance, pt_bh_set_local_ratio, default 0.1) enter
+                                 a second-order local expansion about the group's
+                                 centre instead of every body's interaction list */
 #define PT_BH_LEARNED 0x4u    /* with PT_BH_GROUP: add the learned far-field correction
                                  (pt_mlp_*) of every cell accepted at theta that the
                                  model's inner angle would have opened, evaluated once
@@ -188,6 +193,8 @@ typedef struct pt_bh_stats {
     uint64_t cell_interactions; /* the accepted nodes of `interactions` that are cells
                                    (the ones a PT_BH_QUADRUPOLE walk adds the
                                    quadrupole term to) */
+    uint64_t local_nodes;  /* PT_BH_LOCAL: far nodes added to the groups' local
+                              expansions (per group and node) */
 } pt_bh_stats;
 
 /* cuda::BarnesHut over host buffers (synchronous). Layouts as pt_bf_accel_f32. */
@@ -215,6 +222,8 @@ int pt_bh_tree_generation(pt_ctx *ctx, uint64_t *generation);
 int pt_bh_build(pt_ctx *ctx, const float *affecting, size_t n_src, uint64_t *generation);
 int pt_bh_walk(pt_ctx *ctx, const float *affected, size_t n_aff, float theta, float softening,
                uint32_t flags, float *out_xyz);
+/* The far ratio of PT_BH_LOCAL, in (0, 0.5]: smaller is more accurate and slower. */
+int pt_bh_set_local_ratio(pt_ctx *ctx, float ratio);
 /* Caps the PT_BH_GROUP walk's shared-memory stack at `ranges` entries per warp (2 to
  * the compiled capacity; 0 restores the capacity). A warp that runs out takes the
  * per-body walk instead (counted in pt_bh_stats.overflow): a tuning and test hook. */

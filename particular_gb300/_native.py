@@ -23,6 +23,7 @@ PT_BF_VEC3A = 0x2
 PT_BH_QUADRUPOLE = 0x1
 PT_BH_GROUP = 0x2
 PT_BH_LEARNED = 0x4
+PT_BH_LOCAL = 0x8
 PT_MLP_NPARAM = 5188
 PT_METHOD_BRUTE_FORCE = 0
 PT_METHOD_BARNES_HUT = 1
@@ -37,7 +38,8 @@ class BhStats(ctypes.Structure):
                 ("leaves", ctypes.c_uint64), ("interactions", ctypes.c_uint64),
                 ("visits", ctypes.c_uint64), ("warps", ctypes.c_uint64),
                 ("max_stack", ctypes.c_uint64), ("overflow", ctypes.c_uint64),
-                ("learned", ctypes.c_uint64), ("cell_interactions", ctypes.c_uint64)]
+                ("learned", ctypes.c_uint64), ("cell_interactions", ctypes.c_uint64),
+                ("local_nodes", ctypes.c_uint64)]
 
 _NAMES = {PT_ERR_INVALID: "PT_ERR_INVALID", PT_ERR_CUDA: "PT_ERR_CUDA", PT_ERR_OOM: "PT_ERR_OOM",
           PT_ERR_CAPACITY: "PT_ERR_CAPACITY", PT_ERR_TIMEOUT: "PT_ERR_TIMEOUT",
@@ -93,6 +95,7 @@ def _declare(L):
                                                   c_ptr]),
         "pt_bh_last_stats": (ctypes.c_int, [c_ptr, ctypes.POINTER(BhStats)]),
         "pt_bh_set_stack_limit": (ctypes.c_int, [c_ptr, ctypes.c_int]),
+        "pt_bh_set_local_ratio": (ctypes.c_int, [c_ptr, ctypes.c_float]),
         "pt_bh_build_device": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr]),
         "pt_bh_walk_device": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, ctypes.c_float, ctypes.c_float,
                                              ctypes.c_uint32, c_ptr]),

@@ -67,6 +67,7 @@ struct State {
     int lcap = 0;                     // record chunks allocated
     int stack_cap = 0;                // group-walk stack ranges per warp in use (0 = all)
     uint64_t generation = 0;          // trees built so far (0 = none)
+    float local_ratio = 0.1f;         // PT_BH_LOCAL: far when group radius < ratio * distance
     const uint32_t *mlp_w = nullptr;  // learned correction: packed BF16 weights (owned by the MLP state)
     const float *mlp_b = nullptr;     // and its bias block
     float theta_inner = 0.5f;
@@ -810,6 +811,96 @@ __global__ void bh_learned_apply(LearnedRecords L, const uint32_t *__restrict__ 
     out[3 * size_t(o) + 2] += cz;
 }
 
+// ---- local (Taylor) expansion of far nodes about the group centre -------------
+// PT_BH_LOCAL: an accepted node far from the group (group radius R < ratio * d, d
+// from the group's box centre g to the node's centre of mass) is not added to the
+// interaction lists. The lane that popped it adds the node's softened monopole (+
+// quadrupole) field to a second-order expansion of the acceleration about g:
+// a(g + r) = a0 + T r + 1/2 H : r r, with
+//   a0 = m d s^-3/2,  T_ij = 3m d_i d_j s^-5/2 - m delta_ij s^-3/2,
+//   H_ijk = 15m d_i d_j d_k s^-7/2 - 3m s^-5/2 (delta_ij d_k + delta_ik d_j + delta_jk d_i)
+// (s = |d|^2 + eps^2: the exact derivatives of the softened kernel), plus the
+// quadrupole's a0 and T. The expansion costs one lane ~150 flops per far node
+// instead of every target's list entry; its truncation error is ~(R/d)^3.
+struct LocalExp {
+    float ax, ay, az;                                      // a(g)
+    float txx, txy, txz, tyy, tyz, tzz;                    // d a_i / d x_j
+    float hxxx, hxxy, hxxz, hxyy, hxyz, hxzz, hyyy, hyyz, hyzz, hzzz;  // d2 a_i / dx_j dx_k
+};
+
+// Adds the softened monopole (+ traceless quadrupole q, when given) field of a node
+// at offset d = com - g, mass m, to the expansion about g.
+__device__ __forceinline__ void local_add(LocalExp &L, float dx, float dy, float dz, float m, float eps2,
+                                          const float4 *q0p, const float4 *q1p) {
+    const float s = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+    const float inv = rsqrt_ftz(s);
+    const float inv2 = inv * inv;
+    const float i3 = m * inv * inv2;      // m s^-3/2
+    const float i5 = 3.0f * i3 * inv2;    // 3 m s^-5/2
+    const float i7 = 5.0f * i5 * inv2;    // 15 m s^-7/2
+    L.ax = fmaf(i3, dx, L.ax);
+    L.ay = fmaf(i3, dy, L.ay);
+    L.az = fmaf(i3, dz, L.az);
+    const float xx = dx * dx, yy = dy * dy, zz = dz * dz, xy = dx * dy, xz = dx * dz, yz = dy * dz;
+    L.txx += fmaf(i5, xx, -i3);
+    L.txy = fmaf(i5, xy, L.txy);
+    L.txz = fmaf(i5, xz, L.txz);
+    L.tyy += fmaf(i5, yy, -i3);
+    L.tyz = fmaf(i5, yz, L.tyz);
+    L.tzz += fmaf(i5, zz, -i3);
+    const float ax7 = i7 * dx, ay7 = i7 * dy, az7 = i7 * dz;
+    L.hxxx += fmaf(ax7, xx, -3.0f * i5 * dx);
+    L.hxxy += fmaf(ax7, xy, -i5 * dy);
+    L.hxxz += fmaf(ax7, xz, -i5 * dz);
+    L.hxyy += fmaf(ax7, yy, -i5 * dx);
+    L.hxyz = fmaf(ax7, yz, L.hxyz);
+    L.hxzz += fmaf(ax7, zz, -i5 * dx);
+    L.hyyy += fmaf(ay7, yy, -3.0f * i5 * dy);
+    L.hyyz += fmaf(ay7, yz, -i5 * dz);
+    L.hyzz += fmaf(ay7, zz, -i5 * dy);
+    L.hzzz += fmaf(az7, zz, -3.0f * i5 * dz);
+    if (q0p) {
+        const float4 q0 = __ldg(q0p), q1 = __ldg(q1p);  // Qxx Qxy Qxz Qyy | Qyz Qzz
+        const float ux = fmaf(q0.x, dx, fmaf(q0.y, dy, q0.z * dz));
+        const float uy = fmaf(q0.y, dx, fmaf(q0.w, dy, q1.x * dz));
+        const float uz = fmaf(q0.z, dx, fmaf(q1.x, dy, q1.y * dz));
+        const float c = fmaf(dx, ux, fmaf(dy, uy, dz * uz));
+        const float j5 = inv2 * inv2 * inv, j7 = j5 * inv2, j9 = j7 * inv2;
+        const float c7 = 2.5f * c * j7;
+        L.ax += fmaf(c7, dx, -ux * j5);
+        L.ay += fmaf(c7, dy, -uy * j5);
+        L.az += fmaf(c7, dz, -uz * j5);
+        const float f5 = 5.0f * j7, g9 = 17.5f * c * j9;
+        L.txx += fmaf(q0.x, j5, fmaf(g9, xx, -fmaf(2.0f * f5, ux * dx, c7)));
+        L.tyy += fmaf(q0.w, j5, fmaf(g9, yy, -fmaf(2.0f * f5, uy * dy, c7)));
+        L.tzz += fmaf(q1.y, j5, fmaf(g9, zz, -fmaf(2.0f * f5, uz * dz, c7)));
+        L.txy += fmaf(q0.y, j5, fmaf(g9, xy, -f5 * fmaf(ux, dy, uy * dx)));
+        L.txz += fmaf(q0.z, j5, fmaf(g9, xz, -f5 * fmaf(ux, dz, uz * dx)));
+        L.tyz += fmaf(q1.x, j5, fmaf(g9, yz, -f5 * fmaf(uy, dz, uz * dy)));
+    }
+}
+
+__device__ __forceinline__ void local_reduce(LocalExp &L) {
+    float *f = &L.ax;
+#pragma unroll
+    for (int k = 0; k < 19; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) f[k] += __shfl_xor_sync(0xffffffffu, f[k], o);
+}
+
+// a(g + d) from the expansion
+__device__ __forceinline__ void local_eval(const LocalExp &L, float dx, float dy, float dz, float &ax, float &ay,
+                                           float &az) {
+    const float xx = dx * dx, yy = dy * dy, zz = dz * dz, xy2 = 2.0f * dx * dy, xz2 = 2.0f * dx * dz,
+                yz2 = 2.0f * dy * dz;
+    ax = L.ax + fmaf(L.txx, dx, fmaf(L.txy, dy, L.txz * dz)) +
+         0.5f * fmaf(L.hxxx, xx, fmaf(L.hxyy, yy, fmaf(L.hxzz, zz, fmaf(L.hxxy, xy2, fmaf(L.hxxz, xz2, L.hxyz * yz2)))));
+    ay = L.ay + fmaf(L.txy, dx, fmaf(L.tyy, dy, L.tyz * dz)) +
+         0.5f * fmaf(L.hxxy, xx, fmaf(L.hyyy, yy, fmaf(L.hyzz, zz, fmaf(L.hxyy, xy2, fmaf(L.hxyz, xz2, L.hyyz * yz2)))));
+    az = L.az + fmaf(L.txz, dx, fmaf(L.tyz, dy, L.tzz * dz)) +
+         0.5f * fmaf(L.hxxz, xx, fmaf(L.hyyz, yy, fmaf(L.hzzz, zz, fmaf(L.hxyz, xy2, fmaf(L.hxzz, xz2, L.hyzz * yz2)))));
+}
+
 // Targets per lane of the group walk: a warp walks for 32 * GW_TPL key-adjacent
 // targets, and each list entry read from shared memory serves all of a lane's
 // targets. Measured at N = 4M bulge+disk, theta 0.5, quadrupole: 1 -> 18.3 ms
@@ -826,13 +917,15 @@ static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
 #ifndef PT_GW_MINB
 #define PT_GW_MINB (GW_TPL == 1 ? 6 : 5)  // CTAs per SM the register budget is set for
 #endif
-template <bool QUAD, bool GUARD, bool LEARNED>
-__global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
+template <bool QUAD, bool GUARD, bool LEARNED, bool LOCAL>
+__global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 4 : PT_GW_MINB)
     bh_walk_group(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
                   const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
                   const float4 *__restrict__ nodeG, const float4 *__restrict__ sbody, const int *__restrict__ counters,
                   float th2, float th_in2, LearnedRecords LR, float eps2, float *__restrict__ out,
-                  unsigned long long *__restrict__ stats, int *__restrict__ err, int stack_cap) {
+                  unsigned long long *__restrict__ stats, int *__restrict__ err, int stack_cap,
+                  float local_ratio) {
+    static_assert(!(LEARNED && LOCAL), "PT_BH_LEARNED and PT_BH_LOCAL are exclusive");
     constexpr int NFC = QUAD ? 10 : 4;
     constexpr int TPL = GW_TPL;
     using CellList = IList<NFC, 96>;
@@ -894,6 +987,12 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
         gcy /= nv;
         gcz /= nv;
     }
+    // PT_BH_LOCAL: the expansion centre g (box centre) and the far radius^2
+    const float lgx = 0.5f * (mn0 + mx0), lgy = 0.5f * (mn1 + mx1), lgz = 0.5f * (mn2 + mx2);
+    const float rg2 = 0.25f * fmaf(mx0 - mn0, mx0 - mn0, fmaf(mx1 - mn1, mx1 - mn1, (mx2 - mn2) * (mx2 - mn2)));
+    const float far2 = LOCAL ? rg2 / (local_ratio * local_ratio) : 0.f;
+    LocalExp LX{};
+    unsigned long long nlocal = 0;
     // learned: the warp's current record chunk and its fill; the previous chunk links to
     // the next one (head of the group's chain first)
     int chunk = -1, fill = LCHUNK;
@@ -1031,9 +1130,20 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
         S += total;
         maxS = max(maxS, S);
         const bool acc = have && !open;
+        bool farc = false;
+        if (LOCAL && acc && (B.z < 0 || B.w == 1) && A.w != 0.0f) {  // cells and single bodies
+            const float dx = A.x - lgx, dy = A.y - lgy, dz = A.z - lgz;
+            if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > far2) {
+                farc = true;
+                const bool q = QUAD && B.z < 0;
+                local_add(LX, dx, dy, dz, A.w, eps2, q ? nodeQ + 2 * node : nullptr,
+                          q ? nodeQ + 2 * node + 1 : nullptr);
+                ++nlocal;
+            }
+        }
         const bool bucket = acc && B.z >= 0 && B.w > 1;
-        const bool cellacc = acc && B.z < 0;
-        const bool bodyacc = acc && B.z >= 0 && B.w == 1;
+        const bool cellacc = acc && B.z < 0 && !farc;
+        const bool bodyacc = acc && B.z >= 0 && B.w == 1 && !farc;
         // accepted cells -> the cell list (with their quadrupoles)
         const unsigned mc = __ballot_sync(0xffffffffu, cellacc);
         const int nc1 = __popc(mc);
@@ -1117,6 +1227,19 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
         ry[i] = y0 + y1;
         rz[i] = z0 + z1;
     }
+    if (LOCAL) {
+        local_reduce(LX);
+#pragma unroll
+        for (int i = 0; i < TPL; ++i) {
+            float lx, ly, lz;
+            local_eval(LX, p[i].x - lgx, p[i].y - lgy, p[i].z - lgz, lx, ly, lz);
+            rx[i] += lx;
+            ry[i] += ly;
+            rz[i] += lz;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nlocal += __shfl_xor_sync(0xffffffffu, nlocal, o);
+    }
     const unsigned long long nv = unsigned(nvalid);
     unsigned long long s_acc = entries * nv, s_vis = visits * nv, s_cell = centries * nv;
     if (failed) {
@@ -1160,6 +1283,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, PT_GW_MINB)
         atomicAdd(stats + 0, s_acc);
         atomicAdd(stats + 1, s_vis);
         if (LEARNED) atomicAdd(stats + 4, learned);
+        if (LOCAL && !failed) atomicAdd(stats + 7, nlocal);
         atomicAdd(stats + 5, s_cell);
         atomicAdd(stats + 2, 1ull);
         atomicMax(stats + 3, (unsigned long long)maxS);
@@ -1171,17 +1295,20 @@ using WalkKernel = void (*)(const float4 *, const uint32_t *, int, const float4 
                             const float4 *, const int *, float, float, float *, unsigned long long *);
 using GroupKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
                              const float4 *, const float4 *, const int *, float, float, LearnedRecords, float,
-                             float *, unsigned long long *, int *, int);
+                             float *, unsigned long long *, int *, int, float);
 
 static WalkKernel walk_kernel(bool quad) { return quad ? bh_walk<true> : bh_walk<false>; }
 
-static GroupKernel group_kernel(bool quad, bool guard, bool learned) {
-    if (learned) {
-        if (quad) return guard ? bh_walk_group<true, true, true> : bh_walk_group<true, false, true>;
-        return guard ? bh_walk_group<false, true, true> : bh_walk_group<false, false, true>;
-    }
-    if (quad) return guard ? bh_walk_group<true, true, false> : bh_walk_group<true, false, false>;
-    return guard ? bh_walk_group<false, true, false> : bh_walk_group<false, false, false>;
+template <bool LEARNED, bool LOCAL>
+static GroupKernel group_kernel_q(bool quad, bool guard) {
+    if (quad) return guard ? bh_walk_group<true, true, LEARNED, LOCAL> : bh_walk_group<true, false, LEARNED, LOCAL>;
+    return guard ? bh_walk_group<false, true, LEARNED, LOCAL> : bh_walk_group<false, false, LEARNED, LOCAL>;
+}
+
+static GroupKernel group_kernel(bool quad, bool guard, bool learned, bool local) {
+    if (learned) return group_kernel_q<true, false>(quad, guard);
+    if (local) return group_kernel_q<false, true>(quad, guard);
+    return group_kernel_q<false, false>(quad, guard);
 }
 
 static State *state(pt_ctx *ctx) {
@@ -1338,12 +1465,12 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
 static int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n_aff, float theta,
                 float softening, uint32_t flags, float *d_out) {
     cudaStream_t st = ctx->stream;
-    // counters: int[4] = {leaves, nodes, cells, error} then u64[7] = {interactions,
+    // counters: int[4] = {leaves, nodes, cells, error} then u64[8] = {interactions,
     // visits, warps, max group stack, learned records, cell interactions, warps that
-    // fell back to the per-body walk}
+    // fell back to the per-body walk, far nodes taken by the local expansion}
     unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 2;
     int *err = as<int>(S.counters) + 3;
-    PT_CUDA(cudaMemsetAsync(stats, 0, 7 * sizeof(unsigned long long), st));
+    PT_CUDA(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
     PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     const float th2 = theta * theta;
     const float eps2 = softening * softening;
@@ -1370,10 +1497,11 @@ static int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx
                                     as<float4>(S.lcentre), as<float4>(S.lpart), as<int>(S.lused), S.lcap};
                 PT_CUDA(cudaMemsetAsync(LR.used, 0, sizeof(int), st));
             }
-            group_kernel(quad, eps2 == 0.0f, learned)<<<(groups + GW_WARPS - 1) / GW_WARPS, 32 * GW_WARPS, 0, st>>>(
+            group_kernel(quad, eps2 == 0.0f, learned, flags & PT_BH_LOCAL)<<<(groups + GW_WARPS - 1) / GW_WARPS,
+                                                                          32 * GW_WARPS, 0, st>>>(
                 tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.nodeG),
                 as<float4>(S.sbody), as<int>(S.counters), th2, S.theta_inner * S.theta_inner, LR, eps2, d_out, stats,
-                err, S.stack_cap > 0 ? S.stack_cap : GW_STACK);
+                err, S.stack_cap > 0 ? S.stack_cap : GW_STACK, S.local_ratio);
             PT_TRY(check_launch(ctx, "bh_walk_group"));
             // Outside stream capture the record count is checked and the walk rerun
             // with room for all records; inside, an overflow sets error bit 2.
@@ -1384,7 +1512,7 @@ static int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx
             if (used <= S.lcap) break;
             S.lcap = used + used / 4;
             PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-            PT_CUDA(cudaMemsetAsync(stats, 0, 7 * sizeof(unsigned long long), st));
+            PT_CUDA(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
         }
         if (learned) {
             bh_learned_eval<<<ctx->sm_count * 4, 128, 0, st>>>(LR, as<float4>(S.nodeA), as<float4>(S.nodeQ),
@@ -1410,10 +1538,14 @@ static int validate(const char *fn, size_t n_aff, size_t n_src, uint32_t flags) 
     const size_t lim = size_t(INT_MAX) / 8;
     if (n_aff > lim || n_src > lim)
         return set_error(PT_ERR_INVALID, "%s: n_aff=%zu n_src=%zu exceed the limit %zu", fn, n_aff, n_src, lim);
-    if (flags & ~(PT_BH_QUADRUPOLE | PT_BH_GROUP | PT_BH_LEARNED))
+    if (flags & ~(PT_BH_QUADRUPOLE | PT_BH_GROUP | PT_BH_LEARNED | PT_BH_LOCAL))
         return set_error(PT_ERR_INVALID, "%s: unknown flags 0x%x", fn, flags);
     if ((flags & PT_BH_LEARNED) && !(flags & PT_BH_GROUP))
         return set_error(PT_ERR_INVALID, "%s: PT_BH_LEARNED requires PT_BH_GROUP", fn);
+    if ((flags & PT_BH_LOCAL) && !(flags & PT_BH_GROUP))
+        return set_error(PT_ERR_INVALID, "%s: PT_BH_LOCAL requires PT_BH_GROUP", fn);
+    if ((flags & PT_BH_LOCAL) && (flags & PT_BH_LEARNED))
+        return set_error(PT_ERR_INVALID, "%s: PT_BH_LOCAL and PT_BH_LEARNED are exclusive", fn);
     return PT_OK;
 }
 
@@ -1622,6 +1754,18 @@ int pt_bh_tree_generation(pt_ctx *ctx, uint64_t *generation) {
     return PT_OK;
 }
 
+int pt_bh_set_local_ratio(pt_ctx *ctx, float ratio) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_set_local_ratio: ctx is NULL");
+    if (!(ratio > 0.0f && ratio <= 0.5f))
+        return set_error(PT_ERR_INVALID, "pt_bh_set_local_ratio: %g outside (0, 0.5]", double(ratio));
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    S->local_ratio = ratio;
+    return PT_OK;
+}
+
 int pt_bh_set_stack_limit(pt_ctx *ctx, int ranges) {
     using namespace pt;
     clear_error();
@@ -1642,7 +1786,7 @@ int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out) {
     auto *S = static_cast<bh::State *>(ctx->bh);
     if (!S || !S->counters.ptr) return set_error(PT_ERR_INVALID, "pt_bh_last_stats: no Barnes-Hut call yet");
     PT_CUDA(cudaSetDevice(ctx->device));
-    unsigned long long h[9];
+    unsigned long long h[10];
     PT_CUDA(cudaMemcpyAsync(h, S->counters.ptr, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
     PT_CUDA(cudaStreamSynchronize(ctx->stream));
     const int *hi = reinterpret_cast<const int *>(h);
@@ -1650,6 +1794,7 @@ int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out) {
     out->nodes = uint64_t(hi[1]);
     out->cells = uint64_t(hi[2]);
     out->overflow = h[8];
+    out->local_nodes = h[9];
     out->interactions = h[2];
     out->visits = h[3];
     out->warps = h[4];

@@ -153,23 +153,27 @@ class BarnesHut:
     and walked with the reference's opening rule (sequential.rs:466-505).
 
     quadrupole=True adds the accepted cells' quadrupole terms; group=True opens a
-    cell for a warp of 32 neighbouring bodies whenever one of them opens it. Both
+    cell for a warp of 64 neighbouring bodies whenever one of them opens it. Both
     only ever reduce the error relative to the reference's monopole walk.
+    local=True (with group) sends nodes far from the group into a second-order
+    local expansion about the group's centre (resources-wide ratio:
+    pt_bh_set_local_ratio); its truncation error is judged against FP64.
     """
 
     def __init__(self, theta, resources, interaction, quadrupole=False, group=False,
-                 learned=False):
+                 learned=False, local=False):
         self.theta = float(np.float32(theta))
         self.resources = resources
         self.interaction = interaction
         self.quadrupole = bool(quadrupole)
         self.group = bool(group)
         self.learned = bool(learned)  # needs a model (particular_gb300.learned) and group
+        self.local = bool(local)      # far nodes through the group's local expansion
 
     @property
     def flags(self):
         return ((N.PT_BH_QUADRUPOLE if self.quadrupole else 0) | (N.PT_BH_GROUP if self.group else 0)
-                | (N.PT_BH_LEARNED if self.learned else 0))
+                | (N.PT_BH_LEARNED if self.learned else 0) | (N.PT_BH_LOCAL if self.local else 0))
 
     def build(self, affecting):
         """Builds the tree over `affecting` (any storage of particles) once; pass the
@@ -205,6 +209,7 @@ class BarnesHut:
         return out
 
     def stats(self):
+        """Counters of the last Barnes-Hut call on these resources (pt_bh_last_stats)."""
         st = N.BhStats()
         N.check(N.lib().pt_bh_last_stats(self.resources.handle, ctypes.byref(st)))
         return {k: int(getattr(st, k)) for k, _ in N.BhStats._fields_}

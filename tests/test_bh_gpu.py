@@ -364,3 +364,72 @@ def test_tree_reuse_device_entry_points(res):
     g2 = ctypes.c_uint64(0)
     N.check(L.pt_bh_tree_generation(res.handle, ctypes.byref(g2)))
     assert g2.value > g.value > 0
+
+
+def test_local_expansion_matches_direct_far_field(res):
+    """A compact group of targets and an elongated far cluster (a quadrupole): with
+    PT_BH_LOCAL the cluster enters the group's second-order expansion. The result
+    differs from the direct evaluation only by the expansion's truncation, O((R/d)^3)
+    ~ 2e-4 here; a wrong first- or second-order term would show at (R/d) ~ 6e-2 or
+    (R/d)^2 ~ 3e-3."""
+    rng = np.random.default_rng(52)
+    tgt = np.zeros((64, 4), np.float32)
+    tgt[:, :3] = rng.uniform(-0.1, 0.1, (64, 3))
+    clu = np.zeros((400, 4), np.float32)
+    clu[:, 0] = 3.0 + rng.uniform(-0.25, 0.25, 400)
+    clu[:, 1] = 0.5 + rng.uniform(-0.05, 0.05, 400)
+    clu[:, 2] = rng.uniform(-0.05, 0.05, 400)
+    clu[:, 3] = 1.0 / 400
+    L = N.lib()
+    for quad in (False, True):
+        direct = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=quad, group=True)
+        local = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=quad, group=True, local=True)
+        want = direct.compute(Between(tgt, clu))
+        st0 = direct.stats()  # stats describe the context's last call
+        got = local.compute(Between(tgt, clu))
+        st = local.stats()
+        assert st["local_nodes"] > 0 and st["interactions"] < st0["interactions"]
+        rel = np.abs(got - want).max() / np.abs(want).max()
+        assert rel < 1e-3, (quad, rel)
+    # a tiny ratio keeps every node direct: identical to the walk without PT_BH_LOCAL
+    N.check(L.pt_bh_set_local_ratio(res.handle, 1e-4))
+    try:
+        b = ics.plummer(20000, seed=53)["bodies"]
+        got = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=True, group=True,
+                             local=True).compute(b)
+        want = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=True, group=True).compute(b)
+        np.testing.assert_array_equal(got, want)
+    finally:
+        N.check(L.pt_bh_set_local_ratio(res.handle, 0.1))
+
+
+@pytest.mark.parametrize("kind", ["plummer", "bulge_disk"])
+def test_local_expansion_accuracy(res, oracle, kind):
+    """PT_BH_LOCAL at the default ratio (0.1): the FP64-judged error stays within 10 %
+    of the walk without it on every reported percentile, with fewer list entries."""
+    b = {"plummer": lambda: ics.plummer(60000, seed=54)["bodies"],
+         "bulge_disk": lambda: ics.bulge_disk(60000, seed=55)["bodies"]}[kind]()
+    ref64 = oracle.bf_f64(b[::20], b, 0.01, True)
+    plain = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=True, group=True)
+    local = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=True, group=True, local=True)
+    e0 = rel(plain.compute(b)[::20], ref64)
+    s0 = plain.stats()  # stats describe the context's last call
+    e1 = rel(local.compute(b)[::20], ref64)
+    s1 = local.stats()
+    print(f"{kind}: p50/p95/max plain {np.median(e0):.2e}/{np.percentile(e0, 95):.2e}/{e0.max():.2e} "
+          f"local {np.median(e1):.2e}/{np.percentile(e1, 95):.2e}/{e1.max():.2e}; list entries "
+          f"{s0['interactions']} -> {s1['interactions']} (+{s1['local_nodes']} local)")
+    assert s1["interactions"] < s0["interactions"] and s1["local_nodes"] > 0
+    for q in (50, 95, 99):
+        assert np.percentile(e1, q) <= 1.1 * np.percentile(e0, q) + 1e-7, q
+
+
+def test_local_flag_validation(res):
+    L = N.lib()
+    b = ics.plummer(1000, seed=56)["bodies"]
+    with pytest.raises(N.CudaError):
+        cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), local=True).compute(b)  # needs group
+    with pytest.raises(N.CudaError):
+        N.check(L.pt_bh_set_local_ratio(res.handle, 0.0))
+    with pytest.raises(N.CudaError):
+        N.check(L.pt_bh_set_local_ratio(res.handle, 0.7))
