@@ -999,6 +999,8 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 4 : PT_GW_MINB)
     unsigned long long learned = 0;
 
     const f2 e2 = pk2(eps2, eps2);
+    // the lane's two targets packed, for the opening vote
+    const f2 vx01 = pk2(p[0].x, p[TPL - 1].x), vy01 = pk2(p[0].y, p[TPL - 1].y), vz01 = pk2(p[0].z, p[TPL - 1].z);
     f2 px[TPL], py[TPL], pz[TPL], ax[TPL], ay[TPL], az[TPL];
 #pragma unroll
     for (int i = 0; i < TPL; ++i) {
@@ -1065,12 +1067,21 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 4 : PT_GW_MINB)
             const float cz = __shfl_sync(0xffffffffu, A.z, j);
             const float cw = __shfl_sync(0xffffffffu, w, j);
             bool o1 = false, i1 = false;
+            const float cw2 = cw * cw;
+            if constexpr (TPL == 2) {  // both targets in one packed pass (same IEEE ops)
+                const f2 dx = sub2(pk2(cx, cx), vx01), dy = sub2(pk2(cy, cy), vy01), dz = sub2(pk2(cz, cz), vz01);
+                float d0, d1;
+                upk2(fma2(dx, dx, fma2(dy, dy, mul2(dz, dz))), d0, d1);
+                o1 = (d0 > 0.0f && th2 * d0 < cw2) || (d1 > 0.0f && th2 * d1 < cw2);
+                if (LEARNED) i1 = (d0 > 0.0f && th_in2 * d0 < cw2) || (d1 > 0.0f && th_in2 * d1 < cw2);
+            } else {
 #pragma unroll
-            for (int i = 0; i < TPL; ++i) {
-                const float dx = cx - p[i].x, dy = cy - p[i].y, dz = cz - p[i].z;
-                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                o1 |= d2 > 0.0f && th2 * d2 < cw * cw;
-                if (LEARNED) i1 |= d2 > 0.0f && th_in2 * d2 < cw * cw;
+                for (int i = 0; i < TPL; ++i) {
+                    const float dx = cx - p[i].x, dy = cy - p[i].y, dz = cz - p[i].z;
+                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    o1 |= d2 > 0.0f && th2 * d2 < cw2;
+                    if (LEARNED) i1 |= d2 > 0.0f && th_in2 * d2 < cw2;
+                }
             }
             const unsigned vo = __ballot_sync(0xffffffffu, o1);
             if (lane == j) open = vo != 0u;
@@ -1109,14 +1120,10 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 4 : PT_GW_MINB)
         }
         const bool rest = have && B.y < range.y;  // later siblings remain
         const int np = int(rest) + int(open);
-        int incl = np;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        int slot = S + incl - np;
+        // each lane's pushes follow those of the lanes below it
+        const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, open);
+        const int total = __popc(mrest) + __popc(mopen);
+        int slot = S + __popc(mrest & lt) + __popc(mopen & lt);
         if (slot + np > stack_cap) {
             failed = true;  // never written out of bounds
         } else {
