@@ -918,7 +918,7 @@ static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
 #define PT_GW_MINB (GW_TPL == 1 ? 6 : 5)  // CTAs per SM the register budget is set for
 #endif
 template <bool QUAD, bool GUARD, bool LEARNED, bool LOCAL>
-__global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 4 : PT_GW_MINB)
+__global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
     bh_walk_group(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
                   const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
                   const float4 *__restrict__ nodeG, const float4 *__restrict__ sbody, const int *__restrict__ counters,
@@ -930,9 +930,15 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 4 : PT_GW_MINB)
     constexpr int TPL = GW_TPL;
     using CellList = IList<NFC, 96>;
     using BodyList = IList<4, 128>;
-    __shared__ int2 s_stack[GW_WARPS][GW_STACK];
+    // PT_BH_LOCAL keeps its 19 expansion coefficients per lane in shared memory
+    // ([coefficient][lane]: no bank conflicts) and trims the stack to 320 ranges, so
+    // that 5 CTAs stay resident at 96 registers and 44 KB.
+    constexpr int STK = LOCAL ? 320 : GW_STACK;
+    stack_cap = min(stack_cap, STK);
+    __shared__ int2 s_stack[GW_WARPS][STK];
     __shared__ __align__(16) CellList s_cells[GW_WARPS];
     __shared__ __align__(16) BodyList s_bodies[GW_WARPS];
+    __shared__ float s_lx[GW_WARPS][LOCAL ? 19 : 1][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int group = blockIdx.x * GW_WARPS + warp;
     const int g0 = group * GW_GROUP;
@@ -991,7 +997,8 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 4 : PT_GW_MINB)
     const float lgx = 0.5f * (mn0 + mx0), lgy = 0.5f * (mn1 + mx1), lgz = 0.5f * (mn2 + mx2);
     const float rg2 = 0.25f * fmaf(mx0 - mn0, mx0 - mn0, fmaf(mx1 - mn1, mx1 - mn1, (mx2 - mn2) * (mx2 - mn2)));
     const float far2 = LOCAL ? rg2 / (local_ratio * local_ratio) : 0.f;
-    LocalExp LX{};
+    if (LOCAL)
+        for (int k = 0; k < 19; ++k) s_lx[warp][k][lane] = 0.f;
     unsigned long long nlocal = 0;
     // learned: the warp's current record chunk and its fill; the previous chunk links to
     // the next one (head of the group's chain first)
@@ -1143,8 +1150,14 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 4 : PT_GW_MINB)
             if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > far2) {
                 farc = true;
                 const bool q = QUAD && B.z < 0;
-                local_add(LX, dx, dy, dz, A.w, eps2, q ? nodeQ + 2 * node : nullptr,
+                LocalExp t;
+                float *tf = &t.ax;
+#pragma unroll
+                for (int k = 0; k < 19; ++k) tf[k] = s_lx[warp][k][lane];
+                local_add(t, dx, dy, dz, A.w, eps2, q ? nodeQ + 2 * node : nullptr,
                           q ? nodeQ + 2 * node + 1 : nullptr);
+#pragma unroll
+                for (int k = 0; k < 19; ++k) s_lx[warp][k][lane] = tf[k];
                 ++nlocal;
             }
         }
@@ -1235,6 +1248,10 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 4 : PT_GW_MINB)
         rz[i] = z0 + z1;
     }
     if (LOCAL) {
+        LocalExp LX;
+        float *lf = &LX.ax;
+#pragma unroll
+        for (int k = 0; k < 19; ++k) lf[k] = s_lx[warp][k][lane];
         local_reduce(LX);
 #pragma unroll
         for (int i = 0; i < TPL; ++i) {
