@@ -454,37 +454,31 @@ __global__ void cell_moments_level(int L, const int *__restrict__ levels, const 
         const float4 g = nodeG[pv];
         const double gx = g.x, gy = g.y, gz = g.z;
         Moments m{};
-        double px = 0, py = 0, pz = 0, ux = 0, uy = 0, uz = 0;
+        double px = 0, py = 0, pz = 0;
         for (int c = pv + 1; c < end;) {
             const int4 cb = nodeB[c];
-            Moments cm;
-            if (cb.z >= 0 && cb.w == 1) {  // a single body: read from nodeA
+            double cx, cy, cz, cmm, cn, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
+            if (cb.z >= 0 && cb.w == 1) {  // a single body, read from nodeA
                 const float4 a = nodeA[c];
-                cm = Moments{};
-                cm.m = a.w;
-                cm.cx = a.x;
-                cm.cy = a.y;
-                cm.cz = a.z;
-                cm.count = 1.0;
+                cx = a.x, cy = a.y, cz = a.z, cmm = a.w, cn = 1.0;
             } else {
-                cm = mom[c];
+                const Moments &cm = mom[c];
+                cx = cm.cx, cy = cm.cy, cz = cm.cz, cmm = cm.m, cn = cm.count;
+                sxx = cm.sxx, sxy = cm.sxy, sxz = cm.sxz, syy = cm.syy, syz = cm.syz, szz = cm.szz;
             }
-            const double dx = cm.cx - gx, dy = cm.cy - gy, dz = cm.cz - gz;
-            m.m += cm.m;
-            m.count += cm.count;
-            const double mx = cm.m * dx, my = cm.m * dy, mz = cm.m * dz;
+            const double dx = cx - gx, dy = cy - gy, dz = cz - gz;
+            m.m += cmm;
+            m.count += cn;
+            const double mx = cmm * dx, my = cmm * dy, mz = cmm * dz;
             px += mx;
             py += my;
             pz += mz;
-            ux += cm.count * dx;
-            uy += cm.count * dy;
-            uz += cm.count * dz;
-            m.sxx += cm.sxx + mx * dx;
-            m.sxy += cm.sxy + mx * dy;
-            m.sxz += cm.sxz + mx * dz;
-            m.syy += cm.syy + my * dy;
-            m.syz += cm.syz + my * dz;
-            m.szz += cm.szz + mz * dz;
+            m.sxx += sxx + mx * dx;
+            m.sxy += sxy + mx * dy;
+            m.sxz += sxz + mx * dz;
+            m.syy += syy + my * dy;
+            m.syz += syz + my * dz;
+            m.szz += szz + mz * dz;
             c = cb.y;
         }
         if (m.m != 0.0) {
@@ -499,7 +493,22 @@ __global__ void cell_moments_level(int L, const int *__restrict__ levels, const 
             m.syy -= py * oy;
             m.syz -= py * oz;
             m.szz -= pz * oz;
-        } else {  // massless: plain mean of the bodies (gravity/impls/mod.rs:127-129)
+        } else {  // massless: plain mean of the bodies (gravity/impls/mod.rs:127-129), a rare second pass
+            double ux = 0, uy = 0, uz = 0;
+            for (int c = pv + 1; c < end;) {
+                const int4 cb = nodeB[c];
+                double cx, cy, cz, cn;
+                if (cb.z >= 0 && cb.w == 1) {
+                    const float4 a = nodeA[c];
+                    cx = a.x, cy = a.y, cz = a.z, cn = 1.0;
+                } else {
+                    cx = mom[c].cx, cy = mom[c].cy, cz = mom[c].cz, cn = mom[c].count;
+                }
+                ux += cn * (cx - gx);
+                uy += cn * (cy - gy);
+                uz += cn * (cz - gz);
+                c = cb.y;
+            }
             m.cx = gx + ux / m.count;
             m.cy = gy + uy / m.count;
             m.cz = gz + uz / m.count;

@@ -433,3 +433,49 @@ def test_local_flag_validation(res):
         N.check(L.pt_bh_set_local_ratio(res.handle, 0.0))
     with pytest.raises(N.CudaError):
         N.check(L.pt_bh_set_local_ratio(res.handle, 0.7))
+
+
+def _pathological(kind, n, seed):
+    rng = np.random.default_rng(seed)
+    b = np.zeros((n, 4), np.float32)
+    b[:, 3] = 1.0 / n
+    if kind == "two_clusters":  # two Plummer spheres 1000 apart
+        h = n // 2
+        b[:h] = ics.plummer(h, seed=seed)["bodies"]
+        b[h:] = ics.plummer(n - h, seed=seed + 1)["bodies"]
+        b[h:, 0] += 1000.0
+    elif kind == "ring":  # a thin ring of radius 5
+        a = rng.uniform(0, 2 * np.pi, n)
+        b[:, 0], b[:, 1] = 5 * np.cos(a), 5 * np.sin(a)
+        b[:, 2] = rng.normal(scale=1e-3, size=n)
+    elif kind == "line":  # collinear bodies: the box is degenerate in two axes
+        b[:, 0] = rng.uniform(-1, 1, n)
+    elif kind == "core_and_halo":  # a very compact core (keys reach full depth) and far outliers
+        b[:, :3] = rng.normal(scale=1e-5, size=(n, 3))
+        b[: n // 20, :3] = rng.uniform(-100, 100, (n // 20, 3))
+    elif kind == "offset":  # a unit cube far from the origin: few mantissa bits left
+        b[:, :3] = 1e4 + rng.uniform(0, 1, (n, 3))
+    elif kind == "plane":  # 2D bodies (z = 0)
+        b[:, :2] = rng.uniform(-1, 1, (n, 2))
+    return b
+
+
+@pytest.mark.parametrize("kind", ["two_clusters", "ring", "line", "core_and_halo", "offset", "plane"])
+def test_headline_configuration_on_unusual_distributions(res, oracle, kind):
+    """The headline walk (quadrupole + 64-body groups + local expansion) stays finite
+    and at least as accurate as the reference rule at the same theta, judged against
+    FP64, on distributions that stress the box, the keys and the group radius. (On
+    the line the interior accelerations nearly cancel, so relative errors are large
+    for every method and only the percentiles are compared.)"""
+    b = _pathological(kind, 20000, 57)
+    ref64 = oracle.bf_f64(b[::10], b, 0.01, True)
+    plain = oracle.bh_f32(b[::10], b, 0.52, 0.01, True)
+    head = cuda.BarnesHut(0.52, res, AccelerationSoftened(0.01), quadrupole=True, group=True,
+                          local=True).compute(b)[::10]
+    assert np.isfinite(head).all()
+    e_ref, e_head = rel(plain, ref64), rel(head, ref64)
+    print(f"{kind}: p95 reference rule {np.percentile(e_ref, 95):.2e}, headline {np.percentile(e_head, 95):.2e}, "
+          f"max {e_ref.max():.2e} / {e_head.max():.2e}")
+    assert np.percentile(e_head, 95) <= np.percentile(e_ref, 95) + 1e-6
+    if kind != "line":
+        assert e_head.max() <= 2 * e_ref.max() + 1e-5
