@@ -387,7 +387,7 @@ class BarnesHutWorkload:
                 "build": {"bound": "hbm", "achieved": build_gbs, "peak": hbm, "unit": "GB/s",
                           "frac": build_gbs / hbm if hbm else None, "bytes": build_bytes,
                           "ms": build_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy)"},
-                "kernel": "bh_walk_group" if self.flags & 2 else "bh_walk",
+                "kernel": "bh_walk_group" if self.flags & 2 else "bh_walk_masked",
                 "walk_ms": walk_ms, "build_ms": statistics.mean(build),
                 "interactions_per_body": st.interactions / self.n,
                 "cell_interactions_per_body": st.cell_interactions / self.n,

@@ -42,7 +42,6 @@ namespace pt {
 namespace bh {
 
 constexpr int LEVELS = 21;   // 63-bit keys
-constexpr int WALK_THREADS = 128;
 
 struct Moments {  // FP64 cell data used while combining children
     double m, cx, cy, cz;
@@ -593,44 +592,6 @@ __device__ __forceinline__ void lane_walk(float4 p, bool valid, int T, const flo
             }
         }
         node = __reduce_min_sync(0xffffffffu, next);
-    }
-}
-
-template <bool QUAD>
-__global__ void __launch_bounds__(WALK_THREADS)
-    bh_walk(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
-            const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
-            const float4 *__restrict__ sbody, const int *__restrict__ counters, float th2, float eps2,
-            float *__restrict__ out, unsigned long long *__restrict__ stats) {
-    const int lane = threadIdx.x & 31;
-    const int t = blockIdx.x * WALK_THREADS + threadIdx.x;
-    if ((t & ~31) >= n_aff) return;  // whole warp past the end
-    const bool valid = t < n_aff;
-    const int T = counters[1];
-    const float4 p = valid ? tbody[t] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float ax = 0.f, ay = 0.f, az = 0.f;
-    unsigned nacc = 0, nvisit = 0, ncell = 0;
-    lane_walk<QUAD>(p, valid, T, nodeA, nodeB, nodeQ, sbody, th2, eps2, ax, ay, az, nacc, nvisit, ncell);
-    if (valid) {
-        const uint32_t o = tidx[t];
-        out[3 * size_t(o) + 0] = ax;
-        out[3 * size_t(o) + 1] = ay;
-        out[3 * size_t(o) + 2] = az;
-    }
-    if (stats) {
-        unsigned long long a = nacc, v = nvisit, c = ncell;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_down_sync(0xffffffffu, a, o);
-            v += __shfl_down_sync(0xffffffffu, v, o);
-            c += __shfl_down_sync(0xffffffffu, c, o);
-        }
-        if (lane == 0) {
-            atomicAdd(stats + 0, a);
-            atomicAdd(stats + 1, v);
-            atomicAdd(stats + 2, 1ull);
-            atomicAdd(stats + 5, c);
-        }
     }
 }
 
@@ -1324,13 +1285,324 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
     }
 }
 
+// ---- masked group walk: the reference's rule, per body, with shared traversal ----
+// The default method (no PT_BH_GROUP). One warp walks for 32 key-adjacent bodies like
+// bh_walk_group, but every stack range carries the mask of the bodies that still
+// descend into it, and every list entry the mask of the bodies that accept it: each
+// body's accepted set is exactly the reference's (sequential.rs:470-505: skip a node
+// at d^2 == 0, open a cell when theta^2 d^2 < w^2, else accept). A list entry is
+// evaluated by every lane and weighted by the lane's mask bit. Sums run in list
+// order instead of the reference's visit order (rounding-level differences).
+constexpr int MW_WARPS = 4;
+constexpr int MW_STACK = 384;
+
+template <int NF, bool GUARD>
+__device__ __forceinline__ void eval_pair_masked(const f2 (&q)[NF + 1], f2 px, f2 py, f2 pz, f2 e2, f2 &ax,
+                                                 f2 &ay, f2 &az) {
+    const int lane = threadIdx.x & 31;
+    float m0, m1;
+    upk2(q[NF], m0, m1);
+    const f2 bit = pk2(float((__float_as_uint(m0) >> lane) & 1u), float((__float_as_uint(m1) >> lane) & 1u));
+    const f2 dx = sub2(q[0], px);
+    const f2 dy = sub2(q[1], py);
+    const f2 dz = sub2(q[2], pz);
+    const f2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+    float r0, r1;
+    upk2(r2, r0, r1);
+    float i0 = rsqrt_ftz(r0), i1 = rsqrt_ftz(r1);
+    if (GUARD) {
+        i0 = (r0 > 0.0f) ? i0 : 0.0f;
+        i1 = (r1 > 0.0f) ? i1 : 0.0f;
+    }
+    const f2 inv = mul2(pk2(i0, i1), bit);  // a body outside the entry's mask adds exactly 0
+    const f2 inv2 = mul2(inv, inv);
+    const f2 sc = mul2(mul2(q[3], inv), inv2);
+    if constexpr (NF == 10) {
+        const f2 ux = fma2(q[4], dx, fma2(q[5], dy, mul2(q[6], dz)));
+        const f2 uy = fma2(q[5], dx, fma2(q[7], dy, mul2(q[8], dz)));
+        const f2 uz = fma2(q[6], dx, fma2(q[8], dy, mul2(q[9], dz)));
+        const f2 c = fma2(dx, ux, fma2(dy, uy, mul2(dz, uz)));
+        const f2 inv5 = mul2(mul2(inv2, inv2), inv);
+        const f2 k = mul2(c, mul2(inv2, pk2(-2.5f, -2.5f)));
+        const f2 s2 = fma2(inv5, k, sc);
+        ax = fma2(dx, s2, fma2(inv5, ux, ax));
+        ay = fma2(dy, s2, fma2(inv5, uy, ay));
+        az = fma2(dz, s2, fma2(inv5, uz, az));
+    } else {
+        ax = fma2(dx, sc, ax);
+        ay = fma2(dy, sc, ay);
+        az = fma2(dz, sc, az);
+    }
+}
+
+template <int NF, int CAP, bool GUARD>
+__device__ __forceinline__ void eval_list_masked(IList<NF + 1, CAP> &Lst, int cnt, f2 px, f2 py, f2 pz, f2 e2,
+                                                 f2 &ax, f2 &ay, f2 &az) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    if (cnt & 1) {  // pad: far away, massless, empty mask
+        if (lane <= NF) Lst.f[lane][cnt] = (lane < 3) ? 1e30f : 0.0f;
+        __syncwarp();
+        ++cnt;
+    }
+#pragma unroll 2
+    for (int e = 0; e < cnt; e += 2) {
+        f2 q[NF + 1];
+#pragma unroll
+        for (int k = 0; k <= NF; ++k) q[k] = *reinterpret_cast<const f2 *>(&Lst.f[k][e]);
+        eval_pair_masked<NF, GUARD>(q, px, py, pz, e2, ax, ay, az);
+    }
+    __syncwarp();
+}
+
+template <bool QUAD, bool GUARD>
+__global__ void __launch_bounds__(32 * MW_WARPS)
+    bh_walk_masked(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
+                   const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB,
+                   const float4 *__restrict__ nodeQ, const float4 *__restrict__ sbody,
+                   const int *__restrict__ counters, float th2, float eps2, float *__restrict__ out,
+                   unsigned long long *__restrict__ stats) {
+    constexpr int NFC = QUAD ? 10 : 4;
+    using CellList = IList<NFC + 1, 96>;  // + the mask of the accepting bodies
+    using BodyList = IList<5, 128>;
+    __shared__ int4 s_stack[MW_WARPS][MW_STACK];  // (first, end, mask of descending bodies, -)
+    __shared__ __align__(16) CellList s_cells[MW_WARPS];
+    __shared__ __align__(16) BodyList s_bodies[MW_WARPS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int group = blockIdx.x * MW_WARPS + warp;
+    if (group * 32 >= n_aff) return;
+    const int t = group * 32 + lane;
+    const bool valid = t < n_aff;
+    const float4 p = tbody[valid ? t : group * 32];
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned valid_mask = __ballot_sync(0xffffffffu, valid);
+    int4 *stack = s_stack[warp];
+    const int T = counters[1];
+    CellList &Lc = s_cells[warp];
+    BodyList &Lb = s_bodies[warp];
+    float mn0 = p.x, mn1 = p.y, mn2 = p.z, mx0 = p.x, mx1 = p.y, mx2 = p.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn0 = fminf(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
+        mn1 = fminf(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
+        mn2 = fminf(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
+        mx0 = fmaxf(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
+        mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
+        mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
+    }
+    const f2 px = pk2(p.x, p.x), py = pk2(p.y, p.y), pz = pk2(p.z, p.z), e2 = pk2(eps2, eps2);
+    f2 ax = pk2(0.f, 0.f), ay = ax, az = ax;
+    if (lane == 0) stack[0] = make_int4(0, T, int(valid_mask), 0);
+    __syncwarp();
+    int S = 1, Nc = 0, Nb = 0;
+    unsigned long long acc_pairs = 0, cell_pairs = 0, visit_pairs = 0;
+    bool failed = false;
+    while (S > 0) {
+        const int k = min(min(32, S), max(1, (MW_STACK - S) / 2));
+        const bool have = lane < k;
+        const int4 r = have ? stack[S - 1 - lane] : make_int4(0, 0, 0, 0);
+        __syncwarp();
+        S -= k;
+        const int node = r.x;
+        const unsigned mask = unsigned(r.z);
+        float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
+        int4 B = make_int4(0, 0, 0, 0);
+        if (have) {
+            A = __ldg(nodeA + node);
+            B = __ldg(nodeB + node);
+        }
+        visit_pairs += __popc(mask);
+        // Per node: which of its bodies open it and which accept it. The box of the
+        // bodies settles most nodes; a node whose centre of mass lies inside the box
+        // (a body may coincide with it: skipped) or whose rule differs across the box
+        // is voted on, each lane testing its own body.
+        const bool cell = B.z < 0;
+        const float w = cell ? __int_as_float(B.x) : 0.f;
+        unsigned open_m = 0, acc_m = 0;
+        bool need = false;
+        if (have && mask) {
+            const float e0 = fmaxf(fmaxf(mn0 - A.x, A.x - mx0), 0.f);
+            const float e1 = fmaxf(fmaxf(mn1 - A.y, A.y - mx1), 0.f);
+            const float e2b = fmaxf(fmaxf(mn2 - A.z, A.z - mx2), 0.f);
+            const float db2 = fmaf(e0, e0, fmaf(e1, e1, e2b * e2b));
+            const bool inside = !(db2 > 0.0f);
+            if (!cell) {
+                if (inside) need = true;
+                else acc_m = mask;
+            } else {
+                const float f0 = fmaxf(A.x - mn0, mx0 - A.x);
+                const float f1 = fmaxf(A.y - mn1, mx1 - A.y);
+                const float f2b = fmaxf(A.z - mn2, mx2 - A.z);
+                const float dmax2 = fmaf(f0, f0, fmaf(f1, f1, f2b * f2b));
+                if (inside) need = true;
+                else if (!(th2 * db2 < w * w)) acc_m = mask;      // every body accepts
+                else if (th2 * dmax2 < w * w) open_m = mask;      // every body opens
+                else need = true;
+            }
+        }
+        unsigned vm = __ballot_sync(0xffffffffu, need);
+        while (vm) {
+            const int j = __ffs(vm) - 1;
+            vm &= vm - 1;
+            const float cx = __shfl_sync(0xffffffffu, A.x, j);
+            const float cy = __shfl_sync(0xffffffffu, A.y, j);
+            const float cz = __shfl_sync(0xffffffffu, A.z, j);
+            const float cw = __shfl_sync(0xffffffffu, w, j);
+            const unsigned mj = __shfl_sync(0xffffffffu, mask, j);
+            const bool cj = __shfl_sync(0xffffffffu, cell, j);
+            const float dx = cx - p.x, dy = cy - p.y, dz = cz - p.z;
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const bool mine = (mj >> lane) & 1u;
+            const bool o = mine && cj && d2 > 0.0f && th2 * d2 < cw * cw;
+            const bool a = mine && !o && d2 > 0.0f;
+            const unsigned om = __ballot_sync(0xffffffffu, o), am = __ballot_sync(0xffffffffu, a);
+            if (lane == j) {
+                open_m = om;
+                acc_m = am;
+            }
+        }
+        // push: later siblings share the parent's mask; children get the opening bodies
+        const bool rest = have && mask && B.y < r.y;
+        const bool opn = open_m != 0u;
+        const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, opn);
+        const int total = __popc(mrest) + __popc(mopen);
+        int slot = S + __popc(mrest & lt) + __popc(mopen & lt);
+        if (slot + int(rest) + int(opn) > MW_STACK) {
+            failed = true;
+        } else {
+            if (rest) stack[slot++] = make_int4(B.y, r.y, int(mask), 0);
+            if (opn) stack[slot++] = make_int4(node + 1, B.y, int(open_m), 0);
+        }
+        if (__any_sync(0xffffffffu, failed)) {
+            failed = true;
+            break;
+        }
+        S += total;
+        acc_pairs += __popc(acc_m);
+        const bool accd = acc_m != 0u;
+        const bool bucket = accd && !cell && B.w > 1;
+        const bool cellacc = accd && cell;
+        const bool bodyacc = accd && !cell && B.w == 1;
+        if (cellacc) cell_pairs += __popc(acc_m);
+        const unsigned mc = __ballot_sync(0xffffffffu, cellacc);
+        const int nc1 = __popc(mc);
+        if (Nc + nc1 > CellList::CAP) {
+            eval_list_masked<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
+            Nc = 0;
+        }
+        if (cellacc) {
+            const int e = Nc + __popc(mc & lt);
+            Lc.f[0][e] = A.x;
+            Lc.f[1][e] = A.y;
+            Lc.f[2][e] = A.z;
+            Lc.f[3][e] = A.w;
+            if constexpr (QUAD) {  // negated: the list evaluation's form
+                const float4 q0 = __ldg(nodeQ + 2 * node);
+                const float4 q1 = __ldg(nodeQ + 2 * node + 1);
+                Lc.f[4][e] = -q0.x;
+                Lc.f[5][e] = -q0.y;
+                Lc.f[6][e] = -q0.z;
+                Lc.f[7][e] = -q0.w;
+                Lc.f[8][e] = -q1.x;
+                Lc.f[9][e] = -q1.y;
+            }
+            Lc.f[NFC][e] = __uint_as_float(acc_m);
+        }
+        Nc += nc1;
+        const unsigned mb1 = __ballot_sync(0xffffffffu, bodyacc);
+        const int nb1 = __popc(mb1);
+        if (Nb + nb1 > BodyList::CAP) {
+            eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+            Nb = 0;
+        }
+        if (bodyacc) {
+            const int e = Nb + __popc(mb1 & lt);
+            Lb.f[0][e] = A.x;
+            Lb.f[1][e] = A.y;
+            Lb.f[2][e] = A.z;
+            Lb.f[3][e] = A.w;
+            Lb.f[4][e] = __uint_as_float(acc_m);
+        }
+        Nb += nb1;
+        unsigned mbk = __ballot_sync(0xffffffffu, bucket);
+        while (mbk) {  // leaves holding several bodies: one entry per body, the leaf's mask
+            const int src = __ffs(mbk) - 1;
+            mbk &= mbk - 1;
+            const int f = __shfl_sync(0xffffffffu, B.z, src);
+            const int c = __shfl_sync(0xffffffffu, B.w, src);
+            const unsigned bm = __shfl_sync(0xffffffffu, acc_m, src);
+            for (int base = 0; base < c; base += 32) {
+                const int n = min(32, c - base);
+                if (Nb + n > BodyList::CAP) {
+                    eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+                    Nb = 0;
+                }
+                if (lane < n) {
+                    const float4 q = __ldg(sbody + f + base + lane);
+                    Lb.f[0][Nb + lane] = q.x;
+                    Lb.f[1][Nb + lane] = q.y;
+                    Lb.f[2][Nb + lane] = q.z;
+                    Lb.f[3][Nb + lane] = q.w;
+                    Lb.f[4][Nb + lane] = __uint_as_float(bm);
+                }
+                Nb += n;
+            }
+        }
+        __syncwarp();
+    }
+    eval_list_masked<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
+    eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+    float x0, x1, y0, y1, z0, z1;
+    upk2(ax, x0, x1);
+    upk2(ay, y0, y1);
+    upk2(az, z0, z1);
+    float rx = x0 + x1, ry = y0 + y1, rz = z0 + z1;
+    if (failed) {  // the stack ran out: the per-body cursor walk instead (warp-uniform)
+        rx = ry = rz = 0.f;
+        unsigned na = 0, nv = 0, nc = 0;
+        lane_walk<QUAD>(p, valid, T, nodeA, nodeB, nodeQ, sbody, th2, eps2, rx, ry, rz, na, nv, nc);
+        acc_pairs = na;
+        cell_pairs = nc;
+        visit_pairs = nv;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            acc_pairs += __shfl_xor_sync(0xffffffffu, acc_pairs, o);
+            cell_pairs += __shfl_xor_sync(0xffffffffu, cell_pairs, o);
+            visit_pairs += __shfl_xor_sync(0xffffffffu, visit_pairs, o);
+        }
+    } else {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            acc_pairs += __shfl_xor_sync(0xffffffffu, acc_pairs, o);
+            cell_pairs += __shfl_xor_sync(0xffffffffu, cell_pairs, o);
+            visit_pairs += __shfl_xor_sync(0xffffffffu, visit_pairs, o);
+        }
+    }
+    if (valid) {
+        const uint32_t o = tidx[t];
+        out[3 * size_t(o) + 0] = rx;
+        out[3 * size_t(o) + 1] = ry;
+        out[3 * size_t(o) + 2] = rz;
+    }
+    if (stats && lane == 0) {
+        atomicAdd(stats + 0, acc_pairs);
+        atomicAdd(stats + 1, visit_pairs);
+        atomicAdd(stats + 2, 1ull);
+        atomicAdd(stats + 5, cell_pairs);
+        if (failed) atomicAdd(stats + 6, 1ull);
+    }
+}
+
 using WalkKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
                             const float4 *, const int *, float, float, float *, unsigned long long *);
 using GroupKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
                              const float4 *, const float4 *, const int *, float, float, LearnedRecords, float,
                              float *, unsigned long long *, int *, int, float);
 
-static WalkKernel walk_kernel(bool quad) { return quad ? bh_walk<true> : bh_walk<false>; }
+static WalkKernel masked_kernel(bool quad, bool guard) {
+    if (quad) return guard ? bh_walk_masked<true, true> : bh_walk_masked<true, false>;
+    return guard ? bh_walk_masked<false, true> : bh_walk_masked<false, false>;
+}
 
 template <bool LEARNED, bool LOCAL>
 static GroupKernel group_kernel_q(bool quad, bool guard) {
@@ -1559,10 +1831,10 @@ static int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx
         mark(ctx, 2);
         return PT_OK;
     }
-    walk_kernel(quad)<<<blocks(n_aff, WALK_THREADS), WALK_THREADS, 0, st>>>(
+    masked_kernel(quad, eps2 == 0.0f)<<<(n_aff + 32 * MW_WARPS - 1) / (32 * MW_WARPS), 32 * MW_WARPS, 0, st>>>(
         tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.sbody),
         as<int>(S.counters), th2, eps2, d_out, stats);
-    PT_TRY(check_launch(ctx, "bh_walk"));
+    PT_TRY(check_launch(ctx, "bh_walk_masked"));
     mark(ctx, 2);
     return PT_OK;
 }

@@ -282,10 +282,12 @@ def test_group_walk_eps0_and_separate_targets(res, oracle):
 
 @pytest.mark.parametrize("learned", [False, True])
 def test_group_walk_stack_fallback(res, oracle, learned):
-    """A warp whose shared-memory stack runs out takes the per-body walk. With room
-    for 2 ranges every warp does: the result is the per-body walk's, bit for bit (and
-    the learned correction is dropped for those warps). With room for 48 some warps
-    do, and the error stays within the per-body walk's."""
+    """A warp whose shared-memory stack runs out takes the per-body cursor walk. With
+    room for 2 ranges every warp does: the result is the reference rule's, as the
+    default method computes it (same accepted nodes per body; the default sums them
+    in list order, hence rounding-level differences), and the learned correction is
+    dropped for those warps. With room for 48 some warps do, and the error stays
+    within the reference rule's."""
     from particular_gb300 import learned as LM
     b = ics.plummer(20000, seed=46)["bodies"]
     ref64 = oracle.bf_f64(b[::4], b, 0.01, True)
@@ -299,7 +301,8 @@ def test_group_walk_stack_fallback(res, oracle, learned):
         got = m.compute(b)
         st = m.stats()
         assert st["overflow"] == st["warps"] > 0
-        np.testing.assert_array_equal(got, lane)
+        d = rel(got, lane)
+        assert np.median(d) < 1e-6 and d.max() < 1e-4
         N.check(L.pt_bh_set_stack_limit(res.handle, 48))
         got = m.compute(b)
         st = m.stats()
