@@ -1286,22 +1286,26 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
 }
 
 // ---- masked group walk: the reference's rule, per body, with shared traversal ----
-// The default method (no PT_BH_GROUP). One warp walks for 32 key-adjacent bodies like
-// bh_walk_group, but every stack range carries the mask of the bodies that still
-// descend into it, and every list entry the mask of the bodies that accept it: each
-// body's accepted set is exactly the reference's (sequential.rs:470-505: skip a node
-// at d^2 == 0, open a cell when theta^2 d^2 < w^2, else accept). A list entry is
-// evaluated by every lane and weighted by the lane's mask bit. Sums run in list
-// order instead of the reference's visit order (rounding-level differences).
+// The default method (no PT_BH_GROUP). One warp walks for MW_TPL x 32 key-adjacent
+// bodies (MW_TPL per lane) like bh_walk_group, but every stack range carries the
+// masks of the bodies that still descend into it, and every list entry the masks of
+// the bodies that accept it: each body's accepted set is exactly the reference's
+// (sequential.rs:470-505: skip a node at d^2 == 0, open a cell when theta^2 d^2 <
+// w^2, else accept). A list entry is evaluated for every body and weighted by the
+// body's mask bit. Sums run in list order instead of the reference's visit order
+// (rounding-level differences).
 constexpr int MW_WARPS = 4;
 constexpr int MW_STACK = 384;
+constexpr int MW_TPL = 2;  // bodies per lane; mask word i covers bodies g0 + 32 i + lane
 
+// Entry pair (packed lo/hi) for one body, weighted by the body's bits of the two
+// entries' masks (qm = the pair's mask words for this body's word).
 template <int NF, bool GUARD>
-__device__ __forceinline__ void eval_pair_masked(const f2 (&q)[NF + 1], f2 px, f2 py, f2 pz, f2 e2, f2 &ax,
-                                                 f2 &ay, f2 &az) {
+__device__ __forceinline__ void eval_pair_masked(const f2 *q, f2 qm, f2 px, f2 py, f2 pz, f2 e2, f2 &ax, f2 &ay,
+                                                 f2 &az) {
     const int lane = threadIdx.x & 31;
     float m0, m1;
-    upk2(q[NF], m0, m1);
+    upk2(qm, m0, m1);
     const f2 bit = pk2(float((__float_as_uint(m0) >> lane) & 1u), float((__float_as_uint(m1) >> lane) & 1u));
     const f2 dx = sub2(q[0], px);
     const f2 dy = sub2(q[1], py);
@@ -1335,22 +1339,26 @@ __device__ __forceinline__ void eval_pair_masked(const f2 (&q)[NF + 1], f2 px, f
     }
 }
 
+// Lists hold NF fields then MW_TPL mask words per entry.
 template <int NF, int CAP, bool GUARD>
-__device__ __forceinline__ void eval_list_masked(IList<NF + 1, CAP> &Lst, int cnt, f2 px, f2 py, f2 pz, f2 e2,
-                                                 f2 &ax, f2 &ay, f2 &az) {
+__device__ __forceinline__ void eval_list_masked(IList<NF + MW_TPL, CAP> &Lst, int cnt, const f2 (&px)[MW_TPL],
+                                                 const f2 (&py)[MW_TPL], const f2 (&pz)[MW_TPL], f2 e2,
+                                                 f2 (&ax)[MW_TPL], f2 (&ay)[MW_TPL], f2 (&az)[MW_TPL]) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
-    if (cnt & 1) {  // pad: far away, massless, empty mask
-        if (lane <= NF) Lst.f[lane][cnt] = (lane < 3) ? 1e30f : 0.0f;
+    if (cnt & 1) {  // pad: far away, massless, empty masks
+        if (lane < NF + MW_TPL) Lst.f[lane][cnt] = (lane < 3) ? 1e30f : 0.0f;
         __syncwarp();
         ++cnt;
     }
 #pragma unroll 2
     for (int e = 0; e < cnt; e += 2) {
-        f2 q[NF + 1];
+        f2 q[NF + MW_TPL];
 #pragma unroll
-        for (int k = 0; k <= NF; ++k) q[k] = *reinterpret_cast<const f2 *>(&Lst.f[k][e]);
-        eval_pair_masked<NF, GUARD>(q, px, py, pz, e2, ax, ay, az);
+        for (int k = 0; k < NF + MW_TPL; ++k) q[k] = *reinterpret_cast<const f2 *>(&Lst.f[k][e]);
+#pragma unroll
+        for (int i = 0; i < MW_TPL; ++i)
+            eval_pair_masked<NF, GUARD>(q, q[NF + i], px[i], py[i], pz[i], e2, ax[i], ay[i], az[i]);
     }
     __syncwarp();
 }
@@ -1363,24 +1371,33 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
                    const int *__restrict__ counters, float th2, float eps2, float *__restrict__ out,
                    unsigned long long *__restrict__ stats) {
     constexpr int NFC = QUAD ? 10 : 4;
-    using CellList = IList<NFC + 1, 96>;  // + the mask of the accepting bodies
-    using BodyList = IList<5, 128>;
-    __shared__ int4 s_stack[MW_WARPS][MW_STACK];  // (first, end, mask of descending bodies, -)
+    constexpr int TPL = MW_TPL;
+    static_assert(TPL == 2, "stack entries hold two mask words");
+    using CellList = IList<NFC + TPL, 96>;  // + the masks of the accepting bodies
+    using BodyList = IList<4 + TPL, 128>;
+    __shared__ int4 s_stack[MW_WARPS][MW_STACK];  // (first, end, mask word 0, mask word 1)
     __shared__ __align__(16) CellList s_cells[MW_WARPS];
     __shared__ __align__(16) BodyList s_bodies[MW_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int group = blockIdx.x * MW_WARPS + warp;
-    if (group * 32 >= n_aff) return;
-    const int t = group * 32 + lane;
-    const bool valid = t < n_aff;
-    const float4 p = tbody[valid ? t : group * 32];
+    const int g0 = (blockIdx.x * MW_WARPS + warp) * 32 * TPL;
+    if (g0 >= n_aff) return;
+    float4 p[TPL];
+    bool valid[TPL];
+    unsigned vmask[TPL];
+#pragma unroll
+    for (int i = 0; i < TPL; ++i) {
+        const int t = g0 + 32 * i + lane;
+        valid[i] = t < n_aff;
+        p[i] = tbody[valid[i] ? t : g0];
+        vmask[i] = __ballot_sync(0xffffffffu, valid[i]);
+    }
     const unsigned lt = (1u << lane) - 1u;
-    const unsigned valid_mask = __ballot_sync(0xffffffffu, valid);
     int4 *stack = s_stack[warp];
     const int T = counters[1];
     CellList &Lc = s_cells[warp];
     BodyList &Lb = s_bodies[warp];
-    float mn0 = p.x, mn1 = p.y, mn2 = p.z, mx0 = p.x, mx1 = p.y, mx2 = p.z;
+    float mn0 = fminf(p[0].x, p[1].x), mn1 = fminf(p[0].y, p[1].y), mn2 = fminf(p[0].z, p[1].z);
+    float mx0 = fmaxf(p[0].x, p[1].x), mx1 = fmaxf(p[0].y, p[1].y), mx2 = fmaxf(p[0].z, p[1].z);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         mn0 = fminf(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
@@ -1390,9 +1407,16 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
         mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
         mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
     }
-    const f2 px = pk2(p.x, p.x), py = pk2(p.y, p.y), pz = pk2(p.z, p.z), e2 = pk2(eps2, eps2);
-    f2 ax = pk2(0.f, 0.f), ay = ax, az = ax;
-    if (lane == 0) stack[0] = make_int4(0, T, int(valid_mask), 0);
+    const f2 e2 = pk2(eps2, eps2);
+    f2 px[TPL], py[TPL], pz[TPL], ax[TPL], ay[TPL], az[TPL];
+#pragma unroll
+    for (int i = 0; i < TPL; ++i) {
+        px[i] = pk2(p[i].x, p[i].x);
+        py[i] = pk2(p[i].y, p[i].y);
+        pz[i] = pk2(p[i].z, p[i].z);
+        ax[i] = ay[i] = az[i] = pk2(0.f, 0.f);
+    }
+    if (lane == 0) stack[0] = make_int4(0, T, int(vmask[0]), int(vmask[1]));
     __syncwarp();
     int S = 1, Nc = 0, Nb = 0;
     unsigned long long acc_pairs = 0, cell_pairs = 0, visit_pairs = 0;
@@ -1404,40 +1428,43 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
         __syncwarp();
         S -= k;
         const int node = r.x;
-        const unsigned mask = unsigned(r.z);
+        const unsigned mk0 = unsigned(r.z), mk1 = unsigned(r.w);
         float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
         int4 B = make_int4(0, 0, 0, 0);
         if (have) {
             A = __ldg(nodeA + node);
             B = __ldg(nodeB + node);
         }
-        visit_pairs += __popc(mask);
-        // Per node: which of its bodies open it and which accept it. The box of the
-        // bodies settles most nodes; a node whose centre of mass lies inside the box
-        // (a body may coincide with it: skipped) or whose rule differs across the box
-        // is voted on, each lane testing its own body.
+        visit_pairs += __popc(mk0) + __popc(mk1);
+        // Per node: which of its bodies open it and which accept it. The bodies' box
+        // settles most nodes; a node whose centre of mass lies inside the box (a body
+        // may coincide with it: skipped) or whose rule differs across the box is
+        // voted on, each lane testing its own bodies.
         const bool cell = B.z < 0;
         const float w = cell ? __int_as_float(B.x) : 0.f;
-        unsigned open_m = 0, acc_m = 0;
+        unsigned op0 = 0, op1 = 0, ac0 = 0, ac1 = 0;
         bool need = false;
-        if (have && mask) {
+        if (have && (mk0 | mk1)) {
             const float e0 = fmaxf(fmaxf(mn0 - A.x, A.x - mx0), 0.f);
             const float e1 = fmaxf(fmaxf(mn1 - A.y, A.y - mx1), 0.f);
             const float e2b = fmaxf(fmaxf(mn2 - A.z, A.z - mx2), 0.f);
             const float db2 = fmaf(e0, e0, fmaf(e1, e1, e2b * e2b));
             const bool inside = !(db2 > 0.0f);
-            if (!cell) {
-                if (inside) need = true;
-                else acc_m = mask;
+            if (inside) {
+                need = true;
+            } else if (!cell || !(th2 * db2 < w * w)) {  // every body accepts
+                ac0 = mk0;
+                ac1 = mk1;
             } else {
                 const float f0 = fmaxf(A.x - mn0, mx0 - A.x);
                 const float f1 = fmaxf(A.y - mn1, mx1 - A.y);
                 const float f2b = fmaxf(A.z - mn2, mx2 - A.z);
-                const float dmax2 = fmaf(f0, f0, fmaf(f1, f1, f2b * f2b));
-                if (inside) need = true;
-                else if (!(th2 * db2 < w * w)) acc_m = mask;      // every body accepts
-                else if (th2 * dmax2 < w * w) open_m = mask;      // every body opens
-                else need = true;
+                if (th2 * fmaf(f0, f0, fmaf(f1, f1, f2b * f2b)) < w * w) {  // every body opens
+                    op0 = mk0;
+                    op1 = mk1;
+                } else {
+                    need = true;
+                }
             }
         }
         unsigned vm = __ballot_sync(0xffffffffu, need);
@@ -1448,42 +1475,50 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
             const float cy = __shfl_sync(0xffffffffu, A.y, j);
             const float cz = __shfl_sync(0xffffffffu, A.z, j);
             const float cw = __shfl_sync(0xffffffffu, w, j);
-            const unsigned mj = __shfl_sync(0xffffffffu, mask, j);
+            const unsigned mj0 = __shfl_sync(0xffffffffu, mk0, j), mj1 = __shfl_sync(0xffffffffu, mk1, j);
             const bool cj = __shfl_sync(0xffffffffu, cell, j);
-            const float dx = cx - p.x, dy = cy - p.y, dz = cz - p.z;
-            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const bool mine = (mj >> lane) & 1u;
-            const bool o = mine && cj && d2 > 0.0f && th2 * d2 < cw * cw;
-            const bool a = mine && !o && d2 > 0.0f;
-            const unsigned om = __ballot_sync(0xffffffffu, o), am = __ballot_sync(0xffffffffu, a);
+            const f2 dx = sub2(pk2(cx, cx), pk2(p[0].x, p[1].x));
+            const f2 dy = sub2(pk2(cy, cy), pk2(p[0].y, p[1].y));
+            const f2 dz = sub2(pk2(cz, cz), pk2(p[0].z, p[1].z));
+            float d0, d1;
+            upk2(fma2(dx, dx, fma2(dy, dy, mul2(dz, dz))), d0, d1);
+            const bool in0 = (mj0 >> lane) & 1u, in1 = (mj1 >> lane) & 1u;
+            const bool o0 = in0 && cj && d0 > 0.0f && th2 * d0 < cw * cw;
+            const bool o1 = in1 && cj && d1 > 0.0f && th2 * d1 < cw * cw;
+            const unsigned om0 = __ballot_sync(0xffffffffu, o0), om1 = __ballot_sync(0xffffffffu, o1);
+            const unsigned am0 = __ballot_sync(0xffffffffu, in0 && !o0 && d0 > 0.0f);
+            const unsigned am1 = __ballot_sync(0xffffffffu, in1 && !o1 && d1 > 0.0f);
             if (lane == j) {
-                open_m = om;
-                acc_m = am;
+                op0 = om0;
+                op1 = om1;
+                ac0 = am0;
+                ac1 = am1;
             }
         }
-        // push: later siblings share the parent's mask; children get the opening bodies
-        const bool rest = have && mask && B.y < r.y;
-        const bool opn = open_m != 0u;
+        // push: later siblings share the parent's masks; children get the opening bodies
+        const bool rest = have && (mk0 | mk1) && B.y < r.y;
+        const bool opn = (op0 | op1) != 0u;
         const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, opn);
         const int total = __popc(mrest) + __popc(mopen);
         int slot = S + __popc(mrest & lt) + __popc(mopen & lt);
         if (slot + int(rest) + int(opn) > MW_STACK) {
             failed = true;
         } else {
-            if (rest) stack[slot++] = make_int4(B.y, r.y, int(mask), 0);
-            if (opn) stack[slot++] = make_int4(node + 1, B.y, int(open_m), 0);
+            if (rest) stack[slot++] = make_int4(B.y, r.y, int(mk0), int(mk1));
+            if (opn) stack[slot++] = make_int4(node + 1, B.y, int(op0), int(op1));
         }
         if (__any_sync(0xffffffffu, failed)) {
             failed = true;
             break;
         }
         S += total;
-        acc_pairs += __popc(acc_m);
-        const bool accd = acc_m != 0u;
+        const int na = __popc(ac0) + __popc(ac1);
+        acc_pairs += na;
+        const bool accd = na != 0;
         const bool bucket = accd && !cell && B.w > 1;
         const bool cellacc = accd && cell;
         const bool bodyacc = accd && !cell && B.w == 1;
-        if (cellacc) cell_pairs += __popc(acc_m);
+        if (cellacc) cell_pairs += na;
         const unsigned mc = __ballot_sync(0xffffffffu, cellacc);
         const int nc1 = __popc(mc);
         if (Nc + nc1 > CellList::CAP) {
@@ -1506,7 +1541,8 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
                 Lc.f[8][e] = -q1.x;
                 Lc.f[9][e] = -q1.y;
             }
-            Lc.f[NFC][e] = __uint_as_float(acc_m);
+            Lc.f[NFC][e] = __uint_as_float(ac0);
+            Lc.f[NFC + 1][e] = __uint_as_float(ac1);
         }
         Nc += nc1;
         const unsigned mb1 = __ballot_sync(0xffffffffu, bodyacc);
@@ -1521,16 +1557,17 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
             Lb.f[1][e] = A.y;
             Lb.f[2][e] = A.z;
             Lb.f[3][e] = A.w;
-            Lb.f[4][e] = __uint_as_float(acc_m);
+            Lb.f[4][e] = __uint_as_float(ac0);
+            Lb.f[5][e] = __uint_as_float(ac1);
         }
         Nb += nb1;
         unsigned mbk = __ballot_sync(0xffffffffu, bucket);
-        while (mbk) {  // leaves holding several bodies: one entry per body, the leaf's mask
+        while (mbk) {  // leaves holding several bodies: one entry per body, the leaf's masks
             const int src = __ffs(mbk) - 1;
             mbk &= mbk - 1;
             const int f = __shfl_sync(0xffffffffu, B.z, src);
             const int c = __shfl_sync(0xffffffffu, B.w, src);
-            const unsigned bm = __shfl_sync(0xffffffffu, acc_m, src);
+            const unsigned b0 = __shfl_sync(0xffffffffu, ac0, src), b1 = __shfl_sync(0xffffffffu, ac1, src);
             for (int base = 0; base < c; base += 32) {
                 const int n = min(32, c - base);
                 if (Nb + n > BodyList::CAP) {
@@ -1543,7 +1580,8 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
                     Lb.f[1][Nb + lane] = q.y;
                     Lb.f[2][Nb + lane] = q.z;
                     Lb.f[3][Nb + lane] = q.w;
-                    Lb.f[4][Nb + lane] = __uint_as_float(bm);
+                    Lb.f[4][Nb + lane] = __uint_as_float(b0);
+                    Lb.f[5][Nb + lane] = __uint_as_float(b1);
                 }
                 Nb += n;
             }
@@ -1552,38 +1590,43 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
     }
     eval_list_masked<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
     eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
-    float x0, x1, y0, y1, z0, z1;
-    upk2(ax, x0, x1);
-    upk2(ay, y0, y1);
-    upk2(az, z0, z1);
-    float rx = x0 + x1, ry = y0 + y1, rz = z0 + z1;
+    float rx[TPL], ry[TPL], rz[TPL];
+#pragma unroll
+    for (int i = 0; i < TPL; ++i) {
+        float x0, x1, y0, y1, z0, z1;
+        upk2(ax[i], x0, x1);
+        upk2(ay[i], y0, y1);
+        upk2(az[i], z0, z1);
+        rx[i] = x0 + x1;
+        ry[i] = y0 + y1;
+        rz[i] = z0 + z1;
+    }
     if (failed) {  // the stack ran out: the per-body cursor walk instead (warp-uniform)
-        rx = ry = rz = 0.f;
         unsigned na = 0, nv = 0, nc = 0;
-        lane_walk<QUAD>(p, valid, T, nodeA, nodeB, nodeQ, sbody, th2, eps2, rx, ry, rz, na, nv, nc);
+#pragma unroll
+        for (int i = 0; i < TPL; ++i) {
+            rx[i] = ry[i] = rz[i] = 0.f;
+            lane_walk<QUAD>(p[i], valid[i], T, nodeA, nodeB, nodeQ, sbody, th2, eps2, rx[i], ry[i], rz[i], na, nv,
+                            nc);
+        }
         acc_pairs = na;
         cell_pairs = nc;
         visit_pairs = nv;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            acc_pairs += __shfl_xor_sync(0xffffffffu, acc_pairs, o);
-            cell_pairs += __shfl_xor_sync(0xffffffffu, cell_pairs, o);
-            visit_pairs += __shfl_xor_sync(0xffffffffu, visit_pairs, o);
-        }
-    } else {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            acc_pairs += __shfl_xor_sync(0xffffffffu, acc_pairs, o);
-            cell_pairs += __shfl_xor_sync(0xffffffffu, cell_pairs, o);
-            visit_pairs += __shfl_xor_sync(0xffffffffu, visit_pairs, o);
-        }
     }
-    if (valid) {
-        const uint32_t o = tidx[t];
-        out[3 * size_t(o) + 0] = rx;
-        out[3 * size_t(o) + 1] = ry;
-        out[3 * size_t(o) + 2] = rz;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {  // per-lane counts -> the warp's
+        acc_pairs += __shfl_xor_sync(0xffffffffu, acc_pairs, o);
+        cell_pairs += __shfl_xor_sync(0xffffffffu, cell_pairs, o);
+        visit_pairs += __shfl_xor_sync(0xffffffffu, visit_pairs, o);
     }
+#pragma unroll
+    for (int i = 0; i < TPL; ++i)
+        if (valid[i]) {
+            const uint32_t o = tidx[g0 + 32 * i + lane];
+            out[3 * size_t(o) + 0] = rx[i];
+            out[3 * size_t(o) + 1] = ry[i];
+            out[3 * size_t(o) + 2] = rz[i];
+        }
     if (stats && lane == 0) {
         atomicAdd(stats + 0, acc_pairs);
         atomicAdd(stats + 1, visit_pairs);
@@ -1831,7 +1874,8 @@ static int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx
         mark(ctx, 2);
         return PT_OK;
     }
-    masked_kernel(quad, eps2 == 0.0f)<<<(n_aff + 32 * MW_WARPS - 1) / (32 * MW_WARPS), 32 * MW_WARPS, 0, st>>>(
+    masked_kernel(quad, eps2 == 0.0f)<<<(n_aff + 32 * MW_TPL * MW_WARPS - 1) / (32 * MW_TPL * MW_WARPS),
+                                        32 * MW_WARPS, 0, st>>>(
         tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.sbody),
         as<int>(S.counters), th2, eps2, d_out, stats);
     PT_TRY(check_launch(ctx, "bh_walk_masked"));

@@ -482,3 +482,22 @@ def test_headline_configuration_on_unusual_distributions(res, oracle, kind):
     assert np.percentile(e_head, 95) <= np.percentile(e_ref, 95) + 1e-6
     if kind != "line":
         assert e_head.max() <= 2 * e_ref.max() + 1e-5
+
+
+@pytest.mark.parametrize("softened", [True, False])
+def test_local_expansion_separate_targets(res, oracle, softened):
+    """PT_BH_LOCAL with targets that are not the sources (Between) and without
+    softening (eps = 0: far nodes never sit at zero distance from the group): FP64-judged
+    error within 10 % of the group walk without the expansion."""
+    src = ics.plummer(30000, seed=58)["bodies"]
+    tgt = ics.uniform_cube(3000, 59)["bodies"] * 3.0
+    tgt[:, 3] = 0.0
+    it = AccelerationSoftened(0.01) if softened else Acceleration.checked()
+    eps = 0.01 if softened else 0.0
+    ref64 = oracle.bf_f64(tgt, src, eps, True)
+    plain = cuda.BarnesHut(0.5, res, it, quadrupole=True, group=True).compute(Between(tgt, src))
+    local = cuda.BarnesHut(0.5, res, it, quadrupole=True, group=True, local=True).compute(Between(tgt, src))
+    assert np.isfinite(local).all()
+    e0, e1 = rel(plain, ref64), rel(local, ref64)
+    for q in (50, 95, 99):
+        assert np.percentile(e1, q) <= 1.1 * np.percentile(e0, q) + 1e-7, q
