@@ -613,9 +613,121 @@ class EnsembleWorkload:
                                  "scaled by the ensemble's pair count per leapfrog step"}
 
 
+class LeapfrogBarnesHutWorkload:
+    """N=1,048,576 bulge+disk (70 % Plummer bulge a=0.5, 30 % exponential disk),
+    softening 0.01: 10 kick-drift-kick leapfrog steps of dt = 1e-3, each with a full
+    tree rebuild and Barnes-Hut accelerations (theta 0.5, quadrupole + 64-body groups
+    + local expansion), replayed from one CUDA graph: one bench step = the 10 leapfrog
+    steps. The first evaluation's error against FP64 is reported for theta 0.3, 0.5
+    and 0.8 with the same flags."""
+
+    name = "leapfrog_bh_bulge_disk_1048576"
+    metric = "body-steps/s"
+    unit = "body-steps/s"
+    steps_per_call = 10
+    theta = 0.5
+    flags = 11  # quadrupole | group | local
+
+    def __init__(self, n=1048576, softening=0.01, dt=1e-3):
+        from particular_gb300 import ics
+        d = ics.bulge_disk(n, seed=1808 + 3)
+        self.n, self.softening, self.dt = n, softening, dt
+        self.bodies = d["bodies"]
+        self.vel = np.zeros((n, 4), np.float32)
+        self.vel[:, :3] = d["vel"]
+        self.errors = None
+
+    def config(self):
+        return {"workload": self.name, "n_bodies": self.n, "softening": self.softening,
+                "dt": self.dt, "leapfrog_steps_per_step": self.steps_per_call,
+                "method": "cuda::BarnesHut(0.5), quadrupole + group + local expansion, "
+                          "tree rebuilt every step", "graph": True,
+                "l2": "flushed between timed steps (256 MiB write)"}
+
+    def setup_gpu(self, res, torch, stream):
+        from particular_gb300 import _native as N
+        self.res, self.torch = res, torch
+        L = N.lib()
+        self.d_b = torch.from_numpy(self.bodies).to("cuda")
+        self.d_v = torch.from_numpy(self.vel).to("cuda")
+        self.d_a = torch.zeros((self.n, 3), device="cuda")
+        # accuracy of one evaluation per theta, FP64 judge on 2048 seeded bodies
+        idx = torch.from_numpy(np.sort(np.random.default_rng(7).choice(self.n, 2048, replace=False))).cuda()
+        ds = self.d_b[idx].contiguous()
+        ref = torch.empty((2048, 3), dtype=torch.float64, device="cuda")
+        N.check(L.pt_bf_accel_f64_device(res.handle, ds.data_ptr(), 2048, self.d_b.data_ptr(), self.n,
+                                         self.softening, 1, ref.data_ptr()))
+        torch.cuda.synchronize()
+        ref = ref.cpu().numpy()
+        self.errors = []
+        for th in (0.3, 0.5, 0.8):
+            N.check(L.pt_bh_accel_f32_device(res.handle, self.d_b.data_ptr(), self.n, self.d_b.data_ptr(),
+                                             self.n, th, self.softening, self.flags, self.d_a.data_ptr()))
+            torch.cuda.synchronize()
+            self.errors.append({"theta": th, **err_stats(rel_err(self.d_a[idx].cpu().numpy(), ref))})
+        N.check(L.pt_bh_accel_f32_device(res.handle, self.d_b.data_ptr(), self.n, self.d_b.data_ptr(),
+                                         self.n, self.theta, self.softening, self.flags, self.d_a.data_ptr()))
+        self.h_b = torch.from_numpy(self.bodies).pin_memory()
+        self.h_v = torch.from_numpy(self.vel).pin_memory()
+
+    def step_device(self):
+        from particular_gb300 import _native as N
+        N.check(N.lib().pt_leapfrog_device(self.res.handle, self.d_b.data_ptr(), self.d_v.data_ptr(),
+                                           self.d_a.data_ptr(), self.n, self.dt, self.steps_per_call,
+                                           N.PT_METHOD_BARNES_HUT, self.theta, self.softening, self.flags, 1))
+
+    def step_e2e(self):
+        from particular_gb300 import _native as N
+        N.check(N.lib().pt_leapfrog(self.res.handle, self.h_b.data_ptr(), self.h_v.data_ptr(),
+                                    self.n, self.dt, self.steps_per_call, N.PT_METHOD_BARNES_HUT,
+                                    self.theta, self.softening, self.flags))
+
+    def work_per_step(self):
+        return self.n * self.steps_per_call
+
+    def h2d_d2h_bytes(self):
+        return 32 * self.n, 32 * self.n
+
+    def roofline(self, res, step_ms):
+        import ctypes
+        from particular_gb300 import _native as N
+        st = N.BhStats()
+        N.check(N.lib().pt_bh_last_stats(res.handle, ctypes.byref(st)))
+        peak = ctypes.c_double(0)
+        N.check(N.lib().pt_measure_fp32_peak(res.handle, ctypes.byref(peak)))
+        flops = (20 * st.interactions + 38 * st.cell_interactions + 180 * st.local_nodes) * self.steps_per_call
+        achieved = flops / (step_ms * 1e-3) / 1e12
+        return {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                "frac": achieved / peak.value, "traffic": None,
+                "kernel": "bh_walk_group (whole leapfrog step timed, tree build included)",
+                "algorithmic": "per evaluation: 20 flop per accepted node per body + 38 per accepted cell "
+                               "+ 180 per far node of a local expansion (counts of the last evaluation)"
+                               " x 10 evaluations per step",
+                "peak_source": "measured FFMA-chain kernel over all SMs (pt_measure_fp32_peak)"}
+
+    def extra(self):
+        return {"errors_first_evaluation": self.errors}
+
+    def cpu_reference(self, threads, steps=1):
+        from oracle import oracle as O
+        t0 = time.perf_counter()
+        tree = O.Tree(self.bodies)
+        t_build = time.perf_counter() - t0
+        sample = 8192
+        idx = np.linspace(0, self.n - 1, sample).astype(np.int64)
+        t0 = time.perf_counter()
+        tree.walk(self.bodies[idx], 0.25, self.softening, True, threads=threads)
+        t_walk = (time.perf_counter() - t0) * (self.n / sample)
+        value = self.n / (t_build + t_walk)  # one leapfrog step = one build + one walk
+        return value, {"theta": 0.25, "sample": f"sequential tree build over {self.n} bodies + walk of "
+                                                f"{sample} targets at theta 0.25 (the monopole rule's "
+                                                "theta for p95 <= 1e-3), scaled to one leapfrog step"}
+
+
 WORKLOADS = {BruteForceWorkload.name: BruteForceWorkload,
              BarnesHutWorkload.name: BarnesHutWorkload,
              LeapfrogWorkload.name: LeapfrogWorkload,
+             LeapfrogBarnesHutWorkload.name: LeapfrogBarnesHutWorkload,
              EnsembleWorkload.name: EnsembleWorkload}
 DEFAULT_WORKLOAD = BarnesHutWorkload.name
 

@@ -48,15 +48,19 @@ def test_leapfrog_matches_oracle_integration(res, oracle):
     assert np.array_equal(b[:, 3], d["bodies"][:, 3])
 
 
-@pytest.mark.parametrize("method", ["bf", "bh"])
+@pytest.mark.parametrize("method", ["bf", "bh", "bh_local", "bh_reference_rule"])
 def test_graph_replay_equals_eager(res, method):
     import torch
     d = ics.plummer(20000, seed=52)
     L = N.lib()
     if method == "bf":
         args = (N.PT_METHOD_BRUTE_FORCE, 0.0, 0.01, 0)
-    else:
+    elif method == "bh":
         args = (N.PT_METHOD_BARNES_HUT, 0.5, 0.01, N.PT_BH_QUADRUPOLE | N.PT_BH_GROUP)
+    elif method == "bh_local":
+        args = (N.PT_METHOD_BARNES_HUT, 0.5, 0.01, N.PT_BH_QUADRUPOLE | N.PT_BH_GROUP | N.PT_BH_LOCAL)
+    else:
+        args = (N.PT_METHOD_BARNES_HUT, 0.5, 0.01, 0)
     outs = []
     for use_graph in (0, 1):
         b = torch.from_numpy(d["bodies"]).cuda()
