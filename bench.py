@@ -49,12 +49,13 @@ def dist_env():
 
 
 def measured_hbm_gbs():
-    """The measured HBM copy bandwidth of this GPU pool (MEASURED_PEAKS.json), or None."""
+    """(GB/s, source): the measured HBM copy bandwidth of this GPU pool
+    (MEASURED_PEAKS.json), else the earlier GB300 measurement of 6.8 TB/s."""
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            return float(json.load(f)["hbm_gbs"])
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured copy)"
     except (OSError, ValueError, KeyError):
-        return None
+        return 6800.0, "fallback: 6.8 TB/s, an earlier GB300 copy measurement"
 
 
 def max_over_ranks(values, dist, device):
@@ -380,13 +381,13 @@ class BarnesHutWorkload:
         # leaf moments 16N + 56M + 8M; cell moments (children read + cell written)
         # 32M + 256C
         build_bytes = (16 + 28 + 8 * 32 + 36 + 24 + 16) * n + (24 + 20 + 56 + 8 + 32) * M + 44 * T + 256 * C
-        hbm = measured_hbm_gbs()
+        hbm, hbm_source = measured_hbm_gbs()
         build_gbs = build_bytes / (build_ms * 1e-3) / 1e9
         return {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                 "frac": achieved / peak.value, "traffic": None,
                 "build": {"bound": "hbm", "achieved": build_gbs, "peak": hbm, "unit": "GB/s",
-                          "frac": build_gbs / hbm if hbm else None, "bytes": build_bytes,
-                          "ms": build_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy)"},
+                          "frac": build_gbs / hbm, "bytes": build_bytes,
+                          "ms": build_ms, "peak_source": hbm_source},
                 "kernel": "bh_walk_group" if self.flags & 2 else "bh_walk_masked",
                 "walk_ms": walk_ms, "build_ms": statistics.mean(build),
                 "interactions_per_body": st.interactions / self.n,
