@@ -228,6 +228,22 @@ int pt_bh_set_local_ratio(pt_ctx *ctx, float ratio);
  * the compiled capacity; 0 restores the capacity). A warp that runs out takes the
  * per-body walk instead (counted in pt_bh_stats.overflow): a tuning and test hook. */
 int pt_bh_set_stack_limit(pt_ctx *ctx, int ranges);
+/* cuda::BarnesHut over glam DVec3 bodies: double[4] (x, y, z, mu) in, double[3] out.
+ * The reference's BarnesHut over f64 particles (sequential.rs:456-543 with
+ * BoundingBox<DVec3>, f64 theta and the f64 per-pair kernel, gravity/impls/glam.rs:234):
+ * the orthtree is built by replaying the subdivision in double and walked with the
+ * per-body rule in double; accepted sets per body equal the reference's. Monopole
+ * only (flags must be 0), as the reference. Synchronous, host buffers. */
+int pt_bh_accel_dvec3(pt_ctx *ctx, const double *affected, size_t n_aff, const double *affecting,
+                      size_t n_src, double theta, double softening, uint32_t flags, double *out_xyz);
+/* Same on 32-byte aligned device buffers, asynchronous on the context's stream. */
+int pt_bh_accel_dvec3_device(pt_ctx *ctx, const double *d_affected, size_t n_aff,
+                             const double *d_affecting, size_t n_src, double theta, double softening,
+                             uint32_t flags, double *d_out_xyz);
+/* The last f64 tree in preorder: com_mass = (x, y, z, mass), links as pt_bh_export_tree,
+ * centre_width = (cell centre x, y, z, width); NULL skips one. */
+int pt_bh_export_tree_dvec3(pt_ctx *ctx, double *com_mass, int32_t *links, double *centre_width,
+                            size_t rows);
 /* Counters of the last Barnes-Hut call (synchronises the context's stream). */
 int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out);
 /* Copies the last tree in depth-first preorder (rows >= stats.nodes): per node

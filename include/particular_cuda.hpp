@@ -385,13 +385,33 @@ struct BarnesHut {
         return detail::unpack(out);
     }
 
+    // Accelerations of the affected particles: std::vector<Vec3> for f32 particles,
+    // std::vector<DVec3> for DVec3 ones (the reference rule in double; flags must be 0).
     template <class Storage>
-    std::vector<Vec3> compute(const Storage &storage) {
+    auto compute(const Storage &storage) {
         auto b = as_between(storage);
-        const auto aff = detail::pack_fields(b.affected);
+        using P1 = typename decltype(b.affected)::value_type;
         const bool same = static_cast<const void *>(b.affected.ptr) ==
                               static_cast<const void *>(b.affecting.ptr) &&
                           b.affected.size() == b.affecting.size();
+        if constexpr (particular::detail::is_f64_position<P1>::value) {
+            const auto aff = detail::pack_fields64(b.affected);
+            const auto src = same ? std::vector<double>() : detail::pack_fields64(b.affecting);
+            std::vector<double> out(3 * b.affected.size());
+            if (out.empty()) return std::vector<DVec3>();
+            check(pt_bh_accel_dvec3(resources.get(), aff.data(), b.affected.size(),
+                                    same ? aff.data() : src.data(), b.affecting.size(), double(theta),
+                                    interaction.softening64(), flags, out.data()));
+            return detail::unpack64(out);
+        } else {
+            return compute_f32(b, same);
+        }
+    }
+
+  private:
+    template <class P1, class P2>
+    std::vector<Vec3> compute_f32(const Between<Slice<P1>, Slice<P2>> &b, bool same) {
+        const auto aff = detail::pack_fields(b.affected);
         const auto src = same ? std::vector<float>() : detail::pack_fields(b.affecting);
         std::vector<float> out(3 * b.affected.size());
         if (out.empty()) return {};

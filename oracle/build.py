@@ -1,4 +1,4 @@
-"""Builds the C oracle (oracle/pt_oracle.c) into oracle/_build/liboracle.so.
+"""Builds the C oracle (oracle/pt_oracle.c + pt_oracle_bh.inc) into oracle/_build/liboracle.so.
 
 Test infrastructure only. The flags matter: -ffp-contract=off keeps every f32
 multiply and add separately rounded, as Rust evaluates them (rustc never
@@ -13,6 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 SRC = os.path.join(HERE, "pt_oracle.c")
+DEPS = [SRC, os.path.join(HERE, "pt_oracle_bh.inc")]
 
 CFLAGS = ["-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
           "-fopenmp", "-Wall", "-Wno-unknown-pragmas"]
@@ -21,7 +22,7 @@ CFLAGS = ["-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-s
 def build(force=False):
     os.makedirs(OUT_DIR, exist_ok=True)
     if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= os.path.getmtime(SRC)):
+            and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in DEPS)):
         return LIB
     cc = os.environ.get("CC", "gcc")
     tmp = LIB + ".tmp"

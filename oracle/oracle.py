@@ -48,6 +48,16 @@ def lib():
                                     ctypes.c_float, ctypes.c_float, ctypes.c_int, _f32p, _u32p,
                                     ctypes.c_int]
         L.oracle_max_threads.restype = ctypes.c_int
+        L.oracle_bh_dvec3.argtypes = [_f64p, ctypes.c_size_t, _f64p, ctypes.c_size_t,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_int, _f64p, _u32p,
+                                      ctypes.c_int]
+        L.oracle_bh_build_dvec3.argtypes = [_f64p, ctypes.c_size_t, ctypes.c_int]
+        L.oracle_bh_build_dvec3.restype = ctypes.c_void_p
+        L.oracle_tree_free_dvec3.argtypes = [ctypes.c_void_p]
+        L.oracle_tree_node_count_dvec3.argtypes = [ctypes.c_void_p]
+        L.oracle_tree_node_count_dvec3.restype = ctypes.c_size_t
+        L.oracle_tree_max_depth_dvec3.argtypes = [ctypes.c_void_p]
+        L.oracle_tree_export_dvec3.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 6
         _lib = L
     return _lib
 
@@ -144,6 +154,45 @@ def bh_f32(targets, sources, theta, softening=0.0, checked=True, threads=0, acce
     if rc:
         raise RuntimeError(f"oracle_bh_f32 failed: {rc}")
     return (out, acc) if accepted else out
+
+
+def bh_dvec3(targets, sources, theta, softening=0.0, checked=True, threads=0, accepted=False):
+    """sequential::BarnesHut over glam DVec3 bodies (double (n, 4) in, double (n, 3) out)."""
+    t = np.ascontiguousarray(np.asarray(targets, np.float64))
+    if t.shape[1] == 3:
+        t = np.ascontiguousarray(np.concatenate([t, np.zeros((t.shape[0], 1))], axis=1))
+    s = np.ascontiguousarray(np.asarray(sources, np.float64))
+    out = np.zeros((t.shape[0], 3), np.float64)
+    acc = np.zeros(t.shape[0], np.uint32) if accepted else None
+    rc = lib().oracle_bh_dvec3(t, t.shape[0], s, s.shape[0], theta, softening, int(checked), out,
+                               acc.ctypes.data if accepted else None, threads)
+    if rc:
+        raise RuntimeError(f"oracle_bh_dvec3 failed: {rc}")
+    return (out, acc) if accepted else out
+
+
+def tree_dvec3_export(sources):
+    """The reference orthtree over DVec3 bodies, exported like Tree.export (double box/data)."""
+    s = np.ascontiguousarray(np.asarray(sources, np.float64))
+    L = lib()
+    h = L.oracle_bh_build_dvec3(s, s.shape[0], 0)
+    if not h:
+        raise MemoryError("oracle_bh_build_dvec3 failed")
+    try:
+        if L.oracle_tree_max_depth_dvec3(h) < 0:
+            raise RuntimeError("oracle_bh_build_dvec3: depth limit reached")
+        n = L.oracle_tree_node_count_dvec3(h)
+        internal = np.zeros(n, np.int32)
+        child = np.zeros((n, 8), np.int32)
+        box = np.zeros((n, 6), np.float64)
+        data = np.zeros((n, 4), np.float64)
+        rng = np.zeros((n, 2), np.int32)
+        perm = np.zeros(s.shape[0], np.uint32)
+        L.oracle_tree_export_dvec3(h, internal.ctypes.data, child.ctypes.data, box.ctypes.data,
+                                   data.ctypes.data, rng.ctypes.data, perm.ctypes.data)
+        return dict(internal=internal, child=child, box=box, data=data, range=rng, perm=perm)
+    finally:
+        L.oracle_tree_free_dvec3(h)
 
 
 class Tree:

@@ -96,6 +96,12 @@ def _declare(L):
         "pt_bh_last_stats": (ctypes.c_int, [c_ptr, ctypes.POINTER(BhStats)]),
         "pt_bh_set_stack_limit": (ctypes.c_int, [c_ptr, ctypes.c_int]),
         "pt_bh_set_local_ratio": (ctypes.c_int, [c_ptr, ctypes.c_float]),
+        "pt_bh_accel_dvec3": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr, ctypes.c_size_t,
+                                             ctypes.c_double, ctypes.c_double, ctypes.c_uint32, c_ptr]),
+        "pt_bh_accel_dvec3_device": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr, ctypes.c_size_t,
+                                                    ctypes.c_double, ctypes.c_double, ctypes.c_uint32,
+                                                    c_ptr]),
+        "pt_bh_export_tree_dvec3": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_ptr, ctypes.c_size_t]),
         "pt_bh_build_device": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr]),
         "pt_bh_walk_device": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, ctypes.c_float, ctypes.c_float,
                                              ctypes.c_uint32, c_ptr]),

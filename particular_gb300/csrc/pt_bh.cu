@@ -50,6 +50,36 @@ struct Moments {  // FP64 cell data used while combining children
     double pad;
 };
 
+// Scalar type of the bodies: float (glam Vec3) or double (glam DVec3). The build
+// replays the reference's subdivision in that type, with explicitly rounded ops.
+template <class T>
+struct Prec;
+template <>
+struct Prec<float> {
+    using V4 = float4;
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float min(float a, float b) { return fminf(a, b); }
+    static __device__ __forceinline__ float max(float a, float b) { return fmaxf(a, b); }
+    static __device__ __forceinline__ V4 make(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
+};
+template <>
+struct Prec<double> {
+    using V4 = double4_32a;
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double min(double a, double b) { return fmin(a, b); }
+    static __device__ __forceinline__ double max(double a, double b) { return fmax(a, b); }
+    static __device__ __forceinline__ V4 make(double x, double y, double z, double w) {
+        V4 r;
+        r.x = x, r.y = y, r.z = z, r.w = w;
+        return r;
+    }
+};
+
+
 struct State {
     PrimScratch prims;
     DevBuf box_part, box;
@@ -58,6 +88,7 @@ struct State {
     DevBuf bfirst, blast, bdelta, bparent, lparent, top, oparent, loparent;
     DevBuf cnt, pscan, pre, levels, by_level;
     DevBuf nodeA, nodeB, nodeQ, nodeG, nodeR, mom;
+    DevBuf sbody64, nodeA64, nodeG64, tbody64;  // the f64 (DVec3) method's bodies and nodes
     DevBuf tkeys, tidx, tbody;
     DevBuf counters;
     DevBuf out;
@@ -66,6 +97,7 @@ struct State {
     int lcap = 0;                     // record chunks allocated
     int stack_cap = 0;                // group-walk stack ranges per warp in use (0 = all)
     uint64_t generation = 0;          // trees built so far (0 = none)
+    bool f64 = false;                 // the current tree was built over DVec3 bodies
     float local_ratio = 0.1f;         // PT_BH_LOCAL: far when group radius < ratio * distance
     const uint32_t *mlp_w = nullptr;  // learned correction: packed BF16 weights (owned by the MLP state)
     const float *mlp_b = nullptr;     // and its bias block
@@ -75,18 +107,20 @@ struct State {
 };
 
 // ---- 1. root box -----------------------------------------------------------
-__global__ void bbox_partial(const float4 *__restrict__ src, int n, float *__restrict__ part) {
-    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+template <class T>
+__global__ void bbox_partial(const typename Prec<T>::V4 *__restrict__ src, int n, T *__restrict__ part) {
+    using P = Prec<T>;
+    T mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 p = src[i];
-        mn[0] = fminf(mn[0], p.x);
-        mn[1] = fminf(mn[1], p.y);
-        mn[2] = fminf(mn[2], p.z);
-        mx[0] = fmaxf(mx[0], p.x);
-        mx[1] = fmaxf(mx[1], p.y);
-        mx[2] = fmaxf(mx[2], p.z);
+        const typename P::V4 p = src[i];
+        mn[0] = P::min(mn[0], p.x);
+        mn[1] = P::min(mn[1], p.y);
+        mn[2] = P::min(mn[2], p.z);
+        mx[0] = P::max(mx[0], p.x);
+        mx[1] = P::max(mx[1], p.y);
+        mx[2] = P::max(mx[2], p.z);
     }
-    __shared__ float s[6][256];
+    __shared__ T s[6][256];
     for (int a = 0; a < 3; ++a) {
         s[a][threadIdx.x] = mn[a];
         s[3 + a][threadIdx.x] = mx[a];
@@ -95,8 +129,8 @@ __global__ void bbox_partial(const float4 *__restrict__ src, int n, float *__res
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w)
             for (int a = 0; a < 3; ++a) {
-                s[a][threadIdx.x] = fminf(s[a][threadIdx.x], s[a][threadIdx.x + w]);
-                s[3 + a][threadIdx.x] = fmaxf(s[3 + a][threadIdx.x], s[3 + a][threadIdx.x + w]);
+                s[a][threadIdx.x] = P::min(s[a][threadIdx.x], s[a][threadIdx.x + w]);
+                s[3 + a][threadIdx.x] = P::max(s[3 + a][threadIdx.x], s[3 + a][threadIdx.x + w]);
             }
         __syncthreads();
     }
@@ -107,19 +141,21 @@ __global__ void bbox_partial(const float4 *__restrict__ src, int n, float *__res
 // AABB, half = (max extent + 0) / 2 (MidPoint::half), min/max = centre -/+ half.
 // One block of 256 threads folds the per-block extents (min/max: exact in any
 // order), then thread 0 forms the reference's square root box.
-__global__ void bbox_final(const float *__restrict__ part, int nb, float *__restrict__ box) {
-    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+template <class T>
+__global__ void bbox_final(const T *__restrict__ part, int nb, T *__restrict__ box) {
+    using P = Prec<T>;
+    T mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int b = threadIdx.x; b < nb; b += blockDim.x)
         for (int a = 0; a < 3; ++a) {
-            mn[a] = fminf(mn[a], part[b * 6 + a]);
-            mx[a] = fmaxf(mx[a], part[b * 6 + 3 + a]);
+            mn[a] = P::min(mn[a], part[b * 6 + a]);
+            mx[a] = P::max(mx[a], part[b * 6 + 3 + a]);
         }
     for (int o = 16; o > 0; o >>= 1)
         for (int a = 0; a < 3; ++a) {
-            mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
-            mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+            mn[a] = P::min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = P::max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
         }
-    __shared__ float s[6][8];
+    __shared__ T s[6][8];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0)
         for (int a = 0; a < 3; ++a) {
@@ -130,31 +166,33 @@ __global__ void bbox_final(const float *__restrict__ part, int nb, float *__rest
     if (threadIdx.x != 0) return;
     for (int w = 1; w < int(blockDim.x >> 5); ++w)
         for (int a = 0; a < 3; ++a) {
-            mn[a] = fminf(mn[a], s[a][w]);
-            mx[a] = fmaxf(mx[a], s[3 + a][w]);
+            mn[a] = P::min(mn[a], s[a][w]);
+            mx[a] = P::max(mx[a], s[3 + a][w]);
         }
-    float half = 0.0f;
-    float c[3];
+    T half = 0;
+    T c[3];
     for (int a = 0; a < 3; ++a) {
-        c[a] = __fmul_rn(__fadd_rn(mn[a], mx[a]), 0.5f);
-        half = fmaxf(half, __fsub_rn(mx[a], mn[a]));
+        c[a] = P::mul(P::add(mn[a], mx[a]), T(0.5));
+        half = P::max(half, P::sub(mx[a], mn[a]));
     }
-    half = __fmul_rn(__fadd_rn(half, 0.0f), 0.5f);
+    half = P::mul(P::add(half, T(0)), T(0.5));
     for (int a = 0; a < 3; ++a) {
-        box[a] = __fsub_rn(c[a], half);
-        box[3 + a] = __fadd_rn(c[a], half);
+        box[a] = P::sub(c[a], half);
+        box[3 + a] = P::add(c[a], half);
     }
 }
 
 // ---- 2. keys ---------------------------------------------------------------
-__device__ __forceinline__ uint64_t key_of(float px, float py, float pz, const float *box) {
-    float mn0 = box[0], mn1 = box[1], mn2 = box[2], mx0 = box[3], mx1 = box[4], mx2 = box[5];
+template <class T>
+__device__ __forceinline__ uint64_t key_of(T px, T py, T pz, const T *box) {
+    using P = Prec<T>;
+    T mn0 = box[0], mn1 = box[1], mn2 = box[2], mx0 = box[3], mx1 = box[4], mx2 = box[5];
     uint64_t key = 0;
 #pragma unroll 3
     for (int l = 0; l < LEVELS; ++l) {
-        const float c0 = __fmul_rn(__fadd_rn(mn0, mx0), 0.5f);
-        const float c1 = __fmul_rn(__fadd_rn(mn1, mx1), 0.5f);
-        const float c2 = __fmul_rn(__fadd_rn(mn2, mx2), 0.5f);
+        const T c0 = P::mul(P::add(mn0, mx0), T(0.5));
+        const T c1 = P::mul(P::add(mn1, mx1), T(0.5));
+        const T c2 = P::mul(P::add(mn2, mx2), T(0.5));
         const int b0 = px < c0, b1 = py < c1, b2 = pz < c2;
         if (b0) mx0 = c0; else mn0 = c0;
         if (b1) mx1 = c1; else mn1 = c1;
@@ -165,20 +203,22 @@ __device__ __forceinline__ uint64_t key_of(float px, float py, float pz, const f
     return key;
 }
 
-__global__ void make_keys(const float4 *__restrict__ bodies, int n, const float *__restrict__ box_g,
+template <class T>
+__global__ void make_keys(const typename Prec<T>::V4 *__restrict__ bodies, int n, const T *__restrict__ box_g,
                           uint64_t *__restrict__ keys, uint32_t *__restrict__ idx) {
-    __shared__ float box[6];
+    __shared__ T box[6];
     if (threadIdx.x < 6) box[threadIdx.x] = box_g[threadIdx.x];
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float4 p = bodies[i];
-    keys[i] = key_of(p.x, p.y, p.z, box);
+    const typename Prec<T>::V4 p = bodies[i];
+    keys[i] = key_of<T>(p.x, p.y, p.z, box);
     idx[i] = uint32_t(i);
 }
 
-__global__ void gather_bodies(const float4 *__restrict__ src, const uint32_t *__restrict__ idx, int n,
-                              float4 *__restrict__ out) {
+template <class V4>
+__global__ void gather_bodies(const V4 *__restrict__ src, const uint32_t *__restrict__ idx, int n,
+                              V4 *__restrict__ out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) out[k] = src[idx[k]];
 }
@@ -279,13 +319,15 @@ __global__ void octree_links(const int *__restrict__ counters, const int *__rest
 // ---- 6. preorder layout ------------------------------------------------------
 // nodeB = {width bits, skip, first body (-1: internal cell), body count}.
 // counters[1] = T (cells + leaves), counters[2] = internal cells.
+template <class T>
 __global__ void layout(int *counters, const int *__restrict__ bfirst,
                        const int *__restrict__ blast, const int *__restrict__ bdelta,
                        const uint8_t *__restrict__ top, const int *__restrict__ oparent,
                        const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ pscan,
                        const uint64_t *__restrict__ ukey, const uint32_t *__restrict__ ufirst,
-                       const float *__restrict__ box, int *__restrict__ pre, int4 *__restrict__ nodeB,
-                       float4 *__restrict__ nodeG, int2 *__restrict__ nodeR) {
+                       const T *__restrict__ box, int *__restrict__ pre, int4 *__restrict__ nodeB,
+                       typename Prec<T>::V4 *__restrict__ nodeG, int2 *__restrict__ nodeR) {
+    using P = Prec<T>;
     const int M = counters[0];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0) {
@@ -305,35 +347,38 @@ __global__ void layout(int *counters, const int *__restrict__ bfirst,
         // f32 ops.
         const int L = bdelta[k] / 3;
         const uint64_t key = ukey[b];
-        float mn0 = box[0], mn1 = box[1], mn2 = box[2], mx0 = box[3], mx1 = box[4], mx2 = box[5];
+        T mn0 = box[0], mn1 = box[1], mn2 = box[2], mx0 = box[3], mx1 = box[4], mx2 = box[5];
         for (int l = 0; l < L; ++l) {
             const int o = 7 - int((key >> (3 * (LEVELS - 1 - l))) & 7u);
-            const float c0 = __fmul_rn(__fadd_rn(mn0, mx0), 0.5f);
-            const float c1 = __fmul_rn(__fadd_rn(mn1, mx1), 0.5f);
-            const float c2 = __fmul_rn(__fadd_rn(mn2, mx2), 0.5f);
+            const T c0 = P::mul(P::add(mn0, mx0), T(0.5));
+            const T c1 = P::mul(P::add(mn1, mx1), T(0.5));
+            const T c2 = P::mul(P::add(mn2, mx2), T(0.5));
             if (o & 1) mx0 = c0; else mn0 = c0;
             if (o & 2) mx1 = c1; else mn1 = c1;
             if (o & 4) mx2 = c2; else mn2 = c2;
         }
-        const float w = __fsub_rn(mx0, mn0);
-        nodeB[pk] = make_int4(__float_as_int(w), skip, -1, 0);
-        nodeG[pk] = make_float4(0.5f * (mn0 + mx0), 0.5f * (mn1 + mx1), 0.5f * (mn2 + mx2), w);
+        const T w = P::sub(mx0, mn0);
+        // the f32 walk reads the width from nodeB.x; the f64 walk from nodeG.w
+        nodeB[pk] = make_int4(sizeof(T) == 4 ? __float_as_int(float(w)) : 0, skip, -1, 0);
+        nodeG[pk] = P::make(T(0.5) * (mn0 + mx0), T(0.5) * (mn1 + mx1), T(0.5) * (mn2 + mx2), w);
         nodeR[pk] = make_int2(int(ufirst[b]), int(ufirst[blast[k] + 1]));
     }
     if (k < M) {
         const int pk = k + int(pscan[k]) + int(cnt[k]);
         const int f = int(ufirst[k]);
         nodeB[pk] = make_int4(0, pk + 1, f, int(ufirst[k + 1]) - f);
-        nodeG[pk] = make_float4(0.f, 0.f, 0.f, 0.f);
+        nodeG[pk] = P::make(T(0), T(0), T(0), T(0));
         nodeR[pk] = make_int2(f, int(ufirst[k + 1]));
     }
 }
 
 // ---- 7. moments ------------------------------------------------------------
-__device__ void store_cell(const Moments &m, int pk, Moments *__restrict__ mom, float4 *__restrict__ nodeA,
+template <class T>
+__device__ void store_cell(const Moments &m, int pk, Moments *__restrict__ mom, typename Prec<T>::V4 *__restrict__ nodeA,
                            float4 *__restrict__ nodeQ) {
     mom[pk] = m;
-    nodeA[pk] = make_float4(float(m.cx), float(m.cy), float(m.cz), float(m.m));
+    nodeA[pk] = Prec<T>::make(T(m.cx), T(m.cy), T(m.cz), T(m.m));
+    if (!nodeQ) return;  // the f64 method is monopole only
     const double tr = m.sxx + m.syy + m.szz;
     nodeQ[2 * pk] = make_float4(float(3 * m.sxx - tr), float(3 * m.sxy), float(3 * m.sxz), float(3 * m.syy - tr));
     nodeQ[2 * pk + 1] = make_float4(float(3 * m.syz), float(3 * m.szz - tr), 0.f, 0.f);
@@ -341,10 +386,12 @@ __device__ void store_cell(const Moments &m, int pk, Moments *__restrict__ mom, 
 
 // Leaves: a single body is its own cell data; several (coincident, or closer than
 // the key resolution) get FP64 moments.
+template <class T>
 __global__ void leaf_moments(const int *__restrict__ counters, const uint32_t *__restrict__ ufirst,
-                             const float4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
-                             const uint32_t *__restrict__ cnt, Moments *__restrict__ mom, float4 *__restrict__ nodeA,
-                             float4 *__restrict__ nodeQ) {
+                             const typename Prec<T>::V4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
+                             const uint32_t *__restrict__ cnt, Moments *__restrict__ mom,
+                             typename Prec<T>::V4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
+    using V4 = typename Prec<T>::V4;
     const int M = counters[0];
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= M) return;
@@ -352,14 +399,16 @@ __global__ void leaf_moments(const int *__restrict__ counters, const uint32_t *_
     const int pk = u + int(pscan[u]) + int(cnt[u]);
     if (e - f == 1) {
         nodeA[pk] = sbody[f];
-        nodeQ[2 * pk] = make_float4(0.f, 0.f, 0.f, 0.f);
-        nodeQ[2 * pk + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (nodeQ) {
+            nodeQ[2 * pk] = make_float4(0.f, 0.f, 0.f, 0.f);
+            nodeQ[2 * pk + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
         return;
     }
     Moments m{};
     double sx = 0, sy = 0, sz = 0;
     for (int b = f; b < e; ++b) {
-        const float4 p = sbody[b];
+        const V4 p = sbody[b];
         m.m += p.w;
         sx += double(p.w) * p.x;
         sy += double(p.w) * p.y;
@@ -372,7 +421,7 @@ __global__ void leaf_moments(const int *__restrict__ counters, const uint32_t *_
         m.cz = sz / m.m;
     } else {  // massless: plain mean (gravity/impls/mod.rs:127-129)
         for (int b = f; b < e; ++b) {
-            const float4 p = sbody[b];
+            const V4 p = sbody[b];
             m.cx += p.x;
             m.cy += p.y;
             m.cz += p.z;
@@ -382,7 +431,7 @@ __global__ void leaf_moments(const int *__restrict__ counters, const uint32_t *_
         m.cz /= m.count;
     }
     for (int b = f; b < e; ++b) {
-        const float4 p = sbody[b];
+        const V4 p = sbody[b];
         const double dx = p.x - m.cx, dy = p.y - m.cy, dz = p.z - m.cz;
         m.sxx += p.w * dx * dx;
         m.sxy += p.w * dx * dy;
@@ -391,7 +440,7 @@ __global__ void leaf_moments(const int *__restrict__ counters, const uint32_t *_
         m.syz += p.w * dy * dz;
         m.szz += p.w * dz * dz;
     }
-    store_cell(m, pk, mom, nodeA, nodeQ);
+    store_cell<T>(m, pk, mom, nodeA, nodeQ);
 }
 
 // Cells per octree level: lcount[L], then by_level sorted by level (counting sort).
@@ -442,15 +491,17 @@ __global__ void cell_level_scatter(const int *__restrict__ counters, const int *
 // pass over the children: sums about the cell's geometric centre G (offsets within
 // a cell width, no cancellation), then moved to the centre of mass C by the
 // parallel-axis rule S_C = S_G - P P^T / M with P = sum m (c - G) = M (C - G).
+template <class T>
 __global__ void cell_moments_level(int L, const int *__restrict__ levels, const int *__restrict__ by_level,
                                    const int *__restrict__ pre, const int4 *__restrict__ nodeB,
-                                   const float4 *__restrict__ nodeG, Moments *__restrict__ mom,
-                                   float4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
+                                   const typename Prec<T>::V4 *__restrict__ nodeG, Moments *__restrict__ mom,
+                                   typename Prec<T>::V4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
+    using V4 = typename Prec<T>::V4;
     const int begin = levels[LEVELS + 1 + L], end_l = begin + levels[L];
     for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end_l; i += gridDim.x * blockDim.x) {
         const int pv = pre[by_level[i]];
         const int end = nodeB[pv].y;
-        const float4 g = nodeG[pv];
+        const V4 g = nodeG[pv];
         const double gx = g.x, gy = g.y, gz = g.z;
         Moments m{};
         double px = 0, py = 0, pz = 0;
@@ -458,7 +509,7 @@ __global__ void cell_moments_level(int L, const int *__restrict__ levels, const 
             const int4 cb = nodeB[c];
             double cx, cy, cz, cmm, cn, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
             if (cb.z >= 0 && cb.w == 1) {  // a single body, read from nodeA
-                const float4 a = nodeA[c];
+                const V4 a = nodeA[c];
                 cx = a.x, cy = a.y, cz = a.z, cmm = a.w, cn = 1.0;
             } else {
                 const Moments &cm = mom[c];
@@ -498,7 +549,7 @@ __global__ void cell_moments_level(int L, const int *__restrict__ levels, const 
                 const int4 cb = nodeB[c];
                 double cx, cy, cz, cn;
                 if (cb.z >= 0 && cb.w == 1) {
-                    const float4 a = nodeA[c];
+                    const V4 a = nodeA[c];
                     cx = a.x, cy = a.y, cz = a.z, cn = 1.0;
                 } else {
                     cx = mom[c].cx, cy = mom[c].cy, cz = mom[c].cz, cn = mom[c].count;
@@ -512,7 +563,7 @@ __global__ void cell_moments_level(int L, const int *__restrict__ levels, const 
             m.cy = gy + uy / m.count;
             m.cz = gz + uz / m.count;
         }
-        store_cell(m, pv, mom, nodeA, nodeQ);
+        store_cell<T>(m, pv, mom, nodeA, nodeQ);
     }
 }
 
@@ -1636,6 +1687,217 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
     }
 }
 
+// ---- the reference rule over DVec3 bodies (f64 method) -------------------------
+// As bh_walk_masked with one body per lane, in double: node data, widths and the
+// per-pair kernel (impl_acceleration_cpu_scalar!(DVec3, f64): d * (m / (n_s sqrt
+// n_s)), IEEE-rounded in the reference's order) are f64; accepted sets per body
+// are the reference's. Monopole only, as the reference.
+constexpr int W64_WARPS = 4;
+constexpr int W64_STACK = 384;
+
+__device__ __forceinline__ void pair64(double px, double py, double pz, double cx, double cy, double cz, double m,
+                                       double eps2, double &ax, double &ay, double &az) {
+    const double dx = __dsub_rn(cx, px), dy = __dsub_rn(cy, py), dz = __dsub_rn(cz, pz);
+    const double n = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    if (n == 0.0) return;  // checked: d itself, which is zero
+    const double ns = __dadd_rn(n, eps2);
+    const double s = __ddiv_rn(m, __dmul_rn(ns, __dsqrt_rn(ns)));
+    ax = __dadd_rn(ax, __dmul_rn(dx, s));
+    ay = __dadd_rn(ay, __dmul_rn(dy, s));
+    az = __dadd_rn(az, __dmul_rn(dz, s));
+}
+
+struct List64 {
+    static constexpr int CAP = 128;
+    double f[4][CAP];
+    unsigned mask[CAP];
+};
+
+__device__ __forceinline__ void eval_list64(const List64 &Lst, int cnt, double px, double py, double pz, double eps2,
+                                            double &ax, double &ay, double &az) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    for (int e = 0; e < cnt; ++e)
+        if ((Lst.mask[e] >> lane) & 1u) pair64(px, py, pz, Lst.f[0][e], Lst.f[1][e], Lst.f[2][e], Lst.f[3][e], eps2, ax, ay, az);
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(32 * W64_WARPS)
+    bh_walk64(const double4_32a *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
+              const double4_32a *__restrict__ nodeA, const int4 *__restrict__ nodeB,
+              const double4_32a *__restrict__ nodeG, const double4_32a *__restrict__ sbody,
+              const int *__restrict__ counters, double th2, double eps2, double *__restrict__ out,
+              unsigned long long *__restrict__ stats, int *__restrict__ err) {
+    __shared__ int4 s_stack[W64_WARPS][W64_STACK];
+    __shared__ List64 s_list[W64_WARPS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int group = blockIdx.x * W64_WARPS + warp;
+    if (group * 32 >= n_aff) return;
+    const int t = group * 32 + lane;
+    const bool valid = t < n_aff;
+    const double4_32a p = tbody[valid ? t : group * 32];
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned valid_mask = __ballot_sync(0xffffffffu, valid);
+    int4 *stack = s_stack[warp];
+    List64 &Lst = s_list[warp];
+    const int T = counters[1];
+    double mn0 = p.x, mn1 = p.y, mn2 = p.z, mx0 = p.x, mx1 = p.y, mx2 = p.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn0 = fmin(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
+        mn1 = fmin(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
+        mn2 = fmin(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
+        mx0 = fmax(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
+        mx1 = fmax(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
+        mx2 = fmax(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
+    }
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (lane == 0) stack[0] = make_int4(0, T, int(valid_mask), 0);
+    __syncwarp();
+    int S = 1, Nl = 0;
+    unsigned long long acc_pairs = 0, visit_pairs = 0;
+    bool failed = false;
+    while (S > 0) {
+        const int k = min(min(32, S), max(1, (W64_STACK - S) / 2));
+        const bool have = lane < k;
+        const int4 r = have ? stack[S - 1 - lane] : make_int4(0, 0, 0, 0);
+        __syncwarp();
+        S -= k;
+        const int node = r.x;
+        const unsigned mask = unsigned(r.z);
+        double4_32a A;
+        A.x = A.y = A.z = A.w = 0.0;
+        int4 B = make_int4(0, 0, 0, 0);
+        double w = 0.0;
+        if (have) {
+            A = nodeA[node];
+            B = __ldg(nodeB + node);
+            if (B.z < 0) w = nodeG[node].w;
+        }
+        visit_pairs += __popc(mask);
+        const bool cell = B.z < 0;
+        unsigned open_m = 0, acc_m = 0;
+        bool need = false;
+        if (have && mask) {
+            const double e0 = fmax(fmax(mn0 - A.x, A.x - mx0), 0.0);
+            const double e1 = fmax(fmax(mn1 - A.y, A.y - mx1), 0.0);
+            const double e2b = fmax(fmax(mn2 - A.z, A.z - mx2), 0.0);
+            const double db2 = __dadd_rn(__dadd_rn(__dmul_rn(e0, e0), __dmul_rn(e1, e1)), __dmul_rn(e2b, e2b));
+            if (!(db2 > 0.0)) {
+                need = true;
+            } else if (!cell || !(__dmul_rn(th2, db2) < __dmul_rn(w, w))) {
+                acc_m = mask;
+            } else {
+                const double f0 = fmax(A.x - mn0, mx0 - A.x), f1 = fmax(A.y - mn1, mx1 - A.y);
+                const double f2b = fmax(A.z - mn2, mx2 - A.z);
+                const double dm2 = __dadd_rn(__dadd_rn(__dmul_rn(f0, f0), __dmul_rn(f1, f1)), __dmul_rn(f2b, f2b));
+                if (__dmul_rn(th2, dm2) < __dmul_rn(w, w)) open_m = mask;
+                else need = true;
+            }
+        }
+        unsigned vm = __ballot_sync(0xffffffffu, need);
+        while (vm) {
+            const int j = __ffs(vm) - 1;
+            vm &= vm - 1;
+            const double cx = __shfl_sync(0xffffffffu, A.x, j), cy = __shfl_sync(0xffffffffu, A.y, j);
+            const double cz = __shfl_sync(0xffffffffu, A.z, j), cw = __shfl_sync(0xffffffffu, w, j);
+            const unsigned mj = __shfl_sync(0xffffffffu, mask, j);
+            const bool cj = __shfl_sync(0xffffffffu, cell, j);
+            // the reference's d^2: (com - body) squared, x, y, z in order
+            const double dx = __dsub_rn(cx, p.x), dy = __dsub_rn(cy, p.y), dz = __dsub_rn(cz, p.z);
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            const bool mine = (mj >> lane) & 1u;
+            const bool o = mine && cj && d2 > 0.0 && __dmul_rn(th2, d2) < __dmul_rn(cw, cw);
+            const bool a = mine && !o && d2 > 0.0;
+            const unsigned om = __ballot_sync(0xffffffffu, o), am = __ballot_sync(0xffffffffu, a);
+            if (lane == j) {
+                open_m = om;
+                acc_m = am;
+            }
+        }
+        const bool rest = have && mask && B.y < r.y;
+        const bool opn = open_m != 0u;
+        const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, opn);
+        const int total = __popc(mrest) + __popc(mopen);
+        int slot = S + __popc(mrest & lt) + __popc(mopen & lt);
+        if (slot + int(rest) + int(opn) > W64_STACK) {
+            failed = true;
+        } else {
+            if (rest) stack[slot++] = make_int4(B.y, r.y, int(mask), 0);
+            if (opn) stack[slot++] = make_int4(node + 1, B.y, int(open_m), 0);
+        }
+        if (__any_sync(0xffffffffu, failed)) {
+            failed = true;
+            break;
+        }
+        S += total;
+        acc_pairs += __popc(acc_m);
+        // accepted cells and single bodies: one list entry with the accepting mask;
+        // several-body leaves: one entry per body
+        const bool single = acc_m != 0u && (cell || B.w == 1);
+        const unsigned ms = __ballot_sync(0xffffffffu, single);
+        const int ns = __popc(ms);
+        if (Nl + ns > List64::CAP) {
+            eval_list64(Lst, Nl, p.x, p.y, p.z, eps2, ax, ay, az);
+            Nl = 0;
+        }
+        if (single) {
+            const int e = Nl + __popc(ms & lt);
+            Lst.f[0][e] = A.x;
+            Lst.f[1][e] = A.y;
+            Lst.f[2][e] = A.z;
+            Lst.f[3][e] = A.w;
+            Lst.mask[e] = acc_m;
+        }
+        Nl += ns;
+        unsigned mbk = __ballot_sync(0xffffffffu, acc_m != 0u && !cell && B.w > 1);
+        while (mbk) {
+            const int src = __ffs(mbk) - 1;
+            mbk &= mbk - 1;
+            const int f = __shfl_sync(0xffffffffu, B.z, src), c = __shfl_sync(0xffffffffu, B.w, src);
+            const unsigned bm = __shfl_sync(0xffffffffu, acc_m, src);
+            for (int base = 0; base < c; base += 32) {
+                const int n = min(32, c - base);
+                if (Nl + n > List64::CAP) {
+                    eval_list64(Lst, Nl, p.x, p.y, p.z, eps2, ax, ay, az);
+                    Nl = 0;
+                }
+                if (lane < n) {
+                    const double4_32a q = sbody[f + base + lane];
+                    Lst.f[0][Nl + lane] = q.x;
+                    Lst.f[1][Nl + lane] = q.y;
+                    Lst.f[2][Nl + lane] = q.z;
+                    Lst.f[3][Nl + lane] = q.w;
+                    Lst.mask[Nl + lane] = bm;
+                }
+                Nl += n;
+            }
+        }
+        __syncwarp();
+    }
+    eval_list64(Lst, Nl, p.x, p.y, p.z, eps2, ax, ay, az);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        acc_pairs += __shfl_xor_sync(0xffffffffu, acc_pairs, o);
+        visit_pairs += __shfl_xor_sync(0xffffffffu, visit_pairs, o);
+    }
+    if (failed) {  // no stackless fallback in f64: the bodies are NaN and the call fails
+        ax = ay = az = __longlong_as_double(0x7ff8000000000000ll);
+        if (lane == 0) atomicOr(err, 1);
+    }
+    if (valid) {
+        const uint32_t o = tidx[t];
+        out[3 * size_t(o) + 0] = ax;
+        out[3 * size_t(o) + 1] = ay;
+        out[3 * size_t(o) + 2] = az;
+    }
+    if (stats && lane == 0) {
+        atomicAdd(stats + 0, acc_pairs);
+        atomicAdd(stats + 1, visit_pairs);
+        atomicAdd(stats + 2, 1ull);
+    }
+}
+
 using WalkKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
                             const float4 *, const int *, float, float, float *, unsigned long long *);
 using GroupKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
@@ -1672,14 +1934,21 @@ static T *as(DevBuf &b) {
 static inline int blocks(int n, int t = 256) { return (n + t - 1) / t; }
 
 // Builds the tree over d_src (n_src >= 1 bodies) into the context's state.
-static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
+template <class T>
+static int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
+    using V4 = typename Prec<T>::V4;
+    constexpr bool F64 = sizeof(T) == 8;
+    // the f64 method keeps its own body, node and box arrays (the rest is shared)
+    DevBuf &sb = F64 ? S.sbody64 : S.sbody;
+    DevBuf &nA = F64 ? S.nodeA64 : S.nodeA;
+    DevBuf &nG = F64 ? S.nodeG64 : S.nodeG;
     cudaStream_t st = ctx->stream;
     const size_t N = size_t(n);
-    PT_TRY(ensure_buf(ctx, S.box_part, sizeof(float) * 6 * 1024));
-    PT_TRY(ensure_buf(ctx, S.box, sizeof(float) * 8));
+    PT_TRY(ensure_buf(ctx, S.box_part, sizeof(T) * 6 * 1024));
+    PT_TRY(ensure_buf(ctx, S.box, sizeof(T) * 8));
     PT_TRY(ensure_buf(ctx, S.keys, sizeof(uint64_t) * N));
     PT_TRY(ensure_buf(ctx, S.idx, sizeof(uint32_t) * N));
-    PT_TRY(ensure_buf(ctx, S.sbody, sizeof(float4) * N));
+    PT_TRY(ensure_buf(ctx, sb, sizeof(V4) * N));
     PT_TRY(ensure_buf(ctx, S.flags, sizeof(uint32_t) * N));
     PT_TRY(ensure_buf(ctx, S.uscan, sizeof(uint32_t) * (N + 1)));
     PT_TRY(ensure_buf(ctx, S.ukey, sizeof(uint64_t) * N));
@@ -1697,23 +1966,24 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
     PT_TRY(ensure_buf(ctx, S.pre, sizeof(int) * N));
     PT_TRY(ensure_buf(ctx, S.levels, sizeof(int) * (3 * LEVELS + 8)));
     PT_TRY(ensure_buf(ctx, S.by_level, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.nodeA, sizeof(float4) * 2 * N));
+    PT_TRY(ensure_buf(ctx, nA, sizeof(V4) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.nodeB, sizeof(int4) * 2 * N));
-    PT_TRY(ensure_buf(ctx, S.nodeQ, sizeof(float4) * 4 * N));
-    PT_TRY(ensure_buf(ctx, S.nodeG, sizeof(float4) * 2 * N));
+    if (!F64) PT_TRY(ensure_buf(ctx, S.nodeQ, sizeof(float4) * 4 * N));
+    PT_TRY(ensure_buf(ctx, nG, sizeof(V4) * 2 * N));
+    float4 *nodeQ = F64 ? nullptr : as<float4>(S.nodeQ);
     PT_TRY(ensure_buf(ctx, S.nodeR, sizeof(int2) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.mom, sizeof(Moments) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.counters, sizeof(unsigned long long) * 16));
 
     const int nb = std::min(1024, blocks(n));
-    bbox_partial<<<nb, 256, 0, st>>>(d_src, n, as<float>(S.box_part));
+    bbox_partial<T><<<nb, 256, 0, st>>>(d_src, n, as<T>(S.box_part));
     PT_TRY(check_launch(ctx, "bbox_partial"));
-    bbox_final<<<1, 256, 0, st>>>(as<float>(S.box_part), nb, as<float>(S.box));
+    bbox_final<T><<<1, 256, 0, st>>>(as<T>(S.box_part), nb, as<T>(S.box));
     PT_TRY(check_launch(ctx, "bbox_final"));
-    make_keys<<<blocks(n), 256, 0, st>>>(d_src, n, as<float>(S.box), as<uint64_t>(S.keys), as<uint32_t>(S.idx));
+    make_keys<T><<<blocks(n), 256, 0, st>>>(d_src, n, as<T>(S.box), as<uint64_t>(S.keys), as<uint32_t>(S.idx));
     PT_TRY(check_launch(ctx, "make_keys"));
     PT_TRY(radix_sort_u64(ctx, S.prims, as<uint64_t>(S.keys), as<uint32_t>(S.idx), n, 3 * LEVELS));
-    gather_bodies<<<blocks(n), 256, 0, st>>>(d_src, as<uint32_t>(S.idx), n, as<float4>(S.sbody));
+    gather_bodies<V4><<<blocks(n), 256, 0, st>>>(d_src, as<uint32_t>(S.idx), n, as<V4>(sb));
     PT_TRY(check_launch(ctx, "gather_bodies"));
     unit_flags<<<blocks(n), 256, 0, st>>>(as<uint64_t>(S.keys), n, as<uint32_t>(S.flags));
     PT_TRY(check_launch(ctx, "unit_flags"));
@@ -1734,10 +2004,10 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
                                            as<uint32_t>(S.cnt));
     PT_TRY(check_launch(ctx, "octree_links"));
     PT_TRY(scan_u32(ctx, S.prims, as<uint32_t>(S.cnt), as<uint32_t>(S.pscan), n + 1));
-    layout<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.blast), as<int>(S.bdelta),
+    layout<T><<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.blast), as<int>(S.bdelta),
                                      as<uint8_t>(S.top), as<int>(S.oparent), as<uint32_t>(S.cnt),
                                      as<uint32_t>(S.pscan), as<uint64_t>(S.ukey), as<uint32_t>(S.ufirst),
-                                     as<float>(S.box), as<int>(S.pre), as<int4>(S.nodeB), as<float4>(S.nodeG),
+                                     as<T>(S.box), as<int>(S.pre), as<int4>(S.nodeB), as<V4>(nG),
                                      as<int2>(S.nodeR));
     PT_TRY(check_launch(ctx, "layout"));
 
@@ -1749,33 +2019,43 @@ static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) {
     cell_level_scatter<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<uint8_t>(S.top), levels,
                                                  as<int>(S.by_level));
     PT_TRY(check_launch(ctx, "cell_level_scatter"));
-    leaf_moments<<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<float4>(S.sbody),
-                                           as<uint32_t>(S.pscan), as<uint32_t>(S.cnt), as<Moments>(S.mom),
-                                           as<float4>(S.nodeA), as<float4>(S.nodeQ));
+    leaf_moments<T><<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<V4>(sb),
+                                              as<uint32_t>(S.pscan), as<uint32_t>(S.cnt), as<Moments>(S.mom),
+                                              as<V4>(nA), nodeQ);
     PT_TRY(check_launch(ctx, "leaf_moments"));
     const int lvl_grid = std::max(1, std::min(blocks(n), 8 * ctx->sm_count));
     for (int L = LEVELS - 1; L >= 0; --L) {
-        cell_moments_level<<<lvl_grid, 256, 0, st>>>(L, levels, as<int>(S.by_level), as<int>(S.pre),
-                                                     as<int4>(S.nodeB), as<float4>(S.nodeG), as<Moments>(S.mom),
-                                                     as<float4>(S.nodeA), as<float4>(S.nodeQ));
+        cell_moments_level<T><<<lvl_grid, 256, 0, st>>>(L, levels, as<int>(S.by_level), as<int>(S.pre),
+                                                        as<int4>(S.nodeB), as<V4>(nG), as<Moments>(S.mom),
+                                                        as<V4>(nA), nodeQ);
         PT_TRY(check_launch(ctx, "cell_moments_level"));
     }
     S.last_n_src = n;
+    S.f64 = F64;
     ++S.generation;
     return PT_OK;
 }
 
+static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) { return build_t<float>(ctx, S, d_src, n); }
+
 // Sorts separate targets along the same keys (same root box) for coherent warps.
-static int sort_targets(pt_ctx *ctx, State &S, const float4 *d_aff, int n) {
+template <class T>
+static int sort_targets_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_aff, int n) {
+    using V4 = typename Prec<T>::V4;
+    DevBuf &tb = sizeof(T) == 8 ? S.tbody64 : S.tbody;
     cudaStream_t st = ctx->stream;
     PT_TRY(ensure_buf(ctx, S.tkeys, sizeof(uint64_t) * size_t(n)));
     PT_TRY(ensure_buf(ctx, S.tidx, sizeof(uint32_t) * size_t(n)));
-    PT_TRY(ensure_buf(ctx, S.tbody, sizeof(float4) * size_t(n)));
-    make_keys<<<blocks(n), 256, 0, st>>>(d_aff, n, as<float>(S.box), as<uint64_t>(S.tkeys), as<uint32_t>(S.tidx));
+    PT_TRY(ensure_buf(ctx, tb, sizeof(V4) * size_t(n)));
+    make_keys<T><<<blocks(n), 256, 0, st>>>(d_aff, n, as<T>(S.box), as<uint64_t>(S.tkeys), as<uint32_t>(S.tidx));
     PT_TRY(check_launch(ctx, "make_keys(targets)"));
     PT_TRY(radix_sort_u64(ctx, S.prims, as<uint64_t>(S.tkeys), as<uint32_t>(S.tidx), n, 3 * LEVELS));
-    gather_bodies<<<blocks(n), 256, 0, st>>>(d_aff, as<uint32_t>(S.tidx), n, as<float4>(S.tbody));
+    gather_bodies<V4><<<blocks(n), 256, 0, st>>>(d_aff, as<uint32_t>(S.tidx), n, as<V4>(tb));
     return check_launch(ctx, "gather_bodies(targets)");
+}
+
+static int sort_targets(pt_ctx *ctx, State &S, const float4 *d_aff, int n) {
+    return sort_targets_t<float>(ctx, S, d_aff, n);
 }
 
 static int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n_aff, float theta,
@@ -1808,11 +2088,43 @@ static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src,
     return walk(ctx, S, tbody, tidx, n_aff, theta, softening, flags, d_out);
 }
 
+// The f64 method: build over DVec3 bodies, walk with the reference rule in double.
+static int run64(pt_ctx *ctx, const double4_32a *d_aff, int n_aff, const double4_32a *d_src, int n_src,
+                 double theta, double softening, double *d_out) {
+    cudaStream_t st = ctx->stream;
+    if (n_aff == 0) return PT_OK;
+    if (n_src == 0) {
+        PT_CUDA(cudaMemsetAsync(d_out, 0, sizeof(double) * 3 * size_t(n_aff), st));
+        return PT_OK;
+    }
+    State *Sp = state(ctx);
+    if (!Sp) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    State &S = *Sp;
+    mark(ctx, 0);
+    PT_TRY(build_t<double>(ctx, S, d_src, n_src));
+    const bool same = (d_aff == d_src) && (n_aff == n_src);
+    if (!same) PT_TRY(sort_targets_t<double>(ctx, S, d_aff, n_aff));
+    const double4_32a *tbody = same ? as<double4_32a>(S.sbody64) : as<double4_32a>(S.tbody64);
+    const uint32_t *tidx = same ? as<uint32_t>(S.idx) : as<uint32_t>(S.tidx);
+    unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 2;
+    int *err = as<int>(S.counters) + 3;
+    PT_CUDA(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
+    PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    mark(ctx, 1);
+    bh_walk64<<<(n_aff + 32 * W64_WARPS - 1) / (32 * W64_WARPS), 32 * W64_WARPS, 0, st>>>(
+        tbody, tidx, n_aff, as<double4_32a>(S.nodeA64), as<int4>(S.nodeB), as<double4_32a>(S.nodeG64),
+        as<double4_32a>(S.sbody64), as<int>(S.counters), theta * theta, softening * softening, d_out, stats, err);
+    PT_TRY(check_launch(ctx, "bh_walk64"));
+    mark(ctx, 2);
+    return PT_OK;
+}
+
 // Walks the context's current tree for targets tbody (key-sorted; tidx maps them back
 // to the caller's order) and writes accelerations to d_out.
 static int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n_aff, float theta,
                 float softening, uint32_t flags, float *d_out) {
     cudaStream_t st = ctx->stream;
+    if (S.f64) return set_error(PT_ERR_INVALID, "the context's tree holds DVec3 bodies: walk it with the f64 method");
     // counters: int[4] = {leaves, nodes, cells, error} then u64[8] = {interactions,
     // visits, warps, max group stack, learned records, cell interactions, warps that
     // fell back to the per-body walk, far nodes taken by the local expansion}
@@ -1912,6 +2224,7 @@ int bh_build_only(pt_ctx *ctx, const float4 *d_src, int n) {
 int bh_tree_view(pt_ctx *ctx, TreeView *out) {
     auto *S = static_cast<bh::State *>(ctx->bh);
     if (!S || !S->nodeA.ptr) return set_error(PT_ERR_INVALID, "no Barnes-Hut tree built yet");
+    if (S->f64) return set_error(PT_ERR_INVALID, "the current tree holds DVec3 bodies");
     out->nodeA = static_cast<const float4 *>(S->nodeA.ptr);
     out->nodeB = static_cast<const int4 *>(S->nodeB.ptr);
     out->nodeQ = static_cast<const float4 *>(S->nodeQ.ptr);
@@ -1944,7 +2257,8 @@ void pt_bh_state_free(pt_ctx *ctx) {
                      &S->top,      &S->oparent, &S->loparent, &S->cnt, &S->pscan,   &S->pre,    &S->levels,
                      &S->by_level,   &S->nodeA,  &S->nodeB,  &S->nodeQ,  &S->nodeG, &S->nodeR, &S->mom,     &S->tkeys,  &S->tidx,
                      &S->tbody,    &S->counters, &S->out,  &S->aff_h,  &S->src_h, &S->lrec, &S->lgroup,
-                     &S->lnext,    &S->lpart,  &S->lhead, &S->lcentre, &S->lused};
+                     &S->lnext,    &S->lpart,  &S->lhead, &S->lcentre, &S->lused, &S->sbody64, &S->nodeA64,
+                     &S->nodeG64,  &S->tbody64};
     for (DevBuf *b : all) free_buf(ctx, *b);
     delete S;
     ctx->bh = nullptr;
@@ -1998,6 +2312,56 @@ int pt_bh_accel_f32(pt_ctx *ctx, const float *aff, size_t n_aff, const float *sr
     PT_CUDA(cudaStreamSynchronize(st));
     if (err & 2)
         return set_error(PT_ERR_CAPACITY, "pt_bh_accel_f32: learned-correction records overflowed");
+    return PT_OK;
+}
+
+int pt_bh_accel_dvec3_device(pt_ctx *ctx, const double *d_aff, size_t n_aff, const double *d_src, size_t n_src,
+                             double theta, double softening, uint32_t flags, double *d_out) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_accel_dvec3_device: ctx is NULL");
+    PT_TRY(bh::validate("pt_bh_accel_dvec3_device", n_aff, n_src, 0));
+    if (flags) return set_error(PT_ERR_INVALID, "pt_bh_accel_dvec3_device: the f64 method takes no flags");
+    if (n_aff && (!d_aff || !d_out)) return set_error(PT_ERR_INVALID, "pt_bh_accel_dvec3_device: NULL buffer");
+    if (n_src && !d_src) return set_error(PT_ERR_INVALID, "pt_bh_accel_dvec3_device: NULL affecting buffer");
+    if ((n_aff && reinterpret_cast<uintptr_t>(d_aff) % 32) || (n_src && reinterpret_cast<uintptr_t>(d_src) % 32))
+        return set_error(PT_ERR_INVALID, "pt_bh_accel_dvec3_device: body buffers must be 32-byte aligned");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    return bh::run64(ctx, reinterpret_cast<const double4_32a *>(d_aff), int(n_aff),
+                     reinterpret_cast<const double4_32a *>(d_src), int(n_src), theta, softening, d_out);
+}
+
+int pt_bh_accel_dvec3(pt_ctx *ctx, const double *aff, size_t n_aff, const double *src, size_t n_src, double theta,
+                      double softening, uint32_t flags, double *out) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_accel_dvec3: ctx is NULL");
+    PT_TRY(bh::validate("pt_bh_accel_dvec3", n_aff, n_src, 0));
+    if (flags) return set_error(PT_ERR_INVALID, "pt_bh_accel_dvec3: the f64 method takes no flags");
+    if (n_aff && (!aff || !out)) return set_error(PT_ERR_INVALID, "pt_bh_accel_dvec3: NULL buffer");
+    if (n_src && !src) return set_error(PT_ERR_INVALID, "pt_bh_accel_dvec3: NULL affecting buffer");
+    if (n_aff == 0) return PT_OK;
+    PT_CUDA(cudaSetDevice(ctx->device));
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    const bool same = (aff == src) && (n_aff == n_src);
+    PT_TRY(ensure_buf(ctx, S->aff_h, 32 * n_aff));
+    if (!same && n_src) PT_TRY(ensure_buf(ctx, S->src_h, 32 * n_src));
+    PT_TRY(ensure_buf(ctx, S->out, 24 * n_aff));
+    double *d_aff = static_cast<double *>(S->aff_h.ptr);
+    double *d_src = same ? d_aff : static_cast<double *>(S->src_h.ptr);
+    double *d_out = static_cast<double *>(S->out.ptr);
+    cudaStream_t st = ctx->stream;
+    PT_CUDA(cudaMemcpyAsync(d_aff, aff, 32 * n_aff, cudaMemcpyHostToDevice, st));
+    if (!same && n_src) PT_CUDA(cudaMemcpyAsync(d_src, src, 32 * n_src, cudaMemcpyHostToDevice, st));
+    PT_TRY(bh::run64(ctx, reinterpret_cast<const double4_32a *>(d_aff), int(n_aff),
+                     reinterpret_cast<const double4_32a *>(d_src), int(n_src), theta, softening, d_out));
+    PT_CUDA(cudaMemcpyAsync(out, d_out, 24 * n_aff, cudaMemcpyDeviceToHost, st));
+    int err = 0;
+    if (n_src) PT_CUDA(cudaMemcpyAsync(&err, static_cast<int *>(S->counters.ptr) + 3, sizeof(int),
+                                       cudaMemcpyDeviceToHost, st));
+    PT_CUDA(cudaStreamSynchronize(st));
+    if (err & 1) return set_error(PT_ERR_CAPACITY, "pt_bh_accel_dvec3: a warp's stack ran out; its bodies are NaN");
     return PT_OK;
 }
 
@@ -2154,12 +2518,32 @@ int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out) {
 }
 
 // Copies the last tree (preorder) to host arrays of pt_bh_last_stats().nodes rows.
+int pt_bh_export_tree_dvec3(pt_ctx *ctx, double *com_mass, int32_t *links, double *centre_width, size_t rows) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_export_tree_dvec3: ctx is NULL");
+    auto *S = static_cast<bh::State *>(ctx->bh);
+    if (!S || !S->f64 || !S->nodeA64.ptr)
+        return set_error(PT_ERR_INVALID, "pt_bh_export_tree_dvec3: the last Barnes-Hut call was not the f64 method");
+    pt_bh_stats st;
+    PT_TRY(pt_bh_last_stats(ctx, &st));
+    if (rows < st.nodes) return set_error(PT_ERR_INVALID, "pt_bh_export_tree_dvec3: %zu rows < %llu nodes", rows,
+                                          (unsigned long long)st.nodes);
+    cudaStream_t s = ctx->stream;
+    if (com_mass) PT_CUDA(cudaMemcpyAsync(com_mass, S->nodeA64.ptr, 32 * st.nodes, cudaMemcpyDeviceToHost, s));
+    if (links) PT_CUDA(cudaMemcpyAsync(links, S->nodeB.ptr, 16 * st.nodes, cudaMemcpyDeviceToHost, s));
+    if (centre_width) PT_CUDA(cudaMemcpyAsync(centre_width, S->nodeG64.ptr, 32 * st.nodes, cudaMemcpyDeviceToHost, s));
+    PT_CUDA(cudaStreamSynchronize(s));
+    return PT_OK;
+}
+
 int pt_bh_export_tree(pt_ctx *ctx, float *com_mass, int32_t *links, float *quad, size_t rows) {
     using namespace pt;
     clear_error();
     if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_export_tree: ctx is NULL");
     auto *S = static_cast<bh::State *>(ctx->bh);
     if (!S || !S->nodeA.ptr) return set_error(PT_ERR_INVALID, "pt_bh_export_tree: no Barnes-Hut call yet");
+    if (S->f64) return set_error(PT_ERR_INVALID, "pt_bh_export_tree: the tree holds DVec3 bodies (pt_bh_export_tree_dvec3)");
     pt_bh_stats st;
     PT_TRY(pt_bh_last_stats(ctx, &st));
     if (rows < st.nodes) return set_error(PT_ERR_INVALID, "pt_bh_export_tree: %zu rows < %llu nodes", rows,

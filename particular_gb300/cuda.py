@@ -161,7 +161,9 @@ class BarnesHut:
     """
 
     def __init__(self, theta, resources, interaction, quadrupole=False, group=False,
-                 learned=False, local=False):
+                 learned=False, local=False, dvec3=False):
+        self.dvec3 = bool(dvec3)  # glam DVec3 bodies: the f64 method (reference rule only)
+        self.theta64 = float(theta)
         self.theta = float(np.float32(theta))
         self.resources = resources
         self.interaction = interaction
@@ -185,6 +187,20 @@ class BarnesHut:
 
     def compute(self, storage):
         b = as_between(storage)
+        if self.dvec3:
+            if self.flags:
+                raise N.CudaError(N.PT_ERR_INVALID, "the f64 method is the reference rule: no flags")
+            aff = positions(b.affected, np.float64)
+            src = fields(b.affecting, np.float64)
+            out = np.zeros((aff.shape[0], 3), np.float64)
+            if aff.shape[0] == 0:
+                return out
+            same = b.affected is b.affecting
+            it = self.interaction
+            N.check(N.lib().pt_bh_accel_dvec3(self.resources.handle, _ptr(aff), aff.shape[0],
+                                              _ptr(aff) if same else _ptr(src), src.shape[0], self.theta64,
+                                              getattr(it, "softening64", it.softening), 0, _ptr(out)))
+            return out
         if isinstance(b.affecting, DeviceTree):
             tree = b.affecting
             if tree.resources is not self.resources:
@@ -213,6 +229,15 @@ class BarnesHut:
         st = N.BhStats()
         N.check(N.lib().pt_bh_last_stats(self.resources.handle, ctypes.byref(st)))
         return {k: int(getattr(st, k)) for k, _ in N.BhStats._fields_}
+
+    def export_tree_dvec3(self):
+        """The last f64 tree in preorder: com_mass (n, 4), links (n, 4), centre_width (n, 4)."""
+        n = self.stats()["nodes"]
+        cm = np.zeros((n, 4), np.float64)
+        ln = np.zeros((n, 4), np.int32)
+        cw = np.zeros((n, 4), np.float64)
+        N.check(N.lib().pt_bh_export_tree_dvec3(self.resources.handle, _ptr(cm), _ptr(ln), _ptr(cw), n))
+        return {"com_mass": cm, "links": ln, "centre_width": cw, "width": cw[:, 3]}
 
     def export_tree(self):
         """The last tree in preorder: com_mass (n, 4), links (n, 4) int32, quad (n, 8)."""

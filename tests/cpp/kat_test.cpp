@@ -141,6 +141,18 @@ int main() {
     }
     std::printf("%-40s %s\n", "cuda::BruteForce over DVec3 (bit-exact)", exact64 ? "ok" : "FAIL");
     ok &= exact64;
+    // and Barnes-Hut over DVec3 at theta 0: every leaf, the same sums up to order
+    cuda::BarnesHut<double, AccelerationSoftened<double, true>> bh64{0.0, res, softened_checked(1e-3)};
+    const auto h64 = bh64.compute(b64);
+    double worst64 = 0.0, scale64 = 0.0;
+    for (size_t i = 0; i < b64.size(); ++i) {
+        worst64 = std::fmax(worst64, std::fabs(h64[i].x - g64[i].x) + std::fabs(h64[i].y - g64[i].y) +
+                                         std::fabs(h64[i].z - g64[i].z));
+        scale64 = std::fmax(scale64, std::fabs(g64[i].x) + std::fabs(g64[i].y) + std::fabs(g64[i].z));
+    }
+    const bool bhok = h64.size() == b64.size() && worst64 <= 1e-12 * scale64;
+    std::printf("%-40s %s (max diff %.1e)\n", "cuda::BarnesHut(0) over DVec3", bhok ? "ok" : "FAIL", worst64);
+    ok &= bhok;
 
     // tree reuse: build once, walk two target sets; equal to the combined calls
     std::vector<Body> srcs, t1, t2;

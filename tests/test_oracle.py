@@ -215,3 +215,17 @@ def test_mlp_oracle_gradient_by_finite_differences():
         pm[k] -= h
         fd = (M.loss_grad(pp, f, t)[0] - M.loss_grad(pm, f, t)[0]) / (2 * h)
         assert abs(fd - g[k]) <= 1e-6 + 1e-5 * abs(fd), k
+
+
+def test_dvec3_barnes_hut_restatement(oracle):
+    """The f64 orthtree and walk: theta 0 is the f64 brute force up to summation order,
+    and at theta 0.5 the accepted sets match the f32 walk's on f32-exact positions."""
+    b = ics.plummer(3000, seed=12)["bodies"].astype(np.float64)
+    ref = oracle.bf_dvec3(b, b, 0.01)
+    a0 = oracle.bh_dvec3(b, b, 0.0, 0.01)
+    assert np.abs(a0 - ref).max() <= 1e-12 * np.abs(ref).max()
+    a64, acc64 = oracle.bh_dvec3(b, b, 0.5, 0.01, accepted=True)
+    a32, acc32 = oracle.bh_f32(b.astype(np.float32), b.astype(np.float32), 0.5, 0.01, accepted=True)
+    assert np.array_equal(acc64, acc32)
+    e = np.linalg.norm(a64 - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    assert np.percentile(e, 95) < 2e-2
