@@ -1,2201 +1,12 @@
-// cuda::BarnesHut { theta }: on-device octree build and a warp-synchronous walk.
-//
-// The tree is the reference's orthtree (particular/src/tree/mod.rs:91-138) built in
-// parallel instead of recursively:
-//  1. bbox_*   : the square root box of BoundingBox::square_with
-//                (particular/src/tree/partition.rs:274-292), in the same f32 ops.
-//  2. make_keys: each body replays the reference's subdivision for 21 levels
-//                (centre = (min+max)/2, child bit = pos < centre, tree/mod.rs:116-124,
-//                partition.rs:332-359), giving a 63-bit key whose prefixes are exactly
-//                the reference's cells. The digit stored is 7 - orthant, so ascending
-//                keys follow the reference's LIFO visiting order (children pushed 0..7,
-//                popped 7..0, sequential.rs:489-495).
-//  3. radix sort of (key, body) pairs; bodies gathered into key order.
-//  4. equal keys collapse into one leaf unit (coincident bodies, or bodies closer
-//     than 2^-21 of the root box: deeper than the key resolves).
-//  5. Karras (2012) binary radix tree over the unique keys; a binary node is an
-//     octree cell where its common-prefix level changes. Single-child chains of the
-//     reference tree disappear: accepting a chain cell or its only child adds the
-//     same (COM, M), so the result is unchanged.
-//  6. cells are laid out in depth-first preorder with skip pointers (index after
-//     the subtree), leaves interleaved: the walk needs no stack.
-//  7. moments bottom-up in FP64 (mass, centre of mass, second moment -> traceless
-//     quadrupole): cells are bucketed by octree level and combined level by level,
-//     deepest first, one thread per cell (parallel-axis theorem). No thread ever
-//     waits on another.
-// Walk (sequential.rs:466-505): one warp per 32 key-adjacent targets shares a cursor
-// over the preorder array; each lane applies the reference's rule per node (skip
-// when d2 == 0, open an internal cell when theta^2 d2 < w^2, else accept its
-// monopole) and the warp moves to the smallest next index any lane needs. With
-// PT_BH_GROUP a cell is opened for every lane when any lane opens it (more accurate,
-// same visit count); PT_BH_QUADRUPOLE adds the quadrupole term to accepted cells.
-#include "pt_common.cuh"
-#include "pt_prims.cuh"
-#include "pt_f32x2.cuh"
-#include "pt_mlp.cuh"
-
-#include <algorithm>
-#include <climits>
-#include <new>
+// cuda::BarnesHut: the C ABI (include/particular_cuda.h) over the build
+// (pt_bh_build.cu) and the walks (pt_bh_walk.cu), the tree export, tree reuse and the
+// per-context state.
+#include "pt_bh.cuh"
 
 namespace pt {
 namespace bh {
 
-constexpr int LEVELS = 21;   // 63-bit keys
-
-struct Moments {  // FP64 cell data used while combining children
-    double m, cx, cy, cz;
-    double sxx, sxy, sxz, syy, syz, szz;  // second moment about the centre of mass
-    double count;
-    double pad;
-};
-
-// Scalar type of the bodies: float (glam Vec3) or double (glam DVec3). The build
-// replays the reference's subdivision in that type, with explicitly rounded ops.
-template <class T>
-struct Prec;
-template <>
-struct Prec<float> {
-    using V4 = float4;
-    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
-    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
-    static __device__ __forceinline__ float min(float a, float b) { return fminf(a, b); }
-    static __device__ __forceinline__ float max(float a, float b) { return fmaxf(a, b); }
-    static __device__ __forceinline__ V4 make(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
-};
-template <>
-struct Prec<double> {
-    using V4 = double4_32a;
-    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-    static __device__ __forceinline__ double min(double a, double b) { return fmin(a, b); }
-    static __device__ __forceinline__ double max(double a, double b) { return fmax(a, b); }
-    static __device__ __forceinline__ V4 make(double x, double y, double z, double w) {
-        V4 r;
-        r.x = x, r.y = y, r.z = z, r.w = w;
-        return r;
-    }
-};
-
-
-struct State {
-    PrimScratch prims;
-    DevBuf box_part, box;
-    DevBuf keys, idx, sbody;
-    DevBuf flags, uscan, ukey, ufirst;
-    DevBuf bfirst, blast, bdelta, bparent, lparent, top, oparent, loparent;
-    DevBuf cnt, pscan, pre, levels, by_level;
-    DevBuf nodeA, nodeB, nodeQ, nodeG, nodeR, mom;
-    DevBuf sbody64, nodeA64, nodeG64, tbody64;  // the f64 (DVec3) method's bodies and nodes
-    DevBuf tkeys, tidx, tbody;
-    DevBuf counters;
-    DevBuf out;
-    DevBuf aff_h, src_h;  // staging for the host-pointer entry point
-    DevBuf lrec, lgroup, lnext, lpart, lhead, lcentre, lused;  // learned-correction records
-    int lcap = 0;                     // record chunks allocated
-    int stack_cap = 0;                // group-walk stack ranges per warp in use (0 = all)
-    uint64_t generation = 0;          // trees built so far (0 = none)
-    bool f64 = false;                 // the current tree was built over DVec3 bodies
-    float local_ratio = 0.1f;         // PT_BH_LOCAL: far when group radius < ratio * distance
-    const uint32_t *mlp_w = nullptr;  // learned correction: packed BF16 weights (owned by the MLP state)
-    const float *mlp_b = nullptr;     // and its bias block
-    float theta_inner = 0.5f;
-    int cap_n = 0;
-    int last_n_src = 0;
-};
-
-// ---- 1. root box -----------------------------------------------------------
-template <class T>
-__global__ void bbox_partial(const typename Prec<T>::V4 *__restrict__ src, int n, T *__restrict__ part) {
-    using P = Prec<T>;
-    T mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const typename P::V4 p = src[i];
-        mn[0] = P::min(mn[0], p.x);
-        mn[1] = P::min(mn[1], p.y);
-        mn[2] = P::min(mn[2], p.z);
-        mx[0] = P::max(mx[0], p.x);
-        mx[1] = P::max(mx[1], p.y);
-        mx[2] = P::max(mx[2], p.z);
-    }
-    __shared__ T s[6][256];
-    for (int a = 0; a < 3; ++a) {
-        s[a][threadIdx.x] = mn[a];
-        s[3 + a][threadIdx.x] = mx[a];
-    }
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w)
-            for (int a = 0; a < 3; ++a) {
-                s[a][threadIdx.x] = P::min(s[a][threadIdx.x], s[a][threadIdx.x + w]);
-                s[3 + a][threadIdx.x] = P::max(s[3 + a][threadIdx.x], s[3 + a][threadIdx.x + w]);
-            }
-        __syncthreads();
-    }
-    if (threadIdx.x < 6) part[blockIdx.x * 6 + threadIdx.x] = s[threadIdx.x][0];
-}
-
-// box = {min x,y,z, max x,y,z} of BoundingBox::square_with: centre = midpoint of the
-// AABB, half = (max extent + 0) / 2 (MidPoint::half), min/max = centre -/+ half.
-// One block of 256 threads folds the per-block extents (min/max: exact in any
-// order), then thread 0 forms the reference's square root box.
-template <class T>
-__global__ void bbox_final(const T *__restrict__ part, int nb, T *__restrict__ box) {
-    using P = Prec<T>;
-    T mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int b = threadIdx.x; b < nb; b += blockDim.x)
-        for (int a = 0; a < 3; ++a) {
-            mn[a] = P::min(mn[a], part[b * 6 + a]);
-            mx[a] = P::max(mx[a], part[b * 6 + 3 + a]);
-        }
-    for (int o = 16; o > 0; o >>= 1)
-        for (int a = 0; a < 3; ++a) {
-            mn[a] = P::min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
-            mx[a] = P::max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
-        }
-    __shared__ T s[6][8];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0)
-        for (int a = 0; a < 3; ++a) {
-            s[a][warp] = mn[a];
-            s[3 + a][warp] = mx[a];
-        }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    for (int w = 1; w < int(blockDim.x >> 5); ++w)
-        for (int a = 0; a < 3; ++a) {
-            mn[a] = P::min(mn[a], s[a][w]);
-            mx[a] = P::max(mx[a], s[3 + a][w]);
-        }
-    T half = 0;
-    T c[3];
-    for (int a = 0; a < 3; ++a) {
-        c[a] = P::mul(P::add(mn[a], mx[a]), T(0.5));
-        half = P::max(half, P::sub(mx[a], mn[a]));
-    }
-    half = P::mul(P::add(half, T(0)), T(0.5));
-    for (int a = 0; a < 3; ++a) {
-        box[a] = P::sub(c[a], half);
-        box[3 + a] = P::add(c[a], half);
-    }
-}
-
-// ---- 2. keys ---------------------------------------------------------------
-template <class T>
-__device__ __forceinline__ uint64_t key_of(T px, T py, T pz, const T *box) {
-    using P = Prec<T>;
-    T mn0 = box[0], mn1 = box[1], mn2 = box[2], mx0 = box[3], mx1 = box[4], mx2 = box[5];
-    uint64_t key = 0;
-#pragma unroll 3
-    for (int l = 0; l < LEVELS; ++l) {
-        const T c0 = P::mul(P::add(mn0, mx0), T(0.5));
-        const T c1 = P::mul(P::add(mn1, mx1), T(0.5));
-        const T c2 = P::mul(P::add(mn2, mx2), T(0.5));
-        const int b0 = px < c0, b1 = py < c1, b2 = pz < c2;
-        if (b0) mx0 = c0; else mn0 = c0;
-        if (b1) mx1 = c1; else mn1 = c1;
-        if (b2) mx2 = c2; else mn2 = c2;
-        const int o = b0 | (b1 << 1) | (b2 << 2);
-        key = (key << 3) | uint64_t(7 - o);
-    }
-    return key;
-}
-
-template <class T>
-__global__ void make_keys(const typename Prec<T>::V4 *__restrict__ bodies, int n, const T *__restrict__ box_g,
-                          uint64_t *__restrict__ keys, uint32_t *__restrict__ idx) {
-    __shared__ T box[6];
-    if (threadIdx.x < 6) box[threadIdx.x] = box_g[threadIdx.x];
-    __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const typename Prec<T>::V4 p = bodies[i];
-    keys[i] = key_of<T>(p.x, p.y, p.z, box);
-    idx[i] = uint32_t(i);
-}
-
-template <class V4>
-__global__ void gather_bodies(const V4 *__restrict__ src, const uint32_t *__restrict__ idx, int n,
-                              V4 *__restrict__ out) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) out[k] = src[idx[k]];
-}
-
-// ---- 4. unique keys -> leaf units ------------------------------------------
-__global__ void unit_flags(const uint64_t *__restrict__ keys, int n, uint32_t *__restrict__ flags) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) flags[k] = (k == 0 || keys[k] != keys[k - 1]) ? 1u : 0u;
-}
-
-// counters[0] = M (units)
-__global__ void unit_fill(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ flags,
-                          const uint32_t *__restrict__ uscan, int n, uint64_t *__restrict__ ukey,
-                          uint32_t *__restrict__ ufirst, int *__restrict__ counters) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    if (flags[k]) {
-        const uint32_t u = uscan[k];
-        ukey[u] = keys[k];
-        ufirst[u] = uint32_t(k);
-    }
-    if (k == 0) {
-        const uint32_t M = uscan[n];
-        ufirst[M] = uint32_t(n);
-        counters[0] = int(M);
-    }
-}
-
-// ---- 5. Karras binary radix tree ---------------------------------------------
-__device__ __forceinline__ int kdelta(const uint64_t *__restrict__ k, int M, int i, int j) {
-    if (j < 0 || j >= M) return -1;
-    return __clzll(k[i] ^ k[j]) - 1;  // bit 63 is always 0: prefix length of the 63-bit keys
-}
-
-__global__ void karras(const uint64_t *__restrict__ ukey, const int *__restrict__ counters, int *__restrict__ bfirst,
-                       int *__restrict__ blast, int *__restrict__ bdelta, int *__restrict__ bparent,
-                       int *__restrict__ lparent) {
-    const int M = counters[0];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= M - 1) return;
-    const int d = (kdelta(ukey, M, i, i + 1) - kdelta(ukey, M, i, i - 1)) >= 0 ? 1 : -1;
-    const int dmin = kdelta(ukey, M, i, i - d);
-    int lmax = 2;
-    while (kdelta(ukey, M, i, i + lmax * d) > dmin) lmax <<= 1;
-    int l = 0;
-    for (int t = lmax >> 1; t >= 1; t >>= 1)
-        if (kdelta(ukey, M, i, i + (l + t) * d) > dmin) l += t;
-    const int j = i + l * d;
-    const int dnode = kdelta(ukey, M, i, j);
-    int s = 0, t = l;
-    do {
-        t = (t + 1) >> 1;
-        if (kdelta(ukey, M, i, i + (s + t) * d) > dnode) s += t;
-    } while (t > 1);
-    const int gamma = i + s * d + min(d, 0);
-    const int first = min(i, j), last = max(i, j);
-    bfirst[i] = first;
-    blast[i] = last;
-    bdelta[i] = dnode;
-    if (first == gamma) lparent[gamma] = i; else bparent[gamma] = i;
-    if (last == gamma + 1) lparent[gamma + 1] = i; else bparent[gamma + 1] = i;
-    if (i == 0) bparent[0] = -1;
-}
-
-// A binary node is an octree cell iff it is the root or its common-prefix level
-// (delta / 3) exceeds its parent's.
-__global__ void octree_top(const int *__restrict__ counters, const int *__restrict__ bdelta,
-                           const int *__restrict__ bparent, uint8_t *__restrict__ top) {
-    const int M = counters[0];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= M - 1) return;
-    top[i] = (i == 0 || bdelta[bparent[i]] / 3 < bdelta[i] / 3) ? 1 : 0;
-}
-
-__device__ __forceinline__ int climb(int p, const uint8_t *__restrict__ top, const int *__restrict__ bparent) {
-    while (!top[p]) p = bparent[p];
-    return p;
-}
-
-// Octree parents, child counts and the count of cells starting at each unit.
-__global__ void octree_links(const int *__restrict__ counters, const int *__restrict__ bfirst,
-                             const int *__restrict__ bparent, const int *__restrict__ lparent,
-                             const uint8_t *__restrict__ top, int *__restrict__ oparent, int *__restrict__ loparent,
-                             uint32_t *__restrict__ cnt) {
-    const int M = counters[0];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < M - 1 && top[k]) {
-        const int op = (k == 0) ? -1 : climb(bparent[k], top, bparent);
-        oparent[k] = op;
-        atomicAdd(&cnt[bfirst[k]], 1u);
-    }
-    if (k < M) {
-        const int op = (M == 1) ? -1 : climb(lparent[k], top, bparent);
-        loparent[k] = op;
-    }
-}
-
-// ---- 6. preorder layout ------------------------------------------------------
-// nodeB = {width bits, skip, first body (-1: internal cell), body count}.
-// counters[1] = T (cells + leaves), counters[2] = internal cells.
-template <class T>
-__global__ void layout(int *counters, const int *__restrict__ bfirst,
-                       const int *__restrict__ blast, const int *__restrict__ bdelta,
-                       const uint8_t *__restrict__ top, const int *__restrict__ oparent,
-                       const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ pscan,
-                       const uint64_t *__restrict__ ukey, const uint32_t *__restrict__ ufirst,
-                       const T *__restrict__ box, int *__restrict__ pre, int4 *__restrict__ nodeB,
-                       typename Prec<T>::V4 *__restrict__ nodeG, int2 *__restrict__ nodeR) {
-    using P = Prec<T>;
-    const int M = counters[0];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k == 0) {
-        counters[1] = M + int(pscan[M]);
-        counters[2] = int(pscan[M]);
-    }
-    if (k < M - 1 && top[k]) {
-        const int b = bfirst[k];
-        int r = 0;
-        for (int p = oparent[k]; p >= 0 && bfirst[p] == b; p = oparent[p]) ++r;
-        const int pk = b + int(pscan[b]) + r;
-        pre[k] = pk;
-        const int after = blast[k] + 1;
-        const int skip = after + int(pscan[after]);
-        // Cell box at level L along the key's path: BoundingBox::width() of the
-        // reference cell (partition.rs:322-327) and its centre, replayed in the same
-        // f32 ops.
-        const int L = bdelta[k] / 3;
-        const uint64_t key = ukey[b];
-        T mn0 = box[0], mn1 = box[1], mn2 = box[2], mx0 = box[3], mx1 = box[4], mx2 = box[5];
-        for (int l = 0; l < L; ++l) {
-            const int o = 7 - int((key >> (3 * (LEVELS - 1 - l))) & 7u);
-            const T c0 = P::mul(P::add(mn0, mx0), T(0.5));
-            const T c1 = P::mul(P::add(mn1, mx1), T(0.5));
-            const T c2 = P::mul(P::add(mn2, mx2), T(0.5));
-            if (o & 1) mx0 = c0; else mn0 = c0;
-            if (o & 2) mx1 = c1; else mn1 = c1;
-            if (o & 4) mx2 = c2; else mn2 = c2;
-        }
-        const T w = P::sub(mx0, mn0);
-        // the f32 walk reads the width from nodeB.x; the f64 walk from nodeG.w
-        nodeB[pk] = make_int4(sizeof(T) == 4 ? __float_as_int(float(w)) : 0, skip, -1, 0);
-        nodeG[pk] = P::make(T(0.5) * (mn0 + mx0), T(0.5) * (mn1 + mx1), T(0.5) * (mn2 + mx2), w);
-        nodeR[pk] = make_int2(int(ufirst[b]), int(ufirst[blast[k] + 1]));
-    }
-    if (k < M) {
-        const int pk = k + int(pscan[k]) + int(cnt[k]);
-        const int f = int(ufirst[k]);
-        nodeB[pk] = make_int4(0, pk + 1, f, int(ufirst[k + 1]) - f);
-        nodeG[pk] = P::make(T(0), T(0), T(0), T(0));
-        nodeR[pk] = make_int2(f, int(ufirst[k + 1]));
-    }
-}
-
-// ---- 7. moments ------------------------------------------------------------
-template <class T>
-__device__ void store_cell(const Moments &m, int pk, Moments *__restrict__ mom, typename Prec<T>::V4 *__restrict__ nodeA,
-                           float4 *__restrict__ nodeQ) {
-    mom[pk] = m;
-    nodeA[pk] = Prec<T>::make(T(m.cx), T(m.cy), T(m.cz), T(m.m));
-    if (!nodeQ) return;  // the f64 method is monopole only
-    const double tr = m.sxx + m.syy + m.szz;
-    nodeQ[2 * pk] = make_float4(float(3 * m.sxx - tr), float(3 * m.sxy), float(3 * m.sxz), float(3 * m.syy - tr));
-    nodeQ[2 * pk + 1] = make_float4(float(3 * m.syz), float(3 * m.szz - tr), 0.f, 0.f);
-}
-
-// Leaves: a single body is its own cell data; several (coincident, or closer than
-// the key resolution) get FP64 moments.
-template <class T>
-__global__ void leaf_moments(const int *__restrict__ counters, const uint32_t *__restrict__ ufirst,
-                             const typename Prec<T>::V4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
-                             const uint32_t *__restrict__ cnt, Moments *__restrict__ mom,
-                             typename Prec<T>::V4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
-    using V4 = typename Prec<T>::V4;
-    const int M = counters[0];
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= M) return;
-    const int f = int(ufirst[u]), e = int(ufirst[u + 1]);
-    const int pk = u + int(pscan[u]) + int(cnt[u]);
-    if (e - f == 1) {
-        nodeA[pk] = sbody[f];
-        if (nodeQ) {
-            nodeQ[2 * pk] = make_float4(0.f, 0.f, 0.f, 0.f);
-            nodeQ[2 * pk + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        return;
-    }
-    Moments m{};
-    double sx = 0, sy = 0, sz = 0;
-    for (int b = f; b < e; ++b) {
-        const V4 p = sbody[b];
-        m.m += p.w;
-        sx += double(p.w) * p.x;
-        sy += double(p.w) * p.y;
-        sz += double(p.w) * p.z;
-    }
-    m.count = e - f;
-    if (m.m != 0.0) {
-        m.cx = sx / m.m;
-        m.cy = sy / m.m;
-        m.cz = sz / m.m;
-    } else {  // massless: plain mean (gravity/impls/mod.rs:127-129)
-        for (int b = f; b < e; ++b) {
-            const V4 p = sbody[b];
-            m.cx += p.x;
-            m.cy += p.y;
-            m.cz += p.z;
-        }
-        m.cx /= m.count;
-        m.cy /= m.count;
-        m.cz /= m.count;
-    }
-    for (int b = f; b < e; ++b) {
-        const V4 p = sbody[b];
-        const double dx = p.x - m.cx, dy = p.y - m.cy, dz = p.z - m.cz;
-        m.sxx += p.w * dx * dx;
-        m.sxy += p.w * dx * dy;
-        m.sxz += p.w * dx * dz;
-        m.syy += p.w * dy * dy;
-        m.syz += p.w * dy * dz;
-        m.szz += p.w * dz * dz;
-    }
-    store_cell<T>(m, pk, mom, nodeA, nodeQ);
-}
-
-// Cells per octree level: lcount[L], then by_level sorted by level (counting sort).
-// levels[0..LEVELS] = counts, levels[LEVELS+1 ..] = offsets, then cursors.
-__global__ void cell_level_count(const int *__restrict__ counters, const int *__restrict__ bdelta,
-                                 const uint8_t *__restrict__ top, int *__restrict__ levels) {
-    __shared__ int h[LEVELS];
-    if (threadIdx.x < LEVELS) h[threadIdx.x] = 0;
-    __syncthreads();
-    const int M = counters[0];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < M - 1 && top[k]) atomicAdd(&h[bdelta[k] / 3], 1);
-    __syncthreads();
-    if (threadIdx.x < LEVELS && h[threadIdx.x]) atomicAdd(&levels[threadIdx.x], h[threadIdx.x]);
-}
-
-__global__ void cell_level_offsets(int *__restrict__ levels) {
-    if (threadIdx.x != 0) return;
-    int acc = 0;
-    for (int L = 0; L < LEVELS; ++L) {
-        levels[LEVELS + 1 + L] = acc;      // offset
-        levels[2 * LEVELS + 2 + L] = acc;  // cursor
-        acc += levels[L];
-    }
-    levels[2 * LEVELS + 1] = acc;
-}
-
-// Each block reserves one range per level with a single global atomic.
-__global__ void cell_level_scatter(const int *__restrict__ counters, const int *__restrict__ bdelta,
-                                   const uint8_t *__restrict__ top, int *__restrict__ levels,
-                                   int *__restrict__ by_level) {
-    __shared__ int h[LEVELS], base[LEVELS];
-    if (threadIdx.x < LEVELS) h[threadIdx.x] = 0;
-    __syncthreads();
-    const int M = counters[0];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool cell = k < M - 1 && top[k];
-    const int L = cell ? bdelta[k] / 3 : 0;
-    const int local = cell ? atomicAdd(&h[L], 1) : 0;
-    __syncthreads();
-    if (threadIdx.x < LEVELS && h[threadIdx.x])
-        base[threadIdx.x] = atomicAdd(&levels[2 * LEVELS + 2 + threadIdx.x], h[threadIdx.x]);
-    __syncthreads();
-    if (cell) by_level[base[L] + local] = k;
-}
-
-// Combines every cell of octree level L from its children (levels > L: done), in one
-// pass over the children: sums about the cell's geometric centre G (offsets within
-// a cell width, no cancellation), then moved to the centre of mass C by the
-// parallel-axis rule S_C = S_G - P P^T / M with P = sum m (c - G) = M (C - G).
-template <class T>
-__global__ void cell_moments_level(int L, const int *__restrict__ levels, const int *__restrict__ by_level,
-                                   const int *__restrict__ pre, const int4 *__restrict__ nodeB,
-                                   const typename Prec<T>::V4 *__restrict__ nodeG, Moments *__restrict__ mom,
-                                   typename Prec<T>::V4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
-    using V4 = typename Prec<T>::V4;
-    const int begin = levels[LEVELS + 1 + L], end_l = begin + levels[L];
-    for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end_l; i += gridDim.x * blockDim.x) {
-        const int pv = pre[by_level[i]];
-        const int end = nodeB[pv].y;
-        const V4 g = nodeG[pv];
-        const double gx = g.x, gy = g.y, gz = g.z;
-        Moments m{};
-        double px = 0, py = 0, pz = 0;
-        for (int c = pv + 1; c < end;) {
-            const int4 cb = nodeB[c];
-            double cx, cy, cz, cmm, cn, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
-            if (cb.z >= 0 && cb.w == 1) {  // a single body, read from nodeA
-                const V4 a = nodeA[c];
-                cx = a.x, cy = a.y, cz = a.z, cmm = a.w, cn = 1.0;
-            } else {
-                const Moments &cm = mom[c];
-                cx = cm.cx, cy = cm.cy, cz = cm.cz, cmm = cm.m, cn = cm.count;
-                sxx = cm.sxx, sxy = cm.sxy, sxz = cm.sxz, syy = cm.syy, syz = cm.syz, szz = cm.szz;
-            }
-            const double dx = cx - gx, dy = cy - gy, dz = cz - gz;
-            m.m += cmm;
-            m.count += cn;
-            const double mx = cmm * dx, my = cmm * dy, mz = cmm * dz;
-            px += mx;
-            py += my;
-            pz += mz;
-            m.sxx += sxx + mx * dx;
-            m.sxy += sxy + mx * dy;
-            m.sxz += sxz + mx * dz;
-            m.syy += syy + my * dy;
-            m.syz += syz + my * dz;
-            m.szz += szz + mz * dz;
-            c = cb.y;
-        }
-        if (m.m != 0.0) {
-            const double inv = 1.0 / m.m;
-            const double ox = px * inv, oy = py * inv, oz = pz * inv;  // C - G
-            m.cx = gx + ox;
-            m.cy = gy + oy;
-            m.cz = gz + oz;
-            m.sxx -= px * ox;
-            m.sxy -= px * oy;
-            m.sxz -= px * oz;
-            m.syy -= py * oy;
-            m.syz -= py * oz;
-            m.szz -= pz * oz;
-        } else {  // massless: plain mean of the bodies (gravity/impls/mod.rs:127-129), a rare second pass
-            double ux = 0, uy = 0, uz = 0;
-            for (int c = pv + 1; c < end;) {
-                const int4 cb = nodeB[c];
-                double cx, cy, cz, cn;
-                if (cb.z >= 0 && cb.w == 1) {
-                    const V4 a = nodeA[c];
-                    cx = a.x, cy = a.y, cz = a.z, cn = 1.0;
-                } else {
-                    cx = mom[c].cx, cy = mom[c].cy, cz = mom[c].cz, cn = mom[c].count;
-                }
-                ux += cn * (cx - gx);
-                uy += cn * (cy - gy);
-                uz += cn * (cz - gz);
-                c = cb.y;
-            }
-            m.cx = gx + ux / m.count;
-            m.cy = gy + uy / m.count;
-            m.cz = gz + uz / m.count;
-        }
-        store_cell<T>(m, pv, mom, nodeA, nodeQ);
-    }
-}
-
-// ---- walk ------------------------------------------------------------------
-
-// The reference's per-body walk (sequential.rs) for this lane's target p, the cursor
-// being the warp minimum of the lanes' next nodes: all 32 lanes take part. Adds the
-// accepted nodes' accelerations to (ax, ay, az) and counts them.
-template <bool QUAD>
-__device__ __forceinline__ void lane_walk(float4 p, bool valid, int T, const float4 *__restrict__ nodeA,
-                                          const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
-                                          const float4 *__restrict__ sbody, float th2, float eps2, float &ax,
-                                          float &ay, float &az, unsigned &nacc, unsigned &nvisit,
-                                          unsigned &ncell) {
-    int resume = valid ? 0 : T;
-    int node = 0;
-    while (node < T) {
-        const float4 A = __ldg(nodeA + node);
-        const int4 B = __ldg(nodeB + node);
-        const bool active = node >= resume;
-        float dx = 0.f, dy = 0.f, dz = 0.f, d2 = 0.f;
-        bool open = false, zero = false;
-        if (active) {
-            dx = A.x - p.x;
-            dy = A.y - p.y;
-            dz = A.z - p.z;
-            d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            zero = (d2 == 0.0f);
-            const float w = __int_as_float(B.x);
-            open = !zero && B.z < 0 && th2 * d2 < w * w;
-        }
-        int next = resume;
-        if (active) {
-            ++nvisit;
-            if (zero) {
-                next = resume = B.y;  // the whole node is skipped (sequential.rs:485-487)
-            } else if (open) {
-                next = node + 1;
-            } else {
-                if (B.z >= 0 && B.w > 1) {  // a bucket leaf: its bodies one by one
-                    for (int b = B.z; b < B.z + B.w; ++b) {
-                        const float4 q = __ldg(sbody + b);
-                        const float ex = q.x - p.x, ey = q.y - p.y, ez = q.z - p.z;
-                        const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-                        if (e2 == 0.0f) continue;
-                        const float inv = rsqrt_ftz(e2 + eps2);
-                        const float s = (q.w * inv) * (inv * inv);
-                        ax = fmaf(ex, s, ax);
-                        ay = fmaf(ey, s, ay);
-                        az = fmaf(ez, s, az);
-                    }
-                } else {
-                    const float inv = rsqrt_ftz(d2 + eps2);
-                    const float inv2 = inv * inv;
-                    const float s = (A.w * inv) * inv2;
-                    ax = fmaf(dx, s, ax);
-                    ay = fmaf(dy, s, ay);
-                    az = fmaf(dz, s, az);
-                    if (QUAD && B.z < 0) {  // traceless quadrupole of the cell
-                        const float4 q0 = __ldg(nodeQ + 2 * node);
-                        const float4 q1 = __ldg(nodeQ + 2 * node + 1);
-                        // q0 = (Qxx, Qxy, Qxz, Qyy), q1 = (Qyz, Qzz)
-                        const float qx = fmaf(q0.x, dx, fmaf(q0.y, dy, q0.z * dz));
-                        const float qy = fmaf(q0.y, dx, fmaf(q0.w, dy, q1.x * dz));
-                        const float qz = fmaf(q0.z, dx, fmaf(q1.x, dy, q1.y * dz));
-                        const float dqd = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
-                        const float inv5 = inv2 * inv2 * inv;
-                        const float c7 = 2.5f * dqd * inv5 * inv2;
-                        ax += fmaf(c7, dx, -qx * inv5);
-                        ay += fmaf(c7, dy, -qy * inv5);
-                        az += fmaf(c7, dz, -qz * inv5);
-                    }
-                }
-                ++nacc;
-                ncell += B.z < 0;
-                next = resume = B.y;
-            }
-        }
-        node = __reduce_min_sync(0xffffffffu, next);
-    }
-}
-
-// ---- group walk (PT_BH_GROUP) ----------------------------------------------
-// One warp walks for 32 key-adjacent targets. Each step pops up to 32 nodes from a
-// shared-memory stack of sibling ranges (independent loads, one per lane), opens a
-// cell when the reference's per-body rule opens it for at least one of the 32
-// targets (so never less accurate than that rule), and appends accepted nodes to a
-// shared-memory interaction list. A full list is evaluated densely: every lane runs its target
-// against all entries, two entries per packed f32x2 instruction.
-constexpr int GW_WARPS = 4;
-// Sibling ranges per warp. A pop takes fewer nodes when the stack is nearly full, and
-// a warp that still runs out takes the per-body walk (counted, not an error). At
-// N = 4M bulge+disk the deepest stack seen is 239 ranges at theta 0.5 and 379 at 0.3.
-// 384 ranges keep a CTA at 36 KB of shared memory (5-6 CTAs per SM).
-#ifndef PT_GW_STACK
-#define PT_GW_STACK 384
-#endif
-constexpr int GW_STACK = PT_GW_STACK;
-
-// Interaction lists in structure-of-arrays form. Cells carry their quadrupole
-// when QUAD; single bodies never need one.
-template <int NF, int CAP_>
-struct IList {
-    static constexpr int CAP = CAP_;
-    float f[NF][CAP + 2];
-};
-
-// Two list entries (packed lo/hi: monopole x, y, z, m and, for NF = 10, the negated
-// traceless quadrupole N = -Q as Nxx Nxy Nxz Nyy Nyz Nzz) for one target. With
-// u = N d and c = d.u:
-//   a += d (m / r^3 + 2.5 (d.Q.d) / r^7) - (Q d) / r^5 = d (sc - 2.5 c / r^7) + u / r^5
-template <int NF, bool GUARD>
-__device__ __forceinline__ void eval_pair(const f2 (&q)[NF], f2 px, f2 py, f2 pz, f2 e2, f2 &ax, f2 &ay, f2 &az) {
-    const f2 dx = sub2(q[0], px);
-    const f2 dy = sub2(q[1], py);
-    const f2 dz = sub2(q[2], pz);
-    const f2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-    float r0, r1;
-    upk2(r2, r0, r1);
-    float i0 = rsqrt_ftz(r0), i1 = rsqrt_ftz(r1);
-    if (GUARD) {
-        i0 = (r0 > 0.0f) ? i0 : 0.0f;
-        i1 = (r1 > 0.0f) ? i1 : 0.0f;
-    }
-    const f2 inv = pk2(i0, i1);
-    const f2 inv2 = mul2(inv, inv);
-    const f2 sc = mul2(mul2(q[3], inv), inv2);
-    if constexpr (NF == 10) {
-        const f2 ux = fma2(q[4], dx, fma2(q[5], dy, mul2(q[6], dz)));
-        const f2 uy = fma2(q[5], dx, fma2(q[7], dy, mul2(q[8], dz)));
-        const f2 uz = fma2(q[6], dx, fma2(q[8], dy, mul2(q[9], dz)));
-        const f2 c = fma2(dx, ux, fma2(dy, uy, mul2(dz, uz)));
-        const f2 inv5 = mul2(mul2(inv2, inv2), inv);
-        const f2 k = mul2(c, mul2(inv2, pk2(-2.5f, -2.5f)));
-        const f2 s2 = fma2(inv5, k, sc);
-        ax = fma2(dx, s2, fma2(inv5, ux, ax));
-        ay = fma2(dy, s2, fma2(inv5, uy, ay));
-        az = fma2(dz, s2, fma2(inv5, uz, az));
-    } else {
-        ax = fma2(dx, sc, ax);
-        ay = fma2(dy, sc, ay);
-        az = fma2(dz, sc, az);
-    }
-}
-
-// Evaluates entries [0, cnt) of a list for this lane's TPL targets, two entries per
-// packed instruction; each pair of entries is read from shared memory once for all
-// of the lane's targets.
-template <int NF, int CAP, bool GUARD, int TPL>
-__device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, const f2 (&px)[TPL], const f2 (&py)[TPL],
-                                          const f2 (&pz)[TPL], f2 e2, f2 (&ax)[TPL], f2 (&ay)[TPL],
-                                          f2 (&az)[TPL]) {
-    const int lane = threadIdx.x & 31;
-    __syncwarp();
-    if (cnt & 1) {  // pad with a massless entry far away: contributes exactly 0
-        if (lane < NF) Lst.f[lane][cnt] = (lane < 3) ? 1e30f : 0.0f;
-        __syncwarp();
-        ++cnt;
-    }
-#pragma unroll 2
-    for (int e = 0; e < cnt; e += 2) {
-        f2 q[NF];
-#pragma unroll
-        for (int k = 0; k < NF; ++k) q[k] = *reinterpret_cast<const f2 *>(&Lst.f[k][e]);
-#pragma unroll
-        for (int i = 0; i < TPL; ++i) eval_pair<NF, GUARD>(q, px[i], py[i], pz[i], e2, ax[i], ay[i], az[i]);
-    }
-    __syncwarp();
-}
-
-// ---- learned correction: records of marginal cells ---------------------------
-// The walk (PT_BH_LEARNED) does not evaluate the network itself: it records the
-// node index of every marginal cell (accepted at theta, opened at theta_inner) in
-// chunks of LCHUNK entries that each belong to one warp (one group of 32 targets),
-// chained per group in walk order, and the group's centre. A tensor-core kernel then
-// evaluates all records (bh_learned_eval) and bh_learned_apply adds each group's
-// sum, chunk by chunk in chain order, so results do not depend on scheduling.
-constexpr int LCHUNK = 128;
-
-struct LearnedRecords {
-    int *rec;        // [cap][LCHUNK] node indices, -1 = padding
-    int *chunk_group;  // [cap]
-    int *next;       // [cap] next chunk of the same group, -1 = last
-    int *head;       // [groups] first chunk of the group, -1 = none
-    float4 *centre;  // [groups] mean position of the group's targets
-    float4 *part;    // [cap] the chunk's summed correction
-    int *used;       // chunks handed out (may exceed cap: then nothing past cap is written)
-    int cap;
-};
-
-// One warp per chunk (grid-stride): features of the 128 recorded cells at the group
-// centre, four 32-row tensor-core batches, the chunk's sum into part[chunk].
-// Cells whose size/distance ratio at the group centre lies outside the range the
-// model was trained on ([lo, hi]) get no correction.
-__global__ void __launch_bounds__(128) bh_learned_eval(LearnedRecords L, const float4 *__restrict__ nodeA,
-                                                      const float4 *__restrict__ nodeQ,
-                                                      const float4 *__restrict__ nodeG,
-                                                      const uint32_t *__restrict__ W, const float *__restrict__ bias,
-                                                      float lo, float hi) {
-    __shared__ float X[4][32 * mlp::TC_XS];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = lane >> 2, t = lane & 3;
-    const int used = min(*L.used, L.cap);
-    const float sc = __ldg(bias + mlp::TC_SCALE);
-    float *Xw = X[warp];
-    for (int c = blockIdx.x * 4 + warp; c < used; c += gridDim.x * 4) {
-        const float4 gc = L.centre[L.chunk_group[c]];
-        float rx = 0.f, ry = 0.f, rz = 0.f;
-        for (int b = 0; b < LCHUNK / 32; ++b) {
-            const int node = L.rec[size_t(c) * LCHUNK + b * 32 + lane];
-            if (__ballot_sync(0xffffffffu, node >= 0) == 0u) break;  // padding fills the chunk's tail
-            float f[mlp::IN];
-            float a = 0.f;  // M / |r|^2 of this row's cell, 0 = no correction
-            if (node >= 0) {
-                const float4 A = __ldg(nodeA + node);
-                const float4 q0 = __ldg(nodeQ + 2 * node), q1 = __ldg(nodeQ + 2 * node + 1);
-                const float q[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
-                const float r2 = mlp::features(gc.x, gc.y, gc.z, A, q, __ldg(nodeG + node), f);
-                if (f[3] >= lo && f[3] <= hi) a = A.w / r2;
-            }
-#pragma unroll
-            for (int i = 0; i < 16; ++i) Xw[lane * mlp::TC_XS + i] = (i < mlp::IN && a != 0.f) ? f[i] : 0.f;
-            __syncwarp();
-            float y[2][4];
-            mlp::tc_batch(Xw, W, bias, y);
-            __syncwarp();
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const float s = __shfl_sync(0xffffffffu, a, 16 * mt + 8 * h + g);
-                    if (t == 0) {
-                        rx = fmaf(y[mt][2 * h], s, rx);
-                        ry = fmaf(y[mt][2 * h + 1], s, ry);
-                    } else if (t == 1) {
-                        rz = fmaf(y[mt][2 * h], s, rz);
-                    }
-                }
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            rx += __shfl_xor_sync(0xffffffffu, rx, off);
-            ry += __shfl_xor_sync(0xffffffffu, ry, off);
-            rz += __shfl_xor_sync(0xffffffffu, rz, off);
-        }
-        if (lane == 0) L.part[c] = make_float4(rx * sc, ry * sc, rz * sc, 0.f);
-    }
-}
-
-// out[target] += the sum of its group's chunk corrections, in chain order.
-__global__ void bh_learned_apply(LearnedRecords L, const uint32_t *__restrict__ tidx, int n_aff, int group_shift,
-                                 float *__restrict__ out) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_aff) return;
-    float cx = 0.f, cy = 0.f, cz = 0.f;
-    // chunk indices grow along a chain (each is taken after its predecessor)
-    for (int c = L.head[t >> group_shift], prev = -1; c > prev && c < L.cap; prev = c, c = L.next[c]) {
-        const float4 v = L.part[c];
-        cx += v.x;
-        cy += v.y;
-        cz += v.z;
-    }
-    const uint32_t o = tidx[t];
-    out[3 * size_t(o) + 0] += cx;
-    out[3 * size_t(o) + 1] += cy;
-    out[3 * size_t(o) + 2] += cz;
-}
-
-// ---- local (Taylor) expansion of far nodes about the group centre -------------
-// PT_BH_LOCAL: an accepted node far from the group (group radius R < ratio * d, d
-// from the group's box centre g to the node's centre of mass) is not added to the
-// interaction lists. The lane that popped it adds the node's softened monopole (+
-// quadrupole) field to a second-order expansion of the acceleration about g:
-// a(g + r) = a0 + T r + 1/2 H : r r, with
-//   a0 = m d s^-3/2,  T_ij = 3m d_i d_j s^-5/2 - m delta_ij s^-3/2,
-//   H_ijk = 15m d_i d_j d_k s^-7/2 - 3m s^-5/2 (delta_ij d_k + delta_ik d_j + delta_jk d_i)
-// (s = |d|^2 + eps^2: the exact derivatives of the softened kernel), plus the
-// quadrupole's a0 and T. The expansion costs one lane ~150 flops per far node
-// instead of every target's list entry; its truncation error is ~(R/d)^3.
-struct LocalExp {
-    float ax, ay, az;                                      // a(g)
-    float txx, txy, txz, tyy, tyz, tzz;                    // d a_i / d x_j
-    float hxxx, hxxy, hxxz, hxyy, hxyz, hxzz, hyyy, hyyz, hyzz, hzzz;  // d2 a_i / dx_j dx_k
-};
-
-// Adds the softened monopole (+ traceless quadrupole q, when given) field of a node
-// at offset d = com - g, mass m, to the expansion about g.
-__device__ __forceinline__ void local_add(LocalExp &L, float dx, float dy, float dz, float m, float eps2,
-                                          const float4 *q0p, const float4 *q1p) {
-    const float s = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-    const float inv = rsqrt_ftz(s);
-    const float inv2 = inv * inv;
-    const float i3 = m * inv * inv2;      // m s^-3/2
-    const float i5 = 3.0f * i3 * inv2;    // 3 m s^-5/2
-    const float i7 = 5.0f * i5 * inv2;    // 15 m s^-7/2
-    L.ax = fmaf(i3, dx, L.ax);
-    L.ay = fmaf(i3, dy, L.ay);
-    L.az = fmaf(i3, dz, L.az);
-    const float xx = dx * dx, yy = dy * dy, zz = dz * dz, xy = dx * dy, xz = dx * dz, yz = dy * dz;
-    L.txx += fmaf(i5, xx, -i3);
-    L.txy = fmaf(i5, xy, L.txy);
-    L.txz = fmaf(i5, xz, L.txz);
-    L.tyy += fmaf(i5, yy, -i3);
-    L.tyz = fmaf(i5, yz, L.tyz);
-    L.tzz += fmaf(i5, zz, -i3);
-    const float ax7 = i7 * dx, ay7 = i7 * dy, az7 = i7 * dz;
-    L.hxxx += fmaf(ax7, xx, -3.0f * i5 * dx);
-    L.hxxy += fmaf(ax7, xy, -i5 * dy);
-    L.hxxz += fmaf(ax7, xz, -i5 * dz);
-    L.hxyy += fmaf(ax7, yy, -i5 * dx);
-    L.hxyz = fmaf(ax7, yz, L.hxyz);
-    L.hxzz += fmaf(ax7, zz, -i5 * dx);
-    L.hyyy += fmaf(ay7, yy, -3.0f * i5 * dy);
-    L.hyyz += fmaf(ay7, yz, -i5 * dz);
-    L.hyzz += fmaf(ay7, zz, -i5 * dy);
-    L.hzzz += fmaf(az7, zz, -3.0f * i5 * dz);
-    if (q0p) {
-        const float4 q0 = __ldg(q0p), q1 = __ldg(q1p);  // Qxx Qxy Qxz Qyy | Qyz Qzz
-        const float ux = fmaf(q0.x, dx, fmaf(q0.y, dy, q0.z * dz));
-        const float uy = fmaf(q0.y, dx, fmaf(q0.w, dy, q1.x * dz));
-        const float uz = fmaf(q0.z, dx, fmaf(q1.x, dy, q1.y * dz));
-        const float c = fmaf(dx, ux, fmaf(dy, uy, dz * uz));
-        const float j5 = inv2 * inv2 * inv, j7 = j5 * inv2, j9 = j7 * inv2;
-        const float c7 = 2.5f * c * j7;
-        L.ax += fmaf(c7, dx, -ux * j5);
-        L.ay += fmaf(c7, dy, -uy * j5);
-        L.az += fmaf(c7, dz, -uz * j5);
-        const float f5 = 5.0f * j7, g9 = 17.5f * c * j9;
-        L.txx += fmaf(q0.x, j5, fmaf(g9, xx, -fmaf(2.0f * f5, ux * dx, c7)));
-        L.tyy += fmaf(q0.w, j5, fmaf(g9, yy, -fmaf(2.0f * f5, uy * dy, c7)));
-        L.tzz += fmaf(q1.y, j5, fmaf(g9, zz, -fmaf(2.0f * f5, uz * dz, c7)));
-        L.txy += fmaf(q0.y, j5, fmaf(g9, xy, -f5 * fmaf(ux, dy, uy * dx)));
-        L.txz += fmaf(q0.z, j5, fmaf(g9, xz, -f5 * fmaf(ux, dz, uz * dx)));
-        L.tyz += fmaf(q1.x, j5, fmaf(g9, yz, -f5 * fmaf(uy, dz, uz * dy)));
-    }
-}
-
-__device__ __forceinline__ void local_reduce(LocalExp &L) {
-    float *f = &L.ax;
-#pragma unroll
-    for (int k = 0; k < 19; ++k)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) f[k] += __shfl_xor_sync(0xffffffffu, f[k], o);
-}
-
-// a(g + d) from the expansion
-__device__ __forceinline__ void local_eval(const LocalExp &L, float dx, float dy, float dz, float &ax, float &ay,
-                                           float &az) {
-    const float xx = dx * dx, yy = dy * dy, zz = dz * dz, xy2 = 2.0f * dx * dy, xz2 = 2.0f * dx * dz,
-                yz2 = 2.0f * dy * dz;
-    ax = L.ax + fmaf(L.txx, dx, fmaf(L.txy, dy, L.txz * dz)) +
-         0.5f * fmaf(L.hxxx, xx, fmaf(L.hxyy, yy, fmaf(L.hxzz, zz, fmaf(L.hxxy, xy2, fmaf(L.hxxz, xz2, L.hxyz * yz2)))));
-    ay = L.ay + fmaf(L.txy, dx, fmaf(L.tyy, dy, L.tyz * dz)) +
-         0.5f * fmaf(L.hxxy, xx, fmaf(L.hyyy, yy, fmaf(L.hyzz, zz, fmaf(L.hxyy, xy2, fmaf(L.hxyz, xz2, L.hyyz * yz2)))));
-    az = L.az + fmaf(L.txz, dx, fmaf(L.tyz, dy, L.tzz * dz)) +
-         0.5f * fmaf(L.hxxz, xx, fmaf(L.hyyz, yy, fmaf(L.hzzz, zz, fmaf(L.hxyz, xy2, fmaf(L.hxzz, xz2, L.hyzz * yz2)))));
-}
-
-// Targets per lane of the group walk: a warp walks for 32 * GW_TPL key-adjacent
-// targets, and each list entry read from shared memory serves all of a lane's
-// targets. Measured at N = 4M bulge+disk, theta 0.5, quadrupole: 1 -> 18.3 ms
-// (p95 8.2e-4), 2 -> 16.6 ms (7.7e-4), 4 -> 17.7 ms (7.5e-4); the larger box opens
-// more cells (13.5e9 -> 15.2e9 -> 17.6e9 pairs) but traversal is shared by more
-// targets.
-#ifndef PT_GW_TPL
-#define PT_GW_TPL 2
-#endif
-constexpr int GW_TPL = PT_GW_TPL;
-constexpr int GW_GROUP = 32 * GW_TPL;
-constexpr int GW_SHIFT = GW_TPL == 1 ? 5 : GW_TPL == 2 ? 6 : 7;
-static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
-#ifndef PT_GW_MINB
-#define PT_GW_MINB (GW_TPL == 1 ? 6 : 5)  // CTAs per SM the register budget is set for
-#endif
-template <bool QUAD, bool GUARD, bool LEARNED, bool LOCAL>
-__global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
-    bh_walk_group(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
-                  const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
-                  const float4 *__restrict__ nodeG, const float4 *__restrict__ sbody, const int *__restrict__ counters,
-                  float th2, float th_in2, LearnedRecords LR, float eps2, float *__restrict__ out,
-                  unsigned long long *__restrict__ stats, int *__restrict__ err, int stack_cap,
-                  float local_ratio) {
-    static_assert(!(LEARNED && LOCAL), "PT_BH_LEARNED and PT_BH_LOCAL are exclusive");
-    constexpr int NFC = QUAD ? 10 : 4;
-    constexpr int TPL = GW_TPL;
-    using CellList = IList<NFC, 96>;
-    using BodyList = IList<4, 128>;
-    // PT_BH_LOCAL keeps its 19 expansion coefficients per lane in shared memory
-    // ([coefficient][lane]: no bank conflicts) and trims the stack to 320 ranges, so
-    // that 5 CTAs stay resident at 96 registers and 44 KB.
-    constexpr int STK = LOCAL ? 320 : GW_STACK;
-    stack_cap = min(stack_cap, STK);
-    __shared__ int2 s_stack[GW_WARPS][STK];
-    __shared__ __align__(16) CellList s_cells[GW_WARPS];
-    __shared__ __align__(16) BodyList s_bodies[GW_WARPS];
-    __shared__ float s_lx[GW_WARPS][LOCAL ? 19 : 1][32];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int group = blockIdx.x * GW_WARPS + warp;
-    const int g0 = group * GW_GROUP;
-    if (g0 >= n_aff) return;
-    // this lane's targets: g0 + lane, g0 + 32 + lane, ...
-    float4 p[TPL];
-    bool valid[TPL];
-#pragma unroll
-    for (int i = 0; i < TPL; ++i) {
-        const int t = g0 + 32 * i + lane;
-        valid[i] = t < n_aff;
-        p[i] = tbody[valid[i] ? t : g0];
-    }
-    const int nvalid = min(GW_GROUP, n_aff - g0);
-    const unsigned lt = (1u << lane) - 1u;
-    int2 *stack = s_stack[warp];
-    const int T = counters[1];
-    CellList &Lc = s_cells[warp];
-    BodyList &Lb = s_bodies[warp];
-
-    // the bounding box of the group's targets: it settles most opening decisions
-    // without the per-target vote
-    float mn0 = p[0].x, mn1 = p[0].y, mn2 = p[0].z, mx0 = p[0].x, mx1 = p[0].y, mx2 = p[0].z;
-#pragma unroll
-    for (int i = 1; i < TPL; ++i) {
-        mn0 = fminf(mn0, p[i].x), mn1 = fminf(mn1, p[i].y), mn2 = fminf(mn2, p[i].z);
-        mx0 = fmaxf(mx0, p[i].x), mx1 = fmaxf(mx1, p[i].y), mx2 = fmaxf(mx2, p[i].z);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mn0 = fminf(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
-        mn1 = fminf(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
-        mn2 = fminf(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
-        mx0 = fmaxf(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
-        mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
-        mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
-    }
-    // the group centre, where learned corrections are evaluated
-    float gcx = 0.f, gcy = 0.f, gcz = 0.f;
-    if (LEARNED) {
-#pragma unroll
-        for (int i = 0; i < TPL; ++i)
-            if (valid[i]) gcx += p[i].x, gcy += p[i].y, gcz += p[i].z;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            gcx += __shfl_xor_sync(0xffffffffu, gcx, o);
-            gcy += __shfl_xor_sync(0xffffffffu, gcy, o);
-            gcz += __shfl_xor_sync(0xffffffffu, gcz, o);
-        }
-        const float nv = float(nvalid);
-        gcx /= nv;
-        gcy /= nv;
-        gcz /= nv;
-    }
-    // PT_BH_LOCAL: the expansion centre g (box centre) and the far radius^2
-    const float lgx = 0.5f * (mn0 + mx0), lgy = 0.5f * (mn1 + mx1), lgz = 0.5f * (mn2 + mx2);
-    const float rg2 = 0.25f * fmaf(mx0 - mn0, mx0 - mn0, fmaf(mx1 - mn1, mx1 - mn1, (mx2 - mn2) * (mx2 - mn2)));
-    const float far2 = LOCAL ? rg2 / (local_ratio * local_ratio) : 0.f;
-    if (LOCAL)
-        for (int k = 0; k < 19; ++k) s_lx[warp][k][lane] = 0.f;
-    unsigned long long nlocal = 0;
-    // learned: the warp's current record chunk and its fill; the previous chunk links to
-    // the next one (head of the group's chain first)
-    int chunk = -1, fill = LCHUNK;
-    unsigned long long learned = 0;
-
-    const f2 e2 = pk2(eps2, eps2);
-    // the lane's two targets packed, for the opening vote
-    const f2 vx01 = pk2(p[0].x, p[TPL - 1].x), vy01 = pk2(p[0].y, p[TPL - 1].y), vz01 = pk2(p[0].z, p[TPL - 1].z);
-    f2 px[TPL], py[TPL], pz[TPL], ax[TPL], ay[TPL], az[TPL];
-#pragma unroll
-    for (int i = 0; i < TPL; ++i) {
-        px[i] = pk2(p[i].x, p[i].x);
-        py[i] = pk2(p[i].y, p[i].y);
-        pz[i] = pk2(p[i].z, p[i].z);
-        ax[i] = ay[i] = az[i] = pk2(0.f, 0.f);
-    }
-    // Stack entries are sibling ranges (first, end): `first` is the next node to
-    // visit, its later siblings follow by skip pointers up to `end`. A pop visits one
-    // node and pushes back at most two ranges: its remaining siblings and, for an
-    // opened cell, its children (pre+1, skip). The stack therefore stays within about
-    // 32 ranges per tree level.
-    if (lane == 0) stack[0] = make_int2(0, T);
-    __syncwarp();
-    int S = 1, Nc = 0, Nb = 0, maxS = 1;
-    unsigned long long entries = 0, visits = 0, centries = 0;
-    bool failed = false;
-    while (S > 0) {
-        // each pop pushes at most two ranges: never more than the room left
-        const int k = min(min(32, S), max(1, (stack_cap - S) / 2));
-        const bool have = lane < k;
-        const int2 range = have ? stack[S - 1 - lane] : make_int2(0, 0);
-        __syncwarp();
-        S -= k;
-        visits += k;
-        const int node = range.x;
-        float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
-        int4 B = make_int4(0, 0, 0, 0);
-        bool open = false;
-        if (have) {
-            A = __ldg(nodeA + node);
-            B = __ldg(nodeB + node);
-        }
-        // Open iff the per-body rule opens for at least one target: some target with
-        // nonzero d^2 (targets with d^2 == 0 skip the cell under that rule and do not
-        // vote) and theta^2 d^2 < w^2. Settled without a vote: cells accepted even from
-        // the nearest point of the targets' box (maybe false) and cells opened even
-        // from its farthest corner (sure). Rounding is monotone, so these box bounds
-        // never contradict the per-target values. The remaining cells are voted on one
-        // at a time: each lane tests its own target, a ballot collects the votes.
-        bool maybe = false, sure = false;
-        float w = 0.f;
-        if (have && B.z < 0) {
-            w = __int_as_float(B.x);
-            const float e0 = fmaxf(fmaxf(mn0 - A.x, A.x - mx0), 0.f);
-            const float e1 = fmaxf(fmaxf(mn1 - A.y, A.y - mx1), 0.f);
-            const float e2b = fmaxf(fmaxf(mn2 - A.z, A.z - mx2), 0.f);
-            maybe = (LEARNED ? th_in2 : th2) * fmaf(e0, e0, fmaf(e1, e1, e2b * e2b)) < w * w;
-            const float f0 = fmaxf(A.x - mn0, mx0 - A.x);
-            const float f1 = fmaxf(A.y - mn1, mx1 - A.y);
-            const float f2b = fmaxf(A.z - mn2, mx2 - A.z);
-            const float dmax2 = fmaf(f0, f0, fmaf(f1, f1, f2b * f2b));
-            sure = dmax2 > 0.0f && th2 * dmax2 < w * w;  // dmax2 > 0: some target is off the centre of mass
-        }
-        open = sure;
-        bool marginal = false;
-        unsigned amb = __ballot_sync(0xffffffffu, maybe && !sure);
-        while (amb) {
-            const int j = __ffs(amb) - 1;
-            amb &= amb - 1;
-            const float cx = __shfl_sync(0xffffffffu, A.x, j);
-            const float cy = __shfl_sync(0xffffffffu, A.y, j);
-            const float cz = __shfl_sync(0xffffffffu, A.z, j);
-            const float cw = __shfl_sync(0xffffffffu, w, j);
-            bool o1 = false, i1 = false;
-            const float cw2 = cw * cw;
-            if constexpr (TPL == 2) {  // both targets in one packed pass (same IEEE ops)
-                const f2 dx = sub2(pk2(cx, cx), vx01), dy = sub2(pk2(cy, cy), vy01), dz = sub2(pk2(cz, cz), vz01);
-                float d0, d1;
-                upk2(fma2(dx, dx, fma2(dy, dy, mul2(dz, dz))), d0, d1);
-                o1 = (d0 > 0.0f && th2 * d0 < cw2) || (d1 > 0.0f && th2 * d1 < cw2);
-                if (LEARNED) i1 = (d0 > 0.0f && th_in2 * d0 < cw2) || (d1 > 0.0f && th_in2 * d1 < cw2);
-            } else {
-#pragma unroll
-                for (int i = 0; i < TPL; ++i) {
-                    const float dx = cx - p[i].x, dy = cy - p[i].y, dz = cz - p[i].z;
-                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    o1 |= d2 > 0.0f && th2 * d2 < cw2;
-                    if (LEARNED) i1 |= d2 > 0.0f && th_in2 * d2 < cw2;
-                }
-            }
-            const unsigned vo = __ballot_sync(0xffffffffu, o1);
-            if (lane == j) open = vo != 0u;
-            if (LEARNED) {
-                // accepted by every target, but opened by one at theta_inner
-                const unsigned vi = __ballot_sync(0xffffffffu, i1);
-                if (lane == j) marginal = vo == 0u && vi != 0u && A.w > 0.0f;
-            }
-        }
-        if (LEARNED) {
-            const unsigned mm = __ballot_sync(0xffffffffu, marginal);
-            const int nm = __popc(mm);
-            if (nm && fill + nm > LCHUNK) {
-                // pad the current chunk's tail, take the next chunk and link it
-                if (chunk >= 0 && chunk < LR.cap)
-                    for (int i = fill + lane; i < LCHUNK; i += 32) LR.rec[size_t(chunk) * LCHUNK + i] = -1;
-                int nc = 0;
-                if (lane == 0) nc = atomicAdd(LR.used, 1);
-                nc = __shfl_sync(0xffffffffu, nc, 0);
-                if (lane == 0) {
-                    if (nc < LR.cap) {
-                        LR.chunk_group[nc] = group;
-                        LR.next[nc] = -1;
-                    } else {
-                        atomicOr(err, 2);
-                    }
-                    if (chunk < 0) LR.head[group] = nc;
-                    else if (chunk < LR.cap) LR.next[chunk] = nc;
-                }
-                chunk = nc;
-                fill = 0;
-            }
-            if (marginal && chunk < LR.cap) LR.rec[size_t(chunk) * LCHUNK + fill + __popc(mm & lt)] = node;
-            fill += nm;
-            learned += nm;
-        }
-        const bool rest = have && B.y < range.y;  // later siblings remain
-        const int np = int(rest) + int(open);
-        // each lane's pushes follow those of the lanes below it
-        const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, open);
-        const int total = __popc(mrest) + __popc(mopen);
-        int slot = S + __popc(mrest & lt) + __popc(mopen & lt);
-        if (slot + np > stack_cap) {
-            failed = true;  // never written out of bounds
-        } else {
-            if (rest) stack[slot++] = make_int2(B.y, range.y);
-            if (open) stack[slot++] = make_int2(node + 1, B.y);  // children on top: popped first
-        }
-        if (__any_sync(0xffffffffu, failed)) {
-            failed = true;
-            break;
-        }
-        S += total;
-        maxS = max(maxS, S);
-        const bool acc = have && !open;
-        bool farc = false;
-        if (LOCAL && acc && (B.z < 0 || B.w == 1) && A.w != 0.0f) {  // cells and single bodies
-            const float dx = A.x - lgx, dy = A.y - lgy, dz = A.z - lgz;
-            if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > far2) {
-                farc = true;
-                const bool q = QUAD && B.z < 0;
-                LocalExp t;
-                float *tf = &t.ax;
-#pragma unroll
-                for (int k = 0; k < 19; ++k) tf[k] = s_lx[warp][k][lane];
-                local_add(t, dx, dy, dz, A.w, eps2, q ? nodeQ + 2 * node : nullptr,
-                          q ? nodeQ + 2 * node + 1 : nullptr);
-#pragma unroll
-                for (int k = 0; k < 19; ++k) s_lx[warp][k][lane] = tf[k];
-                ++nlocal;
-            }
-        }
-        const bool bucket = acc && B.z >= 0 && B.w > 1;
-        const bool cellacc = acc && B.z < 0 && !farc;
-        const bool bodyacc = acc && B.z >= 0 && B.w == 1 && !farc;
-        // accepted cells -> the cell list (with their quadrupoles)
-        const unsigned mc = __ballot_sync(0xffffffffu, cellacc);
-        const int nc1 = __popc(mc);
-        if (Nc + nc1 > CellList::CAP) {
-            eval_list<NFC, CellList::CAP, GUARD, TPL>(Lc, Nc, px, py, pz, e2, ax, ay, az);
-            entries += Nc;
-            centries += Nc;
-            Nc = 0;
-        }
-        if (cellacc) {
-            const int e = Nc + __popc(mc & lt);
-            Lc.f[0][e] = A.x;
-            Lc.f[1][e] = A.y;
-            Lc.f[2][e] = A.z;
-            Lc.f[3][e] = A.w;
-            if constexpr (QUAD) {  // negated: the list evaluation's form
-                const float4 q0 = __ldg(nodeQ + 2 * node);
-                const float4 q1 = __ldg(nodeQ + 2 * node + 1);
-                Lc.f[4][e] = -q0.x;
-                Lc.f[5][e] = -q0.y;
-                Lc.f[6][e] = -q0.z;
-                Lc.f[7][e] = -q0.w;
-                Lc.f[8][e] = -q1.x;
-                Lc.f[9][e] = -q1.y;
-            }
-        }
-        Nc += nc1;
-        // accepted single-body leaves -> the body list (monopole only)
-        const unsigned mb1 = __ballot_sync(0xffffffffu, bodyacc);
-        const int nb1 = __popc(mb1);
-        if (Nb + nb1 > BodyList::CAP) {
-            eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, ax, ay, az);
-            entries += Nb;
-            Nb = 0;
-        }
-        if (bodyacc) {
-            const int e = Nb + __popc(mb1 & lt);
-            Lb.f[0][e] = A.x;
-            Lb.f[1][e] = A.y;
-            Lb.f[2][e] = A.z;
-            Lb.f[3][e] = A.w;
-        }
-        Nb += nb1;
-        unsigned mb = __ballot_sync(0xffffffffu, bucket);
-        while (mb) {  // leaves holding several bodies: one entry per body
-            const int src = __ffs(mb) - 1;
-            mb &= mb - 1;
-            const int f = __shfl_sync(0xffffffffu, B.z, src);
-            const int c = __shfl_sync(0xffffffffu, B.w, src);
-            for (int base = 0; base < c; base += 32) {
-                const int n = min(32, c - base);
-                if (Nb + n > BodyList::CAP) {
-                    eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, ax, ay, az);
-                    entries += Nb;
-                    Nb = 0;
-                }
-                if (lane < n) {
-                    const float4 q = __ldg(sbody + f + base + lane);
-                    Lb.f[0][Nb + lane] = q.x;
-                    Lb.f[1][Nb + lane] = q.y;
-                    Lb.f[2][Nb + lane] = q.z;
-                    Lb.f[3][Nb + lane] = q.w;
-                }
-                Nb += n;
-            }
-        }
-        __syncwarp();
-    }
-    eval_list<NFC, CellList::CAP, GUARD, TPL>(Lc, Nc, px, py, pz, e2, ax, ay, az);
-    eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, ax, ay, az);
-    entries += Nc + Nb;
-    centries += Nc;
-    float rx[TPL], ry[TPL], rz[TPL];
-#pragma unroll
-    for (int i = 0; i < TPL; ++i) {
-        float x0, x1, y0, y1, z0, z1;
-        upk2(ax[i], x0, x1);
-        upk2(ay[i], y0, y1);
-        upk2(az[i], z0, z1);
-        rx[i] = x0 + x1;
-        ry[i] = y0 + y1;
-        rz[i] = z0 + z1;
-    }
-    if (LOCAL) {
-        LocalExp LX;
-        float *lf = &LX.ax;
-#pragma unroll
-        for (int k = 0; k < 19; ++k) lf[k] = s_lx[warp][k][lane];
-        local_reduce(LX);
-#pragma unroll
-        for (int i = 0; i < TPL; ++i) {
-            float lx, ly, lz;
-            local_eval(LX, p[i].x - lgx, p[i].y - lgy, p[i].z - lgz, lx, ly, lz);
-            rx[i] += lx;
-            ry[i] += ly;
-            rz[i] += lz;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) nlocal += __shfl_xor_sync(0xffffffffu, nlocal, o);
-    }
-    const unsigned long long nv = unsigned(nvalid);
-    unsigned long long s_acc = entries * nv, s_vis = visits * nv, s_cell = centries * nv;
-    if (failed) {
-        // The stack ran out (failed is warp-uniform): this warp's targets take the
-        // reference's per-body walk instead, which needs no stack.
-        unsigned na = 0, nvis = 0, nc = 0;
-#pragma unroll
-        for (int i = 0; i < TPL; ++i) {
-            rx[i] = ry[i] = rz[i] = 0.f;
-            lane_walk<QUAD>(p[i], valid[i], T, nodeA, nodeB, nodeQ, sbody, th2, eps2, rx[i], ry[i], rz[i], na, nvis,
-                            nc);
-        }
-        unsigned long long a = na, v = nvis, c = nc;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_xor_sync(0xffffffffu, a, o);
-            v += __shfl_xor_sync(0xffffffffu, v, o);
-            c += __shfl_xor_sync(0xffffffffu, c, o);
-        }
-        s_acc = a;
-        s_vis = v;
-        s_cell = c;
-    }
-    if (LEARNED) {
-        if (chunk >= 0 && chunk < LR.cap)
-            for (int i = fill + lane; i < LCHUNK; i += 32) LR.rec[size_t(chunk) * LCHUNK + i] = -1;
-        if (lane == 0) {
-            if (chunk < 0 || failed) LR.head[group] = -1;  // a fallback warp keeps the plain result
-            LR.centre[group] = make_float4(gcx, gcy, gcz, 0.f);
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < TPL; ++i)
-        if (valid[i]) {
-            const uint32_t o = tidx[g0 + 32 * i + lane];
-            out[3 * size_t(o) + 0] = rx[i];
-            out[3 * size_t(o) + 1] = ry[i];
-            out[3 * size_t(o) + 2] = rz[i];
-        }
-    if (stats && lane == 0) {
-        atomicAdd(stats + 0, s_acc);
-        atomicAdd(stats + 1, s_vis);
-        if (LEARNED) atomicAdd(stats + 4, learned);
-        if (LOCAL && !failed) atomicAdd(stats + 7, nlocal);
-        atomicAdd(stats + 5, s_cell);
-        atomicAdd(stats + 2, 1ull);
-        atomicMax(stats + 3, (unsigned long long)maxS);
-        if (failed) atomicAdd(stats + 6, 1ull);
-    }
-}
-
-// ---- masked group walk: the reference's rule, per body, with shared traversal ----
-// The default method (no PT_BH_GROUP). One warp walks for MW_TPL x 32 key-adjacent
-// bodies (MW_TPL per lane) like bh_walk_group, but every stack range carries the
-// masks of the bodies that still descend into it, and every list entry the masks of
-// the bodies that accept it: each body's accepted set is exactly the reference's
-// (sequential.rs:470-505: skip a node at d^2 == 0, open a cell when theta^2 d^2 <
-// w^2, else accept). A list entry is evaluated for every body and weighted by the
-// body's mask bit. Sums run in list order instead of the reference's visit order
-// (rounding-level differences).
-constexpr int MW_WARPS = 4;
-constexpr int MW_STACK = 384;
-constexpr int MW_TPL = 2;  // bodies per lane; mask word i covers bodies g0 + 32 i + lane
-
-// Entry pair (packed lo/hi) for one body, weighted by the body's bits of the two
-// entries' masks (qm = the pair's mask words for this body's word).
-template <int NF, bool GUARD>
-__device__ __forceinline__ void eval_pair_masked(const f2 *q, f2 qm, f2 px, f2 py, f2 pz, f2 e2, f2 &ax, f2 &ay,
-                                                 f2 &az) {
-    const int lane = threadIdx.x & 31;
-    float m0, m1;
-    upk2(qm, m0, m1);
-    const f2 bit = pk2(float((__float_as_uint(m0) >> lane) & 1u), float((__float_as_uint(m1) >> lane) & 1u));
-    const f2 dx = sub2(q[0], px);
-    const f2 dy = sub2(q[1], py);
-    const f2 dz = sub2(q[2], pz);
-    const f2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-    float r0, r1;
-    upk2(r2, r0, r1);
-    float i0 = rsqrt_ftz(r0), i1 = rsqrt_ftz(r1);
-    if (GUARD) {
-        i0 = (r0 > 0.0f) ? i0 : 0.0f;
-        i1 = (r1 > 0.0f) ? i1 : 0.0f;
-    }
-    const f2 inv = mul2(pk2(i0, i1), bit);  // a body outside the entry's mask adds exactly 0
-    const f2 inv2 = mul2(inv, inv);
-    const f2 sc = mul2(mul2(q[3], inv), inv2);
-    if constexpr (NF == 10) {
-        const f2 ux = fma2(q[4], dx, fma2(q[5], dy, mul2(q[6], dz)));
-        const f2 uy = fma2(q[5], dx, fma2(q[7], dy, mul2(q[8], dz)));
-        const f2 uz = fma2(q[6], dx, fma2(q[8], dy, mul2(q[9], dz)));
-        const f2 c = fma2(dx, ux, fma2(dy, uy, mul2(dz, uz)));
-        const f2 inv5 = mul2(mul2(inv2, inv2), inv);
-        const f2 k = mul2(c, mul2(inv2, pk2(-2.5f, -2.5f)));
-        const f2 s2 = fma2(inv5, k, sc);
-        ax = fma2(dx, s2, fma2(inv5, ux, ax));
-        ay = fma2(dy, s2, fma2(inv5, uy, ay));
-        az = fma2(dz, s2, fma2(inv5, uz, az));
-    } else {
-        ax = fma2(dx, sc, ax);
-        ay = fma2(dy, sc, ay);
-        az = fma2(dz, sc, az);
-    }
-}
-
-// Lists hold NF fields then MW_TPL mask words per entry.
-template <int NF, int CAP, bool GUARD>
-__device__ __forceinline__ void eval_list_masked(IList<NF + MW_TPL, CAP> &Lst, int cnt, const f2 (&px)[MW_TPL],
-                                                 const f2 (&py)[MW_TPL], const f2 (&pz)[MW_TPL], f2 e2,
-                                                 f2 (&ax)[MW_TPL], f2 (&ay)[MW_TPL], f2 (&az)[MW_TPL]) {
-    const int lane = threadIdx.x & 31;
-    __syncwarp();
-    if (cnt & 1) {  // pad: far away, massless, empty masks
-        if (lane < NF + MW_TPL) Lst.f[lane][cnt] = (lane < 3) ? 1e30f : 0.0f;
-        __syncwarp();
-        ++cnt;
-    }
-#pragma unroll 2
-    for (int e = 0; e < cnt; e += 2) {
-        f2 q[NF + MW_TPL];
-#pragma unroll
-        for (int k = 0; k < NF + MW_TPL; ++k) q[k] = *reinterpret_cast<const f2 *>(&Lst.f[k][e]);
-#pragma unroll
-        for (int i = 0; i < MW_TPL; ++i)
-            eval_pair_masked<NF, GUARD>(q, q[NF + i], px[i], py[i], pz[i], e2, ax[i], ay[i], az[i]);
-    }
-    __syncwarp();
-}
-
-template <bool QUAD, bool GUARD>
-__global__ void __launch_bounds__(32 * MW_WARPS)
-    bh_walk_masked(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
-                   const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB,
-                   const float4 *__restrict__ nodeQ, const float4 *__restrict__ sbody,
-                   const int *__restrict__ counters, float th2, float eps2, float *__restrict__ out,
-                   unsigned long long *__restrict__ stats) {
-    constexpr int NFC = QUAD ? 10 : 4;
-    constexpr int TPL = MW_TPL;
-    static_assert(TPL == 2, "stack entries hold two mask words");
-    using CellList = IList<NFC + TPL, 96>;  // + the masks of the accepting bodies
-    using BodyList = IList<4 + TPL, 128>;
-    __shared__ int4 s_stack[MW_WARPS][MW_STACK];  // (first, end, mask word 0, mask word 1)
-    __shared__ __align__(16) CellList s_cells[MW_WARPS];
-    __shared__ __align__(16) BodyList s_bodies[MW_WARPS];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g0 = (blockIdx.x * MW_WARPS + warp) * 32 * TPL;
-    if (g0 >= n_aff) return;
-    float4 p[TPL];
-    bool valid[TPL];
-    unsigned vmask[TPL];
-#pragma unroll
-    for (int i = 0; i < TPL; ++i) {
-        const int t = g0 + 32 * i + lane;
-        valid[i] = t < n_aff;
-        p[i] = tbody[valid[i] ? t : g0];
-        vmask[i] = __ballot_sync(0xffffffffu, valid[i]);
-    }
-    const unsigned lt = (1u << lane) - 1u;
-    int4 *stack = s_stack[warp];
-    const int T = counters[1];
-    CellList &Lc = s_cells[warp];
-    BodyList &Lb = s_bodies[warp];
-    float mn0 = fminf(p[0].x, p[1].x), mn1 = fminf(p[0].y, p[1].y), mn2 = fminf(p[0].z, p[1].z);
-    float mx0 = fmaxf(p[0].x, p[1].x), mx1 = fmaxf(p[0].y, p[1].y), mx2 = fmaxf(p[0].z, p[1].z);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mn0 = fminf(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
-        mn1 = fminf(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
-        mn2 = fminf(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
-        mx0 = fmaxf(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
-        mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
-        mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
-    }
-    const f2 e2 = pk2(eps2, eps2);
-    f2 px[TPL], py[TPL], pz[TPL], ax[TPL], ay[TPL], az[TPL];
-#pragma unroll
-    for (int i = 0; i < TPL; ++i) {
-        px[i] = pk2(p[i].x, p[i].x);
-        py[i] = pk2(p[i].y, p[i].y);
-        pz[i] = pk2(p[i].z, p[i].z);
-        ax[i] = ay[i] = az[i] = pk2(0.f, 0.f);
-    }
-    if (lane == 0) stack[0] = make_int4(0, T, int(vmask[0]), int(vmask[1]));
-    __syncwarp();
-    int S = 1, Nc = 0, Nb = 0;
-    unsigned long long acc_pairs = 0, cell_pairs = 0, visit_pairs = 0;
-    bool failed = false;
-    while (S > 0) {
-        const int k = min(min(32, S), max(1, (MW_STACK - S) / 2));
-        const bool have = lane < k;
-        const int4 r = have ? stack[S - 1 - lane] : make_int4(0, 0, 0, 0);
-        __syncwarp();
-        S -= k;
-        const int node = r.x;
-        const unsigned mk0 = unsigned(r.z), mk1 = unsigned(r.w);
-        float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
-        int4 B = make_int4(0, 0, 0, 0);
-        if (have) {
-            A = __ldg(nodeA + node);
-            B = __ldg(nodeB + node);
-        }
-        visit_pairs += __popc(mk0) + __popc(mk1);
-        // Per node: which of its bodies open it and which accept it. The bodies' box
-        // settles most nodes; a node whose centre of mass lies inside the box (a body
-        // may coincide with it: skipped) or whose rule differs across the box is
-        // voted on, each lane testing its own bodies.
-        const bool cell = B.z < 0;
-        const float w = cell ? __int_as_float(B.x) : 0.f;
-        unsigned op0 = 0, op1 = 0, ac0 = 0, ac1 = 0;
-        bool need = false;
-        if (have && (mk0 | mk1)) {
-            const float e0 = fmaxf(fmaxf(mn0 - A.x, A.x - mx0), 0.f);
-            const float e1 = fmaxf(fmaxf(mn1 - A.y, A.y - mx1), 0.f);
-            const float e2b = fmaxf(fmaxf(mn2 - A.z, A.z - mx2), 0.f);
-            const float db2 = fmaf(e0, e0, fmaf(e1, e1, e2b * e2b));
-            const bool inside = !(db2 > 0.0f);
-            if (inside) {
-                need = true;
-            } else if (!cell || !(th2 * db2 < w * w)) {  // every body accepts
-                ac0 = mk0;
-                ac1 = mk1;
-            } else {
-                const float f0 = fmaxf(A.x - mn0, mx0 - A.x);
-                const float f1 = fmaxf(A.y - mn1, mx1 - A.y);
-                const float f2b = fmaxf(A.z - mn2, mx2 - A.z);
-                if (th2 * fmaf(f0, f0, fmaf(f1, f1, f2b * f2b)) < w * w) {  // every body opens
-                    op0 = mk0;
-                    op1 = mk1;
-                } else {
-                    need = true;
-                }
-            }
-        }
-        unsigned vm = __ballot_sync(0xffffffffu, need);
-        while (vm) {
-            const int j = __ffs(vm) - 1;
-            vm &= vm - 1;
-            const float cx = __shfl_sync(0xffffffffu, A.x, j);
-            const float cy = __shfl_sync(0xffffffffu, A.y, j);
-            const float cz = __shfl_sync(0xffffffffu, A.z, j);
-            const float cw = __shfl_sync(0xffffffffu, w, j);
-            const unsigned mj0 = __shfl_sync(0xffffffffu, mk0, j), mj1 = __shfl_sync(0xffffffffu, mk1, j);
-            const bool cj = __shfl_sync(0xffffffffu, cell, j);
-            const f2 dx = sub2(pk2(cx, cx), pk2(p[0].x, p[1].x));
-            const f2 dy = sub2(pk2(cy, cy), pk2(p[0].y, p[1].y));
-            const f2 dz = sub2(pk2(cz, cz), pk2(p[0].z, p[1].z));
-            float d0, d1;
-            upk2(fma2(dx, dx, fma2(dy, dy, mul2(dz, dz))), d0, d1);
-            const bool in0 = (mj0 >> lane) & 1u, in1 = (mj1 >> lane) & 1u;
-            const bool o0 = in0 && cj && d0 > 0.0f && th2 * d0 < cw * cw;
-            const bool o1 = in1 && cj && d1 > 0.0f && th2 * d1 < cw * cw;
-            const unsigned om0 = __ballot_sync(0xffffffffu, o0), om1 = __ballot_sync(0xffffffffu, o1);
-            const unsigned am0 = __ballot_sync(0xffffffffu, in0 && !o0 && d0 > 0.0f);
-            const unsigned am1 = __ballot_sync(0xffffffffu, in1 && !o1 && d1 > 0.0f);
-            if (lane == j) {
-                op0 = om0;
-                op1 = om1;
-                ac0 = am0;
-                ac1 = am1;
-            }
-        }
-        // push: later siblings share the parent's masks; children get the opening bodies
-        const bool rest = have && (mk0 | mk1) && B.y < r.y;
-        const bool opn = (op0 | op1) != 0u;
-        const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, opn);
-        const int total = __popc(mrest) + __popc(mopen);
-        int slot = S + __popc(mrest & lt) + __popc(mopen & lt);
-        if (slot + int(rest) + int(opn) > MW_STACK) {
-            failed = true;
-        } else {
-            if (rest) stack[slot++] = make_int4(B.y, r.y, int(mk0), int(mk1));
-            if (opn) stack[slot++] = make_int4(node + 1, B.y, int(op0), int(op1));
-        }
-        if (__any_sync(0xffffffffu, failed)) {
-            failed = true;
-            break;
-        }
-        S += total;
-        const int na = __popc(ac0) + __popc(ac1);
-        acc_pairs += na;
-        const bool accd = na != 0;
-        const bool bucket = accd && !cell && B.w > 1;
-        const bool cellacc = accd && cell;
-        const bool bodyacc = accd && !cell && B.w == 1;
-        if (cellacc) cell_pairs += na;
-        const unsigned mc = __ballot_sync(0xffffffffu, cellacc);
-        const int nc1 = __popc(mc);
-        if (Nc + nc1 > CellList::CAP) {
-            eval_list_masked<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
-            Nc = 0;
-        }
-        if (cellacc) {
-            const int e = Nc + __popc(mc & lt);
-            Lc.f[0][e] = A.x;
-            Lc.f[1][e] = A.y;
-            Lc.f[2][e] = A.z;
-            Lc.f[3][e] = A.w;
-            if constexpr (QUAD) {  // negated: the list evaluation's form
-                const float4 q0 = __ldg(nodeQ + 2 * node);
-                const float4 q1 = __ldg(nodeQ + 2 * node + 1);
-                Lc.f[4][e] = -q0.x;
-                Lc.f[5][e] = -q0.y;
-                Lc.f[6][e] = -q0.z;
-                Lc.f[7][e] = -q0.w;
-                Lc.f[8][e] = -q1.x;
-                Lc.f[9][e] = -q1.y;
-            }
-            Lc.f[NFC][e] = __uint_as_float(ac0);
-            Lc.f[NFC + 1][e] = __uint_as_float(ac1);
-        }
-        Nc += nc1;
-        const unsigned mb1 = __ballot_sync(0xffffffffu, bodyacc);
-        const int nb1 = __popc(mb1);
-        if (Nb + nb1 > BodyList::CAP) {
-            eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
-            Nb = 0;
-        }
-        if (bodyacc) {
-            const int e = Nb + __popc(mb1 & lt);
-            Lb.f[0][e] = A.x;
-            Lb.f[1][e] = A.y;
-            Lb.f[2][e] = A.z;
-            Lb.f[3][e] = A.w;
-            Lb.f[4][e] = __uint_as_float(ac0);
-            Lb.f[5][e] = __uint_as_float(ac1);
-        }
-        Nb += nb1;
-        unsigned mbk = __ballot_sync(0xffffffffu, bucket);
-        while (mbk) {  // leaves holding several bodies: one entry per body, the leaf's masks
-            const int src = __ffs(mbk) - 1;
-            mbk &= mbk - 1;
-            const int f = __shfl_sync(0xffffffffu, B.z, src);
-            const int c = __shfl_sync(0xffffffffu, B.w, src);
-            const unsigned b0 = __shfl_sync(0xffffffffu, ac0, src), b1 = __shfl_sync(0xffffffffu, ac1, src);
-            for (int base = 0; base < c; base += 32) {
-                const int n = min(32, c - base);
-                if (Nb + n > BodyList::CAP) {
-                    eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
-                    Nb = 0;
-                }
-                if (lane < n) {
-                    const float4 q = __ldg(sbody + f + base + lane);
-                    Lb.f[0][Nb + lane] = q.x;
-                    Lb.f[1][Nb + lane] = q.y;
-                    Lb.f[2][Nb + lane] = q.z;
-                    Lb.f[3][Nb + lane] = q.w;
-                    Lb.f[4][Nb + lane] = __uint_as_float(b0);
-                    Lb.f[5][Nb + lane] = __uint_as_float(b1);
-                }
-                Nb += n;
-            }
-        }
-        __syncwarp();
-    }
-    eval_list_masked<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
-    eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
-    float rx[TPL], ry[TPL], rz[TPL];
-#pragma unroll
-    for (int i = 0; i < TPL; ++i) {
-        float x0, x1, y0, y1, z0, z1;
-        upk2(ax[i], x0, x1);
-        upk2(ay[i], y0, y1);
-        upk2(az[i], z0, z1);
-        rx[i] = x0 + x1;
-        ry[i] = y0 + y1;
-        rz[i] = z0 + z1;
-    }
-    if (failed) {  // the stack ran out: the per-body cursor walk instead (warp-uniform)
-        unsigned na = 0, nv = 0, nc = 0;
-#pragma unroll
-        for (int i = 0; i < TPL; ++i) {
-            rx[i] = ry[i] = rz[i] = 0.f;
-            lane_walk<QUAD>(p[i], valid[i], T, nodeA, nodeB, nodeQ, sbody, th2, eps2, rx[i], ry[i], rz[i], na, nv,
-                            nc);
-        }
-        acc_pairs = na;
-        cell_pairs = nc;
-        visit_pairs = nv;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {  // per-lane counts -> the warp's
-        acc_pairs += __shfl_xor_sync(0xffffffffu, acc_pairs, o);
-        cell_pairs += __shfl_xor_sync(0xffffffffu, cell_pairs, o);
-        visit_pairs += __shfl_xor_sync(0xffffffffu, visit_pairs, o);
-    }
-#pragma unroll
-    for (int i = 0; i < TPL; ++i)
-        if (valid[i]) {
-            const uint32_t o = tidx[g0 + 32 * i + lane];
-            out[3 * size_t(o) + 0] = rx[i];
-            out[3 * size_t(o) + 1] = ry[i];
-            out[3 * size_t(o) + 2] = rz[i];
-        }
-    if (stats && lane == 0) {
-        atomicAdd(stats + 0, acc_pairs);
-        atomicAdd(stats + 1, visit_pairs);
-        atomicAdd(stats + 2, 1ull);
-        atomicAdd(stats + 5, cell_pairs);
-        if (failed) atomicAdd(stats + 6, 1ull);
-    }
-}
-
-// ---- the reference rule over DVec3 bodies (f64 method) -------------------------
-// As bh_walk_masked with one body per lane, in double: node data, widths and the
-// per-pair kernel (impl_acceleration_cpu_scalar!(DVec3, f64): d * (m / (n_s sqrt
-// n_s)), IEEE-rounded in the reference's order) are f64; accepted sets per body
-// are the reference's. Monopole only, as the reference.
-constexpr int W64_WARPS = 4;
-constexpr int W64_STACK = 384;
-
-__device__ __forceinline__ void pair64(double px, double py, double pz, double cx, double cy, double cz, double m,
-                                       double eps2, double &ax, double &ay, double &az) {
-    const double dx = __dsub_rn(cx, px), dy = __dsub_rn(cy, py), dz = __dsub_rn(cz, pz);
-    const double n = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-    if (n == 0.0) return;  // checked: d itself, which is zero
-    const double ns = __dadd_rn(n, eps2);
-    const double s = __ddiv_rn(m, __dmul_rn(ns, __dsqrt_rn(ns)));
-    ax = __dadd_rn(ax, __dmul_rn(dx, s));
-    ay = __dadd_rn(ay, __dmul_rn(dy, s));
-    az = __dadd_rn(az, __dmul_rn(dz, s));
-}
-
-struct List64 {
-    static constexpr int CAP = 128;
-    double f[4][CAP];
-    unsigned mask[CAP];
-};
-
-__device__ __forceinline__ void eval_list64(const List64 &Lst, int cnt, double px, double py, double pz, double eps2,
-                                            double &ax, double &ay, double &az) {
-    const int lane = threadIdx.x & 31;
-    __syncwarp();
-    for (int e = 0; e < cnt; ++e)
-        if ((Lst.mask[e] >> lane) & 1u) pair64(px, py, pz, Lst.f[0][e], Lst.f[1][e], Lst.f[2][e], Lst.f[3][e], eps2, ax, ay, az);
-    __syncwarp();
-}
-
-__global__ void __launch_bounds__(32 * W64_WARPS)
-    bh_walk64(const double4_32a *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
-              const double4_32a *__restrict__ nodeA, const int4 *__restrict__ nodeB,
-              const double4_32a *__restrict__ nodeG, const double4_32a *__restrict__ sbody,
-              const int *__restrict__ counters, double th2, double eps2, double *__restrict__ out,
-              unsigned long long *__restrict__ stats, int *__restrict__ err) {
-    __shared__ int4 s_stack[W64_WARPS][W64_STACK];
-    __shared__ List64 s_list[W64_WARPS];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int group = blockIdx.x * W64_WARPS + warp;
-    if (group * 32 >= n_aff) return;
-    const int t = group * 32 + lane;
-    const bool valid = t < n_aff;
-    const double4_32a p = tbody[valid ? t : group * 32];
-    const unsigned lt = (1u << lane) - 1u;
-    const unsigned valid_mask = __ballot_sync(0xffffffffu, valid);
-    int4 *stack = s_stack[warp];
-    List64 &Lst = s_list[warp];
-    const int T = counters[1];
-    double mn0 = p.x, mn1 = p.y, mn2 = p.z, mx0 = p.x, mx1 = p.y, mx2 = p.z;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mn0 = fmin(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
-        mn1 = fmin(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
-        mn2 = fmin(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
-        mx0 = fmax(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
-        mx1 = fmax(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
-        mx2 = fmax(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
-    }
-    double ax = 0.0, ay = 0.0, az = 0.0;
-    if (lane == 0) stack[0] = make_int4(0, T, int(valid_mask), 0);
-    __syncwarp();
-    int S = 1, Nl = 0;
-    unsigned long long acc_pairs = 0, visit_pairs = 0;
-    bool failed = false;
-    while (S > 0) {
-        const int k = min(min(32, S), max(1, (W64_STACK - S) / 2));
-        const bool have = lane < k;
-        const int4 r = have ? stack[S - 1 - lane] : make_int4(0, 0, 0, 0);
-        __syncwarp();
-        S -= k;
-        const int node = r.x;
-        const unsigned mask = unsigned(r.z);
-        double4_32a A;
-        A.x = A.y = A.z = A.w = 0.0;
-        int4 B = make_int4(0, 0, 0, 0);
-        double w = 0.0;
-        if (have) {
-            A = nodeA[node];
-            B = __ldg(nodeB + node);
-            if (B.z < 0) w = nodeG[node].w;
-        }
-        visit_pairs += __popc(mask);
-        const bool cell = B.z < 0;
-        unsigned open_m = 0, acc_m = 0;
-        bool need = false;
-        if (have && mask) {
-            const double e0 = fmax(fmax(mn0 - A.x, A.x - mx0), 0.0);
-            const double e1 = fmax(fmax(mn1 - A.y, A.y - mx1), 0.0);
-            const double e2b = fmax(fmax(mn2 - A.z, A.z - mx2), 0.0);
-            const double db2 = __dadd_rn(__dadd_rn(__dmul_rn(e0, e0), __dmul_rn(e1, e1)), __dmul_rn(e2b, e2b));
-            if (!(db2 > 0.0)) {
-                need = true;
-            } else if (!cell || !(__dmul_rn(th2, db2) < __dmul_rn(w, w))) {
-                acc_m = mask;
-            } else {
-                const double f0 = fmax(A.x - mn0, mx0 - A.x), f1 = fmax(A.y - mn1, mx1 - A.y);
-                const double f2b = fmax(A.z - mn2, mx2 - A.z);
-                const double dm2 = __dadd_rn(__dadd_rn(__dmul_rn(f0, f0), __dmul_rn(f1, f1)), __dmul_rn(f2b, f2b));
-                if (__dmul_rn(th2, dm2) < __dmul_rn(w, w)) open_m = mask;
-                else need = true;
-            }
-        }
-        unsigned vm = __ballot_sync(0xffffffffu, need);
-        while (vm) {
-            const int j = __ffs(vm) - 1;
-            vm &= vm - 1;
-            const double cx = __shfl_sync(0xffffffffu, A.x, j), cy = __shfl_sync(0xffffffffu, A.y, j);
-            const double cz = __shfl_sync(0xffffffffu, A.z, j), cw = __shfl_sync(0xffffffffu, w, j);
-            const unsigned mj = __shfl_sync(0xffffffffu, mask, j);
-            const bool cj = __shfl_sync(0xffffffffu, cell, j);
-            // the reference's d^2: (com - body) squared, x, y, z in order
-            const double dx = __dsub_rn(cx, p.x), dy = __dsub_rn(cy, p.y), dz = __dsub_rn(cz, p.z);
-            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-            const bool mine = (mj >> lane) & 1u;
-            const bool o = mine && cj && d2 > 0.0 && __dmul_rn(th2, d2) < __dmul_rn(cw, cw);
-            const bool a = mine && !o && d2 > 0.0;
-            const unsigned om = __ballot_sync(0xffffffffu, o), am = __ballot_sync(0xffffffffu, a);
-            if (lane == j) {
-                open_m = om;
-                acc_m = am;
-            }
-        }
-        const bool rest = have && mask && B.y < r.y;
-        const bool opn = open_m != 0u;
-        const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, opn);
-        const int total = __popc(mrest) + __popc(mopen);
-        int slot = S + __popc(mrest & lt) + __popc(mopen & lt);
-        if (slot + int(rest) + int(opn) > W64_STACK) {
-            failed = true;
-        } else {
-            if (rest) stack[slot++] = make_int4(B.y, r.y, int(mask), 0);
-            if (opn) stack[slot++] = make_int4(node + 1, B.y, int(open_m), 0);
-        }
-        if (__any_sync(0xffffffffu, failed)) {
-            failed = true;
-            break;
-        }
-        S += total;
-        acc_pairs += __popc(acc_m);
-        // accepted cells and single bodies: one list entry with the accepting mask;
-        // several-body leaves: one entry per body
-        const bool single = acc_m != 0u && (cell || B.w == 1);
-        const unsigned ms = __ballot_sync(0xffffffffu, single);
-        const int ns = __popc(ms);
-        if (Nl + ns > List64::CAP) {
-            eval_list64(Lst, Nl, p.x, p.y, p.z, eps2, ax, ay, az);
-            Nl = 0;
-        }
-        if (single) {
-            const int e = Nl + __popc(ms & lt);
-            Lst.f[0][e] = A.x;
-            Lst.f[1][e] = A.y;
-            Lst.f[2][e] = A.z;
-            Lst.f[3][e] = A.w;
-            Lst.mask[e] = acc_m;
-        }
-        Nl += ns;
-        unsigned mbk = __ballot_sync(0xffffffffu, acc_m != 0u && !cell && B.w > 1);
-        while (mbk) {
-            const int src = __ffs(mbk) - 1;
-            mbk &= mbk - 1;
-            const int f = __shfl_sync(0xffffffffu, B.z, src), c = __shfl_sync(0xffffffffu, B.w, src);
-            const unsigned bm = __shfl_sync(0xffffffffu, acc_m, src);
-            for (int base = 0; base < c; base += 32) {
-                const int n = min(32, c - base);
-                if (Nl + n > List64::CAP) {
-                    eval_list64(Lst, Nl, p.x, p.y, p.z, eps2, ax, ay, az);
-                    Nl = 0;
-                }
-                if (lane < n) {
-                    const double4_32a q = sbody[f + base + lane];
-                    Lst.f[0][Nl + lane] = q.x;
-                    Lst.f[1][Nl + lane] = q.y;
-                    Lst.f[2][Nl + lane] = q.z;
-                    Lst.f[3][Nl + lane] = q.w;
-                    Lst.mask[Nl + lane] = bm;
-                }
-                Nl += n;
-            }
-        }
-        __syncwarp();
-    }
-    eval_list64(Lst, Nl, p.x, p.y, p.z, eps2, ax, ay, az);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        acc_pairs += __shfl_xor_sync(0xffffffffu, acc_pairs, o);
-        visit_pairs += __shfl_xor_sync(0xffffffffu, visit_pairs, o);
-    }
-    if (failed) {  // no stackless fallback in f64: the bodies are NaN and the call fails
-        ax = ay = az = __longlong_as_double(0x7ff8000000000000ll);
-        if (lane == 0) atomicOr(err, 1);
-    }
-    if (valid) {
-        const uint32_t o = tidx[t];
-        out[3 * size_t(o) + 0] = ax;
-        out[3 * size_t(o) + 1] = ay;
-        out[3 * size_t(o) + 2] = az;
-    }
-    if (stats && lane == 0) {
-        atomicAdd(stats + 0, acc_pairs);
-        atomicAdd(stats + 1, visit_pairs);
-        atomicAdd(stats + 2, 1ull);
-    }
-}
-
-using WalkKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
-                            const float4 *, const int *, float, float, float *, unsigned long long *);
-using GroupKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
-                             const float4 *, const float4 *, const int *, float, float, LearnedRecords, float,
-                             float *, unsigned long long *, int *, int, float);
-
-static WalkKernel masked_kernel(bool quad, bool guard) {
-    if (quad) return guard ? bh_walk_masked<true, true> : bh_walk_masked<true, false>;
-    return guard ? bh_walk_masked<false, true> : bh_walk_masked<false, false>;
-}
-
-template <bool LEARNED, bool LOCAL>
-static GroupKernel group_kernel_q(bool quad, bool guard) {
-    if (quad) return guard ? bh_walk_group<true, true, LEARNED, LOCAL> : bh_walk_group<true, false, LEARNED, LOCAL>;
-    return guard ? bh_walk_group<false, true, LEARNED, LOCAL> : bh_walk_group<false, false, LEARNED, LOCAL>;
-}
-
-static GroupKernel group_kernel(bool quad, bool guard, bool learned, bool local) {
-    if (learned) return group_kernel_q<true, false>(quad, guard);
-    if (local) return group_kernel_q<false, true>(quad, guard);
-    return group_kernel_q<false, false>(quad, guard);
-}
-
-static State *state(pt_ctx *ctx) {
-    if (!ctx->bh) ctx->bh = new (std::nothrow) State();
-    return static_cast<State *>(ctx->bh);
-}
-
-template <class T>
-static T *as(DevBuf &b) {
-    return static_cast<T *>(b.ptr);
-}
-
-static inline int blocks(int n, int t = 256) { return (n + t - 1) / t; }
-
-// Builds the tree over d_src (n_src >= 1 bodies) into the context's state.
-template <class T>
-static int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
-    using V4 = typename Prec<T>::V4;
-    constexpr bool F64 = sizeof(T) == 8;
-    // the f64 method keeps its own body, node and box arrays (the rest is shared)
-    DevBuf &sb = F64 ? S.sbody64 : S.sbody;
-    DevBuf &nA = F64 ? S.nodeA64 : S.nodeA;
-    DevBuf &nG = F64 ? S.nodeG64 : S.nodeG;
-    cudaStream_t st = ctx->stream;
-    const size_t N = size_t(n);
-    PT_TRY(ensure_buf(ctx, S.box_part, sizeof(T) * 6 * 1024));
-    PT_TRY(ensure_buf(ctx, S.box, sizeof(T) * 8));
-    PT_TRY(ensure_buf(ctx, S.keys, sizeof(uint64_t) * N));
-    PT_TRY(ensure_buf(ctx, S.idx, sizeof(uint32_t) * N));
-    PT_TRY(ensure_buf(ctx, sb, sizeof(V4) * N));
-    PT_TRY(ensure_buf(ctx, S.flags, sizeof(uint32_t) * N));
-    PT_TRY(ensure_buf(ctx, S.uscan, sizeof(uint32_t) * (N + 1)));
-    PT_TRY(ensure_buf(ctx, S.ukey, sizeof(uint64_t) * N));
-    PT_TRY(ensure_buf(ctx, S.ufirst, sizeof(uint32_t) * (N + 1)));
-    PT_TRY(ensure_buf(ctx, S.bfirst, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.blast, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.bdelta, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.bparent, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.lparent, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.top, N));
-    PT_TRY(ensure_buf(ctx, S.oparent, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.loparent, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.cnt, sizeof(uint32_t) * (N + 1)));
-    PT_TRY(ensure_buf(ctx, S.pscan, sizeof(uint32_t) * (N + 2)));
-    PT_TRY(ensure_buf(ctx, S.pre, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.levels, sizeof(int) * (3 * LEVELS + 8)));
-    PT_TRY(ensure_buf(ctx, S.by_level, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, nA, sizeof(V4) * 2 * N));
-    PT_TRY(ensure_buf(ctx, S.nodeB, sizeof(int4) * 2 * N));
-    if (!F64) PT_TRY(ensure_buf(ctx, S.nodeQ, sizeof(float4) * 4 * N));
-    PT_TRY(ensure_buf(ctx, nG, sizeof(V4) * 2 * N));
-    float4 *nodeQ = F64 ? nullptr : as<float4>(S.nodeQ);
-    PT_TRY(ensure_buf(ctx, S.nodeR, sizeof(int2) * 2 * N));
-    PT_TRY(ensure_buf(ctx, S.mom, sizeof(Moments) * 2 * N));
-    PT_TRY(ensure_buf(ctx, S.counters, sizeof(unsigned long long) * 16));
-
-    const int nb = std::min(1024, blocks(n));
-    bbox_partial<T><<<nb, 256, 0, st>>>(d_src, n, as<T>(S.box_part));
-    PT_TRY(check_launch(ctx, "bbox_partial"));
-    bbox_final<T><<<1, 256, 0, st>>>(as<T>(S.box_part), nb, as<T>(S.box));
-    PT_TRY(check_launch(ctx, "bbox_final"));
-    make_keys<T><<<blocks(n), 256, 0, st>>>(d_src, n, as<T>(S.box), as<uint64_t>(S.keys), as<uint32_t>(S.idx));
-    PT_TRY(check_launch(ctx, "make_keys"));
-    PT_TRY(radix_sort_u64(ctx, S.prims, as<uint64_t>(S.keys), as<uint32_t>(S.idx), n, 3 * LEVELS));
-    gather_bodies<V4><<<blocks(n), 256, 0, st>>>(d_src, as<uint32_t>(S.idx), n, as<V4>(sb));
-    PT_TRY(check_launch(ctx, "gather_bodies"));
-    unit_flags<<<blocks(n), 256, 0, st>>>(as<uint64_t>(S.keys), n, as<uint32_t>(S.flags));
-    PT_TRY(check_launch(ctx, "unit_flags"));
-    PT_TRY(scan_u32(ctx, S.prims, as<uint32_t>(S.flags), as<uint32_t>(S.uscan), n));
-    int *counters = as<int>(S.counters);
-    unit_fill<<<blocks(n), 256, 0, st>>>(as<uint64_t>(S.keys), as<uint32_t>(S.flags), as<uint32_t>(S.uscan), n,
-                                        as<uint64_t>(S.ukey), as<uint32_t>(S.ufirst), counters);
-    PT_TRY(check_launch(ctx, "unit_fill"));
-    karras<<<blocks(n), 256, 0, st>>>(as<uint64_t>(S.ukey), counters, as<int>(S.bfirst), as<int>(S.blast),
-                                     as<int>(S.bdelta), as<int>(S.bparent), as<int>(S.lparent));
-    PT_TRY(check_launch(ctx, "karras"));
-    octree_top<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<int>(S.bparent), as<uint8_t>(S.top));
-    PT_TRY(check_launch(ctx, "octree_top"));
-    PT_CUDA(cudaMemsetAsync(S.cnt.ptr, 0, sizeof(uint32_t) * (N + 1), st));
-    PT_CUDA(cudaMemsetAsync(S.levels.ptr, 0, sizeof(int) * (3 * LEVELS + 8), st));
-    octree_links<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.bparent), as<int>(S.lparent),
-                                           as<uint8_t>(S.top), as<int>(S.oparent), as<int>(S.loparent),
-                                           as<uint32_t>(S.cnt));
-    PT_TRY(check_launch(ctx, "octree_links"));
-    PT_TRY(scan_u32(ctx, S.prims, as<uint32_t>(S.cnt), as<uint32_t>(S.pscan), n + 1));
-    layout<T><<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.blast), as<int>(S.bdelta),
-                                     as<uint8_t>(S.top), as<int>(S.oparent), as<uint32_t>(S.cnt),
-                                     as<uint32_t>(S.pscan), as<uint64_t>(S.ukey), as<uint32_t>(S.ufirst),
-                                     as<T>(S.box), as<int>(S.pre), as<int4>(S.nodeB), as<V4>(nG),
-                                     as<int2>(S.nodeR));
-    PT_TRY(check_launch(ctx, "layout"));
-
-    int *levels = as<int>(S.levels);
-    cell_level_count<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<uint8_t>(S.top), levels);
-    PT_TRY(check_launch(ctx, "cell_level_count"));
-    cell_level_offsets<<<1, 32, 0, st>>>(levels);
-    PT_TRY(check_launch(ctx, "cell_level_offsets"));
-    cell_level_scatter<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<uint8_t>(S.top), levels,
-                                                 as<int>(S.by_level));
-    PT_TRY(check_launch(ctx, "cell_level_scatter"));
-    leaf_moments<T><<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<V4>(sb),
-                                              as<uint32_t>(S.pscan), as<uint32_t>(S.cnt), as<Moments>(S.mom),
-                                              as<V4>(nA), nodeQ);
-    PT_TRY(check_launch(ctx, "leaf_moments"));
-    const int lvl_grid = std::max(1, std::min(blocks(n), 8 * ctx->sm_count));
-    for (int L = LEVELS - 1; L >= 0; --L) {
-        cell_moments_level<T><<<lvl_grid, 256, 0, st>>>(L, levels, as<int>(S.by_level), as<int>(S.pre),
-                                                        as<int4>(S.nodeB), as<V4>(nG), as<Moments>(S.mom),
-                                                        as<V4>(nA), nodeQ);
-        PT_TRY(check_launch(ctx, "cell_moments_level"));
-    }
-    S.last_n_src = n;
-    S.f64 = F64;
-    ++S.generation;
-    return PT_OK;
-}
-
-static int build(pt_ctx *ctx, State &S, const float4 *d_src, int n) { return build_t<float>(ctx, S, d_src, n); }
-
-// Sorts separate targets along the same keys (same root box) for coherent warps.
-template <class T>
-static int sort_targets_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_aff, int n) {
-    using V4 = typename Prec<T>::V4;
-    DevBuf &tb = sizeof(T) == 8 ? S.tbody64 : S.tbody;
-    cudaStream_t st = ctx->stream;
-    PT_TRY(ensure_buf(ctx, S.tkeys, sizeof(uint64_t) * size_t(n)));
-    PT_TRY(ensure_buf(ctx, S.tidx, sizeof(uint32_t) * size_t(n)));
-    PT_TRY(ensure_buf(ctx, tb, sizeof(V4) * size_t(n)));
-    make_keys<T><<<blocks(n), 256, 0, st>>>(d_aff, n, as<T>(S.box), as<uint64_t>(S.tkeys), as<uint32_t>(S.tidx));
-    PT_TRY(check_launch(ctx, "make_keys(targets)"));
-    PT_TRY(radix_sort_u64(ctx, S.prims, as<uint64_t>(S.tkeys), as<uint32_t>(S.tidx), n, 3 * LEVELS));
-    gather_bodies<V4><<<blocks(n), 256, 0, st>>>(d_aff, as<uint32_t>(S.tidx), n, as<V4>(tb));
-    return check_launch(ctx, "gather_bodies(targets)");
-}
-
-static int sort_targets(pt_ctx *ctx, State &S, const float4 *d_aff, int n) {
-    return sort_targets_t<float>(ctx, S, d_aff, n);
-}
-
-static int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n_aff, float theta,
-                float softening, uint32_t flags, float *d_out);
-
-static int run(pt_ctx *ctx, const float4 *d_aff, int n_aff, const float4 *d_src, int n_src, float theta,
-               float softening, uint32_t flags, float *d_out) {
-    cudaStream_t st = ctx->stream;
-    if (n_aff == 0) return PT_OK;
-    if (n_src == 0) {
-        PT_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * 3 * size_t(n_aff), st));
-        return PT_OK;
-    }
-    State *Sp = state(ctx);
-    if (!Sp) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
-    State &S = *Sp;
-    mark(ctx, 0);
-    PT_TRY(build(ctx, S, d_src, n_src));
-    const bool same = (d_aff == d_src) && (n_aff == n_src);
-    const float4 *tbody;
-    const uint32_t *tidx;
-    if (same) {
-        tbody = as<float4>(S.sbody);
-        tidx = as<uint32_t>(S.idx);
-    } else {
-        PT_TRY(sort_targets(ctx, S, d_aff, n_aff));
-        tbody = as<float4>(S.tbody);
-        tidx = as<uint32_t>(S.tidx);
-    }
-    return walk(ctx, S, tbody, tidx, n_aff, theta, softening, flags, d_out);
-}
-
-// The f64 method: build over DVec3 bodies, walk with the reference rule in double.
-static int run64(pt_ctx *ctx, const double4_32a *d_aff, int n_aff, const double4_32a *d_src, int n_src,
-                 double theta, double softening, double *d_out) {
-    cudaStream_t st = ctx->stream;
-    if (n_aff == 0) return PT_OK;
-    if (n_src == 0) {
-        PT_CUDA(cudaMemsetAsync(d_out, 0, sizeof(double) * 3 * size_t(n_aff), st));
-        return PT_OK;
-    }
-    State *Sp = state(ctx);
-    if (!Sp) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
-    State &S = *Sp;
-    mark(ctx, 0);
-    PT_TRY(build_t<double>(ctx, S, d_src, n_src));
-    const bool same = (d_aff == d_src) && (n_aff == n_src);
-    if (!same) PT_TRY(sort_targets_t<double>(ctx, S, d_aff, n_aff));
-    const double4_32a *tbody = same ? as<double4_32a>(S.sbody64) : as<double4_32a>(S.tbody64);
-    const uint32_t *tidx = same ? as<uint32_t>(S.idx) : as<uint32_t>(S.tidx);
-    unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 2;
-    int *err = as<int>(S.counters) + 3;
-    PT_CUDA(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
-    PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-    mark(ctx, 1);
-    bh_walk64<<<(n_aff + 32 * W64_WARPS - 1) / (32 * W64_WARPS), 32 * W64_WARPS, 0, st>>>(
-        tbody, tidx, n_aff, as<double4_32a>(S.nodeA64), as<int4>(S.nodeB), as<double4_32a>(S.nodeG64),
-        as<double4_32a>(S.sbody64), as<int>(S.counters), theta * theta, softening * softening, d_out, stats, err);
-    PT_TRY(check_launch(ctx, "bh_walk64"));
-    mark(ctx, 2);
-    return PT_OK;
-}
-
-// Walks the context's current tree for targets tbody (key-sorted; tidx maps them back
-// to the caller's order) and writes accelerations to d_out.
-static int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n_aff, float theta,
-                float softening, uint32_t flags, float *d_out) {
-    cudaStream_t st = ctx->stream;
-    if (S.f64) return set_error(PT_ERR_INVALID, "the context's tree holds DVec3 bodies: walk it with the f64 method");
-    // counters: int[4] = {leaves, nodes, cells, error} then u64[8] = {interactions,
-    // visits, warps, max group stack, learned records, cell interactions, warps that
-    // fell back to the per-body walk, far nodes taken by the local expansion}
-    unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 2;
-    int *err = as<int>(S.counters) + 3;
-    PT_CUDA(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
-    PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-    const float th2 = theta * theta;
-    const float eps2 = softening * softening;
-    const bool quad = flags & PT_BH_QUADRUPOLE;
-    mark(ctx, 1);
-    if (flags & PT_BH_GROUP) {
-        const int groups = (n_aff + GW_GROUP - 1) / GW_GROUP;
-        const bool learned = flags & PT_BH_LEARNED;
-        if (learned && !S.mlp_w) return set_error(PT_ERR_INVALID, "PT_BH_LEARNED needs a model (pt_mlp_*)");
-        LearnedRecords LR{};
-        if (learned) {
-            PT_TRY(ensure_buf(ctx, S.lhead, sizeof(int) * size_t(groups)));
-            PT_TRY(ensure_buf(ctx, S.lcentre, sizeof(float4) * size_t(groups)));
-            PT_TRY(ensure_buf(ctx, S.lused, sizeof(int)));
-            if (S.lcap == 0) S.lcap = std::max(1024, 2 * groups);
-        }
-        for (int attempt = 0;; ++attempt) {
-            if (learned) {
-                PT_TRY(ensure_buf(ctx, S.lrec, sizeof(int) * size_t(S.lcap) * LCHUNK));
-                PT_TRY(ensure_buf(ctx, S.lgroup, sizeof(int) * size_t(S.lcap)));
-                PT_TRY(ensure_buf(ctx, S.lnext, sizeof(int) * size_t(S.lcap)));
-                PT_TRY(ensure_buf(ctx, S.lpart, sizeof(float4) * size_t(S.lcap)));
-                LR = LearnedRecords{as<int>(S.lrec),   as<int>(S.lgroup),   as<int>(S.lnext), as<int>(S.lhead),
-                                    as<float4>(S.lcentre), as<float4>(S.lpart), as<int>(S.lused), S.lcap};
-                PT_CUDA(cudaMemsetAsync(LR.used, 0, sizeof(int), st));
-            }
-            group_kernel(quad, eps2 == 0.0f, learned, flags & PT_BH_LOCAL)<<<(groups + GW_WARPS - 1) / GW_WARPS,
-                                                                          32 * GW_WARPS, 0, st>>>(
-                tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.nodeG),
-                as<float4>(S.sbody), as<int>(S.counters), th2, S.theta_inner * S.theta_inner, LR, eps2, d_out, stats,
-                err, S.stack_cap > 0 ? S.stack_cap : GW_STACK, S.local_ratio);
-            PT_TRY(check_launch(ctx, "bh_walk_group"));
-            // Outside stream capture the record count is checked and the walk rerun
-            // with room for all records; inside, an overflow sets error bit 2.
-            if (!learned || ctx->capturing || attempt > 0) break;
-            int used = 0;
-            PT_CUDA(cudaMemcpyAsync(&used, LR.used, sizeof(int), cudaMemcpyDeviceToHost, st));
-            PT_CUDA(cudaStreamSynchronize(st));
-            if (used <= S.lcap) break;
-            S.lcap = used + used / 4;
-            PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-            PT_CUDA(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
-        }
-        if (learned) {
-            bh_learned_eval<<<ctx->sm_count * 4, 128, 0, st>>>(LR, as<float4>(S.nodeA), as<float4>(S.nodeQ),
-                                                               as<float4>(S.nodeG), S.mlp_w, S.mlp_b,
-                                                               S.theta_inner, theta);
-            PT_TRY(check_launch(ctx, "bh_learned_eval"));
-            bh_learned_apply<<<blocks(n_aff), 256, 0, st>>>(LR, tidx, n_aff, GW_SHIFT, d_out);
-            PT_TRY(check_launch(ctx, "bh_learned_apply"));
-        }
-        PT_TRY(check_launch(ctx, "bh_walk_group"));
-        mark(ctx, 2);
-        return PT_OK;
-    }
-    masked_kernel(quad, eps2 == 0.0f)<<<(n_aff + 32 * MW_TPL * MW_WARPS - 1) / (32 * MW_TPL * MW_WARPS),
-                                        32 * MW_WARPS, 0, st>>>(
-        tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.sbody),
-        as<int>(S.counters), th2, eps2, d_out, stats);
-    PT_TRY(check_launch(ctx, "bh_walk_masked"));
-    mark(ctx, 2);
-    return PT_OK;
-}
-
-static int validate(const char *fn, size_t n_aff, size_t n_src, uint32_t flags) {
+int validate(const char *fn, size_t n_aff, size_t n_src, uint32_t flags) {
     const size_t lim = size_t(INT_MAX) / 8;
     if (n_aff > lim || n_src > lim)
         return set_error(PT_ERR_INVALID, "%s: n_aff=%zu n_src=%zu exceed the limit %zu", fn, n_aff, n_src, lim);
