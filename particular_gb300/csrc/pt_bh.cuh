@@ -18,7 +18,7 @@ namespace bh {
 
 constexpr int LEVELS = 21;   // 63-bit keys
 
-struct Moments {  // FP64 cell data used while combining children
+struct Moments {  // FP64 cell data used while combining children (DVec3 trees, bucket leaves)
     double m, cx, cy, cz;
     double sxx, sxy, sxz, syy, syz, szz;  // second moment about the centre of mass
     double count;
@@ -61,7 +61,7 @@ struct State {
     DevBuf keys, idx, sbody;
     DevBuf flags, uscan, ukey, ufirst;
     DevBuf bfirst, blast, bdelta, bparent, lparent, top, oparent, loparent;
-    DevBuf cnt, pscan, pre, levels, by_level;
+    DevBuf cnt, pscan, pre, pending;
     DevBuf nodeA, nodeB, nodeQ, nodeG, nodeR, mom;
     DevBuf sbody64, nodeA64, nodeG64, tbody64;  // the f64 (DVec3) method's bodies and nodes
     DevBuf tkeys, tidx, tbody;

@@ -19,11 +19,13 @@
 //     same (COM, M), so the result is unchanged.
 //  6. cells are laid out in depth-first preorder with skip pointers (index after
 //     the subtree), leaves interleaved: the walk needs no stack.
-//  7. moments bottom-up in FP64 (mass, centre of mass, second moment -> traceless
-//     quadrupole): cells are bucketed by octree level and combined level by level,
-//     deepest first, one thread per cell (parallel-axis theorem). No thread ever
-//     waits on another.
+//  7. moments bottom-up in one launch (mass, centre of mass, second moment ->
+//     traceless quadrupole): the last child to finish combines its parent cell
+//     (parallel-axis theorem), in compensated FP32 for f32 trees and FP64 for
+//     DVec3 trees. No thread ever waits on another.
 #include "pt_bh.cuh"
+
+#include <type_traits>
 
 namespace pt {
 namespace bh {
@@ -220,21 +222,24 @@ __device__ __forceinline__ int climb(int p, const uint8_t *__restrict__ top, con
     return p;
 }
 
-// Octree parents, child counts and the count of cells starting at each unit.
+// Octree parents, child counts (pending, zeroed before) and the count of cells
+// starting at each unit.
 __global__ void octree_links(const int *__restrict__ counters, const int *__restrict__ bfirst,
                              const int *__restrict__ bparent, const int *__restrict__ lparent,
                              const uint8_t *__restrict__ top, int *__restrict__ oparent, int *__restrict__ loparent,
-                             uint32_t *__restrict__ cnt) {
+                             uint32_t *__restrict__ cnt, int *__restrict__ pending) {
     const int M = counters[0];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < M - 1 && top[k]) {
         const int op = (k == 0) ? -1 : climb(bparent[k], top, bparent);
         oparent[k] = op;
+        if (op >= 0) atomicAdd(&pending[op], 1);
         atomicAdd(&cnt[bfirst[k]], 1u);
     }
     if (k < M) {
         const int op = (M == 1) ? -1 : climb(lparent[k], top, bparent);
         loparent[k] = op;
+        if (op >= 0) atomicAdd(&pending[op], 1);
     }
 }
 
@@ -295,30 +300,77 @@ __global__ void layout(int *counters, const int *__restrict__ bfirst,
 }
 
 // ---- 7. moments ------------------------------------------------------------
-template <class T>
-__device__ void store_cell(const Moments &m, int pk, Moments *__restrict__ mom, typename Prec<T>::V4 *__restrict__ nodeA,
-                           float4 *__restrict__ nodeQ) {
-    mom[pk] = m;
-    nodeA[pk] = Prec<T>::make(T(m.cx), T(m.cy), T(m.cz), T(m.m));
-    if (!nodeQ) return;  // the f64 method is monopole only
-    const double tr = m.sxx + m.syy + m.szz;
-    nodeQ[2 * pk] = make_float4(float(3 * m.sxx - tr), float(3 * m.sxy), float(3 * m.sxz), float(3 * m.syy - tr));
-    nodeQ[2 * pk + 1] = make_float4(float(3 * m.syz), float(3 * m.szz - tr), 0.f, 0.f);
+// One launch, bottom-up: a thread per leaf unit writes the leaf's record, then
+// arrives at its parent cell; the last child to arrive (a per-cell countdown of the
+// children still to come) combines the cell from all its children, in preorder,
+// and climbs on. The order of every sum is fixed by the tree, so results do not
+// depend on which thread arrives last. No thread ever waits on another.
+//
+// Records written earlier in the same launch by other threads are read through L2.
+__device__ __forceinline__ float4 ld_cg(const float4 *p) { return __ldcg(p); }
+__device__ __forceinline__ double4_32a ld_cg(const double4_32a *p) {
+    const double2 a = __ldcg(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldcg(reinterpret_cast<const double2 *>(p) + 1);
+    double4_32a r;
+    r.x = a.x, r.y = a.y, r.z = b.x, r.w = b.y;
+    return r;
+}
+__device__ __forceinline__ Moments ld_cg(const Moments *p) {
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+    double2 v[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) v[i] = __ldcg(q + i);
+    Moments r;
+    r.m = v[0].x, r.cx = v[0].y, r.cy = v[1].x, r.cz = v[1].y;
+    r.sxx = v[2].x, r.sxy = v[2].y, r.sxz = v[3].x, r.syy = v[3].y, r.syz = v[4].x, r.szz = v[4].y;
+    r.count = v[5].x, r.pad = v[5].y;
+    return r;
 }
 
-// Leaves: a single body is its own cell data; several (coincident, or closer than
-// the key resolution) get FP64 moments.
-template <class T>
-__global__ void leaf_moments(const int *__restrict__ counters, const uint32_t *__restrict__ ufirst,
-                             const typename Prec<T>::V4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
-                             const uint32_t *__restrict__ cnt, Moments *__restrict__ mom,
-                             typename Prec<T>::V4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
-    using V4 = typename Prec<T>::V4;
-    const int M = counters[0];
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= M) return;
-    const int f = int(ufirst[u]), e = int(ufirst[u + 1]);
-    const int pk = u + int(pscan[u]) + int(cnt[u]);
+// Cell record of f32 trees, in FP32. The centre of mass and the mass are unevaluated
+// sums hi + lo with hi = nodeA, and a child's offset from its parent's geometric
+// centre G is formed as (hi - G) + lo: hi and G lie within a cell width of each
+// other, so every sum below is relative to the cell width, not to the position.
+struct Rec32 {
+    float4 lo;  // centre of mass - nodeA.xyz, mass - nodeA.w
+    float4 s0;  // second moment about the centre of mass: xx xy xz yy
+    float4 s1;  // yz zz, body count (int bits), 0
+};
+
+// Knuth's TwoSum: returns s = fl(a + b) and sets e with s + e == a + b exactly.
+__device__ __forceinline__ float two_sum(float a, float b, float &e) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+
+__device__ __forceinline__ void store_quad(float4 *nodeQ, int pk, float sxx, float sxy, float sxz, float syy,
+                                           float syz, float szz) {
+    const float tr = sxx + syy + szz;
+    nodeQ[2 * pk] = make_float4(3.f * sxx - tr, 3.f * sxy, 3.f * sxz, 3.f * syy - tr);
+    nodeQ[2 * pk + 1] = make_float4(3.f * syz, 3.f * szz - tr, 0.f, 0.f);
+}
+
+__device__ __forceinline__ void store_cell(const Moments &m, int pk, Moments *mom, double4_32a *nodeA, float4 *) {
+    mom[pk] = m;
+    nodeA[pk] = Prec<double>::make(m.cx, m.cy, m.cz, m.m);  // the f64 method is monopole only
+}
+
+__device__ __forceinline__ void store_cell(const Moments &m, int pk, Rec32 *rec, float4 *nodeA, float4 *nodeQ) {
+    const float hx = float(m.cx), hy = float(m.cy), hz = float(m.cz), hm = float(m.m);
+    nodeA[pk] = make_float4(hx, hy, hz, hm);
+    rec[pk].lo = make_float4(float(m.cx - hx), float(m.cy - hy), float(m.cz - hz), float(m.m - hm));
+    rec[pk].s0 = make_float4(float(m.sxx), float(m.sxy), float(m.sxz), float(m.syy));
+    rec[pk].s1 = make_float4(float(m.syz), float(m.szz), __int_as_float(int(m.count)), 0.f);
+    if (nodeQ)
+        store_quad(nodeQ, pk, float(m.sxx), float(m.sxy), float(m.sxz), float(m.syy), float(m.syz), float(m.szz));
+}
+
+// Leaves: a single body is its own cell data (no record: parents read nodeA);
+// several (coincident, or closer than the key resolution) get FP64 moments.
+template <class V4, class R>
+__device__ void leaf(int pk, int f, int e, const V4 *__restrict__ sbody, R *rec, V4 *nodeA, float4 *nodeQ) {
     if (e - f == 1) {
         nodeA[pk] = sbody[f];
         if (nodeQ) {
@@ -362,130 +414,181 @@ __global__ void leaf_moments(const int *__restrict__ counters, const uint32_t *_
         m.syz += p.w * dy * dz;
         m.szz += p.w * dz * dz;
     }
-    store_cell<T>(m, pk, mom, nodeA, nodeQ);
+    store_cell(m, pk, rec, nodeA, nodeQ);
 }
 
-// Cells per octree level: lcount[L], then by_level sorted by level (counting sort).
-// levels[0..LEVELS] = counts, levels[LEVELS+1 ..] = offsets, then cursors.
-__global__ void cell_level_count(const int *__restrict__ counters, const int *__restrict__ bdelta,
-                                 const uint8_t *__restrict__ top, int *__restrict__ levels) {
-    __shared__ int h[LEVELS];
-    if (threadIdx.x < LEVELS) h[threadIdx.x] = 0;
-    __syncthreads();
-    const int M = counters[0];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < M - 1 && top[k]) atomicAdd(&h[bdelta[k] / 3], 1);
-    __syncthreads();
-    if (threadIdx.x < LEVELS && h[threadIdx.x]) atomicAdd(&levels[threadIdx.x], h[threadIdx.x]);
-}
+__device__ __forceinline__ bool single_body(const int4 &cb) { return cb.z >= 0 && cb.w == 1; }
 
-__global__ void cell_level_offsets(int *__restrict__ levels) {
-    if (threadIdx.x != 0) return;
-    int acc = 0;
-    for (int L = 0; L < LEVELS; ++L) {
-        levels[LEVELS + 1 + L] = acc;      // offset
-        levels[2 * LEVELS + 2 + L] = acc;  // cursor
-        acc += levels[L];
+// f32 trees: one pass over the children in FP32, sums about the cell's geometric
+// centre G, then moved to the centre of mass C by the parallel-axis rule
+// S_C = S_G - P P^T / M with P = sum m (c - G) = M (C - G).
+__device__ void cell(int pv, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeG, Rec32 *rec,
+                     float4 *nodeA, float4 *nodeQ) {
+    const int end = nodeB[pv].y;
+    const float4 g = nodeG[pv];
+    float mh = 0.f, ml = 0.f, px = 0.f, py = 0.f, pz = 0.f;
+    float sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
+    int count = 0;
+    for (int c = pv + 1; c < end;) {
+        const int4 cb = nodeB[c];
+        const float4 a = ld_cg(nodeA + c);
+        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), s0 = lo, s1 = lo;
+        int cn = 1;
+        if (!single_body(cb)) {
+            lo = ld_cg(&rec[c].lo);
+            s0 = ld_cg(&rec[c].s0);
+            s1 = ld_cg(&rec[c].s1);
+            cn = __float_as_int(s1.z);
+        }
+        const float dx = __fsub_rn(a.x, g.x) + lo.x, dy = __fsub_rn(a.y, g.y) + lo.y,
+                    dz = __fsub_rn(a.z, g.z) + lo.z;
+        float e;
+        mh = two_sum(mh, a.w, e);
+        ml += e + lo.w;
+        const float mx = a.w * dx, my = a.w * dy, mz = a.w * dz;
+        px += mx;
+        py += my;
+        pz += mz;
+        sxx += s0.x + mx * dx;
+        sxy += s0.y + mx * dy;
+        sxz += s0.z + mx * dz;
+        syy += s0.w + my * dy;
+        syz += s1.x + my * dz;
+        szz += s1.y + mz * dz;
+        count += cn;
+        c = cb.y;
     }
-    levels[2 * LEVELS + 1] = acc;
-}
-
-// Each block reserves one range per level with a single global atomic.
-__global__ void cell_level_scatter(const int *__restrict__ counters, const int *__restrict__ bdelta,
-                                   const uint8_t *__restrict__ top, int *__restrict__ levels,
-                                   int *__restrict__ by_level) {
-    __shared__ int h[LEVELS], base[LEVELS];
-    if (threadIdx.x < LEVELS) h[threadIdx.x] = 0;
-    __syncthreads();
-    const int M = counters[0];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool cell = k < M - 1 && top[k];
-    const int L = cell ? bdelta[k] / 3 : 0;
-    const int local = cell ? atomicAdd(&h[L], 1) : 0;
-    __syncthreads();
-    if (threadIdx.x < LEVELS && h[threadIdx.x])
-        base[threadIdx.x] = atomicAdd(&levels[2 * LEVELS + 2 + threadIdx.x], h[threadIdx.x]);
-    __syncthreads();
-    if (cell) by_level[base[L] + local] = k;
-}
-
-// Combines every cell of octree level L from its children (levels > L: done), in one
-// pass over the children: sums about the cell's geometric centre G (offsets within
-// a cell width, no cancellation), then moved to the centre of mass C by the
-// parallel-axis rule S_C = S_G - P P^T / M with P = sum m (c - G) = M (C - G).
-template <class T>
-__global__ void cell_moments_level(int L, const int *__restrict__ levels, const int *__restrict__ by_level,
-                                   const int *__restrict__ pre, const int4 *__restrict__ nodeB,
-                                   const typename Prec<T>::V4 *__restrict__ nodeG, Moments *__restrict__ mom,
-                                   typename Prec<T>::V4 *__restrict__ nodeA, float4 *__restrict__ nodeQ) {
-    using V4 = typename Prec<T>::V4;
-    const int begin = levels[LEVELS + 1 + L], end_l = begin + levels[L];
-    for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end_l; i += gridDim.x * blockDim.x) {
-        const int pv = pre[by_level[i]];
-        const int end = nodeB[pv].y;
-        const V4 g = nodeG[pv];
-        const double gx = g.x, gy = g.y, gz = g.z;
-        Moments m{};
-        double px = 0, py = 0, pz = 0;
+    float e;
+    const float M = two_sum(mh, ml, e);
+    const float Ml = e;
+    float ox, oy, oz;
+    if (M != 0.f) {
+        const float inv = 1.f / M;
+        ox = px * inv, oy = py * inv, oz = pz * inv;  // C - G
+        sxx -= px * ox;
+        sxy -= px * oy;
+        sxz -= px * oz;
+        syy -= py * oy;
+        syz -= py * oz;
+        szz -= pz * oz;
+    } else {  // massless: plain mean of the bodies (gravity/impls/mod.rs:127-129), a rare second pass
+        float ux = 0.f, uy = 0.f, uz = 0.f;
         for (int c = pv + 1; c < end;) {
             const int4 cb = nodeB[c];
-            double cx, cy, cz, cmm, cn, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
-            if (cb.z >= 0 && cb.w == 1) {  // a single body, read from nodeA
-                const V4 a = nodeA[c];
-                cx = a.x, cy = a.y, cz = a.z, cmm = a.w, cn = 1.0;
-            } else {
-                const Moments &cm = mom[c];
-                cx = cm.cx, cy = cm.cy, cz = cm.cz, cmm = cm.m, cn = cm.count;
-                sxx = cm.sxx, sxy = cm.sxy, sxz = cm.sxz, syy = cm.syy, syz = cm.syz, szz = cm.szz;
+            const float4 a = ld_cg(nodeA + c);
+            float4 lo = make_float4(0.f, 0.f, 0.f, 0.f);
+            float cn = 1.f;
+            if (!single_body(cb)) {
+                lo = ld_cg(&rec[c].lo);
+                cn = float(__float_as_int(ld_cg(&rec[c].s1).z));
             }
-            const double dx = cx - gx, dy = cy - gy, dz = cz - gz;
-            m.m += cmm;
-            m.count += cn;
-            const double mx = cmm * dx, my = cmm * dy, mz = cmm * dz;
-            px += mx;
-            py += my;
-            pz += mz;
-            m.sxx += sxx + mx * dx;
-            m.sxy += sxy + mx * dy;
-            m.sxz += sxz + mx * dz;
-            m.syy += syy + my * dy;
-            m.syz += syz + my * dz;
-            m.szz += szz + mz * dz;
+            ux += cn * (__fsub_rn(a.x, g.x) + lo.x);
+            uy += cn * (__fsub_rn(a.y, g.y) + lo.y);
+            uz += cn * (__fsub_rn(a.z, g.z) + lo.z);
             c = cb.y;
         }
-        if (m.m != 0.0) {
-            const double inv = 1.0 / m.m;
-            const double ox = px * inv, oy = py * inv, oz = pz * inv;  // C - G
-            m.cx = gx + ox;
-            m.cy = gy + oy;
-            m.cz = gz + oz;
-            m.sxx -= px * ox;
-            m.sxy -= px * oy;
-            m.sxz -= px * oz;
-            m.syy -= py * oy;
-            m.syz -= py * oz;
-            m.szz -= pz * oz;
-        } else {  // massless: plain mean of the bodies (gravity/impls/mod.rs:127-129), a rare second pass
-            double ux = 0, uy = 0, uz = 0;
-            for (int c = pv + 1; c < end;) {
-                const int4 cb = nodeB[c];
-                double cx, cy, cz, cn;
-                if (cb.z >= 0 && cb.w == 1) {
-                    const V4 a = nodeA[c];
-                    cx = a.x, cy = a.y, cz = a.z, cn = 1.0;
-                } else {
-                    cx = mom[c].cx, cy = mom[c].cy, cz = mom[c].cz, cn = mom[c].count;
-                }
-                ux += cn * (cx - gx);
-                uy += cn * (cy - gy);
-                uz += cn * (cz - gz);
-                c = cb.y;
-            }
-            m.cx = gx + ux / m.count;
-            m.cy = gy + uy / m.count;
-            m.cz = gz + uz / m.count;
+        ox = ux / float(count), oy = uy / float(count), oz = uz / float(count);
+    }
+    float ex, ey, ez;
+    const float hx = two_sum(g.x, ox, ex), hy = two_sum(g.y, oy, ey), hz = two_sum(g.z, oz, ez);
+    nodeA[pv] = make_float4(hx, hy, hz, M);
+    rec[pv].lo = make_float4(ex, ey, ez, Ml);
+    rec[pv].s0 = make_float4(sxx, sxy, sxz, syy);
+    rec[pv].s1 = make_float4(syz, szz, __int_as_float(count), 0.f);
+    if (nodeQ) store_quad(nodeQ, pv, sxx, sxy, sxz, syy, syz, szz);
+}
+
+// f64 trees (DVec3 bodies): the same combination in FP64.
+__device__ void cell(int pv, const int4 *__restrict__ nodeB, const double4_32a *__restrict__ nodeG, Moments *mom,
+                     double4_32a *nodeA, float4 *) {
+    const int end = nodeB[pv].y;
+    const double4_32a g = nodeG[pv];
+    const double gx = g.x, gy = g.y, gz = g.z;
+    Moments m{};
+    double px = 0, py = 0, pz = 0;
+    for (int c = pv + 1; c < end;) {
+        const int4 cb = nodeB[c];
+        double cx, cy, cz, cmm, cn, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
+        if (single_body(cb)) {
+            const double4_32a a = ld_cg(nodeA + c);
+            cx = a.x, cy = a.y, cz = a.z, cmm = a.w, cn = 1.0;
+        } else {
+            const Moments cm = ld_cg(mom + c);
+            cx = cm.cx, cy = cm.cy, cz = cm.cz, cmm = cm.m, cn = cm.count;
+            sxx = cm.sxx, sxy = cm.sxy, sxz = cm.sxz, syy = cm.syy, syz = cm.syz, szz = cm.szz;
         }
-        store_cell<T>(m, pv, mom, nodeA, nodeQ);
+        const double dx = cx - gx, dy = cy - gy, dz = cz - gz;
+        m.m += cmm;
+        m.count += cn;
+        const double mx = cmm * dx, my = cmm * dy, mz = cmm * dz;
+        px += mx;
+        py += my;
+        pz += mz;
+        m.sxx += sxx + mx * dx;
+        m.sxy += sxy + mx * dy;
+        m.sxz += sxz + mx * dz;
+        m.syy += syy + my * dy;
+        m.syz += syz + my * dz;
+        m.szz += szz + mz * dz;
+        c = cb.y;
+    }
+    if (m.m != 0.0) {
+        const double inv = 1.0 / m.m;
+        const double ox = px * inv, oy = py * inv, oz = pz * inv;  // C - G
+        m.cx = gx + ox;
+        m.cy = gy + oy;
+        m.cz = gz + oz;
+        m.sxx -= px * ox;
+        m.sxy -= px * oy;
+        m.sxz -= px * oz;
+        m.syy -= py * oy;
+        m.syz -= py * oz;
+        m.szz -= pz * oz;
+    } else {  // massless: plain mean of the bodies (gravity/impls/mod.rs:127-129), a rare second pass
+        double ux = 0, uy = 0, uz = 0;
+        for (int c = pv + 1; c < end;) {
+            const int4 cb = nodeB[c];
+            double cx, cy, cz, cn;
+            if (single_body(cb)) {
+                const double4_32a a = ld_cg(nodeA + c);
+                cx = a.x, cy = a.y, cz = a.z, cn = 1.0;
+            } else {
+                const Moments cm = ld_cg(mom + c);
+                cx = cm.cx, cy = cm.cy, cz = cm.cz, cn = cm.count;
+            }
+            ux += cn * (cx - gx);
+            uy += cn * (cy - gy);
+            uz += cn * (cz - gz);
+            c = cb.y;
+        }
+        m.cx = gx + ux / m.count;
+        m.cy = gy + uy / m.count;
+        m.cz = gz + uz / m.count;
+    }
+    store_cell(m, pv, mom, nodeA, nullptr);
+}
+
+template <class T>
+using Record = typename std::conditional<sizeof(T) == 4, Rec32, Moments>::type;
+
+// pending[p] = children of binary cell p not yet combined (counted by octree_links).
+template <class T>
+__global__ void __launch_bounds__(256)
+    moments_up(const int *__restrict__ counters, const uint32_t *__restrict__ ufirst,
+               const typename Prec<T>::V4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
+               const uint32_t *__restrict__ cnt, const int *__restrict__ loparent, const int *__restrict__ oparent,
+               const int *__restrict__ pre, const int4 *__restrict__ nodeB,
+               const typename Prec<T>::V4 *__restrict__ nodeG, int *pending, Record<T> *rec,
+               typename Prec<T>::V4 *nodeA, float4 *nodeQ) {
+    const int M = counters[0];
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= M) return;
+    leaf(u + int(pscan[u]) + int(cnt[u]), int(ufirst[u]), int(ufirst[u + 1]), sbody, rec, nodeA, nodeQ);
+    for (int p = loparent[u]; p >= 0; p = oparent[p]) {
+        __threadfence();                             // this thread's records before its arrival
+        if (atomicSub(&pending[p], 1) != 1) return;  // a sibling still to come climbs on
+        __threadfence();                             // the siblings' records after their arrivals
+        cell(pre[p], nodeB, nodeG, rec, nodeA, nodeQ);
     }
 }
 
@@ -520,8 +623,7 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     PT_TRY(ensure_buf(ctx, S.cnt, sizeof(uint32_t) * (N + 1)));
     PT_TRY(ensure_buf(ctx, S.pscan, sizeof(uint32_t) * (N + 2)));
     PT_TRY(ensure_buf(ctx, S.pre, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.levels, sizeof(int) * (3 * LEVELS + 8)));
-    PT_TRY(ensure_buf(ctx, S.by_level, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.pending, sizeof(int) * N));
     PT_TRY(ensure_buf(ctx, nA, sizeof(V4) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.nodeB, sizeof(int4) * 2 * N));
     if (!F64) PT_TRY(ensure_buf(ctx, S.nodeQ, sizeof(float4) * 4 * N));
@@ -554,10 +656,10 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     octree_top<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<int>(S.bparent), as<uint8_t>(S.top));
     PT_TRY(check_launch(ctx, "octree_top"));
     PT_CUDA(cudaMemsetAsync(S.cnt.ptr, 0, sizeof(uint32_t) * (N + 1), st));
-    PT_CUDA(cudaMemsetAsync(S.levels.ptr, 0, sizeof(int) * (3 * LEVELS + 8), st));
+    PT_CUDA(cudaMemsetAsync(S.pending.ptr, 0, sizeof(int) * N, st));
     octree_links<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.bparent), as<int>(S.lparent),
                                            as<uint8_t>(S.top), as<int>(S.oparent), as<int>(S.loparent),
-                                           as<uint32_t>(S.cnt));
+                                           as<uint32_t>(S.cnt), as<int>(S.pending));
     PT_TRY(check_launch(ctx, "octree_links"));
     PT_TRY(scan_u32(ctx, S.prims, as<uint32_t>(S.cnt), as<uint32_t>(S.pscan), n + 1));
     layout<T><<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.blast), as<int>(S.bdelta),
@@ -567,25 +669,11 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
                                      as<int2>(S.nodeR));
     PT_TRY(check_launch(ctx, "layout"));
 
-    int *levels = as<int>(S.levels);
-    cell_level_count<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<uint8_t>(S.top), levels);
-    PT_TRY(check_launch(ctx, "cell_level_count"));
-    cell_level_offsets<<<1, 32, 0, st>>>(levels);
-    PT_TRY(check_launch(ctx, "cell_level_offsets"));
-    cell_level_scatter<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<uint8_t>(S.top), levels,
-                                                 as<int>(S.by_level));
-    PT_TRY(check_launch(ctx, "cell_level_scatter"));
-    leaf_moments<T><<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<V4>(sb),
-                                              as<uint32_t>(S.pscan), as<uint32_t>(S.cnt), as<Moments>(S.mom),
-                                              as<V4>(nA), nodeQ);
-    PT_TRY(check_launch(ctx, "leaf_moments"));
-    const int lvl_grid = std::max(1, std::min(blocks(n), 8 * ctx->sm_count));
-    for (int L = LEVELS - 1; L >= 0; --L) {
-        cell_moments_level<T><<<lvl_grid, 256, 0, st>>>(L, levels, as<int>(S.by_level), as<int>(S.pre),
-                                                        as<int4>(S.nodeB), as<V4>(nG), as<Moments>(S.mom),
-                                                        as<V4>(nA), nodeQ);
-        PT_TRY(check_launch(ctx, "cell_moments_level"));
-    }
+    moments_up<T><<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<V4>(sb), as<uint32_t>(S.pscan),
+                                            as<uint32_t>(S.cnt), as<int>(S.loparent), as<int>(S.oparent),
+                                            as<int>(S.pre), as<int4>(S.nodeB), as<V4>(nG), as<int>(S.pending),
+                                            as<Record<T>>(S.mom), as<V4>(nA), nodeQ);
+    PT_TRY(check_launch(ctx, "moments_up"));
     S.last_n_src = n;
     S.f64 = F64;
     ++S.generation;
