@@ -237,10 +237,14 @@ class BarnesHutWorkload:
     metric = "bodies/s at <=1e-3 p95 accel err vs FP64"
     unit = "bodies/s"
     bar = 1e-3
-    # (theta, flags) candidates: quadrupole + group opening; the reference's own
+    # (theta, flags, alpha) candidates: quadrupole + group opening; the reference's own
     # monopole per-body walk at theta 0.5 is measured alongside as "plain".
-    # flags: 1 quadrupole, 2 group, 8 local expansion of far nodes
-    ladder = [(0.45, 3), (0.5, 3), (0.52, 3), (0.55, 3), (0.6, 3), (0.48, 11), (0.5, 11), (0.52, 11), (0.55, 11)]
+    # flags: 1 quadrupole, 2 group, 8 local expansion of far nodes, 16 error-bound
+    # opening (alpha; theta is then the geometric cap)
+    ladder = [(0.45, 3, None), (0.5, 3, None), (0.52, 3, None), (0.55, 3, None), (0.6, 3, None),
+              (0.48, 11, None), (0.5, 11, None), (0.52, 11, None), (0.55, 11, None),
+              (1.0, 19, 1.5e-3), (1.0, 19, 2e-3), (1.0, 19, 2.5e-3), (1.0, 19, 3e-3),
+              (1.0, 27, 1.5e-3), (1.0, 27, 2e-3), (1.0, 27, 2.5e-3), (1.0, 27, 2.75e-3), (1.0, 27, 3e-3)]
 
     def __init__(self, n=4194304, softening=0.01, sample=2048):
         from particular_gb300 import ics
@@ -248,7 +252,7 @@ class BarnesHutWorkload:
         self.softening = softening
         self.bodies = ics.bulge_disk(n, seed=1810)["bodies"]
         self.sample = np.random.default_rng(1808).choice(n, sample, replace=False)
-        self.theta, self.flags = 0.5, 3
+        self.theta, self.flags, self.alpha = 0.5, 3, None
         self.table = []
 
     def config(self):
@@ -279,7 +283,8 @@ class BarnesHutWorkload:
         self.ref64 = ref.cpu().numpy()
         idx_t = idx
 
-        def measure(theta, flags):
+        def measure(theta, flags, alpha=None):
+            self.alpha = alpha
             for _ in range(2):
                 self._run(theta, flags)
             e0 = torch.cuda.Event(enable_timing=True)
@@ -292,8 +297,8 @@ class BarnesHutWorkload:
             ms = e0.elapsed_time(e1) / 3
             e = rel_err(self.d_out[idx_t].cpu().numpy(), self.ref64)
             return {"theta": theta, "quadrupole": bool(flags & 1), "group": bool(flags & 2),
-                    "learned": bool(flags & 4), "local": bool(flags & 8), "ms": ms, "bodies_per_s": self.n / (ms * 1e-3),
-                    **err_stats(e)}
+                    "learned": bool(flags & 4), "local": bool(flags & 8), "relative": alpha, "ms": ms,
+                    "bodies_per_s": self.n / (ms * 1e-3), **err_stats(e)}
 
         self.plain = measure(0.5, 0)
         # the learned correction at theta 1.0 (model trained by `python -m
@@ -310,20 +315,27 @@ class BarnesHutWorkload:
             self.learned_row = row
             self.plain_theta1 = measure(1.0, 3)
         ok = []
-        for theta, flags in self.ladder:
-            row = measure(theta, flags)
+        for theta, flags, alpha in self.ladder:
+            row = measure(theta, flags, alpha)
             self.table.append(row)
             if row["p95"] <= self.bar:
                 ok.append(row)
         best = max(ok, key=lambda r: r["bodies_per_s"]) if ok else min(self.table, key=lambda r: r["p95"])
         self.meets_bar = bool(ok)
         self.theta = best["theta"]
+        self.alpha = best.get("relative")
         self.flags = ((1 if best["quadrupole"] else 0) | (2 if best["group"] else 0)
-                      | (8 if best.get("local") else 0))
+                      | (8 if best.get("local") else 0) | (16 if self.alpha is not None else 0))
         self.selected = best
+
+    def _set_alpha(self, flags):
+        from particular_gb300 import _native as N
+        if flags & 16:
+            N.check(N.lib().pt_bh_set_relative_alpha(self.res.handle, self.alpha))
 
     def _run(self, theta, flags):
         from particular_gb300 import _native as N
+        self._set_alpha(flags)
         N.check(N.lib().pt_bh_accel_f32_device(self.res.handle, self.d_b.data_ptr(), self.n,
                                                self.d_b.data_ptr(), self.n, theta,
                                                self.softening, flags, self.d_out.data_ptr()))
@@ -333,6 +345,7 @@ class BarnesHutWorkload:
 
     def step_e2e(self):
         from particular_gb300 import _native as N
+        self._set_alpha(self.flags)
         N.check(N.lib().pt_bh_accel_f32(self.res.handle, self.h_b.data_ptr(), self.n,
                                         self.h_b.data_ptr(), self.n, self.theta, self.softening,
                                         self.flags, self.h_out.data_ptr()))
@@ -401,7 +414,7 @@ class BarnesHutWorkload:
     def extra(self):
         return {"method": {"name": "cuda::BarnesHut", "theta": self.theta,
                            "quadrupole": bool(self.flags & 1), "group": bool(self.flags & 2),
-                           "local": bool(self.flags & 8)},
+                           "local": bool(self.flags & 8), "relative_alpha": self.alpha},
                 "selected": self.selected, "meets_bar": self.meets_bar,
                 "calibration": self.table, "plain_reference_rule": self.plain,
                 "learned_theta1": self.learned_row,

@@ -162,7 +162,8 @@ int pt_bf_accel_f32_noalloc(const float *d_affected, size_t n_aff, const float *
  * an internal cell when theta^2 d^2 < w^2 (w = cell width), otherwise add the
  * node's monopole through the per-pair kernel. Because coincident nodes are always
  * skipped, Acceleration's CHECKED flag has no effect on this method, as in the
- * reference. Moments are accumulated in FP64 and stored in f32. */
+ * reference. Cell moments are combined bottom-up about each cell's geometric centre
+ * (compensated FP32) and stored in f32. */
 #define PT_BH_QUADRUPOLE 0x1u /* add the traceless quadrupole of accepted cells */
 #define PT_BH_GROUP 0x2u      /* walk per warp of 64 key-adjacent bodies (two per lane):
                                  a cell is opened for all of them when the per-body rule
@@ -173,6 +174,11 @@ int pt_bf_accel_f32_noalloc(const float *d_affected, size_t n_aff, const float *
                                  distance, pt_bh_set_local_ratio, default 0.1) enter
                                  a second-order local expansion about the group's
                                  centre instead of every body's interaction list */
+#define PT_BH_RELATIVE 0x10u  /* with PT_BH_GROUP: also open a cell where its truncation
+                                 bound M w^3 / d^5 (M w^2 / d^4 without quadrupoles)
+                                 exceeds alpha |a| (pt_bh_set_relative_alpha, default
+                                 2.5e-3), |a| estimated once per group at its centre by
+                                 a coarse walk; theta stays the geometric cap */
 #define PT_BH_LEARNED 0x4u    /* with PT_BH_GROUP: add the learned far-field correction
                                  (pt_mlp_*) of every cell accepted at theta that the
                                  model's inner angle would have opened, evaluated once
@@ -224,6 +230,9 @@ int pt_bh_walk(pt_ctx *ctx, const float *affected, size_t n_aff, float theta, fl
                uint32_t flags, float *out_xyz);
 /* The far ratio of PT_BH_LOCAL, in (0, 0.5]: smaller is more accurate and slower. */
 int pt_bh_set_local_ratio(pt_ctx *ctx, float ratio);
+/* The error-bound factor of PT_BH_RELATIVE, in (0, 1]: smaller is more accurate and
+ * slower. */
+int pt_bh_set_relative_alpha(pt_ctx *ctx, float alpha);
 /* Caps the PT_BH_GROUP walk's shared-memory stack at `ranges` entries per warp (2 to
  * the compiled capacity; 0 restores the capacity). A warp that runs out takes the
  * per-body walk instead (counted in pt_bh_stats.overflow): a tuning and test hook. */

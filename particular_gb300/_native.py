@@ -24,6 +24,7 @@ PT_BH_QUADRUPOLE = 0x1
 PT_BH_GROUP = 0x2
 PT_BH_LEARNED = 0x4
 PT_BH_LOCAL = 0x8
+PT_BH_RELATIVE = 0x10
 PT_MLP_NPARAM = 5188
 PT_METHOD_BRUTE_FORCE = 0
 PT_METHOD_BARNES_HUT = 1
@@ -96,6 +97,7 @@ def _declare(L):
         "pt_bh_last_stats": (ctypes.c_int, [c_ptr, ctypes.POINTER(BhStats)]),
         "pt_bh_set_stack_limit": (ctypes.c_int, [c_ptr, ctypes.c_int]),
         "pt_bh_set_local_ratio": (ctypes.c_int, [c_ptr, ctypes.c_float]),
+        "pt_bh_set_relative_alpha": (ctypes.c_int, [c_ptr, ctypes.c_float]),
         "pt_bh_accel_dvec3": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr, ctypes.c_size_t,
                                              ctypes.c_double, ctypes.c_double, ctypes.c_uint32, c_ptr]),
         "pt_bh_accel_dvec3_device": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr, ctypes.c_size_t,

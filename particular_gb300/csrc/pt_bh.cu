@@ -10,7 +10,7 @@ int validate(const char *fn, size_t n_aff, size_t n_src, uint32_t flags) {
     const size_t lim = size_t(INT_MAX) / 8;
     if (n_aff > lim || n_src > lim)
         return set_error(PT_ERR_INVALID, "%s: n_aff=%zu n_src=%zu exceed the limit %zu", fn, n_aff, n_src, lim);
-    if (flags & ~(PT_BH_QUADRUPOLE | PT_BH_GROUP | PT_BH_LEARNED | PT_BH_LOCAL))
+    if (flags & ~(PT_BH_QUADRUPOLE | PT_BH_GROUP | PT_BH_LEARNED | PT_BH_LOCAL | PT_BH_RELATIVE))
         return set_error(PT_ERR_INVALID, "%s: unknown flags 0x%x", fn, flags);
     if ((flags & PT_BH_LEARNED) && !(flags & PT_BH_GROUP))
         return set_error(PT_ERR_INVALID, "%s: PT_BH_LEARNED requires PT_BH_GROUP", fn);
@@ -18,6 +18,10 @@ int validate(const char *fn, size_t n_aff, size_t n_src, uint32_t flags) {
         return set_error(PT_ERR_INVALID, "%s: PT_BH_LOCAL requires PT_BH_GROUP", fn);
     if ((flags & PT_BH_LOCAL) && (flags & PT_BH_LEARNED))
         return set_error(PT_ERR_INVALID, "%s: PT_BH_LOCAL and PT_BH_LEARNED are exclusive", fn);
+    if ((flags & PT_BH_RELATIVE) && !(flags & PT_BH_GROUP))
+        return set_error(PT_ERR_INVALID, "%s: PT_BH_RELATIVE requires PT_BH_GROUP", fn);
+    if ((flags & PT_BH_RELATIVE) && (flags & PT_BH_LEARNED))
+        return set_error(PT_ERR_INVALID, "%s: PT_BH_RELATIVE and PT_BH_LEARNED are exclusive", fn);
     return PT_OK;
 }
 
@@ -69,7 +73,7 @@ void pt_bh_state_free(pt_ctx *ctx) {
                      &S->nodeA,  &S->nodeB,  &S->nodeQ,  &S->nodeG, &S->nodeR, &S->mom,     &S->tkeys,  &S->tidx,
                      &S->tbody,    &S->counters, &S->out,  &S->aff_h,  &S->src_h, &S->lrec, &S->lgroup,
                      &S->lnext,    &S->lpart,  &S->lhead, &S->lcentre, &S->lused, &S->sbody64, &S->nodeA64,
-                     &S->nodeG64,  &S->tbody64};
+                     &S->nodeG64,  &S->tbody64, &S->gscale};
     for (DevBuf *b : all) free_buf(ctx, *b);
     delete S;
     ctx->bh = nullptr;
@@ -287,6 +291,18 @@ int pt_bh_set_local_ratio(pt_ctx *ctx, float ratio) {
     bh::State *S = bh::state(ctx);
     if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
     S->local_ratio = ratio;
+    return PT_OK;
+}
+
+int pt_bh_set_relative_alpha(pt_ctx *ctx, float alpha) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_set_relative_alpha: ctx is NULL");
+    if (!(alpha > 0.0f && alpha <= 1.0f))
+        return set_error(PT_ERR_INVALID, "pt_bh_set_relative_alpha: %g outside (0, 1]", double(alpha));
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    S->rel_alpha = alpha;
     return PT_OK;
 }
 

@@ -69,11 +69,13 @@ struct State {
     DevBuf out;
     DevBuf aff_h, src_h;  // staging for the host-pointer entry point
     DevBuf lrec, lgroup, lnext, lpart, lhead, lcentre, lused;  // learned-correction records
+    DevBuf gscale;                    // PT_BH_RELATIVE: 1 / (alpha |a|) per group
     int lcap = 0;                     // record chunks allocated
     int stack_cap = 0;                // group-walk stack ranges per warp in use (0 = all)
     uint64_t generation = 0;          // trees built so far (0 = none)
     bool f64 = false;                 // the current tree was built over DVec3 bodies
     float local_ratio = 0.1f;         // PT_BH_LOCAL: far when group radius < ratio * distance
+    float rel_alpha = 2.5e-3f;        // PT_BH_RELATIVE: opened where the bound exceeds alpha |a|
     const uint32_t *mlp_w = nullptr;  // learned correction: packed BF16 weights (owned by the MLP state)
     const float *mlp_b = nullptr;     // and its bias block
     float theta_inner = 0.5f;

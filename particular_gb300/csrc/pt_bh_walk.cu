@@ -3,7 +3,9 @@
 //    shared traversal per warp (accept/open masks on stack ranges and list entries);
 //  * bh_walk_group (PT_BH_GROUP): a cell opened for all 64 bodies of a warp when any
 //    of them opens it, lists evaluated densely, optional quadrupoles, local
-//    expansions of far nodes (PT_BH_LOCAL) and the learned correction's records;
+//    expansions of far nodes (PT_BH_LOCAL), the error-bound opening radius
+//    (PT_BH_RELATIVE, with its per-group estimate bh_group_scale) and the learned
+//    correction's records;
 //  * bh_walk64: the reference rule over DVec3 bodies in double;
 //  * lane_walk: the per-body cursor walk the others fall back to when a stack runs out.
 #include "pt_bh.cuh"
@@ -13,6 +15,15 @@ namespace bh {
 
 // ---- walk ------------------------------------------------------------------
 
+// PT_BH_RELATIVE: a cell of mass m and width w is also opened within squared distance
+// r2, where its truncation bound m w^p / d^(p+2) (p = 3 with quadrupoles, 2 without)
+// reaches alpha |a|; ginv = 1 / (alpha |a|) of the target's group, 0 when off.
+template <bool QUAD>
+__device__ __forceinline__ float rel_r2(float m, float w, float ginv) {
+    if (!(ginv > 0.f && m > 0.f)) return 0.f;
+    return QUAD ? __powf(m * w * w * w * ginv, 0.4f) : sqrtf(m * w * w * ginv);
+}
+
 // The reference's per-body walk (sequential.rs) for this lane's target p, the cursor
 // being the warp minimum of the lanes' next nodes: all 32 lanes take part. Adds the
 // accepted nodes' accelerations to (ax, ay, az) and counts them.
@@ -21,7 +32,7 @@ __device__ __forceinline__ void lane_walk(float4 p, bool valid, int T, const flo
                                           const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
                                           const float4 *__restrict__ sbody, float th2, float eps2, float &ax,
                                           float &ay, float &az, unsigned &nacc, unsigned &nvisit,
-                                          unsigned &ncell) {
+                                          unsigned &ncell, float ginv = 0.f) {
     int resume = valid ? 0 : T;
     int node = 0;
     while (node < T) {
@@ -37,7 +48,7 @@ __device__ __forceinline__ void lane_walk(float4 p, bool valid, int T, const flo
             d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             zero = (d2 == 0.0f);
             const float w = __int_as_float(B.x);
-            open = !zero && B.z < 0 && th2 * d2 < w * w;
+            open = !zero && B.z < 0 && (th2 * d2 < w * w || d2 < rel_r2<QUAD>(A.w, w, ginv));
         }
         int next = resume;
         if (active) {
@@ -375,15 +386,16 @@ static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
 #ifndef PT_GW_MINB
 #define PT_GW_MINB (GW_TPL == 1 ? 6 : 5)  // CTAs per SM the register budget is set for
 #endif
-template <bool QUAD, bool GUARD, bool LEARNED, bool LOCAL>
+template <bool QUAD, bool GUARD, bool LEARNED, bool LOCAL, bool REL>
 __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
     bh_walk_group(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
                   const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
                   const float4 *__restrict__ nodeG, const float4 *__restrict__ sbody, const int *__restrict__ counters,
                   float th2, float th_in2, LearnedRecords LR, float eps2, float *__restrict__ out,
                   unsigned long long *__restrict__ stats, int *__restrict__ err, int stack_cap,
-                  float local_ratio) {
+                  float local_ratio, const float *__restrict__ gscale) {
     static_assert(!(LEARNED && LOCAL), "PT_BH_LEARNED and PT_BH_LOCAL are exclusive");
+    static_assert(!(LEARNED && REL), "PT_BH_LEARNED and PT_BH_RELATIVE are exclusive");
     constexpr int NFC = QUAD ? 10 : 4;
     constexpr int TPL = GW_TPL;
     using CellList = IList<NFC, 96>;
@@ -412,6 +424,8 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
     }
     const int nvalid = min(GW_GROUP, n_aff - g0);
     const unsigned lt = (1u << lane) - 1u;
+    // PT_BH_RELATIVE: 1 / (alpha |a|) of this group (warp-uniform)
+    const float ginv = REL ? gscale[group] : 0.f;
     int2 *stack = s_stack[warp];
     const int T = counters[1];
     CellList &Lc = s_cells[warp];
@@ -507,19 +521,23 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
         // from its farthest corner (sure). Rounding is monotone, so these box bounds
         // never contradict the per-target values. The remaining cells are voted on one
         // at a time: each lane tests its own target, a ballot collects the votes.
+        // PT_BH_RELATIVE adds a second opening radius per cell (rr2), tested the same way.
         bool maybe = false, sure = false;
-        float w = 0.f;
+        float w = 0.f, rr2 = 0.f;
         if (have && B.z < 0) {
             w = __int_as_float(B.x);
+            if (REL) rr2 = rel_r2<QUAD>(A.w, w, ginv);
             const float e0 = fmaxf(fmaxf(mn0 - A.x, A.x - mx0), 0.f);
             const float e1 = fmaxf(fmaxf(mn1 - A.y, A.y - mx1), 0.f);
             const float e2b = fmaxf(fmaxf(mn2 - A.z, A.z - mx2), 0.f);
-            maybe = (LEARNED ? th_in2 : th2) * fmaf(e0, e0, fmaf(e1, e1, e2b * e2b)) < w * w;
+            const float emin2 = fmaf(e0, e0, fmaf(e1, e1, e2b * e2b));
+            maybe = (LEARNED ? th_in2 : th2) * emin2 < w * w || (REL && emin2 < rr2);
             const float f0 = fmaxf(A.x - mn0, mx0 - A.x);
             const float f1 = fmaxf(A.y - mn1, mx1 - A.y);
             const float f2b = fmaxf(A.z - mn2, mx2 - A.z);
             const float dmax2 = fmaf(f0, f0, fmaf(f1, f1, f2b * f2b));
-            sure = dmax2 > 0.0f && th2 * dmax2 < w * w;  // dmax2 > 0: some target is off the centre of mass
+            // dmax2 > 0: some target is off the centre of mass
+            sure = dmax2 > 0.0f && (th2 * dmax2 < w * w || (REL && dmax2 < rr2));
         }
         open = sure;
         bool marginal = false;
@@ -531,20 +549,22 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
             const float cy = __shfl_sync(0xffffffffu, A.y, j);
             const float cz = __shfl_sync(0xffffffffu, A.z, j);
             const float cw = __shfl_sync(0xffffffffu, w, j);
+            const float crr = REL ? __shfl_sync(0xffffffffu, rr2, j) : 0.f;
             bool o1 = false, i1 = false;
             const float cw2 = cw * cw;
             if constexpr (TPL == 2) {  // both targets in one packed pass (same IEEE ops)
                 const f2 dx = sub2(pk2(cx, cx), vx01), dy = sub2(pk2(cy, cy), vy01), dz = sub2(pk2(cz, cz), vz01);
                 float d0, d1;
                 upk2(fma2(dx, dx, fma2(dy, dy, mul2(dz, dz))), d0, d1);
-                o1 = (d0 > 0.0f && th2 * d0 < cw2) || (d1 > 0.0f && th2 * d1 < cw2);
+                o1 = (d0 > 0.0f && (th2 * d0 < cw2 || (REL && d0 < crr))) ||
+                     (d1 > 0.0f && (th2 * d1 < cw2 || (REL && d1 < crr)));
                 if (LEARNED) i1 = (d0 > 0.0f && th_in2 * d0 < cw2) || (d1 > 0.0f && th_in2 * d1 < cw2);
             } else {
 #pragma unroll
                 for (int i = 0; i < TPL; ++i) {
                     const float dx = cx - p[i].x, dy = cy - p[i].y, dz = cz - p[i].z;
                     const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    o1 |= d2 > 0.0f && th2 * d2 < cw2;
+                    o1 |= d2 > 0.0f && (th2 * d2 < cw2 || (REL && d2 < crr));
                     if (LEARNED) i1 |= d2 > 0.0f && th_in2 * d2 < cw2;
                 }
             }
@@ -732,7 +752,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
         for (int i = 0; i < TPL; ++i) {
             rx[i] = ry[i] = rz[i] = 0.f;
             lane_walk<QUAD>(p[i], valid[i], T, nodeA, nodeB, nodeQ, sbody, th2, eps2, rx[i], ry[i], rz[i], na, nvis,
-                            nc);
+                            nc, ginv);
         }
         unsigned long long a = na, v = nvis, c = nc;
 #pragma unroll
@@ -771,6 +791,52 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
         atomicMax(stats + 3, (unsigned long long)maxS);
         if (failed) atomicAdd(stats + 6, 1ull);
     }
+}
+
+// PT_BH_RELATIVE: |a| estimated at the centre of each group's box by a per-point
+// cursor walk at theta = 1 with monopoles; gscale[g] = 1 / (alpha |a|), the factor
+// of the group walk's error bound. The node index only grows: the loop ends.
+__global__ void __launch_bounds__(128)
+    bh_group_scale(const float4 *__restrict__ tbody, int n_aff, const float4 *__restrict__ nodeA,
+                   const int4 *__restrict__ nodeB, const int *__restrict__ counters, float eps2, float alpha,
+                   float *__restrict__ gscale) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g0 = g * GW_GROUP;
+    if (g0 >= n_aff) return;
+    const int g1 = min(n_aff, g0 + GW_GROUP);
+    float4 p = tbody[g0];
+    float mn0 = p.x, mn1 = p.y, mn2 = p.z, mx0 = p.x, mx1 = p.y, mx2 = p.z;
+    for (int t = g0 + 1; t < g1; ++t) {
+        p = tbody[t];
+        mn0 = fminf(mn0, p.x), mn1 = fminf(mn1, p.y), mn2 = fminf(mn2, p.z);
+        mx0 = fmaxf(mx0, p.x), mx1 = fmaxf(mx1, p.y), mx2 = fmaxf(mx2, p.z);
+    }
+    const float cx = 0.5f * (mn0 + mx0), cy = 0.5f * (mn1 + mx1), cz = 0.5f * (mn2 + mx2);
+    const int T = counters[1];
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    for (int node = 0; node < T;) {
+        const float4 A = __ldg(nodeA + node);
+        const int4 B = __ldg(nodeB + node);
+        const float dx = A.x - cx, dy = A.y - cy, dz = A.z - cz;
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (B.z < 0) {
+            const float w = __int_as_float(B.x);
+            if (d2 < w * w) {  // theta = 1: open
+                ++node;
+                continue;
+            }
+        }
+        if (d2 > 0.f) {
+            const float inv = rsqrt_ftz(d2 + eps2);
+            const float s = (A.w * inv) * (inv * inv);
+            ax = fmaf(dx, s, ax);
+            ay = fmaf(dy, s, ay);
+            az = fmaf(dz, s, az);
+        }
+        node = B.y;
+    }
+    const float a = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+    gscale[g] = 1.f / (alpha * fmaxf(a, 1e-30f));
 }
 
 // ---- masked group walk: the reference's rule, per body, with shared traversal ----
@@ -1340,23 +1406,24 @@ using WalkKernel = void (*)(const float4 *, const uint32_t *, int, const float4 
                             const float4 *, const int *, float, float, float *, unsigned long long *);
 using GroupKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
                              const float4 *, const float4 *, const int *, float, float, LearnedRecords, float,
-                             float *, unsigned long long *, int *, int, float);
+                             float *, unsigned long long *, int *, int, float, const float *);
 
 static WalkKernel masked_kernel(bool quad, bool guard) {
     if (quad) return guard ? bh_walk_masked<true, true> : bh_walk_masked<true, false>;
     return guard ? bh_walk_masked<false, true> : bh_walk_masked<false, false>;
 }
 
-template <bool LEARNED, bool LOCAL>
+template <bool LEARNED, bool LOCAL, bool REL>
 static GroupKernel group_kernel_q(bool quad, bool guard) {
-    if (quad) return guard ? bh_walk_group<true, true, LEARNED, LOCAL> : bh_walk_group<true, false, LEARNED, LOCAL>;
-    return guard ? bh_walk_group<false, true, LEARNED, LOCAL> : bh_walk_group<false, false, LEARNED, LOCAL>;
+    if (quad)
+        return guard ? bh_walk_group<true, true, LEARNED, LOCAL, REL> : bh_walk_group<true, false, LEARNED, LOCAL, REL>;
+    return guard ? bh_walk_group<false, true, LEARNED, LOCAL, REL> : bh_walk_group<false, false, LEARNED, LOCAL, REL>;
 }
 
-static GroupKernel group_kernel(bool quad, bool guard, bool learned, bool local) {
-    if (learned) return group_kernel_q<true, false>(quad, guard);
-    if (local) return group_kernel_q<false, true>(quad, guard);
-    return group_kernel_q<false, false>(quad, guard);
+static GroupKernel group_kernel(bool quad, bool guard, bool learned, bool local, bool rel) {
+    if (learned) return group_kernel_q<true, false, false>(quad, guard);
+    if (local) return rel ? group_kernel_q<false, true, true>(quad, guard) : group_kernel_q<false, true, false>(quad, guard);
+    return rel ? group_kernel_q<false, false, true>(quad, guard) : group_kernel_q<false, false, false>(quad, guard);
 }
 
 
@@ -1447,6 +1514,15 @@ int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n
             PT_TRY(ensure_buf(ctx, S.lused, sizeof(int)));
             if (S.lcap == 0) S.lcap = std::max(1024, 2 * groups);
         }
+        const float *gscale = nullptr;
+        if (flags & PT_BH_RELATIVE) {
+            PT_TRY(ensure_buf(ctx, S.gscale, sizeof(float) * size_t(groups)));
+            bh_group_scale<<<blocks(groups, 128), 128, 0, st>>>(tbody, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB),
+                                                                as<int>(S.counters), eps2, S.rel_alpha,
+                                                                as<float>(S.gscale));
+            PT_TRY(check_launch(ctx, "bh_group_scale"));
+            gscale = as<float>(S.gscale);
+        }
         for (int attempt = 0;; ++attempt) {
             if (learned) {
                 PT_TRY(ensure_buf(ctx, S.lrec, sizeof(int) * size_t(S.lcap) * LCHUNK));
@@ -1457,11 +1533,11 @@ int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n
                                     as<float4>(S.lcentre), as<float4>(S.lpart), as<int>(S.lused), S.lcap};
                 PT_CUDA(cudaMemsetAsync(LR.used, 0, sizeof(int), st));
             }
-            group_kernel(quad, eps2 == 0.0f, learned, flags & PT_BH_LOCAL)<<<(groups + GW_WARPS - 1) / GW_WARPS,
+            group_kernel(quad, eps2 == 0.0f, learned, flags & PT_BH_LOCAL, gscale != nullptr)<<<(groups + GW_WARPS - 1) / GW_WARPS,
                                                                           32 * GW_WARPS, 0, st>>>(
                 tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.nodeG),
                 as<float4>(S.sbody), as<int>(S.counters), th2, S.theta_inner * S.theta_inner, LR, eps2, d_out, stats,
-                err, S.stack_cap > 0 ? S.stack_cap : GW_STACK, S.local_ratio);
+                err, S.stack_cap > 0 ? S.stack_cap : GW_STACK, S.local_ratio, gscale);
             PT_TRY(check_launch(ctx, "bh_walk_group"));
             // Outside stream capture the record count is checked and the walk rerun
             // with room for all records; inside, an overflow sets error bit 2.

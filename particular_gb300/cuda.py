@@ -158,10 +158,13 @@ class BarnesHut:
     local=True (with group) sends nodes far from the group into a second-order
     local expansion about the group's centre (resources-wide ratio:
     pt_bh_set_local_ratio); its truncation error is judged against FP64.
+    relative=alpha (with group) also opens a cell where its truncation bound
+    M w^3 / d^5 (M w^2 / d^4 without quadrupoles) exceeds alpha |a|, |a| estimated
+    once per group; theta stays the geometric cap.
     """
 
     def __init__(self, theta, resources, interaction, quadrupole=False, group=False,
-                 learned=False, local=False, dvec3=False):
+                 learned=False, local=False, dvec3=False, relative=None):
         self.dvec3 = bool(dvec3)  # glam DVec3 bodies: the f64 method (reference rule only)
         self.theta64 = float(theta)
         self.theta = float(np.float32(theta))
@@ -171,11 +174,17 @@ class BarnesHut:
         self.group = bool(group)
         self.learned = bool(learned)  # needs a model (particular_gb300.learned) and group
         self.local = bool(local)      # far nodes through the group's local expansion
+        self.relative = None if relative is None else float(relative)  # error-bound factor alpha
 
     @property
     def flags(self):
         return ((N.PT_BH_QUADRUPOLE if self.quadrupole else 0) | (N.PT_BH_GROUP if self.group else 0)
-                | (N.PT_BH_LEARNED if self.learned else 0) | (N.PT_BH_LOCAL if self.local else 0))
+                | (N.PT_BH_LEARNED if self.learned else 0) | (N.PT_BH_LOCAL if self.local else 0)
+                | (N.PT_BH_RELATIVE if self.relative is not None else 0))
+
+    def _set_alpha(self):
+        if self.relative is not None:
+            N.check(N.lib().pt_bh_set_relative_alpha(self.resources.handle, self.relative))
 
     def build(self, affecting):
         """Builds the tree over `affecting` (any storage of particles) once; pass the
@@ -209,6 +218,7 @@ class BarnesHut:
                 raise N.CudaError(N.PT_ERR_INVALID, "the tree was replaced by a later Barnes-Hut call")
             aff = positions(b.affected)
             out = np.zeros((aff.shape[0], 3), np.float32)
+            self._set_alpha()
             if aff.shape[0]:
                 N.check(N.lib().pt_bh_walk(self.resources.handle, _ptr(aff), aff.shape[0], self.theta,
                                            self.interaction.softening, self.flags, _ptr(out)))
@@ -219,6 +229,7 @@ class BarnesHut:
         if aff.shape[0] == 0:
             return out
         same = b.affected is b.affecting
+        self._set_alpha()
         N.check(N.lib().pt_bh_accel_f32(self.resources.handle, _ptr(aff), aff.shape[0],
                                         _ptr(aff) if same else _ptr(src), src.shape[0], self.theta,
                                         self.interaction.softening, self.flags, _ptr(out)))

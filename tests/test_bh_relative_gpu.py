@@ -1,0 +1,130 @@
+"""PT_BH_RELATIVE: the group walk also opens a cell where its truncation bound
+M w^3 / d^5 (M w^2 / d^4 without quadrupoles) exceeds alpha |a|, |a| estimated once
+per group by a coarse walk from the group's centre; theta stays the geometric cap.
+Judged against the FP64 brute force of the oracle."""
+import numpy as np
+import pytest
+
+from particular_gb300 import Acceleration, AccelerationSoftened, Between, cuda, ics
+from particular_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, ref):
+    a = np.asarray(a, np.float64)
+    ref = np.asarray(ref, np.float64)
+    return np.linalg.norm(a - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-30)
+
+
+def bh(res, theta, **kw):
+    return cuda.BarnesHut(theta, res, AccelerationSoftened(0.01), group=True, **kw)
+
+
+@pytest.mark.parametrize("quad", [False, True])
+def test_opens_at_least_what_the_cap_opens(res, oracle, quad):
+    """rr2 >= 0 only adds openings to the geometric rule at the same theta: more
+    accepted nodes, and an error no larger on every reported percentile."""
+    b = ics.bulge_disk(30000, seed=61)["bodies"]
+    ref64 = oracle.bf_f64(b[::10], b, 0.01, True)
+    geo = bh(res, 0.6, quadrupole=quad)
+    e0 = rel(geo.compute(b)[::10], ref64)
+    s0 = geo.stats()
+    m = bh(res, 0.6, quadrupole=quad, relative=2.5e-3)
+    e1 = rel(m.compute(b)[::10], ref64)
+    s1 = m.stats()
+    assert s1["interactions"] > s0["interactions"] and s1["overflow"] == 0
+    for q in (50, 95, 99):
+        assert np.percentile(e1, q) <= np.percentile(e0, q) * 1.01 + 1e-7, q
+
+
+def test_tiny_alpha_is_the_direct_sum(res, oracle):
+    """With alpha -> 0 every cell is opened: the walk sums all bodies directly."""
+    b = ics.plummer(4000, seed=62)["bodies"]
+    m = bh(res, 1.0, quadrupole=True, relative=1e-30)
+    got = m.compute(b)
+    st = m.stats()
+    assert st["cell_interactions"] == 0
+    assert st["interactions"] >= 4000 * 3990
+    ref = oracle.bf_f32(b, b, 0.01, True)
+    d = rel(got, ref)
+    assert np.median(d) < 1e-6 and d.max() < 1e-4
+
+
+@pytest.mark.parametrize("kind", ["plummer", "bulge_disk"])
+def test_error_and_work_follow_alpha(res, oracle, kind):
+    """Smaller alpha: more work, smaller error. At alpha 2.5e-3 under a theta-1 cap the
+    walk needs fewer list entries than the geometric theta-0.5 walk for an error of
+    the same order."""
+    b = {"plummer": lambda: ics.plummer(60000, seed=63)["bodies"],
+         "bulge_disk": lambda: ics.bulge_disk(60000, seed=64)["bodies"]}[kind]()
+    ref64 = oracle.bf_f64(b[::20], b, 0.01, True)
+    geo = bh(res, 0.5, quadrupole=True)
+    eg = rel(geo.compute(b)[::20], ref64)
+    sg = geo.stats()
+    rows = []
+    for alpha in (1e-3, 2.5e-3, 1e-2):
+        m = bh(res, 1.0, quadrupole=True, relative=alpha)
+        e = rel(m.compute(b)[::20], ref64)
+        rows.append((alpha, m.stats()["interactions"], np.percentile(e, 95), e.max()))
+    print(f"{kind}: geometric 0.5: {sg['interactions']} entries, p95 {np.percentile(eg, 95):.2e}; "
+          + "; ".join(f"alpha {a:g}: {n} entries, p95 {p:.2e}, max {x:.2e}" for a, n, p, x in rows))
+    assert rows[0][1] > rows[1][1] > rows[2][1]
+    assert rows[0][2] < rows[1][2] < rows[2][2]
+    assert rows[1][1] < sg["interactions"]
+    assert rows[1][2] < 3 * np.percentile(eg, 95)
+
+
+def test_with_local_expansion_separate_targets_and_eps0(res, oracle):
+    """With the local expansion, separate targets (massless, outside the sources) and
+    no softening: finite, and within 10 % of the same walk without the expansion."""
+    src = ics.plummer(30000, seed=65)["bodies"]
+    tgt = ics.uniform_cube(3000, 66)["bodies"] * 3.0
+    tgt[:, 3] = 0.0
+    for it, eps in ((AccelerationSoftened(0.01), 0.01), (Acceleration.checked(), 0.0)):
+        ref64 = oracle.bf_f64(tgt, src, eps, True)
+        kw = dict(quadrupole=True, group=True, relative=2.5e-3)
+        plain = cuda.BarnesHut(1.0, res, it, **kw).compute(Between(tgt, src))
+        local = cuda.BarnesHut(1.0, res, it, local=True, **kw).compute(Between(tgt, src))
+        assert np.isfinite(local).all()
+        e0, e1 = rel(plain, ref64), rel(local, ref64)
+        for q in (50, 95, 99):
+            assert np.percentile(e1, q) <= 1.1 * np.percentile(e0, q) + 1e-7, (eps, q)
+
+
+def test_stack_fallback_keeps_the_criterion(res, oracle):
+    """Warps whose stack runs out take the per-body walk with the same two opening
+    radii: its error stays of the group walk's order."""
+    b = ics.plummer(20000, seed=67)["bodies"]
+    ref64 = oracle.bf_f64(b[::4], b, 0.01, True)
+    m = bh(res, 1.0, quadrupole=True, relative=2.5e-3)
+    e0 = rel(m.compute(b)[::4], ref64)
+    L = N.lib()
+    try:
+        N.check(L.pt_bh_set_stack_limit(res.handle, 2))
+        got = m.compute(b)
+        st = m.stats()
+        assert st["overflow"] == st["warps"] > 0
+    finally:
+        N.check(L.pt_bh_set_stack_limit(res.handle, 0))
+    e1 = rel(got[::4], ref64)
+    assert np.isfinite(got).all()
+    assert np.percentile(e1, 95) <= 3 * np.percentile(e0, 95)
+    # the geometric cap alone (theta 1) is far less accurate: the criterion is applied
+    geo = rel(bh(res, 1.0, quadrupole=True).compute(b)[::4], ref64)
+    assert np.percentile(e1, 95) < 0.5 * np.percentile(geo, 95)
+
+
+def test_relative_flag_validation(res):
+    b = ics.plummer(1000, seed=68)["bodies"]
+    L = N.lib()
+    with pytest.raises(N.CudaError):  # needs group
+        cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), relative=2.5e-3).compute(b)
+    with pytest.raises(N.CudaError):  # not with the learned correction
+        N.check(L.pt_bh_accel_f32(res.handle, b.ctypes.data, 1000, b.ctypes.data, 1000, 0.5, 0.01,
+                                  N.PT_BH_GROUP | N.PT_BH_LEARNED | N.PT_BH_RELATIVE,
+                                  np.zeros((1000, 3), np.float32).ctypes.data))
+    for bad in (0.0, -1.0, 2.0, float("nan")):
+        with pytest.raises(N.CudaError):
+            N.check(L.pt_bh_set_relative_alpha(res.handle, bad))
+    N.check(L.pt_bh_set_relative_alpha(res.handle, 2.5e-3))

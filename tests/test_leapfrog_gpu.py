@@ -48,7 +48,7 @@ def test_leapfrog_matches_oracle_integration(res, oracle):
     assert np.array_equal(b[:, 3], d["bodies"][:, 3])
 
 
-@pytest.mark.parametrize("method", ["bf", "bh", "bh_local", "bh_reference_rule"])
+@pytest.mark.parametrize("method", ["bf", "bh", "bh_local", "bh_relative", "bh_reference_rule"])
 def test_graph_replay_equals_eager(res, method):
     import torch
     d = ics.plummer(20000, seed=52)
@@ -59,6 +59,9 @@ def test_graph_replay_equals_eager(res, method):
         args = (N.PT_METHOD_BARNES_HUT, 0.5, 0.01, N.PT_BH_QUADRUPOLE | N.PT_BH_GROUP)
     elif method == "bh_local":
         args = (N.PT_METHOD_BARNES_HUT, 0.5, 0.01, N.PT_BH_QUADRUPOLE | N.PT_BH_GROUP | N.PT_BH_LOCAL)
+    elif method == "bh_relative":
+        args = (N.PT_METHOD_BARNES_HUT, 1.0, 0.01,
+                N.PT_BH_QUADRUPOLE | N.PT_BH_GROUP | N.PT_BH_LOCAL | N.PT_BH_RELATIVE)
     else:
         args = (N.PT_METHOD_BARNES_HUT, 0.5, 0.01, 0)
     outs = []
