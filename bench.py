@@ -40,6 +40,11 @@ def parse_args():
     p.add_argument("--leapfrog-steps", type=int, default=0,
                    help="leapfrog steps per call for the leapfrog/ensemble workloads "
                         "(default: the workload's own; fewer make short profiling runs)")
+    p.add_argument("--bodies", type=int, default=0,
+                   help="Barnes-Hut workload: bodies (default 4,194,304; smaller cases for profiling)")
+    p.add_argument("--method", default=None,
+                   help="Barnes-Hut workload: 'theta,flags[,alpha[,local ratio]]' instead of the calibration "
+                        "ladder and the comparison rows (short profiling runs)")
     return p.parse_args()
 
 
@@ -237,14 +242,17 @@ class BarnesHutWorkload:
     metric = "bodies/s at <=1e-3 p95 accel err vs FP64"
     unit = "bodies/s"
     bar = 1e-3
-    # (theta, flags, alpha) candidates: quadrupole + group opening; the reference's own
-    # monopole per-body walk at theta 0.5 is measured alongside as "plain".
-    # flags: 1 quadrupole, 2 group, 8 local expansion of far nodes, 16 error-bound
-    # opening (alpha; theta is then the geometric cap)
-    ladder = [(0.45, 3, None), (0.5, 3, None), (0.52, 3, None), (0.55, 3, None), (0.6, 3, None),
-              (0.48, 11, None), (0.5, 11, None), (0.52, 11, None), (0.55, 11, None),
-              (1.0, 19, 1.5e-3), (1.0, 19, 2e-3), (1.0, 19, 2.5e-3), (1.0, 19, 3e-3),
-              (1.0, 27, 1.5e-3), (1.0, 27, 2e-3), (1.0, 27, 2.5e-3), (1.0, 27, 2.75e-3), (1.0, 27, 3e-3)]
+    # (theta, flags, alpha, local ratio) candidates: quadrupole + group opening; the
+    # reference's own monopole per-body walk at theta 0.5 is measured alongside as
+    # "plain". flags: 1 quadrupole, 2 group, 8 local expansion of far nodes (group
+    # radius < ratio x distance), 16 error-bound opening (alpha; theta is then the
+    # geometric cap)
+    ladder = [(0.45, 3, None, 0.1), (0.5, 3, None, 0.1), (0.52, 3, None, 0.1), (0.55, 3, None, 0.1),
+              (0.6, 3, None, 0.1), (0.48, 11, None, 0.1), (0.5, 11, None, 0.1), (0.52, 11, None, 0.1),
+              (0.55, 11, None, 0.1),
+              (1.0, 19, 1.5e-3, 0.1), (1.0, 19, 2e-3, 0.1), (1.0, 19, 2.5e-3, 0.1), (1.0, 19, 3e-3, 0.1),
+              (1.0, 27, 2e-3, 0.1), (1.0, 27, 2.5e-3, 0.1), (1.0, 27, 2.75e-3, 0.1), (1.0, 27, 3e-3, 0.1),
+              (1.0, 27, 2.5e-3, 0.13), (1.0, 27, 2.75e-3, 0.13), (1.0, 27, 3e-3, 0.13)]
 
     def __init__(self, n=4194304, softening=0.01, sample=2048):
         from particular_gb300 import ics
@@ -252,11 +260,13 @@ class BarnesHutWorkload:
         self.softening = softening
         self.bodies = ics.bulge_disk(n, seed=1810)["bodies"]
         self.sample = np.random.default_rng(1808).choice(n, sample, replace=False)
-        self.theta, self.flags, self.alpha = 0.5, 3, None
+        self.theta, self.flags, self.alpha, self.ratio = 0.5, 3, None, 0.1
         self.table = []
+        self.fixed = None  # (theta, flags, alpha, ratio): one configuration, no calibration
 
     def config(self):
-        return {"workload": self.name, "n_bodies": self.n, "softening": self.softening,
+        return {"workload": self.name if self.n == 4194304 else f"bh_bulge_disk_{self.n}",
+                "n_bodies": self.n, "softening": self.softening,
                 "ic": "70% Plummer bulge a=0.5 + 30% exp. disk Rd=2 h=0.05, equal masses, seeded",
                 "step": "full tree rebuild + accelerations of all bodies",
                 "error_judge": "FP64 brute force on a seeded 2048-body sample",
@@ -283,8 +293,8 @@ class BarnesHutWorkload:
         self.ref64 = ref.cpu().numpy()
         idx_t = idx
 
-        def measure(theta, flags, alpha=None):
-            self.alpha = alpha
+        def measure(theta, flags, alpha=None, ratio=0.1):
+            self.alpha, self.ratio = alpha, ratio
             for _ in range(2):
                 self._run(theta, flags)
             e0 = torch.cuda.Event(enable_timing=True)
@@ -297,9 +307,16 @@ class BarnesHutWorkload:
             ms = e0.elapsed_time(e1) / 3
             e = rel_err(self.d_out[idx_t].cpu().numpy(), self.ref64)
             return {"theta": theta, "quadrupole": bool(flags & 1), "group": bool(flags & 2),
-                    "learned": bool(flags & 4), "local": bool(flags & 8), "relative": alpha, "ms": ms,
+                    "learned": bool(flags & 4), "local": bool(flags & 8), "relative": alpha,
+                    "local_ratio": ratio if flags & 8 else None, "ms": ms,
                     "bodies_per_s": self.n / (ms * 1e-3), **err_stats(e)}
 
+        if self.fixed:
+            row = measure(*self.fixed)
+            self.table, self.plain, self.learned_row, self.selected = [row], None, None, row
+            self.theta, self.flags, self.alpha, self.ratio = self.fixed
+            self.meets_bar = row["p95"] <= self.bar
+            return
         self.plain = measure(0.5, 0)
         # the learned correction at theta 1.0 (model trained by `python -m
         # particular_gb300.learned`, shipped in particular_gb300/data)
@@ -315,8 +332,8 @@ class BarnesHutWorkload:
             self.learned_row = row
             self.plain_theta1 = measure(1.0, 3)
         ok = []
-        for theta, flags, alpha in self.ladder:
-            row = measure(theta, flags, alpha)
+        for theta, flags, alpha, ratio in self.ladder:
+            row = measure(theta, flags, alpha, ratio)
             self.table.append(row)
             if row["p95"] <= self.bar:
                 ok.append(row)
@@ -324,6 +341,7 @@ class BarnesHutWorkload:
         self.meets_bar = bool(ok)
         self.theta = best["theta"]
         self.alpha = best.get("relative")
+        self.ratio = best.get("local_ratio") or 0.1
         self.flags = ((1 if best["quadrupole"] else 0) | (2 if best["group"] else 0)
                       | (8 if best.get("local") else 0) | (16 if self.alpha is not None else 0))
         self.selected = best
@@ -332,6 +350,7 @@ class BarnesHutWorkload:
         from particular_gb300 import _native as N
         if flags & 16:
             N.check(N.lib().pt_bh_set_relative_alpha(self.res.handle, self.alpha))
+        N.check(N.lib().pt_bh_set_local_ratio(self.res.handle, self.ratio))
 
     def _run(self, theta, flags):
         from particular_gb300 import _native as N
@@ -414,7 +433,8 @@ class BarnesHutWorkload:
     def extra(self):
         return {"method": {"name": "cuda::BarnesHut", "theta": self.theta,
                            "quadrupole": bool(self.flags & 1), "group": bool(self.flags & 2),
-                           "local": bool(self.flags & 8), "relative_alpha": self.alpha},
+                           "local": bool(self.flags & 8), "relative_alpha": self.alpha,
+                           "local_ratio": self.ratio if self.flags & 8 else None},
                 "selected": self.selected, "meets_bar": self.meets_bar,
                 "calibration": self.table, "plain_reference_rule": self.plain,
                 "learned_theta1": self.learned_row,
@@ -747,9 +767,14 @@ DEFAULT_WORKLOAD = BarnesHutWorkload.name
 
 
 def make_workload(args):
-    wl = WORKLOADS[args.workload or DEFAULT_WORKLOAD]()
+    cls = WORKLOADS[args.workload or DEFAULT_WORKLOAD]
+    wl = cls(n=args.bodies) if args.bodies > 0 and cls is BarnesHutWorkload else cls()
     if args.leapfrog_steps > 0 and hasattr(wl, "steps_per_call"):
         wl.steps_per_call = args.leapfrog_steps
+    if args.method and hasattr(wl, "fixed"):
+        parts = args.method.split(",")
+        wl.fixed = (float(parts[0]), int(parts[1]), float(parts[2]) if len(parts) > 2 and parts[2] else None,
+                    float(parts[3]) if len(parts) > 3 else 0.1)
     return wl
 
 
