@@ -69,7 +69,7 @@ void pt_bh_state_free(pt_ctx *ctx) {
     prim_free(ctx, S->prims);
     DevBuf *all[] = {&S->box_part, &S->box,    &S->keys,   &S->idx,    &S->sbody,   &S->flags,  &S->uscan,
                      &S->ukey,     &S->ufirst, &S->bfirst, &S->blast,  &S->bdelta,  &S->bparent, &S->lparent,
-                     &S->top,      &S->oparent, &S->loparent, &S->cnt, &S->pscan,   &S->pre,    &S->pending,
+                     &S->top,      &S->oparent, &S->loparent, &S->cnt, &S->pscan,   &S->pre,    &S->pending, &S->nkid, &S->kid, &S->cslot, &S->lslot,
                      &S->nodeA,  &S->nodeB,  &S->nodeQ,  &S->nodeG, &S->nodeR, &S->mom,     &S->tkeys,  &S->tidx,
                      &S->tbody,    &S->counters, &S->out,  &S->aff_h,  &S->src_h, &S->lrec, &S->lgroup,
                      &S->lnext,    &S->lpart,  &S->lhead, &S->lcentre, &S->lused, &S->sbody64, &S->nodeA64,
@@ -380,6 +380,11 @@ int pt_bh_export_tree(pt_ctx *ctx, float *com_mass, int32_t *links, float *quad,
     if (links) PT_CUDA(cudaMemcpyAsync(links, S->nodeB.ptr, 16 * st.nodes, cudaMemcpyDeviceToHost, s));
     if (quad) PT_CUDA(cudaMemcpyAsync(quad, S->nodeQ.ptr, 32 * st.nodes, cudaMemcpyDeviceToHost, s));
     PT_CUDA(cudaStreamSynchronize(s));
+    // a cell's last word holds the walk's opening factor on the device: its body
+    // count column reads 0, as documented
+    if (links)
+        for (size_t r = 0; r < st.nodes; ++r)
+            if (links[4 * r + 2] < 0) links[4 * r + 3] = 0;
     return PT_OK;
 }
 

@@ -25,6 +25,7 @@
 //     DVec3 trees. No thread ever waits on another.
 #include "pt_bh.cuh"
 
+#include <cuda/atomic>
 #include <type_traits>
 
 namespace pt {
@@ -222,24 +223,25 @@ __device__ __forceinline__ int climb(int p, const uint8_t *__restrict__ top, con
     return p;
 }
 
-// Octree parents, child counts (pending, zeroed before) and the count of cells
-// starting at each unit.
+// Octree parents, child counts (pending, zeroed before) with each child's slot in
+// its parent's child list, and the count of cells starting at each unit.
 __global__ void octree_links(const int *__restrict__ counters, const int *__restrict__ bfirst,
                              const int *__restrict__ bparent, const int *__restrict__ lparent,
                              const uint8_t *__restrict__ top, int *__restrict__ oparent, int *__restrict__ loparent,
-                             uint32_t *__restrict__ cnt, int *__restrict__ pending) {
+                             uint32_t *__restrict__ cnt, int *__restrict__ pending, uint8_t *__restrict__ cslot,
+                             uint8_t *__restrict__ lslot) {
     const int M = counters[0];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < M - 1 && top[k]) {
         const int op = (k == 0) ? -1 : climb(bparent[k], top, bparent);
         oparent[k] = op;
-        if (op >= 0) atomicAdd(&pending[op], 1);
+        if (op >= 0) cslot[k] = uint8_t(atomicAdd(&pending[op], 1));  // < 8: one child per octant
         atomicAdd(&cnt[bfirst[k]], 1u);
     }
     if (k < M) {
         const int op = (M == 1) ? -1 : climb(lparent[k], top, bparent);
         loparent[k] = op;
-        if (op >= 0) atomicAdd(&pending[op], 1);
+        if (op >= 0) lslot[k] = uint8_t(atomicAdd(&pending[op], 1));
     }
 }
 
@@ -253,7 +255,10 @@ __global__ void layout(int *counters, const int *__restrict__ bfirst,
                        const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ pscan,
                        const uint64_t *__restrict__ ukey, const uint32_t *__restrict__ ufirst,
                        const T *__restrict__ box, int *__restrict__ pre, int4 *__restrict__ nodeB,
-                       typename Prec<T>::V4 *__restrict__ nodeG, int2 *__restrict__ nodeR) {
+                       typename Prec<T>::V4 *__restrict__ nodeG, int2 *__restrict__ nodeR,
+                       const int *__restrict__ loparent, const int *__restrict__ pending,
+                       const uint8_t *__restrict__ cslot, const uint8_t *__restrict__ lslot, int *__restrict__ kid,
+                       int *__restrict__ nkid) {
     using P = Prec<T>;
     const int M = counters[0];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -289,13 +294,19 @@ __global__ void layout(int *counters, const int *__restrict__ bfirst,
         nodeB[pk] = make_int4(sizeof(T) == 4 ? __float_as_int(float(w)) : 0, skip, -1, 0);
         nodeG[pk] = P::make(T(0.5) * (mn0 + mx0), T(0.5) * (mn1 + mx1), T(0.5) * (mn2 + mx2), w);
         nodeR[pk] = make_int2(int(ufirst[b]), int(ufirst[blast[k] + 1]));
+        // the cell's own child count, and its entry in its parent's child list
+        nkid[k] = pending[k];
+        if (k != 0) kid[8 * oparent[k] + cslot[k]] = 2 * pk;
     }
     if (k < M) {
         const int pk = k + int(pscan[k]) + int(cnt[k]);
         const int f = int(ufirst[k]);
-        nodeB[pk] = make_int4(0, pk + 1, f, int(ufirst[k + 1]) - f);
+        const int nb = int(ufirst[k + 1]) - f;
+        nodeB[pk] = make_int4(0, pk + 1, f, nb);
         nodeG[pk] = P::make(T(0), T(0), T(0), T(0));
         nodeR[pk] = make_int2(f, int(ufirst[k + 1]));
+        const int op = loparent[k];
+        if (op >= 0) kid[8 * op + lslot[k]] = 2 * pk + (nb == 1 ? 1 : 0);
     }
 }
 
@@ -417,31 +428,62 @@ __device__ void leaf(int pk, int f, int e, const V4 *__restrict__ sbody, R *rec,
     store_cell(m, pk, rec, nodeA, nodeQ);
 }
 
-__device__ __forceinline__ bool single_body(const int4 &cb) { return cb.z >= 0 && cb.w == 1; }
+// Children of binary cell p: kid[8p .. 8p + nkid[p]) hold 2 x preorder index + 1 for
+// a single body (it has no record: its nodeA is its data). Filled in octree_links'
+// slot order, they are sorted back into preorder, the reference's child order, so
+// every sum runs in a fixed order; their loads are independent of each other.
+struct Kids {
+    int e[8];
+    int n;
+};
+
+__device__ __forceinline__ void cswap(int &a, int &b) {
+    const int lo = min(a, b), hi = max(a, b);
+    a = lo, b = hi;
+}
+
+__device__ __forceinline__ Kids load_kids(int p, const int *__restrict__ kid, const int *__restrict__ nkid) {
+    Kids K;
+    K.n = nkid[p];
+    const int4 a = reinterpret_cast<const int4 *>(kid)[2 * p];
+    const int4 b = reinterpret_cast<const int4 *>(kid)[2 * p + 1];
+    K.e[0] = a.x, K.e[1] = a.y, K.e[2] = a.z, K.e[3] = a.w, K.e[4] = b.x, K.e[5] = b.y, K.e[6] = b.z, K.e[7] = b.w;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+        if (i >= K.n) K.e[i] = INT_MAX;
+    // Batcher's odd-even merge sort of 8 keys (19 compare-exchanges)
+    cswap(K.e[0], K.e[1]), cswap(K.e[2], K.e[3]), cswap(K.e[4], K.e[5]), cswap(K.e[6], K.e[7]);
+    cswap(K.e[0], K.e[2]), cswap(K.e[1], K.e[3]), cswap(K.e[4], K.e[6]), cswap(K.e[5], K.e[7]);
+    cswap(K.e[1], K.e[2]), cswap(K.e[5], K.e[6]);
+    cswap(K.e[0], K.e[4]), cswap(K.e[1], K.e[5]), cswap(K.e[2], K.e[6]), cswap(K.e[3], K.e[7]);
+    cswap(K.e[2], K.e[4]), cswap(K.e[3], K.e[5]);
+    cswap(K.e[1], K.e[2]), cswap(K.e[3], K.e[4]), cswap(K.e[5], K.e[6]);
+    return K;
+}
 
 // f32 trees: one pass over the children in FP32, sums about the cell's geometric
 // centre G, then moved to the centre of mass C by the parallel-axis rule
 // S_C = S_G - P P^T / M with P = sum m (c - G) = M (C - G).
-__device__ void cell(int pv, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeG, Rec32 *rec,
-                     float4 *nodeA, float4 *nodeQ) {
-    const int end = nodeB[pv].y;
+__device__ void cell(int pv, const Kids &K, const float4 *__restrict__ nodeG, Rec32 *rec, float4 *nodeA,
+                     float4 *nodeQ, int4 *nodeB) {
     const float4 g = nodeG[pv];
     float mh = 0.f, ml = 0.f, px = 0.f, py = 0.f, pz = 0.f;
     float sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
     int count = 0;
-    for (int c = pv + 1; c < end;) {
-        const int4 cb = nodeB[c];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        if (i >= K.n) break;
+        const int c = K.e[i] >> 1;
         const float4 a = ld_cg(nodeA + c);
         float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), s0 = lo, s1 = lo;
         int cn = 1;
-        if (!single_body(cb)) {
+        if (!(K.e[i] & 1)) {
             lo = ld_cg(&rec[c].lo);
             s0 = ld_cg(&rec[c].s0);
             s1 = ld_cg(&rec[c].s1);
             cn = __float_as_int(s1.z);
         }
-        const float dx = __fsub_rn(a.x, g.x) + lo.x, dy = __fsub_rn(a.y, g.y) + lo.y,
-                    dz = __fsub_rn(a.z, g.z) + lo.z;
+        const float dx = __fsub_rn(a.x, g.x) + lo.x, dy = __fsub_rn(a.y, g.y) + lo.y, dz = __fsub_rn(a.z, g.z) + lo.z;
         float e;
         mh = two_sum(mh, a.w, e);
         ml += e + lo.w;
@@ -456,7 +498,6 @@ __device__ void cell(int pv, const int4 *__restrict__ nodeB, const float4 *__res
         syz += s1.x + my * dz;
         szz += s1.y + mz * dz;
         count += cn;
-        c = cb.y;
     }
     float e;
     const float M = two_sum(mh, ml, e);
@@ -473,25 +514,29 @@ __device__ void cell(int pv, const int4 *__restrict__ nodeB, const float4 *__res
         szz -= pz * oz;
     } else {  // massless: plain mean of the bodies (gravity/impls/mod.rs:127-129), a rare second pass
         float ux = 0.f, uy = 0.f, uz = 0.f;
-        for (int c = pv + 1; c < end;) {
-            const int4 cb = nodeB[c];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            if (i >= K.n) break;
+            const int c = K.e[i] >> 1;
             const float4 a = ld_cg(nodeA + c);
             float4 lo = make_float4(0.f, 0.f, 0.f, 0.f);
             float cn = 1.f;
-            if (!single_body(cb)) {
+            if (!(K.e[i] & 1)) {
                 lo = ld_cg(&rec[c].lo);
                 cn = float(__float_as_int(ld_cg(&rec[c].s1).z));
             }
             ux += cn * (__fsub_rn(a.x, g.x) + lo.x);
             uy += cn * (__fsub_rn(a.y, g.y) + lo.y);
             uz += cn * (__fsub_rn(a.z, g.z) + lo.z);
-            c = cb.y;
         }
         ox = ux / float(count), oy = uy / float(count), oz = uz / float(count);
     }
     float ex, ey, ez;
     const float hx = two_sum(g.x, ox, ex), hy = two_sum(g.y, oy, ey), hz = two_sum(g.z, oz, ez);
     nodeA[pv] = make_float4(hx, hy, hz, M);
+    // a cell's nodeB.w (a leaf's body count) holds (M w^3)^(2/5): the error-bound
+    // opening radius^2 is this times (alpha |a|)^(-2/5) of the walking group
+    nodeB[pv].w = __float_as_int(M > 0.f ? __powf(M * g.w * g.w * g.w, 0.4f) : 0.f);
     rec[pv].lo = make_float4(ex, ey, ez, Ml);
     rec[pv].s0 = make_float4(sxx, sxy, sxz, syy);
     rec[pv].s1 = make_float4(syz, szz, __int_as_float(count), 0.f);
@@ -499,17 +544,16 @@ __device__ void cell(int pv, const int4 *__restrict__ nodeB, const float4 *__res
 }
 
 // f64 trees (DVec3 bodies): the same combination in FP64.
-__device__ void cell(int pv, const int4 *__restrict__ nodeB, const double4_32a *__restrict__ nodeG, Moments *mom,
-                     double4_32a *nodeA, float4 *) {
-    const int end = nodeB[pv].y;
+__device__ void cell(int pv, const Kids &K, const double4_32a *__restrict__ nodeG, Moments *mom,
+                     double4_32a *nodeA, float4 *, int4 *) {
     const double4_32a g = nodeG[pv];
     const double gx = g.x, gy = g.y, gz = g.z;
     Moments m{};
     double px = 0, py = 0, pz = 0;
-    for (int c = pv + 1; c < end;) {
-        const int4 cb = nodeB[c];
+    for (int i = 0; i < K.n; ++i) {
+        const int c = K.e[i] >> 1;
         double cx, cy, cz, cmm, cn, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
-        if (single_body(cb)) {
+        if (K.e[i] & 1) {
             const double4_32a a = ld_cg(nodeA + c);
             cx = a.x, cy = a.y, cz = a.z, cmm = a.w, cn = 1.0;
         } else {
@@ -530,7 +574,6 @@ __device__ void cell(int pv, const int4 *__restrict__ nodeB, const double4_32a *
         m.syy += syy + my * dy;
         m.syz += syz + my * dz;
         m.szz += szz + mz * dz;
-        c = cb.y;
     }
     if (m.m != 0.0) {
         const double inv = 1.0 / m.m;
@@ -546,10 +589,10 @@ __device__ void cell(int pv, const int4 *__restrict__ nodeB, const double4_32a *
         m.szz -= pz * oz;
     } else {  // massless: plain mean of the bodies (gravity/impls/mod.rs:127-129), a rare second pass
         double ux = 0, uy = 0, uz = 0;
-        for (int c = pv + 1; c < end;) {
-            const int4 cb = nodeB[c];
+        for (int i = 0; i < K.n; ++i) {
+            const int c = K.e[i] >> 1;
             double cx, cy, cz, cn;
-            if (single_body(cb)) {
+            if (K.e[i] & 1) {
                 const double4_32a a = ld_cg(nodeA + c);
                 cx = a.x, cy = a.y, cz = a.z, cn = 1.0;
             } else {
@@ -559,7 +602,6 @@ __device__ void cell(int pv, const int4 *__restrict__ nodeB, const double4_32a *
             ux += cn * (cx - gx);
             uy += cn * (cy - gy);
             uz += cn * (cz - gz);
-            c = cb.y;
         }
         m.cx = gx + ux / m.count;
         m.cy = gy + uy / m.count;
@@ -571,24 +613,30 @@ __device__ void cell(int pv, const int4 *__restrict__ nodeB, const double4_32a *
 template <class T>
 using Record = typename std::conditional<sizeof(T) == 4, Rec32, Moments>::type;
 
+// One child's arrival at binary cell p: true for the last one. Release orders this
+// thread's record stores before the count; acquire makes the siblings' records
+// visible to the combine that follows.
+__device__ __forceinline__ bool arrive(int *pending, int p) {
+    cuda::atomic_ref<int, cuda::thread_scope_device> r(pending[p]);
+    return r.fetch_sub(1, cuda::memory_order_acq_rel) == 1;
+}
+
 // pending[p] = children of binary cell p not yet combined (counted by octree_links).
 template <class T>
 __global__ void __launch_bounds__(256)
     moments_up(const int *__restrict__ counters, const uint32_t *__restrict__ ufirst,
                const typename Prec<T>::V4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
                const uint32_t *__restrict__ cnt, const int *__restrict__ loparent, const int *__restrict__ oparent,
-               const int *__restrict__ pre, const int4 *__restrict__ nodeB,
+               const int *__restrict__ pre, const int *__restrict__ kid, const int *__restrict__ nkid,
                const typename Prec<T>::V4 *__restrict__ nodeG, int *pending, Record<T> *rec,
-               typename Prec<T>::V4 *nodeA, float4 *nodeQ) {
+               typename Prec<T>::V4 *nodeA, float4 *nodeQ, int4 *nodeB) {
     const int M = counters[0];
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= M) return;
     leaf(u + int(pscan[u]) + int(cnt[u]), int(ufirst[u]), int(ufirst[u + 1]), sbody, rec, nodeA, nodeQ);
     for (int p = loparent[u]; p >= 0; p = oparent[p]) {
-        __threadfence();                             // this thread's records before its arrival
-        if (atomicSub(&pending[p], 1) != 1) return;  // a sibling still to come climbs on
-        __threadfence();                             // the siblings' records after their arrivals
-        cell(pre[p], nodeB, nodeG, rec, nodeA, nodeQ);
+        if (!arrive(pending, p)) return;  // a sibling still to come climbs on
+        cell(pre[p], load_kids(p, kid, nkid), nodeG, rec, nodeA, nodeQ, nodeB);
     }
 }
 
@@ -624,6 +672,10 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     PT_TRY(ensure_buf(ctx, S.pscan, sizeof(uint32_t) * (N + 2)));
     PT_TRY(ensure_buf(ctx, S.pre, sizeof(int) * N));
     PT_TRY(ensure_buf(ctx, S.pending, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.nkid, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.kid, sizeof(int) * 8 * N));
+    PT_TRY(ensure_buf(ctx, S.cslot, N));
+    PT_TRY(ensure_buf(ctx, S.lslot, N));
     PT_TRY(ensure_buf(ctx, nA, sizeof(V4) * 2 * N));
     PT_TRY(ensure_buf(ctx, S.nodeB, sizeof(int4) * 2 * N));
     if (!F64) PT_TRY(ensure_buf(ctx, S.nodeQ, sizeof(float4) * 4 * N));
@@ -659,20 +711,23 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     PT_CUDA(cudaMemsetAsync(S.pending.ptr, 0, sizeof(int) * N, st));
     octree_links<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.bparent), as<int>(S.lparent),
                                            as<uint8_t>(S.top), as<int>(S.oparent), as<int>(S.loparent),
-                                           as<uint32_t>(S.cnt), as<int>(S.pending));
+                                           as<uint32_t>(S.cnt), as<int>(S.pending), as<uint8_t>(S.cslot),
+                                           as<uint8_t>(S.lslot));
     PT_TRY(check_launch(ctx, "octree_links"));
     PT_TRY(scan_u32(ctx, S.prims, as<uint32_t>(S.cnt), as<uint32_t>(S.pscan), n + 1));
     layout<T><<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.blast), as<int>(S.bdelta),
                                      as<uint8_t>(S.top), as<int>(S.oparent), as<uint32_t>(S.cnt),
                                      as<uint32_t>(S.pscan), as<uint64_t>(S.ukey), as<uint32_t>(S.ufirst),
                                      as<T>(S.box), as<int>(S.pre), as<int4>(S.nodeB), as<V4>(nG),
-                                     as<int2>(S.nodeR));
+                                     as<int2>(S.nodeR), as<int>(S.loparent), as<int>(S.pending),
+                                     as<uint8_t>(S.cslot), as<uint8_t>(S.lslot), as<int>(S.kid), as<int>(S.nkid));
     PT_TRY(check_launch(ctx, "layout"));
 
     moments_up<T><<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<V4>(sb), as<uint32_t>(S.pscan),
                                             as<uint32_t>(S.cnt), as<int>(S.loparent), as<int>(S.oparent),
-                                            as<int>(S.pre), as<int4>(S.nodeB), as<V4>(nG), as<int>(S.pending),
-                                            as<Record<T>>(S.mom), as<V4>(nA), nodeQ);
+                                            as<int>(S.pre), as<int>(S.kid), as<int>(S.nkid), as<V4>(nG),
+                                            as<int>(S.pending), as<Record<T>>(S.mom), as<V4>(nA), nodeQ,
+                                            as<int4>(S.nodeB));
     PT_TRY(check_launch(ctx, "moments_up"));
     S.last_n_src = n;
     S.f64 = F64;

@@ -424,8 +424,10 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
     }
     const int nvalid = min(GW_GROUP, n_aff - g0);
     const unsigned lt = (1u << lane) - 1u;
-    // PT_BH_RELATIVE: 1 / (alpha |a|) of this group (warp-uniform)
-    const float ginv = REL ? gscale[group] : 0.f;
+    // PT_BH_RELATIVE: 1 / (alpha |a|) of this group (warp-uniform), and its 2/5 power,
+    // the factor of a cell's (M w^3)^(2/5) kept in its nodeB.w
+    const float ginv = (REL && !QUAD) ? gscale[group] : 0.f;
+    const float gq = (REL && QUAD) ? __powf(gscale[group], 0.4f) : 0.f;
     int2 *stack = s_stack[warp];
     const int T = counters[1];
     CellList &Lc = s_cells[warp];
@@ -526,7 +528,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
         float w = 0.f, rr2 = 0.f;
         if (have && B.z < 0) {
             w = __int_as_float(B.x);
-            if (REL) rr2 = rel_r2<QUAD>(A.w, w, ginv);
+            if (REL) rr2 = QUAD ? __int_as_float(B.w) * gq : rel_r2<false>(A.w, w, ginv);
             const float e0 = fmaxf(fmaxf(mn0 - A.x, A.x - mx0), 0.f);
             const float e1 = fmaxf(fmaxf(mn1 - A.y, A.y - mx1), 0.f);
             const float e2b = fmaxf(fmaxf(mn2 - A.z, A.z - mx2), 0.f);
@@ -752,7 +754,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
         for (int i = 0; i < TPL; ++i) {
             rx[i] = ry[i] = rz[i] = 0.f;
             lane_walk<QUAD>(p[i], valid[i], T, nodeA, nodeB, nodeQ, sbody, th2, eps2, rx[i], ry[i], rz[i], na, nvis,
-                            nc, ginv);
+                            nc, REL ? gscale[group] : 0.f);
         }
         unsigned long long a = na, v = nvis, c = nc;
 #pragma unroll
