@@ -370,6 +370,25 @@ __device__ __forceinline__ void local_eval(const LocalExp &L, float dx, float dy
          0.5f * fmaf(L.hxxz, xx, fmaf(L.hyyz, yy, fmaf(L.hzzz, zz, fmaf(L.hxyz, xy2, fmaf(L.hxzz, xz2, L.hyzz * yz2)))));
 }
 
+// PT_BH_LOCAL: adds queued far node e (2 x node index + 1 for a cell) to this lane's
+// expansion coefficients, kept in shared memory as [coefficient][lane].
+template <bool QUAD>
+__device__ __forceinline__ void local_add_node(float (*lx)[32], int lane, int e, const float4 *__restrict__ nodeA,
+                                               const float4 *__restrict__ nodeQ, float gx, float gy, float gz,
+                                               float eps2) {
+    const int node = e >> 1;
+    const bool q = QUAD && (e & 1);
+    const float4 A = __ldg(nodeA + node);
+    LocalExp t;
+    float *tf = &t.ax;
+#pragma unroll
+    for (int k = 0; k < 19; ++k) tf[k] = lx[k][lane];
+    local_add(t, A.x - gx, A.y - gy, A.z - gz, A.w, eps2, q ? nodeQ + 2 * node : nullptr,
+              q ? nodeQ + 2 * node + 1 : nullptr);
+#pragma unroll
+    for (int k = 0; k < 19; ++k) lx[k][lane] = tf[k];
+}
+
 // Targets per lane of the group walk: a warp walks for 32 * GW_TPL key-adjacent
 // targets, and each list entry read from shared memory serves all of a lane's
 // targets. Measured at N = 4M bulge+disk, theta 0.5, quadrupole: 1 -> 18.3 ms
@@ -401,14 +420,16 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
     using CellList = IList<NFC, 96>;
     using BodyList = IList<4, 128>;
     // PT_BH_LOCAL keeps its 19 expansion coefficients per lane in shared memory
-    // ([coefficient][lane]: no bank conflicts) and trims the stack to 320 ranges, so
-    // that 5 CTAs stay resident at 96 registers and 44 KB.
-    constexpr int STK = LOCAL ? 320 : GW_STACK;
+    // ([coefficient][lane]: no bank conflicts) and queues far nodes (up to 63) so that
+    // they are expanded 32 at a time, one per lane, instead of by the few lanes that
+    // popped them; the stack is trimmed to 288 ranges so that 5 CTAs stay resident.
+    constexpr int STK = LOCAL ? 288 : GW_STACK;
     stack_cap = min(stack_cap, STK);
     __shared__ int2 s_stack[GW_WARPS][STK];
     __shared__ __align__(16) CellList s_cells[GW_WARPS];
     __shared__ __align__(16) BodyList s_bodies[GW_WARPS];
     __shared__ float s_lx[GW_WARPS][LOCAL ? 19 : 1][32];
+    __shared__ int s_far[GW_WARPS][LOCAL ? 64 : 1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int group = blockIdx.x * GW_WARPS + warp;
     const int g0 = group * GW_GROUP;
@@ -473,7 +494,8 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
     const float far2 = LOCAL ? rg2 / (local_ratio * local_ratio) : 0.f;
     if (LOCAL)
         for (int k = 0; k < 19; ++k) s_lx[warp][k][lane] = 0.f;
-    unsigned long long nlocal = 0;
+    unsigned long long nlocal = 0;  // warp-uniform
+    int Nf = 0;                     // queued far nodes
     // learned: the warp's current record chunk and its fill; the previous chunk links to
     // the next one (head of the group's chain first)
     int chunk = -1, fill = LCHUNK;
@@ -627,18 +649,21 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
         bool farc = false;
         if (LOCAL && acc && (B.z < 0 || B.w == 1) && A.w != 0.0f) {  // cells and single bodies
             const float dx = A.x - lgx, dy = A.y - lgy, dz = A.z - lgz;
-            if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > far2) {
-                farc = true;
-                const bool q = QUAD && B.z < 0;
-                LocalExp t;
-                float *tf = &t.ax;
-#pragma unroll
-                for (int k = 0; k < 19; ++k) tf[k] = s_lx[warp][k][lane];
-                local_add(t, dx, dy, dz, A.w, eps2, q ? nodeQ + 2 * node : nullptr,
-                          q ? nodeQ + 2 * node + 1 : nullptr);
-#pragma unroll
-                for (int k = 0; k < 19; ++k) s_lx[warp][k][lane] = tf[k];
-                ++nlocal;
+            farc = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > far2;
+        }
+        if (LOCAL) {
+            const unsigned mf = __ballot_sync(0xffffffffu, farc);
+            if (mf) {
+                if (farc) s_far[warp][Nf + __popc(mf & lt)] = 2 * node + (B.z < 0 ? 1 : 0);
+                Nf += __popc(mf);
+                nlocal += __popc(mf);
+                __syncwarp();
+                if (Nf >= 32) {  // the newest 32: one per lane
+                    Nf -= 32;
+                    local_add_node<QUAD>(s_lx[warp], lane, s_far[warp][Nf + lane], nodeA, nodeQ, lgx, lgy, lgz,
+                                         eps2);
+                    __syncwarp();
+                }
             }
         }
         const bool bucket = acc && B.z >= 0 && B.w > 1;
@@ -728,6 +753,8 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
         rz[i] = z0 + z1;
     }
     if (LOCAL) {
+        if (lane < Nf) local_add_node<QUAD>(s_lx[warp], lane, s_far[warp][lane], nodeA, nodeQ, lgx, lgy, lgz, eps2);
+        __syncwarp();
         LocalExp LX;
         float *lf = &LX.ax;
 #pragma unroll
@@ -741,8 +768,6 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
             ry[i] += ly;
             rz[i] += lz;
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) nlocal += __shfl_xor_sync(0xffffffffu, nlocal, o);
     }
     const unsigned long long nv = unsigned(nvalid);
     unsigned long long s_acc = entries * nv, s_vis = visits * nv, s_cell = centries * nv;
