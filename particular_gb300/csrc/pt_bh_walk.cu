@@ -402,11 +402,24 @@ constexpr int GW_TPL = PT_GW_TPL;
 constexpr int GW_GROUP = 32 * GW_TPL;
 constexpr int GW_SHIFT = GW_TPL == 1 ? 5 : GW_TPL == 2 ? 6 : 7;
 static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
+// PT_BH_LOCAL walk: CTAs per SM and list capacities. Both registers (96) and shared
+// memory (44 KB) hold it at 5 CTAs per SM; 6 CTAs with lists of 64 cells and 96
+// bodies (80 registers, 84 bytes spilled, 37 KB) measured 6.9 ms against 6.1 ms at
+// N = 4M.
+#ifndef PT_GW_LMINB
+#define PT_GW_LMINB 5
+#endif
+#ifndef PT_GW_LCELLS
+#define PT_GW_LCELLS 96
+#endif
+#ifndef PT_GW_LBODIES
+#define PT_GW_LBODIES 128
+#endif
 #ifndef PT_GW_MINB
 #define PT_GW_MINB (GW_TPL == 1 ? 6 : 5)  // CTAs per SM the register budget is set for
 #endif
 template <bool QUAD, bool GUARD, bool LEARNED, bool LOCAL, bool REL>
-__global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
+__global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MINB)
     bh_walk_group(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
                   const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
                   const float4 *__restrict__ nodeG, const float4 *__restrict__ sbody, const int *__restrict__ counters,
@@ -417,8 +430,8 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
     static_assert(!(LEARNED && REL), "PT_BH_LEARNED and PT_BH_RELATIVE are exclusive");
     constexpr int NFC = QUAD ? 10 : 4;
     constexpr int TPL = GW_TPL;
-    using CellList = IList<NFC, 96>;
-    using BodyList = IList<4, 128>;
+    using CellList = IList<NFC, LOCAL ? PT_GW_LCELLS : 96>;
+    using BodyList = IList<4, LOCAL ? PT_GW_LBODIES : 128>;
     // PT_BH_LOCAL keeps its 19 expansion coefficients per lane in shared memory
     // ([coefficient][lane]: no bank conflicts) and queues far nodes (up to 63) so that
     // they are expanded 32 at a time, one per lane, instead of by the few lanes that
@@ -494,7 +507,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
     const float far2 = LOCAL ? rg2 / (local_ratio * local_ratio) : 0.f;
     if (LOCAL)
         for (int k = 0; k < 19; ++k) s_lx[warp][k][lane] = 0.f;
-    unsigned long long nlocal = 0;  // warp-uniform
+    unsigned nlocal = 0;  // warp-uniform
     int Nf = 0;                     // queued far nodes
     // learned: the warp's current record chunk and its fill; the previous chunk links to
     // the next one (head of the group's chain first)
@@ -520,7 +533,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? 5 : PT_GW_MINB)
     if (lane == 0) stack[0] = make_int2(0, T);
     __syncwarp();
     int S = 1, Nc = 0, Nb = 0, maxS = 1;
-    unsigned long long entries = 0, visits = 0, centries = 0;
+    unsigned entries = 0, visits = 0, centries = 0;
     bool failed = false;
     while (S > 0) {
         // each pop pushes at most two ranges: never more than the room left
