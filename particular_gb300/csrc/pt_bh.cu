@@ -69,7 +69,7 @@ void pt_bh_state_free(pt_ctx *ctx) {
     prim_free(ctx, S->prims);
     DevBuf *all[] = {&S->box_part, &S->box,    &S->keys,   &S->idx,    &S->sbody,   &S->flags,  &S->uscan,
                      &S->ukey,     &S->ufirst, &S->bfirst, &S->blast,  &S->bdelta,  &S->bparent, &S->lparent,
-                     &S->top,      &S->oparent, &S->loparent, &S->cnt, &S->pscan,   &S->pre,    &S->pending, &S->nkid, &S->kid, &S->cslot, &S->lslot,
+                     &S->top,      &S->oparent, &S->loparent, &S->cnt, &S->pscan,   &S->pre,    &S->nkid, &S->kid, &S->cslot, &S->lslot, &S->levels, &S->by_level,
                      &S->nodeA,  &S->nodeB,  &S->nodeQ,  &S->nodeG, &S->nodeR, &S->mom,     &S->tkeys,  &S->tidx,
                      &S->tbody,    &S->counters, &S->out,  &S->aff_h,  &S->src_h, &S->lrec, &S->lgroup,
                      &S->lnext,    &S->lpart,  &S->lhead, &S->lcentre, &S->lused, &S->sbody64, &S->nodeA64,

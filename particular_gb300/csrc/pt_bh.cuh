@@ -61,7 +61,7 @@ struct State {
     DevBuf keys, idx, sbody;
     DevBuf flags, uscan, ukey, ufirst;
     DevBuf bfirst, blast, bdelta, bparent, lparent, top, oparent, loparent;
-    DevBuf cnt, pscan, pre, pending, nkid, kid, cslot, lslot;
+    DevBuf cnt, pscan, pre, nkid, kid, cslot, lslot, levels, by_level;
     DevBuf nodeA, nodeB, nodeQ, nodeG, nodeR, mom;
     DevBuf sbody64, nodeA64, nodeG64, tbody64;  // the f64 (DVec3) method's bodies and nodes
     DevBuf tkeys, tidx, tbody;

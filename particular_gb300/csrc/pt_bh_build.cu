@@ -25,7 +25,6 @@
 //     DVec3 trees. No thread ever waits on another.
 #include "pt_bh.cuh"
 
-#include <cuda/atomic>
 #include <type_traits>
 
 namespace pt {
@@ -223,26 +222,47 @@ __device__ __forceinline__ int climb(int p, const uint8_t *__restrict__ top, con
     return p;
 }
 
-// Octree parents, child counts (pending, zeroed before) with each child's slot in
-// its parent's child list, and the count of cells starting at each unit.
+// Octree parents, child counts (nkid, zeroed before) with each child's slot in its
+// parent's child list, the count of cells starting at each unit, and the count of
+// cells per octree level (levels[L], zeroed before).
 __global__ void octree_links(const int *__restrict__ counters, const int *__restrict__ bfirst,
                              const int *__restrict__ bparent, const int *__restrict__ lparent,
-                             const uint8_t *__restrict__ top, int *__restrict__ oparent, int *__restrict__ loparent,
-                             uint32_t *__restrict__ cnt, int *__restrict__ pending, uint8_t *__restrict__ cslot,
-                             uint8_t *__restrict__ lslot) {
+                             const uint8_t *__restrict__ top, const int *__restrict__ bdelta,
+                             int *__restrict__ oparent, int *__restrict__ loparent, uint32_t *__restrict__ cnt,
+                             int *__restrict__ nkid, uint8_t *__restrict__ cslot, uint8_t *__restrict__ lslot,
+                             int *__restrict__ levels) {
+    __shared__ int h[LEVELS];
+    if (threadIdx.x < LEVELS) h[threadIdx.x] = 0;
+    __syncthreads();
     const int M = counters[0];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < M - 1 && top[k]) {
         const int op = (k == 0) ? -1 : climb(bparent[k], top, bparent);
         oparent[k] = op;
-        if (op >= 0) cslot[k] = uint8_t(atomicAdd(&pending[op], 1));  // < 8: one child per octant
+        if (op >= 0) cslot[k] = uint8_t(atomicAdd(&nkid[op], 1));  // < 8: one child per octant
         atomicAdd(&cnt[bfirst[k]], 1u);
+        atomicAdd(&h[bdelta[k] / 3], 1);
     }
     if (k < M) {
         const int op = (M == 1) ? -1 : climb(lparent[k], top, bparent);
         loparent[k] = op;
-        if (op >= 0) lslot[k] = uint8_t(atomicAdd(&pending[op], 1));
+        if (op >= 0) lslot[k] = uint8_t(atomicAdd(&nkid[op], 1));
     }
+    __syncthreads();
+    if (threadIdx.x < LEVELS && h[threadIdx.x]) atomicAdd(&levels[threadIdx.x], h[threadIdx.x]);
+}
+
+// levels[0 .. LEVELS) = cells per level, levels[LEVELS + 1 + L] = offset of level L in
+// by_level, levels[2 LEVELS + 2 + L] = its fill cursor.
+__global__ void level_offsets(int *__restrict__ levels) {
+    if (threadIdx.x != 0) return;
+    int acc = 0;
+    for (int L = 0; L < LEVELS; ++L) {
+        levels[LEVELS + 1 + L] = acc;
+        levels[2 * LEVELS + 2 + L] = acc;
+        acc += levels[L];
+    }
+    levels[2 * LEVELS + 1] = acc;
 }
 
 // ---- 6. preorder layout ------------------------------------------------------
@@ -256,12 +276,16 @@ __global__ void layout(int *counters, const int *__restrict__ bfirst,
                        const uint64_t *__restrict__ ukey, const uint32_t *__restrict__ ufirst,
                        const T *__restrict__ box, int *__restrict__ pre, int4 *__restrict__ nodeB,
                        typename Prec<T>::V4 *__restrict__ nodeG, int2 *__restrict__ nodeR,
-                       const int *__restrict__ loparent, const int *__restrict__ pending,
-                       const uint8_t *__restrict__ cslot, const uint8_t *__restrict__ lslot, int *__restrict__ kid,
-                       int *__restrict__ nkid) {
+                       const int *__restrict__ loparent, const uint8_t *__restrict__ cslot,
+                       const uint8_t *__restrict__ lslot, int *__restrict__ kid, int *__restrict__ levels,
+                       int *__restrict__ by_level) {
     using P = Prec<T>;
+    __shared__ int h[LEVELS], base[LEVELS];
+    if (threadIdx.x < LEVELS) h[threadIdx.x] = 0;
+    __syncthreads();
     const int M = counters[0];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int lvl = -1, lrank = 0;  // this cell's octree level and rank among the block's
     if (k == 0) {
         counters[1] = M + int(pscan[M]);
         counters[2] = int(pscan[M]);
@@ -294,9 +318,10 @@ __global__ void layout(int *counters, const int *__restrict__ bfirst,
         nodeB[pk] = make_int4(sizeof(T) == 4 ? __float_as_int(float(w)) : 0, skip, -1, 0);
         nodeG[pk] = P::make(T(0.5) * (mn0 + mx0), T(0.5) * (mn1 + mx1), T(0.5) * (mn2 + mx2), w);
         nodeR[pk] = make_int2(int(ufirst[b]), int(ufirst[blast[k] + 1]));
-        // the cell's own child count, and its entry in its parent's child list
-        nkid[k] = pending[k];
+        // the cell's entry in its parent's child list
         if (k != 0) kid[8 * oparent[k] + cslot[k]] = 2 * pk;
+        lvl = L;
+        lrank = atomicAdd(&h[L], 1);
     }
     if (k < M) {
         const int pk = k + int(pscan[k]) + int(cnt[k]);
@@ -308,16 +333,21 @@ __global__ void layout(int *counters, const int *__restrict__ bfirst,
         const int op = loparent[k];
         if (op >= 0) kid[8 * op + lslot[k]] = 2 * pk + (nb == 1 ? 1 : 0);
     }
+    // cells bucketed by octree level (one range per level and block)
+    __syncthreads();
+    if (threadIdx.x < LEVELS && h[threadIdx.x])
+        base[threadIdx.x] = atomicAdd(&levels[2 * LEVELS + 2 + threadIdx.x], h[threadIdx.x]);
+    __syncthreads();
+    if (lvl >= 0) by_level[base[lvl] + lrank] = k;
 }
 
 // ---- 7. moments ------------------------------------------------------------
-// One launch, bottom-up: a thread per leaf unit writes the leaf's record, then
-// arrives at its parent cell; the last child to arrive (a per-cell countdown of the
-// children still to come) combines the cell from all its children, in preorder,
-// and climbs on. The order of every sum is fixed by the tree, so results do not
-// depend on which thread arrives last. No thread ever waits on another.
-//
-// Records written earlier in the same launch by other threads are read through L2.
+// Leaves first (one thread per leaf unit), then the cells one octree level per
+// launch, deepest first, one thread per cell: every cell's children are complete
+// when it is combined, and it reads them from its child list, all loads at once.
+// The order of every sum is fixed by the tree. (A single bottom-up launch in which
+// the last child to arrive combined its parent measured the same: its climbing lanes
+// wait on L2 with 4 of 32 lanes active.)
 __device__ __forceinline__ float4 ld_cg(const float4 *p) { return __ldcg(p); }
 __device__ __forceinline__ double4_32a ld_cg(const double4_32a *p) {
     const double2 a = __ldcg(reinterpret_cast<const double2 *>(p));
@@ -613,33 +643,30 @@ __device__ void cell(int pv, const Kids &K, const double4_32a *__restrict__ node
 template <class T>
 using Record = typename std::conditional<sizeof(T) == 4, Rec32, Moments>::type;
 
-// One child's arrival at binary cell p: true for the last one. Release orders this
-// thread's record stores before the count; acquire makes the siblings' records
-// visible to the combine that follows.
-__device__ __forceinline__ bool arrive(int *pending, int p) {
-    cuda::atomic_ref<int, cuda::thread_scope_device> r(pending[p]);
-    return r.fetch_sub(1, cuda::memory_order_acq_rel) == 1;
-}
-
-// pending[p] = children of binary cell p not yet combined (counted by octree_links).
 template <class T>
 __global__ void __launch_bounds__(256)
-    moments_up(const int *__restrict__ counters, const uint32_t *__restrict__ ufirst,
-               const typename Prec<T>::V4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
-               const uint32_t *__restrict__ cnt, const int *__restrict__ loparent, const int *__restrict__ oparent,
-               const int *__restrict__ pre, const int *__restrict__ kid, const int *__restrict__ nkid,
-               const typename Prec<T>::V4 *__restrict__ nodeG, int *pending, Record<T> *rec,
-               typename Prec<T>::V4 *nodeA, float4 *nodeQ, int4 *nodeB) {
+    leaf_records(const int *__restrict__ counters, const uint32_t *__restrict__ ufirst,
+                 const typename Prec<T>::V4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
+                 const uint32_t *__restrict__ cnt, Record<T> *rec, typename Prec<T>::V4 *nodeA, float4 *nodeQ) {
     const int M = counters[0];
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= M) return;
     leaf(u + int(pscan[u]) + int(cnt[u]), int(ufirst[u]), int(ufirst[u + 1]), sbody, rec, nodeA, nodeQ);
-    for (int p = loparent[u]; p >= 0; p = oparent[p]) {
-        if (!arrive(pending, p)) return;  // a sibling still to come climbs on
-        cell(pre[p], load_kids(p, kid, nkid), nodeG, rec, nodeA, nodeQ, nodeB);
-    }
 }
 
+// The cells of octree level L (levels below: done), one thread each.
+template <class T>
+__global__ void __launch_bounds__(256)
+    cells_level(int L, const int *__restrict__ levels, const int *__restrict__ by_level,
+                const int *__restrict__ pre, const int *__restrict__ kid, const int *__restrict__ nkid,
+                const typename Prec<T>::V4 *__restrict__ nodeG, Record<T> *rec, typename Prec<T>::V4 *nodeA,
+                float4 *nodeQ, int4 *nodeB) {
+    const int begin = levels[LEVELS + 1 + L], end = begin + levels[L];
+    for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
+        const int k = by_level[i];
+        cell(pre[k], load_kids(k, kid, nkid), nodeG, rec, nodeA, nodeQ, nodeB);
+    }
+}
 
 template <class T>
 int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
@@ -671,8 +698,9 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     PT_TRY(ensure_buf(ctx, S.cnt, sizeof(uint32_t) * (N + 1)));
     PT_TRY(ensure_buf(ctx, S.pscan, sizeof(uint32_t) * (N + 2)));
     PT_TRY(ensure_buf(ctx, S.pre, sizeof(int) * N));
-    PT_TRY(ensure_buf(ctx, S.pending, sizeof(int) * N));
     PT_TRY(ensure_buf(ctx, S.nkid, sizeof(int) * N));
+    PT_TRY(ensure_buf(ctx, S.levels, sizeof(int) * (3 * LEVELS + 8)));
+    PT_TRY(ensure_buf(ctx, S.by_level, sizeof(int) * N));
     PT_TRY(ensure_buf(ctx, S.kid, sizeof(int) * 8 * N));
     PT_TRY(ensure_buf(ctx, S.cslot, N));
     PT_TRY(ensure_buf(ctx, S.lslot, N));
@@ -708,27 +736,35 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     octree_top<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bdelta), as<int>(S.bparent), as<uint8_t>(S.top));
     PT_TRY(check_launch(ctx, "octree_top"));
     PT_CUDA(cudaMemsetAsync(S.cnt.ptr, 0, sizeof(uint32_t) * (N + 1), st));
-    PT_CUDA(cudaMemsetAsync(S.pending.ptr, 0, sizeof(int) * N, st));
+    PT_CUDA(cudaMemsetAsync(S.nkid.ptr, 0, sizeof(int) * N, st));
+    PT_CUDA(cudaMemsetAsync(S.levels.ptr, 0, sizeof(int) * (3 * LEVELS + 8), st));
+    int *levels = as<int>(S.levels);
     octree_links<<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.bparent), as<int>(S.lparent),
-                                           as<uint8_t>(S.top), as<int>(S.oparent), as<int>(S.loparent),
-                                           as<uint32_t>(S.cnt), as<int>(S.pending), as<uint8_t>(S.cslot),
-                                           as<uint8_t>(S.lslot));
+                                           as<uint8_t>(S.top), as<int>(S.bdelta), as<int>(S.oparent),
+                                           as<int>(S.loparent), as<uint32_t>(S.cnt), as<int>(S.nkid),
+                                           as<uint8_t>(S.cslot), as<uint8_t>(S.lslot), levels);
     PT_TRY(check_launch(ctx, "octree_links"));
+    level_offsets<<<1, 32, 0, st>>>(levels);
+    PT_TRY(check_launch(ctx, "level_offsets"));
     PT_TRY(scan_u32(ctx, S.prims, as<uint32_t>(S.cnt), as<uint32_t>(S.pscan), n + 1));
     layout<T><<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.blast), as<int>(S.bdelta),
                                      as<uint8_t>(S.top), as<int>(S.oparent), as<uint32_t>(S.cnt),
                                      as<uint32_t>(S.pscan), as<uint64_t>(S.ukey), as<uint32_t>(S.ufirst),
                                      as<T>(S.box), as<int>(S.pre), as<int4>(S.nodeB), as<V4>(nG),
-                                     as<int2>(S.nodeR), as<int>(S.loparent), as<int>(S.pending),
-                                     as<uint8_t>(S.cslot), as<uint8_t>(S.lslot), as<int>(S.kid), as<int>(S.nkid));
+                                     as<int2>(S.nodeR), as<int>(S.loparent), as<uint8_t>(S.cslot),
+                                     as<uint8_t>(S.lslot), as<int>(S.kid), levels, as<int>(S.by_level));
     PT_TRY(check_launch(ctx, "layout"));
 
-    moments_up<T><<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<V4>(sb), as<uint32_t>(S.pscan),
-                                            as<uint32_t>(S.cnt), as<int>(S.loparent), as<int>(S.oparent),
-                                            as<int>(S.pre), as<int>(S.kid), as<int>(S.nkid), as<V4>(nG),
-                                            as<int>(S.pending), as<Record<T>>(S.mom), as<V4>(nA), nodeQ,
-                                            as<int4>(S.nodeB));
-    PT_TRY(check_launch(ctx, "moments_up"));
+    leaf_records<T><<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<V4>(sb), as<uint32_t>(S.pscan),
+                                              as<uint32_t>(S.cnt), as<Record<T>>(S.mom), as<V4>(nA), nodeQ);
+    PT_TRY(check_launch(ctx, "leaf_records"));
+    const int lvl_grid = std::max(1, std::min(blocks(n), 8 * ctx->sm_count));
+    for (int L = LEVELS - 1; L >= 0; --L) {
+        cells_level<T><<<lvl_grid, 256, 0, st>>>(L, levels, as<int>(S.by_level), as<int>(S.pre), as<int>(S.kid),
+                                                as<int>(S.nkid), as<V4>(nG), as<Record<T>>(S.mom), as<V4>(nA),
+                                                nodeQ, as<int4>(S.nodeB));
+        PT_TRY(check_launch(ctx, "cells_level"));
+    }
     S.last_n_src = n;
     S.f64 = F64;
     ++S.generation;
