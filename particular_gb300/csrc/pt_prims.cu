@@ -2,9 +2,11 @@
 //
 // scan_u32: blocks of SCAN_TILE items scan in shared memory and publish their
 // totals; the totals are scanned recursively and added back.
-// radix_sort_u64: 8-bit digits, one histogram pass + one scan + one scatter pass per
-// digit. The scatter ranks keys stably inside a CTA tile with warp match/popc and a
-// per-digit running offset, so equal digits keep their input order.
+// radix_sort_u64: 8-bit digits; per digit a histogram pass (per-tile counts), a row
+// scan (one block per digit value over the tiles) and a scatter pass. The scatter
+// ranks keys stably inside a 2048-key tile with warp match/popc and a per-digit
+// running offset, so equal digits keep their input order, stages the tile in shared
+// memory in digit order and writes every digit's run contiguously.
 #include "pt_prims.cuh"
 
 namespace pt {
@@ -74,9 +76,29 @@ __global__ void scan_total(uint32_t *__restrict__ out, int n, const uint32_t *__
 
 // ---- radix sort ------------------------------------------------------------
 constexpr int RS_THREADS = 256;
-constexpr int RS_ROUNDS = 16;
+constexpr int RS_ROUNDS = 8;
 constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
 constexpr int RS_WARPS = RS_THREADS / 32;
+
+// Exclusive scan of one value per thread over the 256 threads of a block; wsum holds
+// RS_WARPS + 1 words. Every thread of the block must call it.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *wsum, uint32_t *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t incl = warp_incl_scan(v);
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = lane < RS_WARPS ? wsum[lane] : 0u;
+        const uint32_t wi = warp_incl_scan(w);
+        if (lane < RS_WARPS) wsum[lane] = wi - w;
+        if (lane == RS_WARPS - 1) wsum[RS_WARPS] = wi;
+    }
+    __syncthreads();
+    const uint32_t r = wsum[warp] + incl - v;
+    if (total) *total = wsum[RS_WARPS];
+    __syncthreads();
+    return r;
+}
 
 // hist[d * nblocks + b] = count of digit d in tile b.
 __global__ void __launch_bounds__(RS_THREADS)
@@ -94,19 +116,55 @@ __global__ void __launch_bounds__(RS_THREADS)
     hist[size_t(threadIdx.x) * nblocks + blockIdx.x] = cnt[threadIdx.x];
 }
 
+// One block per digit d: offs[d * nblocks + b] = count of digit d in tiles before b,
+// rowsum[d] = count of digit d.
+__global__ void __launch_bounds__(RS_THREADS)
+    rs_rowscan(const uint32_t *__restrict__ hist, uint32_t *__restrict__ offs, uint32_t *__restrict__ rowsum,
+               int nblocks) {
+    __shared__ uint32_t wsum[RS_WARPS + 1];
+    const int d = blockIdx.x;
+    const uint32_t *row = hist + size_t(d) * nblocks;
+    uint32_t *orow = offs + size_t(d) * nblocks;
+    const int q = (nblocks + RS_THREADS - 1) / RS_THREADS;
+    const int b0 = min(nblocks, int(threadIdx.x) * q), b1 = min(nblocks, b0 + q);
+    uint32_t s = 0;
+    for (int b = b0; b < b1; ++b) s += row[b];
+    uint32_t total;
+    uint32_t acc = block_excl_scan(s, wsum, &total);
+    for (int b = b0; b < b1; ++b) {
+        const uint32_t h = row[b];
+        orow[b] = acc;
+        acc += h;
+    }
+    if (threadIdx.x == 0) rowsum[d] = total;
+}
+
+// Ranks the tile's keys stably by digit (warp match/popc, per-digit running offsets),
+// stages them in shared memory in digit order, then writes each digit's run to its
+// global range: consecutive threads write consecutive addresses.
 __global__ void __launch_bounds__(RS_THREADS)
     rs_scatter(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin, uint64_t *__restrict__ kout,
-               uint32_t *__restrict__ vout, int n, int shift, const uint32_t *__restrict__ offs, int nblocks) {
+               uint32_t *__restrict__ vout, int n, int shift, const uint32_t *__restrict__ hist,
+               const uint32_t *__restrict__ offs, const uint32_t *__restrict__ rowsum, int nblocks) {
+    __shared__ uint64_t skeys[RS_TILE];
+    __shared__ uint32_t svals[RS_TILE];
     __shared__ uint32_t warp_cnt[RS_WARPS][256];
     __shared__ uint32_t warp_off[RS_WARPS][256];
-    __shared__ uint32_t run[256];
+    __shared__ uint32_t lrun[256], tstart[256], gbase[256];
+    __shared__ uint32_t wsum[RS_WARPS + 1];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    run[t] = offs[size_t(t) * nblocks + blockIdx.x];
+    const int b = blockIdx.x;
+    // digit t's global start for this tile: all smaller digits, then earlier tiles
+    gbase[t] = block_excl_scan(rowsum[t], wsum, nullptr) + offs[size_t(t) * nblocks + b];
+    // digit t's start in this tile's staged (digit-ordered) copy
+    const uint32_t ts = block_excl_scan(hist[size_t(t) * nblocks + b], wsum, nullptr);
+    tstart[t] = ts;
+    lrun[t] = ts;
 #pragma unroll
     for (int w = 0; w < RS_WARPS; ++w) warp_cnt[w][t] = 0;
     __syncthreads();
     const uint32_t lt = (1u << lane) - 1u;
-    const size_t base = size_t(blockIdx.x) * RS_TILE;
+    const size_t base = size_t(b) * RS_TILE;
     for (int r = 0; r < RS_ROUNDS; ++r) {
         const size_t i = base + size_t(r) * RS_THREADS + t;
         const bool valid = i < size_t(n);
@@ -118,7 +176,7 @@ __global__ void __launch_bounds__(RS_THREADS)
         if (valid && rank == 0) warp_cnt[warp][d] = __popc(peers);
         __syncthreads();
         {
-            uint32_t acc = run[t];
+            uint32_t acc = lrun[t];
 #pragma unroll
             for (int w = 0; w < RS_WARPS; ++w) {
                 const uint32_t c = warp_cnt[w][t];
@@ -126,14 +184,23 @@ __global__ void __launch_bounds__(RS_THREADS)
                 warp_cnt[w][t] = 0;
                 acc += c;
             }
-            run[t] = acc;
+            lrun[t] = acc;
         }
         __syncthreads();
         if (valid) {
             const uint32_t pos = warp_off[warp][d] + rank;
-            kout[pos] = key;
-            vout[pos] = val;
+            skeys[pos] = key;
+            svals[pos] = val;
         }
+    }
+    __syncthreads();
+    const int cnt = int(min(size_t(RS_TILE), size_t(n) - base));
+    for (int i = t; i < cnt; i += RS_THREADS) {
+        const uint64_t key = skeys[i];
+        const uint32_t d = uint32_t(key >> shift) & 255u;
+        const uint32_t pos = gbase[d] + (uint32_t(i) - tstart[d]);
+        kout[pos] = key;
+        vout[pos] = svals[i];
     }
 }
 
@@ -186,12 +253,13 @@ int radix_sort_u64(pt_ctx *ctx, PrimScratch &s, uint64_t *keys, uint32_t *vals, 
     using namespace prims;
     if (n <= 1) return PT_OK;
     const int nblocks = (n + RS_TILE - 1) / RS_TILE;
-    const int nhist = 256 * nblocks;
+    const size_t nhist = 256 * size_t(nblocks);
     PT_TRY(ensure_buf(ctx, s.keys2, sizeof(uint64_t) * size_t(n)));
     PT_TRY(ensure_buf(ctx, s.vals2, sizeof(uint32_t) * size_t(n)));
-    PT_TRY(ensure_buf(ctx, s.hist, sizeof(uint32_t) * (2 * size_t(nhist) + 1)));
+    PT_TRY(ensure_buf(ctx, s.hist, sizeof(uint32_t) * (2 * nhist + 256)));
     uint32_t *hist = static_cast<uint32_t *>(s.hist.ptr);
     uint32_t *offs = hist + nhist;
+    uint32_t *rowsum = offs + nhist;
     uint64_t *ka = keys, *kb = static_cast<uint64_t *>(s.keys2.ptr);
     uint32_t *va = vals, *vb = static_cast<uint32_t *>(s.vals2.ptr);
     const int passes = (bits + 7) / 8;
@@ -200,8 +268,9 @@ int radix_sort_u64(pt_ctx *ctx, PrimScratch &s, uint64_t *keys, uint32_t *vals, 
         const int shift = 8 * p;
         rs_hist<<<nblocks, RS_THREADS, 0, st>>>(ka, n, shift, hist, nblocks);
         PT_TRY(check_launch(ctx, "rs_hist"));
-        PT_TRY(scan_u32(ctx, s, hist, offs, nhist));
-        rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, shift, offs, nblocks);
+        rs_rowscan<<<256, RS_THREADS, 0, st>>>(hist, offs, rowsum, nblocks);
+        PT_TRY(check_launch(ctx, "rs_rowscan"));
+        rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, shift, hist, offs, rowsum, nblocks);
         PT_TRY(check_launch(ctx, "rs_scatter"));
         std::swap(ka, kb);
         std::swap(va, vb);
