@@ -3,6 +3,8 @@
 // per-context state.
 #include "pt_bh.cuh"
 
+#include <vector>
+
 namespace pt {
 namespace bh {
 
@@ -380,11 +382,23 @@ int pt_bh_export_tree(pt_ctx *ctx, float *com_mass, int32_t *links, float *quad,
     if (links) PT_CUDA(cudaMemcpyAsync(links, S->nodeB.ptr, 16 * st.nodes, cudaMemcpyDeviceToHost, s));
     if (quad) PT_CUDA(cudaMemcpyAsync(quad, S->nodeQ.ptr, 32 * st.nodes, cudaMemcpyDeviceToHost, s));
     PT_CUDA(cudaStreamSynchronize(s));
-    // a cell's last word holds the walk's opening factor on the device: its body
-    // count column reads 0, as documented
-    if (links)
-        for (size_t r = 0; r < st.nodes; ++r)
-            if (links[4 * r + 2] < 0) links[4 * r + 3] = 0;
+    // On the device a cell's last word holds the walk's opening factor and a
+    // single-body leaf has no quadrupole: the columns read as documented (body count
+    // 0 for cells, a zero quadrupole for single bodies). Single-body rows need the
+    // links to be told apart.
+    std::vector<int32_t> own;
+    if (quad && !links) {
+        own.resize(4 * size_t(st.nodes));
+        PT_CUDA(cudaMemcpy(own.data(), S->nodeB.ptr, 16 * st.nodes, cudaMemcpyDeviceToHost));
+    }
+    const int32_t *L = links ? links : own.data();
+    for (size_t r = 0; r < st.nodes && (links || quad); ++r) {
+        if (L[4 * r + 2] < 0) {
+            if (links) links[4 * r + 3] = 0;
+        } else if (quad && L[4 * r + 3] == 1) {
+            for (int k = 0; k < 8; ++k) quad[8 * r + k] = 0.f;
+        }
+    }
     return PT_OK;
 }
 

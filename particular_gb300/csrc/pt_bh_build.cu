@@ -408,16 +408,13 @@ __device__ __forceinline__ void store_cell(const Moments &m, int pk, Rec32 *rec,
         store_quad(nodeQ, pk, float(m.sxx), float(m.sxy), float(m.sxz), float(m.syy), float(m.syz), float(m.szz));
 }
 
-// Leaves: a single body is its own cell data (no record: parents read nodeA);
-// several (coincident, or closer than the key resolution) get FP64 moments.
+// Leaves: a single body is its own cell data (no record: parents read nodeA; no
+// quadrupole: the walks read it for cells only); several (coincident, or closer
+// than the key resolution) get FP64 moments.
 template <class V4, class R>
 __device__ void leaf(int pk, int f, int e, const V4 *__restrict__ sbody, R *rec, V4 *nodeA, float4 *nodeQ) {
     if (e - f == 1) {
         nodeA[pk] = sbody[f];
-        if (nodeQ) {
-            nodeQ[2 * pk] = make_float4(0.f, 0.f, 0.f, 0.f);
-            nodeQ[2 * pk + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
         return;
     }
     Moments m{};
@@ -760,7 +757,10 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     PT_TRY(check_launch(ctx, "leaf_records"));
     const int lvl_grid = std::max(1, std::min(blocks(n), 8 * ctx->sm_count));
     for (int L = LEVELS - 1; L >= 0; --L) {
-        cells_level<T><<<lvl_grid, 256, 0, st>>>(L, levels, as<int>(S.by_level), as<int>(S.pre), as<int>(S.kid),
+        // level L holds at most 8^L cells: shallow levels get a grid of their size
+        const long long cap = L < 10 ? (1ll << (3 * L)) : (long long)n;
+        const int grid = int(std::max(1ll, std::min<long long>(lvl_grid, (std::min<long long>(cap, n) + 255) / 256)));
+        cells_level<T><<<grid, 256, 0, st>>>(L, levels, as<int>(S.by_level), as<int>(S.pre), as<int>(S.kid),
                                                 as<int>(S.nkid), as<V4>(nG), as<Record<T>>(S.mom), as<V4>(nA),
                                                 nodeQ, as<int4>(S.nodeB));
         PT_TRY(check_launch(ctx, "cells_level"));

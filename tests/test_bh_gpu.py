@@ -501,3 +501,24 @@ def test_local_expansion_separate_targets(res, oracle, softened):
     e0, e1 = rel(plain, ref64), rel(local, ref64)
     for q in (50, 95, 99):
         assert np.percentile(e1, q) <= 1.1 * np.percentile(e0, q) + 1e-7, q
+
+
+def test_export_columns(res):
+    """pt_bh_export_tree: cells carry -1 as first body and 0 as body count; leaves their
+    body range; single bodies a zero quadrupole (exported with or without links)."""
+    b = ics.plummer(5000, seed=60)["bodies"]
+    m = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=True, group=True,
+                       local=True, relative=2.5e-3)
+    m.compute(b)
+    g = m.export_tree()
+    ln, q = g["links"], g["quad"]
+    cells = ln[:, 2] < 0
+    assert (ln[cells, 3] == 0).all()
+    assert (ln[~cells, 3] >= 1).all() and ln[~cells, 3].sum() == b.shape[0]
+    single = ~cells & (ln[:, 3] == 1)
+    assert (q[single] == 0).all()
+    assert np.abs(q[cells]).max() > 0
+    n = m.stats()["nodes"]
+    q2 = np.zeros((n, 8), np.float32)
+    N.check(N.lib().pt_bh_export_tree(res.handle, None, None, q2.ctypes.data, n))
+    np.testing.assert_array_equal(q2, q)
