@@ -195,7 +195,9 @@ class BruteForceWorkload:
         N.check(N.lib().pt_measure_fp32_peak(res.handle, ctypes.byref(peak)))
         achieved = 20.0 * self.n * self.n / (step_ms * 1e-3) / 1e12
         return {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                "frac": achieved / peak.value, "traffic": None,
+                "frac": achieved / peak.value, "traffic": 4.2e6 * self.n / 131072,
+                "traffic_source": "ncu dram__bytes_read + write of one bf_fast launch at N = 131072 "
+                                  "(profiles/bf_fast_plummer_131072.md), scaled by N",
                 "kernel": "bf_fast (+ bf_fixup)",
                 "algorithmic": "20 flop per pair interaction x N^2 pairs per launch",
                 "peak_source": "measured FFMA-chain kernel over all SMs (pt_measure_fp32_peak)"}
@@ -416,7 +418,9 @@ class BarnesHutWorkload:
         hbm, hbm_source = measured_hbm_gbs()
         build_gbs = build_bytes / (build_ms * 1e-3) / 1e9
         return {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                "frac": achieved / peak.value, "traffic": None,
+                "frac": achieved / peak.value, "traffic": 124.14e6 * self.n / 1048576,
+                "traffic_source": "ncu dram__bytes_read + write of one bh_walk_group launch at N = 1M "
+                                  "(profiles/bh_walk_group_bulge_disk_4M.md), scaled by bodies",
                 "build": {"bound": "hbm", "achieved": build_gbs, "peak": hbm, "unit": "GB/s",
                           "frac": build_gbs / hbm, "bytes": build_bytes,
                           "ms": build_ms, "peak_source": hbm_source},
@@ -625,7 +629,11 @@ class EnsembleWorkload:
         N.check(N.lib().pt_measure_fp32_peak(res.handle, ctypes.byref(peak)))
         achieved = 20.0 * self.pairs_per_step * (self.steps_per_call + 1) / (step_ms * 1e-3) / 1e12
         return {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                "frac": achieved / peak.value, "traffic": None, "kernel": "ens_persistent",
+                "frac": achieved / peak.value, "traffic": 1.85e9 * (self.steps_per_call + 1) / 3,
+                "traffic_source": "ncu dram__bytes_read + write of one ens_persistent launch of 3 "
+                                  "evaluations (profiles/ens_persistent_ensemble_4096.md), scaled by "
+                                  "evaluations",
+                "kernel": "ens_persistent",
                 "algorithmic": "20 flop per pair x sum(n_k^2) x 101 evaluations per step",
                 "autotuned_K_per_size_class": self.table,
                 "peak_source": "measured FFMA-chain kernel over all SMs (pt_measure_fp32_peak)"}
