@@ -538,19 +538,39 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
     while (S > 0) {
         // each pop pushes at most two ranges: never more than the room left
         const int k = min(min(32, S), max(1, (stack_cap - S) / 2));
-        const bool have = lane < k;
-        const int2 range = have ? stack[S - 1 - lane] : make_int2(0, 0);
+        const bool first = lane < k;
+        int2 range = first ? stack[S - 1 - lane] : make_int2(0, 0);
         __syncwarp();
         S -= k;
-        visits += k;
-        const int node = range.x;
+        int node = range.x;
         float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
         int4 B = make_int4(0, 0, 0, 0);
         bool open = false;
-        if (have) {
+        if (first) {
             A = __ldg(nodeA + node);
             B = __ldg(nodeB + node);
         }
+        // A pop of at most 16 ranges leaves lanes idle: lane 16 + i then also takes
+        // the second node of range i (its first node's skip pointer), and the rest of
+        // the range passes to it. Each range still pushes at most three ranges, within
+        // the room k was sized for (2 per popped range).
+        bool second = false;
+        if (k <= 16) {
+            const int src = lane & 15;
+            const int nxt = __shfl_sync(0xffffffffu, B.y, src);
+            const int end = __shfl_sync(0xffffffffu, range.y, src);
+            if (lane >= 16 && src < k && nxt < end) {
+                second = true;
+                node = nxt;
+                range = make_int2(nxt, end);
+                A = __ldg(nodeA + node);
+                B = __ldg(nodeB + node);
+            }
+        }
+        const unsigned msecond = __ballot_sync(0xffffffffu, second);
+        const bool handed = first && lane < 16 && ((msecond >> (lane + 16)) & 1u);  // its rest went to lane + 16
+        const bool have = first || second;
+        visits += k + __popc(msecond);
         // Open iff the per-body rule opens for at least one target: some target with
         // nonzero d^2 (targets with d^2 == 0 skip the cell under that rule and do not
         // vote) and theta^2 d^2 < w^2. Settled without a vote: cells accepted even from
@@ -640,7 +660,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
             fill += nm;
             learned += nm;
         }
-        const bool rest = have && B.y < range.y;  // later siblings remain
+        const bool rest = have && !handed && B.y < range.y;  // later siblings remain
         const int np = int(rest) + int(open);
         // each lane's pushes follow those of the lanes below it
         const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, open);
