@@ -550,16 +550,16 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
             A = __ldg(nodeA + node);
             B = __ldg(nodeB + node);
         }
-        // A pop of at most 16 ranges leaves lanes idle: lane 16 + i then also takes
+        // A pop of fewer than 32 ranges leaves lanes idle: lane k + i then also takes
         // the second node of range i (its first node's skip pointer), and the rest of
         // the range passes to it. Each range still pushes at most three ranges, within
         // the room k was sized for (2 per popped range).
         bool second = false;
-        if (k <= 16) {
-            const int src = lane & 15;
+        if (k < 32) {
+            const int src = lane >= k ? lane - k : lane;
             const int nxt = __shfl_sync(0xffffffffu, B.y, src);
             const int end = __shfl_sync(0xffffffffu, range.y, src);
-            if (lane >= 16 && src < k && nxt < end) {
+            if (lane >= k && src < k && nxt < end) {
                 second = true;
                 node = nxt;
                 range = make_int2(nxt, end);
@@ -568,7 +568,8 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
             }
         }
         const unsigned msecond = __ballot_sync(0xffffffffu, second);
-        const bool handed = first && lane < 16 && ((msecond >> (lane + 16)) & 1u);  // its rest went to lane + 16
+        // its rest went to lane + k
+        const bool handed = first && lane + k < 32 && ((msecond >> (lane + k)) & 1u);
         const bool have = first || second;
         visits += k + __popc(msecond);
         // Open iff the per-body rule opens for at least one target: some target with
