@@ -18,11 +18,12 @@
 //     reference tree disappear: accepting a chain cell or its only child adds the
 //     same (COM, M), so the result is unchanged.
 //  6. cells are laid out in depth-first preorder with skip pointers (index after
-//     the subtree), leaves interleaved: the walk needs no stack.
-//  7. moments bottom-up in one launch (mass, centre of mass, second moment ->
-//     traceless quadrupole): the last child to finish combines its parent cell
-//     (parallel-axis theorem), in compensated FP32 for f32 trees and FP64 for
-//     DVec3 trees. No thread ever waits on another.
+//     the subtree), leaves interleaved; every cell gets a list of its children and
+//     the cells are bucketed by octree level.
+//  7. moments (mass, centre of mass, second moment -> traceless quadrupole): the
+//     leaves, then one launch per octree level, deepest first, a thread per cell
+//     combining its children (parallel-axis theorem), in compensated FP32 for f32
+//     trees and FP64 for DVec3 trees.
 #include "pt_bh.cuh"
 
 #include <type_traits>
@@ -346,8 +347,9 @@ __global__ void layout(int *counters, const int *__restrict__ bfirst,
 // launch, deepest first, one thread per cell: every cell's children are complete
 // when it is combined, and it reads them from its child list, all loads at once.
 // The order of every sum is fixed by the tree. (A single bottom-up launch in which
-// the last child to arrive combined its parent measured the same: its climbing lanes
-// wait on L2 with 4 of 32 lanes active.)
+// the last child to arrive combined its parent was slower, 2.04 against 1.81 ms of
+// build at N = 4M: its climbing lanes wait on L2 with 4 of 32 lanes active.)
+// Children's records are read once, through L2 (ld.global.cg).
 __device__ __forceinline__ float4 ld_cg(const float4 *p) { return __ldcg(p); }
 __device__ __forceinline__ double4_32a ld_cg(const double4_32a *p) {
     const double2 a = __ldcg(reinterpret_cast<const double2 *>(p));
