@@ -527,9 +527,9 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
     }
     // Stack entries are sibling ranges (first, end): `first` is the next node to
     // visit, its later siblings follow by skip pointers up to `end`. A pop visits one
-    // node and pushes back at most two ranges: its remaining siblings and, for an
-    // opened cell, its children (pre+1, skip). The stack therefore stays within about
-    // 32 ranges per tree level.
+    // node of a range (two when lanes are idle) and pushes back its remaining
+    // siblings and, for each opened cell, its children (pre+1, skip). The stack
+    // therefore stays within about 32 ranges per tree level.
     if (lane == 0) stack[0] = make_int2(0, T);
     __syncwarp();
     int S = 1, Nc = 0, Nb = 0, maxS = 1;
