@@ -463,18 +463,25 @@ def _pathological(kind, n, seed):
     return b
 
 
+@pytest.mark.parametrize("relative", [False, True])
 @pytest.mark.parametrize("kind", ["two_clusters", "ring", "line", "core_and_halo", "offset", "plane"])
-def test_headline_configuration_on_unusual_distributions(res, oracle, kind):
-    """The headline walk (quadrupole + 64-body groups + local expansion) stays finite
-    and at least as accurate as the reference rule at the same theta, judged against
-    FP64, on distributions that stress the box, the keys and the group radius. (On
-    the line the interior accelerations nearly cancel, so relative errors are large
-    for every method and only the percentiles are compared.)"""
+def test_headline_configuration_on_unusual_distributions(res, oracle, kind, relative):
+    """The headline walks (quadrupole + 64-body groups + local expansion at theta 0.52;
+    the same with the error-bound opening, alpha 2.75e-3 under a theta-1 cap) stay
+    finite and at least as accurate as the reference rule at theta 0.52, judged
+    against FP64, on distributions that stress the box, the keys, the group radius
+    and the per-group |a| estimate. (On the line the interior accelerations nearly
+    cancel, so relative errors are large for every method and only the percentiles
+    are compared.)"""
     b = _pathological(kind, 20000, 57)
     ref64 = oracle.bf_f64(b[::10], b, 0.01, True)
     plain = oracle.bh_f32(b[::10], b, 0.52, 0.01, True)
-    head = cuda.BarnesHut(0.52, res, AccelerationSoftened(0.01), quadrupole=True, group=True,
-                          local=True).compute(b)[::10]
+    if relative:
+        m = cuda.BarnesHut(1.0, res, AccelerationSoftened(0.01), quadrupole=True, group=True, local=True,
+                           relative=2.75e-3)
+    else:
+        m = cuda.BarnesHut(0.52, res, AccelerationSoftened(0.01), quadrupole=True, group=True, local=True)
+    head = m.compute(b)[::10]
     assert np.isfinite(head).all()
     e_ref, e_head = rel(plain, ref64), rel(head, ref64)
     print(f"{kind}: p95 reference rule {np.percentile(e_ref, 95):.2e}, headline {np.percentile(e_head, 95):.2e}, "
