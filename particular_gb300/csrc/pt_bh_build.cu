@@ -266,85 +266,9 @@ __global__ void level_offsets(int *__restrict__ levels) {
     levels[2 * LEVELS + 1] = acc;
 }
 
-// ---- 6. preorder layout ------------------------------------------------------
-// nodeB = {width bits, skip, first body (-1: internal cell), body count}.
-// counters[1] = T (cells + leaves), counters[2] = internal cells.
-template <class T>
-__global__ void layout(int *counters, const int *__restrict__ bfirst,
-                       const int *__restrict__ blast, const int *__restrict__ bdelta,
-                       const uint8_t *__restrict__ top, const int *__restrict__ oparent,
-                       const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ pscan,
-                       const uint64_t *__restrict__ ukey, const uint32_t *__restrict__ ufirst,
-                       const T *__restrict__ box, int *__restrict__ pre, int4 *__restrict__ nodeB,
-                       typename Prec<T>::V4 *__restrict__ nodeG, int2 *__restrict__ nodeR,
-                       const int *__restrict__ loparent, const uint8_t *__restrict__ cslot,
-                       const uint8_t *__restrict__ lslot, int *__restrict__ kid, int *__restrict__ levels,
-                       int *__restrict__ by_level) {
-    using P = Prec<T>;
-    __shared__ int h[LEVELS], base[LEVELS];
-    if (threadIdx.x < LEVELS) h[threadIdx.x] = 0;
-    __syncthreads();
-    const int M = counters[0];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int lvl = -1, lrank = 0;  // this cell's octree level and rank among the block's
-    if (k == 0) {
-        counters[1] = M + int(pscan[M]);
-        counters[2] = int(pscan[M]);
-    }
-    if (k < M - 1 && top[k]) {
-        const int b = bfirst[k];
-        int r = 0;
-        for (int p = oparent[k]; p >= 0 && bfirst[p] == b; p = oparent[p]) ++r;
-        const int pk = b + int(pscan[b]) + r;
-        pre[k] = pk;
-        const int after = blast[k] + 1;
-        const int skip = after + int(pscan[after]);
-        // Cell box at level L along the key's path: BoundingBox::width() of the
-        // reference cell (partition.rs:322-327) and its centre, replayed in the same
-        // f32 ops.
-        const int L = bdelta[k] / 3;
-        const uint64_t key = ukey[b];
-        T mn0 = box[0], mn1 = box[1], mn2 = box[2], mx0 = box[3], mx1 = box[4], mx2 = box[5];
-        for (int l = 0; l < L; ++l) {
-            const int o = 7 - int((key >> (3 * (LEVELS - 1 - l))) & 7u);
-            const T c0 = P::mul(P::add(mn0, mx0), T(0.5));
-            const T c1 = P::mul(P::add(mn1, mx1), T(0.5));
-            const T c2 = P::mul(P::add(mn2, mx2), T(0.5));
-            if (o & 1) mx0 = c0; else mn0 = c0;
-            if (o & 2) mx1 = c1; else mn1 = c1;
-            if (o & 4) mx2 = c2; else mn2 = c2;
-        }
-        const T w = P::sub(mx0, mn0);
-        // the f32 walk reads the width from nodeB.x; the f64 walk from nodeG.w
-        nodeB[pk] = make_int4(sizeof(T) == 4 ? __float_as_int(float(w)) : 0, skip, -1, 0);
-        nodeG[pk] = P::make(T(0.5) * (mn0 + mx0), T(0.5) * (mn1 + mx1), T(0.5) * (mn2 + mx2), w);
-        nodeR[pk] = make_int2(int(ufirst[b]), int(ufirst[blast[k] + 1]));
-        // the cell's entry in its parent's child list
-        if (k != 0) kid[8 * oparent[k] + cslot[k]] = 2 * pk;
-        lvl = L;
-        lrank = atomicAdd(&h[L], 1);
-    }
-    if (k < M) {
-        const int pk = k + int(pscan[k]) + int(cnt[k]);
-        const int f = int(ufirst[k]);
-        const int nb = int(ufirst[k + 1]) - f;
-        nodeB[pk] = make_int4(0, pk + 1, f, nb);
-        nodeG[pk] = P::make(T(0), T(0), T(0), T(0));
-        nodeR[pk] = make_int2(f, int(ufirst[k + 1]));
-        const int op = loparent[k];
-        if (op >= 0) kid[8 * op + lslot[k]] = 2 * pk + (nb == 1 ? 1 : 0);
-    }
-    // cells bucketed by octree level (one range per level and block)
-    __syncthreads();
-    if (threadIdx.x < LEVELS && h[threadIdx.x])
-        base[threadIdx.x] = atomicAdd(&levels[2 * LEVELS + 2 + threadIdx.x], h[threadIdx.x]);
-    __syncthreads();
-    if (lvl >= 0) by_level[base[lvl] + lrank] = k;
-}
-
 // ---- 7. moments ------------------------------------------------------------
-// Leaves first (one thread per leaf unit), then the cells one octree level per
-// launch, deepest first, one thread per cell: every cell's children are complete
+// Leaves first (in the layout pass, one thread per leaf unit), then the cells one
+// octree level per launch, deepest first, one thread per cell: every cell's children are complete
 // when it is combined, and it reads them from its child list, all loads at once.
 // The order of every sum is fixed by the tree. (A single bottom-up launch in which
 // the last child to arrive combined its parent was slower, 2.04 against 1.81 ms of
@@ -642,15 +566,82 @@ __device__ void cell(int pv, const Kids &K, const double4_32a *__restrict__ node
 template <class T>
 using Record = typename std::conditional<sizeof(T) == 4, Rec32, Moments>::type;
 
+// ---- 6. preorder layout (and the leaves' records) ---------------------------
+// nodeB = {width bits, skip, first body (-1: internal cell), body count}.
+// counters[1] = T (cells + leaves), counters[2] = internal cells.
 template <class T>
-__global__ void __launch_bounds__(256)
-    leaf_records(const int *__restrict__ counters, const uint32_t *__restrict__ ufirst,
-                 const typename Prec<T>::V4 *__restrict__ sbody, const uint32_t *__restrict__ pscan,
-                 const uint32_t *__restrict__ cnt, Record<T> *rec, typename Prec<T>::V4 *nodeA, float4 *nodeQ) {
+__global__ void layout(int *counters, const int *__restrict__ bfirst,
+                       const int *__restrict__ blast, const int *__restrict__ bdelta,
+                       const uint8_t *__restrict__ top, const int *__restrict__ oparent,
+                       const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ pscan,
+                       const uint64_t *__restrict__ ukey, const uint32_t *__restrict__ ufirst,
+                       const T *__restrict__ box, int *__restrict__ pre, int4 *__restrict__ nodeB,
+                       typename Prec<T>::V4 *__restrict__ nodeG, int2 *__restrict__ nodeR,
+                       const int *__restrict__ loparent, const uint8_t *__restrict__ cslot,
+                       const uint8_t *__restrict__ lslot, int *__restrict__ kid, int *__restrict__ levels,
+                       int *__restrict__ by_level, const typename Prec<T>::V4 *__restrict__ sbody, Record<T> *rec,
+                       typename Prec<T>::V4 *nodeA, float4 *nodeQ) {
+    using P = Prec<T>;
+    __shared__ int h[LEVELS], base[LEVELS];
+    if (threadIdx.x < LEVELS) h[threadIdx.x] = 0;
+    __syncthreads();
     const int M = counters[0];
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= M) return;
-    leaf(u + int(pscan[u]) + int(cnt[u]), int(ufirst[u]), int(ufirst[u + 1]), sbody, rec, nodeA, nodeQ);
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int lvl = -1, lrank = 0;  // this cell's octree level and rank among the block's
+    if (k == 0) {
+        counters[1] = M + int(pscan[M]);
+        counters[2] = int(pscan[M]);
+    }
+    if (k < M - 1 && top[k]) {
+        const int b = bfirst[k];
+        int r = 0;
+        for (int p = oparent[k]; p >= 0 && bfirst[p] == b; p = oparent[p]) ++r;
+        const int pk = b + int(pscan[b]) + r;
+        pre[k] = pk;
+        const int after = blast[k] + 1;
+        const int skip = after + int(pscan[after]);
+        // Cell box at level L along the key's path: BoundingBox::width() of the
+        // reference cell (partition.rs:322-327) and its centre, replayed in the same
+        // f32 ops.
+        const int L = bdelta[k] / 3;
+        const uint64_t key = ukey[b];
+        T mn0 = box[0], mn1 = box[1], mn2 = box[2], mx0 = box[3], mx1 = box[4], mx2 = box[5];
+        for (int l = 0; l < L; ++l) {
+            const int o = 7 - int((key >> (3 * (LEVELS - 1 - l))) & 7u);
+            const T c0 = P::mul(P::add(mn0, mx0), T(0.5));
+            const T c1 = P::mul(P::add(mn1, mx1), T(0.5));
+            const T c2 = P::mul(P::add(mn2, mx2), T(0.5));
+            if (o & 1) mx0 = c0; else mn0 = c0;
+            if (o & 2) mx1 = c1; else mn1 = c1;
+            if (o & 4) mx2 = c2; else mn2 = c2;
+        }
+        const T w = P::sub(mx0, mn0);
+        // the f32 walk reads the width from nodeB.x; the f64 walk from nodeG.w
+        nodeB[pk] = make_int4(sizeof(T) == 4 ? __float_as_int(float(w)) : 0, skip, -1, 0);
+        nodeG[pk] = P::make(T(0.5) * (mn0 + mx0), T(0.5) * (mn1 + mx1), T(0.5) * (mn2 + mx2), w);
+        nodeR[pk] = make_int2(int(ufirst[b]), int(ufirst[blast[k] + 1]));
+        // the cell's entry in its parent's child list
+        if (k != 0) kid[8 * oparent[k] + cslot[k]] = 2 * pk;
+        lvl = L;
+        lrank = atomicAdd(&h[L], 1);
+    }
+    if (k < M) {
+        const int pk = k + int(pscan[k]) + int(cnt[k]);
+        const int f = int(ufirst[k]);
+        const int nb = int(ufirst[k + 1]) - f;
+        nodeB[pk] = make_int4(0, pk + 1, f, nb);
+        nodeG[pk] = P::make(T(0), T(0), T(0), T(0));
+        nodeR[pk] = make_int2(f, int(ufirst[k + 1]));
+        const int op = loparent[k];
+        if (op >= 0) kid[8 * op + lslot[k]] = 2 * pk + (nb == 1 ? 1 : 0);
+        leaf(pk, f, f + nb, sbody, rec, nodeA, nodeQ);  // the leaf's moment record
+    }
+    // cells bucketed by octree level (one range per level and block)
+    __syncthreads();
+    if (threadIdx.x < LEVELS && h[threadIdx.x])
+        base[threadIdx.x] = atomicAdd(&levels[2 * LEVELS + 2 + threadIdx.x], h[threadIdx.x]);
+    __syncthreads();
+    if (lvl >= 0) by_level[base[lvl] + lrank] = k;
 }
 
 // The cells of octree level L (levels below: done), one thread each.
@@ -751,12 +742,10 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
                                      as<uint32_t>(S.pscan), as<uint64_t>(S.ukey), as<uint32_t>(S.ufirst),
                                      as<T>(S.box), as<int>(S.pre), as<int4>(S.nodeB), as<V4>(nG),
                                      as<int2>(S.nodeR), as<int>(S.loparent), as<uint8_t>(S.cslot),
-                                     as<uint8_t>(S.lslot), as<int>(S.kid), levels, as<int>(S.by_level));
+                                     as<uint8_t>(S.lslot), as<int>(S.kid), levels, as<int>(S.by_level), as<V4>(sb),
+                                     as<Record<T>>(S.mom), as<V4>(nA), nodeQ);
     PT_TRY(check_launch(ctx, "layout"));
 
-    leaf_records<T><<<blocks(n), 256, 0, st>>>(counters, as<uint32_t>(S.ufirst), as<V4>(sb), as<uint32_t>(S.pscan),
-                                              as<uint32_t>(S.cnt), as<Record<T>>(S.mom), as<V4>(nA), nodeQ);
-    PT_TRY(check_launch(ctx, "leaf_records"));
     const int lvl_grid = std::max(1, std::min(blocks(n), 8 * ctx->sm_count));
     for (int L = LEVELS - 1; L >= 0; --L) {
         // level L holds at most 8^L cells: shallow levels get a grid of their size
