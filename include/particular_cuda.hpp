@@ -359,7 +359,8 @@ struct BarnesHut {
     S theta;
     CudaResources &resources;
     T interaction;
-    uint32_t flags = 0;  // PT_BH_QUADRUPOLE | PT_BH_GROUP
+    uint32_t flags = 0;  // PT_BH_QUADRUPOLE | PT_BH_GROUP | PT_BH_LOCAL | PT_BH_RELATIVE
+    float alpha = 0.f;   // PT_BH_RELATIVE: the error-bound factor (0: the resources' current one)
 
     // Builds the tree over the affecting particles of `storage` once.
     template <class Storage>
@@ -380,6 +381,7 @@ struct BarnesHut {
         const auto aff = detail::pack_fields(b.affected);
         std::vector<float> out(3 * b.affected.size());
         if (out.empty()) return {};
+        set_alpha();
         check(pt_bh_walk(resources.get(), aff.data(), b.affected.size(), float(theta), interaction.softening(), flags,
                          out.data()));
         return detail::unpack(out);
@@ -409,12 +411,17 @@ struct BarnesHut {
     }
 
   private:
+    void set_alpha() {
+        if ((flags & PT_BH_RELATIVE) && alpha > 0.f) check(pt_bh_set_relative_alpha(resources.get(), alpha));
+    }
+
     template <class P1, class P2>
     std::vector<Vec3> compute_f32(const Between<Slice<P1>, Slice<P2>> &b, bool same) {
         const auto aff = detail::pack_fields(b.affected);
         const auto src = same ? std::vector<float>() : detail::pack_fields(b.affecting);
         std::vector<float> out(3 * b.affected.size());
         if (out.empty()) return {};
+        set_alpha();
         check(pt_bh_accel_f32(resources.get(), aff.data(), b.affected.size(),
                               same ? aff.data() : src.data(), b.affecting.size(), float(theta),
                               interaction.softening(), flags, out.data()));

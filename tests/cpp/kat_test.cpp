@@ -86,9 +86,11 @@ int main() {
     };
     const Case cases[] = {{0.f, 0, 1e-2f, 1e-2f, "cuda::BarnesHut(0.0)"},
                           {0.5f, 0, 5e-1f, 1e-1f, "cuda::BarnesHut(0.5)"},
-                          {0.5f, PT_BH_GROUP | PT_BH_QUADRUPOLE, 5e-1f, 1e-1f, "cuda::BarnesHut(0.5, quad+group)"}};
+                          {0.5f, PT_BH_GROUP | PT_BH_QUADRUPOLE, 5e-1f, 1e-1f, "cuda::BarnesHut(0.5, quad+group)"},
+                          {1.0f, PT_BH_GROUP | PT_BH_QUADRUPOLE | PT_BH_LOCAL | PT_BH_RELATIVE, 5e-1f, 1e-1f,
+                           "cuda::BarnesHut(1.0, headline)"}};
     for (const auto &c : cases) {
-        cuda::BarnesHut<float, Acceleration<true>> bh{c.theta, res, acceleration_checked(), c.flags};
+        cuda::BarnesHut<float, Acceleration<true>> bh{c.theta, res, acceleration_checked(), c.flags, 2.75e-3f};
         ok &= acceleration_error([&](const Reordered<Body> &r) { return bh.compute(r); }, c.err, c.name);
         ok &= circular_orbit([&](const std::vector<Body> &p) { return bh.compute(p); }, 100, c.orbit, c.name);
     }
