@@ -2,7 +2,12 @@
 """Benchmark of the cuda compute methods (one JSON line on rank 0).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload NAME]
+                    [--workload NAME] [--bodies N] [--method THETA,FLAGS[,ALPHA[,RATIO]]]
+
+The default workload calibrates the Barnes-Hut configuration (theta, flags, the
+error-bound factor alpha and the local-expansion ratio) against the FP64 judge and
+times the fastest one whose p95 error is within the bar; `--method` times one given
+configuration instead and `--bodies` changes N (short profiling runs).
 
 A step is one pass of the hot path over one batch of synthetic input (see
 WORKLOADS). `value` is whole-job throughput with inputs resident in HBM; `e2e`
