@@ -60,3 +60,22 @@ def test_single_process_identity():
     import bench
     assert bench.max_over_ranks([1.0, 2.0], None, "cpu") == [1.0, 2.0]
     assert bench.job_throughput(1, 500, 100.0, 10) == pytest.approx(500 / 10e-3)
+
+
+def test_method_and_bodies_options(monkeypatch):
+    """--bodies and --method select one Barnes-Hut configuration of a given size (no
+    calibration ladder); the ladder's rows carry theta, flags, alpha and ratio."""
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--bodies", "4096", "--method", "1.0,27,0.00275,0.13"])
+    args = bench.parse_args()
+    wl = bench.make_workload(args)
+    assert wl.n == 4096 and wl.bodies.shape == (4096, 4)
+    assert wl.fixed == (1.0, 27, 0.00275, 0.13)
+    assert wl.config()["workload"] == "bh_bulge_disk_4096"
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--bodies", "2048", "--method", "0.5,0"])
+    wl = bench.make_workload(bench.parse_args())
+    assert wl.fixed == (0.5, 0, None, 0.1)
+    for theta, flags, alpha, ratio in bench.BarnesHutWorkload.ladder:
+        assert (alpha is not None) == bool(flags & 16) and 0 < ratio <= 0.5 and 0 < theta <= 1.0
+
