@@ -259,7 +259,8 @@ class BarnesHutWorkload:
               (0.55, 11, None, 0.1),
               (1.0, 19, 1.5e-3, 0.1), (1.0, 19, 2e-3, 0.1), (1.0, 19, 2.5e-3, 0.1), (1.0, 19, 3e-3, 0.1),
               (1.0, 27, 2e-3, 0.1), (1.0, 27, 2.5e-3, 0.1), (1.0, 27, 2.75e-3, 0.1), (1.0, 27, 3e-3, 0.1),
-              (1.0, 27, 2.5e-3, 0.13), (1.0, 27, 2.75e-3, 0.13), (1.0, 27, 3e-3, 0.13)]
+              (1.0, 27, 2.5e-3, 0.13), (1.0, 27, 2.75e-3, 0.13), (1.0, 27, 3e-3, 0.13),
+              (1.0, 27, 2.5e-3, 0.15), (1.0, 27, 2.6e-3, 0.14), (1.0, 27, 2.75e-3, 0.14)]
 
     def __init__(self, n=4194304, softening=0.01, sample=2048):
         from particular_gb300 import ics
