@@ -280,6 +280,7 @@ class Leapfrog:
     def _args(self):
         m = self.method
         if isinstance(m, BarnesHut):
+            m._set_alpha()  # the method's error-bound factor, when it uses one
             return N.PT_METHOD_BARNES_HUT, m.theta, m.interaction.softening, m.flags
         return (N.PT_METHOD_BRUTE_FORCE, 0.0, m.interaction.softening,
                 N.PT_BF_EXACT if m.exact else 0)
