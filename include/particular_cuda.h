@@ -278,8 +278,9 @@ int pt_leapfrog(pt_ctx *ctx, float *bodies, float *vel, size_t n, float dt, int 
 /* Device state (16-byte aligned bodies and velocities; acc = float[3] per body
  * holding the accelerations of the current positions, updated to the final ones).
  * use_graph != 0 captures the whole `steps`-step sequence into a CUDA graph on first
- * use for this (pointers, n, steps, method, dt, theta, softening, flags, stream) and
- * replays it afterwards; that first call also recomputes `acc` from the positions
+ * use for this (pointers, n, steps, method, dt, theta, softening, flags, stream and,
+ * for Barnes-Hut, the context's local ratio, error-bound factor, stack limit and
+ * learned model) and replays it afterwards; that first call also recomputes `acc` from the positions
  * before capturing, so every buffer is sized outside the capture. */
 int pt_leapfrog_device(pt_ctx *ctx, float *d_bodies, float *d_vel, float *d_acc, size_t n, float dt,
                        int steps, int method, float theta, float softening, uint32_t flags,

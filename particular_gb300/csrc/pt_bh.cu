@@ -32,6 +32,22 @@ int validate(const char *fn, size_t n_aff, size_t n_src, uint32_t flags) {
 
 namespace pt {
 
+// The Barnes-Hut settings that captured launches carry as parameters (local ratio,
+// error-bound factor, learned inner angle, stack cap, model weights): a CUDA graph
+// captured under other values has to be captured again.
+BhTuning bh_tuning(pt_ctx *ctx) {
+    BhTuning t{};
+    const auto *S = static_cast<const bh::State *>(ctx->bh);
+    if (S) {
+        t.local_ratio = S->local_ratio;
+        t.rel_alpha = S->rel_alpha;
+        t.theta_inner = S->theta_inner;
+        t.stack_cap = S->stack_cap;
+        t.mlp = S->mlp_w;
+    }
+    return t;
+}
+
 int bh_build_only(pt_ctx *ctx, const float4 *d_src, int n) {
     bh::State *S = bh::state(ctx);
     if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
@@ -295,6 +311,7 @@ int pt_bh_set_local_ratio(pt_ctx *ctx, float ratio) {
     S->local_ratio = ratio;
     return PT_OK;
 }
+
 
 int pt_bh_set_relative_alpha(pt_ctx *ctx, float alpha) {
     using namespace pt;

@@ -57,11 +57,13 @@ struct Graph {
     float dt = 0.f, theta = 0.f, softening = 0.f;
     uint32_t flags = 0;
     cudaStream_t stream = nullptr;
+    BhTuning tune;  // Barnes-Hut settings baked into the captured launches
     uint64_t kernels = 0;
     bool same(const void *b, const void *v, const void *a, size_t n_, int s, int m, float d, float t, float e,
-              uint32_t f, cudaStream_t st) const {
+              uint32_t f, cudaStream_t st, const BhTuning &tu) const {
         return exec && body == b && vel == v && acc == a && n == n_ && steps == s && method == m && dt == d &&
-               theta == t && softening == e && flags == f && stream == st;
+               theta == t && softening == e && flags == f && stream == st &&
+               (method != PT_METHOD_BARNES_HUT || tune == tu);
     }
 };
 
@@ -126,7 +128,8 @@ extern "C" int pt_leapfrog_device(pt_ctx *ctx, float *d_body, float *d_vel, floa
     if (!use_graph)
         return lf::enqueue_steps(ctx, body, vel, d_acc, n, dt, steps, method, theta, softening, flags);
     lf::Graph &G = S->graph;
-    if (!G.same(d_body, d_vel, d_acc, n, steps, method, dt, theta, softening, flags, ctx->stream)) {
+    if (!G.same(d_body, d_vel, d_acc, n, steps, method, dt, theta, softening, flags, ctx->stream,
+                bh_tuning(ctx))) {
         if (G.exec) {
             cudaGraphExecDestroy(G.exec);
             G.exec = nullptr;
@@ -164,6 +167,7 @@ extern "C" int pt_leapfrog_device(pt_ctx *ctx, float *d_body, float *d_vel, floa
         G.softening = softening;
         G.flags = flags;
         G.stream = ctx->stream;
+        G.tune = bh_tuning(ctx);
     }
     PT_CUDA(cudaGraphLaunch(G.exec, ctx->stream));
     ctx->launches += G.kernels;  // the kernels the replayed graph runs

@@ -105,3 +105,35 @@ def test_barnes_hut_leapfrog_tracks_brute_force(res):
     b2, v2 = bh.run(d["bodies"], d["vel"], 10)
     dv = np.linalg.norm(v2 - v1, axis=1) / np.maximum(np.linalg.norm(v1 - d["vel"], axis=1), 1e-12)
     assert np.percentile(dv, 95) < 5e-3  # velocity change agrees to BH accuracy
+
+
+def test_graph_recaptured_when_settings_change(res):
+    """A captured leapfrog carries the context's Barnes-Hut settings (error-bound
+    factor, local ratio) as launch parameters: changing them captures again, so the
+    replay equals the eager steps under the new values."""
+    import torch
+    d = ics.plummer(20000, seed=53)
+    L = N.lib()
+    fl = N.PT_BH_QUADRUPOLE | N.PT_BH_GROUP | N.PT_BH_LOCAL | N.PT_BH_RELATIVE
+    outs = []
+    try:
+        for use_graph in (0, 1):
+            b = torch.from_numpy(d["bodies"]).cuda()
+            v = torch.zeros((20000, 4), device="cuda")
+            v[:, :3] = torch.from_numpy(d["vel"]).cuda()
+            a = torch.zeros((20000, 3), device="cuda")
+            for alpha, ratio in ((2.5e-3, 0.1), (1e-3, 0.13)):
+                N.check(L.pt_bh_set_relative_alpha(res.handle, alpha))
+                N.check(L.pt_bh_set_local_ratio(res.handle, ratio))
+                N.check(L.pt_bh_accel_f32_device(res.handle, b.data_ptr(), 20000, b.data_ptr(), 20000,
+                                                 1.0, 0.01, fl, a.data_ptr()))
+                for _ in range(2):
+                    N.check(L.pt_leapfrog_device(res.handle, b.data_ptr(), v.data_ptr(), a.data_ptr(), 20000,
+                                                 1e-3, 3, N.PT_METHOD_BARNES_HUT, 1.0, 0.01, fl, use_graph))
+            res.synchronize()
+            outs.append((b.cpu().numpy(), v.cpu().numpy()))
+    finally:
+        N.check(L.pt_bh_set_relative_alpha(res.handle, 2.5e-3))
+        N.check(L.pt_bh_set_local_ratio(res.handle, 0.1))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
