@@ -280,7 +280,8 @@ int pt_leapfrog(pt_ctx *ctx, float *bodies, float *vel, size_t n, float dt, int 
  * use_graph != 0 captures the whole `steps`-step sequence into a CUDA graph on first
  * use for this (pointers, n, steps, method, dt, theta, softening, flags, stream and,
  * for Barnes-Hut, the context's local ratio, error-bound factor, stack limit and
- * learned model) and replays it afterwards; that first call also recomputes `acc` from the positions
+ * learned model; any reallocation of a context buffer in between) and replays it
+ * afterwards; that first call also recomputes `acc` from the positions
  * before capturing, so every buffer is sized outside the capture. */
 int pt_leapfrog_device(pt_ctx *ctx, float *d_bodies, float *d_vel, float *d_acc, size_t n, float dt,
                        int steps, int method, float theta, float softening, uint32_t flags,

@@ -46,6 +46,9 @@ struct pt_ctx {
     size_t capacity_limit = 0;  // 0 = unlimited
     size_t bytes_held = 0;
     unsigned long long launches = 0;
+    // Bumped whenever a context buffer is allocated, reallocated or freed: CUDA graphs
+    // that captured buffer addresses are captured again when it has moved.
+    unsigned long long buf_epoch = 0;
     pt::DevBuf bufs[pt::BUF_COUNT];
     // Extra subsystems hang off the context lazily.
     void *bh = nullptr;

@@ -52,6 +52,7 @@ int ensure_buf(pt_ctx *ctx, DevBuf &b, size_t bytes) {
                              "context capacity limit %zu bytes exceeded (need %zu held)",
                              ctx->capacity_limit, after);
     }
+    ++ctx->buf_epoch;  // the buffer's address changes
     if (b.ptr) {
         // Work already enqueued may still read the old buffer.
         cudaStreamSynchronize(ctx->stream);
@@ -73,6 +74,7 @@ int ensure_buf(pt_ctx *ctx, DevBuf &b, size_t bytes) {
 
 void free_buf(pt_ctx *ctx, DevBuf &b) {
     if (b.ptr) {
+        ++ctx->buf_epoch;
         cudaFree(b.ptr);
         ctx->bytes_held -= b.cap;
     }

@@ -205,6 +205,7 @@ struct State {
     const void *g_body = nullptr, *g_vel = nullptr;
     int g_steps = 0;
     float g_dt = 0.f, g_eps = 0.f;
+    unsigned long long g_epoch = 0;  // the context's buffer addresses it captured
     uint64_t g_kernels = 0;
 };
 
@@ -331,7 +332,7 @@ extern "C" int pt_ensemble_run(pt_ctx *ctx, const uint32_t *offsets, uint32_t n_
         PT_TRY(ens::launch(ctx, *S, body, vel, n, steps, dt, eps2));
     } else {
         if (!(S->exec && S->g_body == d_bodies && S->g_vel == d_vel && S->g_steps == steps && S->g_dt == dt &&
-              S->g_eps == softening)) {
+              S->g_eps == softening && S->g_epoch == ctx->buf_epoch)) {
             if (S->exec) {
                 cudaGraphExecDestroy(S->exec);
                 S->exec = nullptr;
@@ -358,6 +359,7 @@ extern "C" int pt_ensemble_run(pt_ctx *ctx, const uint32_t *offsets, uint32_t n_
             S->g_steps = steps;
             S->g_dt = dt;
             S->g_eps = softening;
+            S->g_epoch = ctx->buf_epoch;
         }
         PT_CUDA(cudaGraphLaunch(S->exec, ctx->stream));
         ctx->launches += S->g_kernels;

@@ -57,12 +57,13 @@ struct Graph {
     float dt = 0.f, theta = 0.f, softening = 0.f;
     uint32_t flags = 0;
     cudaStream_t stream = nullptr;
-    BhTuning tune;  // Barnes-Hut settings baked into the captured launches
+    BhTuning tune;                 // Barnes-Hut settings baked into the captured launches
+    unsigned long long epoch = 0;  // the context's buffer addresses it captured
     uint64_t kernels = 0;
     bool same(const void *b, const void *v, const void *a, size_t n_, int s, int m, float d, float t, float e,
-              uint32_t f, cudaStream_t st, const BhTuning &tu) const {
+              uint32_t f, cudaStream_t st, const BhTuning &tu, unsigned long long ep) const {
         return exec && body == b && vel == v && acc == a && n == n_ && steps == s && method == m && dt == d &&
-               theta == t && softening == e && flags == f && stream == st &&
+               theta == t && softening == e && flags == f && stream == st && epoch == ep &&
                (method != PT_METHOD_BARNES_HUT || tune == tu);
     }
 };
@@ -129,7 +130,7 @@ extern "C" int pt_leapfrog_device(pt_ctx *ctx, float *d_body, float *d_vel, floa
         return lf::enqueue_steps(ctx, body, vel, d_acc, n, dt, steps, method, theta, softening, flags);
     lf::Graph &G = S->graph;
     if (!G.same(d_body, d_vel, d_acc, n, steps, method, dt, theta, softening, flags, ctx->stream,
-                bh_tuning(ctx))) {
+                bh_tuning(ctx), ctx->buf_epoch)) {
         if (G.exec) {
             cudaGraphExecDestroy(G.exec);
             G.exec = nullptr;
@@ -168,6 +169,7 @@ extern "C" int pt_leapfrog_device(pt_ctx *ctx, float *d_body, float *d_vel, floa
         G.flags = flags;
         G.stream = ctx->stream;
         G.tune = bh_tuning(ctx);
+        G.epoch = ctx->buf_epoch;  // no buffer grows during the capture
     }
     PT_CUDA(cudaGraphLaunch(G.exec, ctx->stream));
     ctx->launches += G.kernels;  // the kernels the replayed graph runs
