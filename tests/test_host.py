@@ -28,6 +28,11 @@ def test_calls_reject_null_context_without_gpu(native_lib):
     assert native_lib.pt_ctx_create(None, 0) == N.PT_ERR_INVALID
     assert native_lib.pt_ctx_set_capacity_limit(None, 0) == N.PT_ERR_INVALID
     assert native_lib.pt_ctx_launch_count(None) == 0
+    # the Barnes-Hut settings refuse a NULL context before touching any state
+    assert native_lib.pt_bh_set_relative_alpha(None, 2.5e-3) == N.PT_ERR_INVALID
+    assert "ctx is NULL" in N.last_error()
+    assert native_lib.pt_bh_set_local_ratio(None, 0.1) == N.PT_ERR_INVALID
+    assert native_lib.pt_bh_set_stack_limit(None, 0) == N.PT_ERR_INVALID
     native_lib.pt_ctx_destroy(None)
 
 
