@@ -147,6 +147,9 @@ int pt_measure_fp32_peak(pt_ctx *ctx, double *tflops);
  *   whose work overlaps on the GPU (other streams, other threads) race, so
  *   serialise them. Every scratch byte a call reads is written earlier by the
  *   same call; nothing needs clearing.
+ * - The address looked up on a device's first call is kept for the process: a
+ *   device reset (cudaDeviceReset, or anything else that destroys the primary
+ *   context) is not supported afterwards.
  * This entry point has no counterpart in the reference. */
 #define PT_NOALLOC_MAX_SOURCES 524288
 int pt_bf_accel_f32_noalloc(const float *d_affected, size_t n_aff, const float *d_affecting,
@@ -223,6 +226,23 @@ int pt_bh_build_device(pt_ctx *ctx, const float *d_affecting, size_t n_src, uint
 int pt_bh_walk_device(pt_ctx *ctx, const float *d_affected, size_t n_aff, float theta, float softening,
                       uint32_t flags, float *d_out_xyz);
 int pt_bh_tree_generation(pt_ctx *ctx, uint64_t *generation);
+/* Makes a tree the caller built the context's current tree, for pt_bh_walk[_device]:
+ * the GPU counterpart of computing Between(affected, &tree) over a RootedOrthtree the
+ * caller constructed or kept (particular/src/lib.rs:186-199, sequential.rs:466-522,
+ * storage.rs:10-46). The arrays are the reference's Orthtree<8, 3, f32,
+ * GravitationalField<Vec3, f32>> (tree/mod.rs:13-60) flattened per node:
+ *   orthant  int32[8]  SizedOrthant::orthant, child NodeID or -1 for None
+ *   bbox     float[6]  SizedOrthant::bbox, min x, y, z then max x, y, z
+ *   internal uint8     1 = Node::Internal, 0 = Node::External (orthant, bbox unused)
+ *   data     float[4]  the node's GravitationalField: centre of mass x, y, z, mass
+ * and root = RootedOrthtree::root() (-1 = None: every acceleration is zero). A walk
+ * then accepts, for every affected body, exactly the nodes the reference's walk of this
+ * tree accepts (the same opening rule, width = max.x - min.x, skip at d^2 == 0); sums
+ * run in list order (rounding-level differences). Such a tree carries monopoles only:
+ * walks take flags 0 or PT_BH_GROUP. A node reachable twice from the root is rejected
+ * (PT_ERR_INVALID). Synchronous (the host arrays may change after the call). */
+int pt_bh_load_tree(pt_ctx *ctx, const int32_t *orthant, const float *bbox, const uint8_t *internal,
+                    const float *data, size_t n_nodes, int64_t root, uint64_t *generation);
 /* The same over host buffers (synchronous): the bodies are staged in context buffers;
  * the tree keeps its own copy, so `affecting` may change after pt_bh_build returns. */
 int pt_bh_build(pt_ctx *ctx, const float *affecting, size_t n_src, uint64_t *generation);
@@ -237,6 +257,13 @@ int pt_bh_set_relative_alpha(pt_ctx *ctx, float alpha);
  * the compiled capacity; 0 restores the capacity). A warp that runs out takes the
  * per-body walk instead (counted in pt_bh_stats.overflow): a tuning and test hook. */
 int pt_bh_set_stack_limit(pt_ctx *ctx, int ranges);
+/* Fixes the record capacity of PT_BH_LEARNED walks at `chunks` chunks of 128 cells
+ * (0 restores the automatic capacity, which grows and reruns a walk whose records did
+ * not fit). With a fixed capacity, or inside a captured leapfrog graph, a walk whose
+ * records overflow keeps the plain result for the cells that did not fit and the call
+ * fails with PT_ERR_CAPACITY (pt_bh_accel_f32, pt_bh_walk, pt_leapfrog_device). A
+ * tuning and test hook. */
+int pt_bh_set_learned_capacity(pt_ctx *ctx, int chunks);
 /* cuda::BarnesHut over glam DVec3 bodies: double[4] (x, y, z, mu) in, double[3] out.
  * The reference's BarnesHut over f64 particles (sequential.rs:456-543 with
  * BoundingBox<DVec3>, f64 theta and the f64 per-pair kernel, gravity/impls/glam.rs:234):
@@ -282,7 +309,11 @@ int pt_leapfrog(pt_ctx *ctx, float *bodies, float *vel, size_t n, float dt, int 
  * for Barnes-Hut, the context's local ratio, error-bound factor, stack limit and
  * learned model; any reallocation of a context buffer in between) and replays it
  * afterwards; that first call also recomputes `acc` from the positions
- * before capturing, so every buffer is sized outside the capture. */
+ * before capturing, so every buffer is sized outside the capture.
+ * With PT_BH_LEARNED the call synchronises at the end and fails with PT_ERR_CAPACITY
+ * when any step's learned-correction records overflowed (the state has then advanced
+ * with the plain result for those cells); the next call captures again with room for
+ * them. The forced brute-force plan (pt_bf_set_plan) is part of the captured shape. */
 int pt_leapfrog_device(pt_ctx *ctx, float *d_bodies, float *d_vel, float *d_acc, size_t n, float dt,
                        int steps, int method, float theta, float softening, uint32_t flags,
                        int use_graph);

@@ -96,6 +96,7 @@ def _declare(L):
                                                   c_ptr]),
         "pt_bh_last_stats": (ctypes.c_int, [c_ptr, ctypes.POINTER(BhStats)]),
         "pt_bh_set_stack_limit": (ctypes.c_int, [c_ptr, ctypes.c_int]),
+        "pt_bh_set_learned_capacity": (ctypes.c_int, [c_ptr, ctypes.c_int]),
         "pt_bh_set_local_ratio": (ctypes.c_int, [c_ptr, ctypes.c_float]),
         "pt_bh_set_relative_alpha": (ctypes.c_int, [c_ptr, ctypes.c_float]),
         "pt_bh_accel_dvec3": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr, ctypes.c_size_t,
@@ -108,6 +109,8 @@ def _declare(L):
         "pt_bh_walk_device": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, ctypes.c_float, ctypes.c_float,
                                              ctypes.c_uint32, c_ptr]),
         "pt_bh_tree_generation": (ctypes.c_int, [c_ptr, c_ptr]),
+        "pt_bh_load_tree": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, ctypes.c_size_t, ctypes.c_int64,
+                                           c_ptr]),
         "pt_bh_build": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr]),
         "pt_bh_walk": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, ctypes.c_float, ctypes.c_float,
                                       ctypes.c_uint32, c_ptr]),

@@ -455,6 +455,11 @@ static thread_local Forced g_forced;
 
 }  // namespace bf
 
+void bf_forced_plan(int *targets_per_thread, int *slices) {
+    *targets_per_thread = bf::g_forced.k;
+    *slices = bf::g_forced.s;
+}
+
 // Launches the fast or exact f32 brute force on device buffers (ctx->stream).
 int bf_launch_f32(pt_ctx *ctx, const float4 *aff, int n_aff, const float4 *src, int n_src,
                   float softening, int checked, uint32_t flags, float *out) {

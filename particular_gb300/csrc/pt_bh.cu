@@ -3,6 +3,10 @@
 // per-context state.
 #include "pt_bh.cuh"
 
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
 #include <vector>
 
 namespace pt {
@@ -43,9 +47,32 @@ BhTuning bh_tuning(pt_ctx *ctx) {
         t.rel_alpha = S->rel_alpha;
         t.theta_inner = S->theta_inner;
         t.stack_cap = S->stack_cap;
+        t.learned_cap = S->lcap_fixed;
         t.mlp = S->mlp_w;
     }
     return t;
+}
+
+int *bh_error_word(pt_ctx *ctx) {
+    auto *S = static_cast<bh::State *>(ctx->bh);
+    return (S && S->counters.ptr) ? static_cast<int *>(S->counters.ptr) + 3 : nullptr;
+}
+
+int bh_learned_overflow(pt_ctx *ctx, const char *fn) {
+    auto *S = static_cast<bh::State *>(ctx->bh);
+    if (!S || !S->counters.ptr) return PT_OK;
+    int err = 0, used = 0;
+    PT_CUDA(cudaMemcpyAsync(&err, static_cast<int *>(S->counters.ptr) + 3, sizeof(int), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    if (S->lused.ptr)
+        PT_CUDA(cudaMemcpyAsync(&used, S->lused.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PT_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (!(err & 2)) return PT_OK;
+    if (S->lcap_fixed == 0 && used > S->lcap) S->lcap = used + used / 4;
+    return set_error(PT_ERR_CAPACITY,
+                     "%s: learned-correction records overflowed (%d chunks needed, %d available); the state "
+                     "advanced without the corrections that did not fit",
+                     fn, used, S->lcap_fixed ? S->lcap_fixed : S->lcap);
 }
 
 int bh_build_only(pt_ctx *ctx, const float4 *d_src, int n) {
@@ -238,10 +265,117 @@ int pt_bh_walk_device(pt_ctx *ctx, const float *d_aff, size_t n_aff, float theta
         PT_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * 3 * n_aff, ctx->stream));
         return PT_OK;
     }
+    if (S->user_tree && (flags & ~uint32_t(PT_BH_GROUP)))
+        return set_error(PT_ERR_INVALID,
+                         "pt_bh_walk_device: a caller-built tree carries monopoles only (flags 0 or PT_BH_GROUP)");
     mark(ctx, 0);
     PT_TRY(bh::sort_targets(ctx, *S, reinterpret_cast<const float4 *>(d_aff), int(n_aff)));
     return bh::walk(ctx, *S, bh::as<float4>(S->tbody), bh::as<uint32_t>(S->tidx), int(n_aff), theta, softening,
                     flags, d_out);
+}
+
+// A tree the caller built, in the layout of the reference's RootedOrthtree over
+// GravitationalField<Vec3, f32> (tree/mod.rs:13-60, storage.rs:10-46): per node its
+// eight orthant slots (Option<NodeID>, -1 = None), its bounding box (min, max), whether
+// it is Node::Internal, and its data (centre of mass, mass). It is flattened on the
+// host into the walk's layout: depth-first preorder in the reference's visiting order
+// (sequential.rs:470-505 pushes orthants 0..7 and pops 7..0, so children follow in
+// the order 7..0), skip pointers, widths BoundingBox::width() = max.x - min.x in f32.
+// External nodes become single-body leaves holding their data. Nothing is collapsed
+// or recomputed: the walk accepts, for every body, exactly the nodes the reference's
+// walk of this tree accepts.
+int pt_bh_load_tree(pt_ctx *ctx, const int32_t *orthant, const float *bbox, const uint8_t *internal,
+                    const float *data, size_t n_nodes, int64_t root, uint64_t *generation) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_load_tree: ctx is NULL");
+    if (n_nodes > size_t(INT_MAX / 8)) return set_error(PT_ERR_INVALID, "pt_bh_load_tree: %zu nodes", n_nodes);
+    if (root < -1 || root >= int64_t(n_nodes))
+        return set_error(PT_ERR_INVALID, "pt_bh_load_tree: root %lld outside [-1, %zu)", (long long)root, n_nodes);
+    if (n_nodes && (!orthant || !bbox || !internal || !data))
+        return set_error(PT_ERR_INVALID, "pt_bh_load_tree: NULL array");
+    PT_CUDA(cudaSetDevice(ctx->device));
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    std::vector<float4> A, leaves;
+    std::vector<int4> B;
+    std::vector<uint8_t> seen(n_nodes, 0);
+    int cells = 0;
+    float box[8] = {-1.f, -1.f, -1.f, 1.f, 1.f, 1.f, 0.f, 0.f};
+    if (root >= 0) {
+        // stack entries: a node to open (>= 0) or ~k, the end of preorder node k's subtree
+        std::vector<int64_t> st{root};
+        while (!st.empty()) {
+            const int64_t x = st.back();
+            st.pop_back();
+            if (x < 0) {
+                B[size_t(~x)].y = int(A.size());
+                continue;
+            }
+            if (x >= int64_t(n_nodes))
+                return set_error(PT_ERR_INVALID, "pt_bh_load_tree: orthant slot names node %lld of %zu",
+                                 (long long)x, n_nodes);
+            if (seen[size_t(x)])
+                return set_error(PT_ERR_INVALID, "pt_bh_load_tree: node %lld is reachable twice (not a tree)",
+                                 (long long)x);
+            seen[size_t(x)] = 1;
+            const int k = int(A.size());
+            const float *d = data + 4 * size_t(x);
+            A.push_back(make_float4(d[0], d[1], d[2], d[3]));
+            if (internal[size_t(x)]) {
+                const float *bb = bbox + 6 * size_t(x);
+                const float w = bb[3] - bb[0];  // BoundingBox::width(), as the reference computes it
+                // the opening factor (M w^3)^(2/5) of the error-bound rule, as built trees keep it
+                const float f = std::pow(std::max(d[3], 0.f) * w * w * w, 0.4f);
+                int wb, fb;
+                std::memcpy(&wb, &w, 4);
+                std::memcpy(&fb, &f, 4);
+                B.push_back(make_int4(wb, k + 1, -1, fb));
+                ++cells;
+                if (k == 0)
+                    for (int a = 0; a < 6; ++a) box[a] = bb[a];
+                st.push_back(~int64_t(k));
+                const int32_t *o = orthant + 8 * size_t(x);
+                for (int c = 0; c < 8; ++c)  // pushed 0..7: child 7 is opened first
+                    if (o[c] >= 0) st.push_back(o[c]);
+                    else if (o[c] != -1)
+                        return set_error(PT_ERR_INVALID, "pt_bh_load_tree: orthant slot %d of node %lld is %d",
+                                         c, (long long)x, o[c]);
+            } else {
+                B.push_back(make_int4(0, k + 1, int(leaves.size()), 1));
+                leaves.push_back(A.back());
+                if (k == 0)
+                    for (int a = 0; a < 3; ++a) box[a] = d[a] - 1.f, box[3 + a] = d[a] + 1.f;
+            }
+        }
+    }
+    const size_t T = A.size(), L = leaves.size();
+    if (T) {
+        PT_TRY(ensure_buf(ctx, S->nodeA, 16 * T));
+        PT_TRY(ensure_buf(ctx, S->nodeB, 16 * T));
+        PT_TRY(ensure_buf(ctx, S->nodeQ, 32 * T));
+        PT_TRY(ensure_buf(ctx, S->sbody, 16 * std::max<size_t>(L, 1)));
+    }
+    PT_TRY(ensure_buf(ctx, S->counters, 4 * sizeof(int) + 8 * sizeof(unsigned long long)));
+    PT_TRY(ensure_buf(ctx, S->box, sizeof(float) * 8));
+    cudaStream_t st = ctx->stream;
+    const int counts[4] = {int(L), int(T), cells, 0};
+    if (T) {
+        PT_CUDA(cudaMemcpyAsync(S->nodeA.ptr, A.data(), 16 * T, cudaMemcpyHostToDevice, st));
+        PT_CUDA(cudaMemcpyAsync(S->nodeB.ptr, B.data(), 16 * T, cudaMemcpyHostToDevice, st));
+        PT_CUDA(cudaMemsetAsync(S->nodeQ.ptr, 0, 32 * T, st));
+        if (L) PT_CUDA(cudaMemcpyAsync(S->sbody.ptr, leaves.data(), 16 * L, cudaMemcpyHostToDevice, st));
+    }
+    PT_CUDA(cudaMemsetAsync(S->counters.ptr, 0, 4 * sizeof(int) + 8 * sizeof(unsigned long long), st));
+    PT_CUDA(cudaMemcpyAsync(S->counters.ptr, counts, sizeof(counts), cudaMemcpyHostToDevice, st));
+    PT_CUDA(cudaMemcpyAsync(S->box.ptr, box, sizeof(box), cudaMemcpyHostToDevice, st));
+    PT_CUDA(cudaStreamSynchronize(st));  // the host arrays are freed on return
+    S->f64 = false;
+    S->user_tree = true;
+    S->last_n_src = int(T);  // nonzero when the tree has a node (an internal root alone still adds its data)
+    ++S->generation;
+    if (generation) *generation = S->generation;
+    return PT_OK;
 }
 
 int pt_bh_build(pt_ctx *ctx, const float *src, size_t n_src, uint64_t *generation) {
@@ -335,6 +469,18 @@ int pt_bh_set_stack_limit(pt_ctx *ctx, int ranges) {
     bh::State *S = bh::state(ctx);
     if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
     S->stack_cap = ranges;
+    return PT_OK;
+}
+
+int pt_bh_set_learned_capacity(pt_ctx *ctx, int chunks) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_set_learned_capacity: ctx is NULL");
+    if (chunks < 0) return set_error(PT_ERR_INVALID, "pt_bh_set_learned_capacity: %d < 0", chunks);
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    S->lcap_fixed = chunks;
+    if (chunks > 0) S->lcap = chunks;
     return PT_OK;
 }
 

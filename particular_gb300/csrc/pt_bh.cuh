@@ -71,9 +71,11 @@ struct State {
     DevBuf lrec, lgroup, lnext, lpart, lhead, lcentre, lused;  // learned-correction records
     DevBuf gscale;                    // PT_BH_RELATIVE: 1 / (alpha |a|) per group
     int lcap = 0;                     // record chunks allocated
+    int lcap_fixed = 0;               // > 0: record chunks fixed by pt_bh_set_learned_capacity
     int stack_cap = 0;                // group-walk stack ranges per warp in use (0 = all)
     uint64_t generation = 0;          // trees built so far (0 = none)
     bool f64 = false;                 // the current tree was built over DVec3 bodies
+    bool user_tree = false;           // the current tree came from pt_bh_load_tree (monopoles only)
     float local_ratio = 0.1f;         // PT_BH_LOCAL: far when group radius < ratio * distance
     float rel_alpha = 2.5e-3f;        // PT_BH_RELATIVE: opened where the bound exceeds alpha |a|
     const uint32_t *mlp_w = nullptr;  // learned correction: packed BF16 weights (owned by the MLP state)

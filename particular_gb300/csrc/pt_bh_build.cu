@@ -758,6 +758,7 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     }
     S.last_n_src = n;
     S.f64 = F64;
+    S.user_tree = false;
     ++S.generation;
     return PT_OK;
 }

@@ -119,6 +119,26 @@ struct IList {
     float f[NF][CAP + 2];
 };
 
+// A body's acceleration as a compensated FP32 sum (running sum s, rounding errors c).
+// Each evaluated list chunk (up to 128 entries) is summed in plain FP32 in two packed
+// partials and enters the running sum through TwoSum, so the rounding error of the
+// total does not grow with the number of chunks: it is that of one chunk's sum.
+struct CSum {
+    float sx, sy, sz, cx, cy, cz;
+};
+
+__device__ __forceinline__ void csum_zero(CSum &a) { a.sx = a.sy = a.sz = a.cx = a.cy = a.cz = 0.f; }
+
+__device__ __forceinline__ void csum_fold(CSum &a, f2 tx, f2 ty, f2 tz) {
+    float l, h;
+    upk2(tx, l, h);
+    two_sum_acc(a.sx, a.cx, l + h);
+    upk2(ty, l, h);
+    two_sum_acc(a.sy, a.cy, l + h);
+    upk2(tz, l, h);
+    two_sum_acc(a.sz, a.cz, l + h);
+}
+
 // Two list entries (packed lo/hi: monopole x, y, z, m and, for NF = 10, the negated
 // traceless quadrupole N = -Q as Nxx Nxy Nxz Nyy Nyz Nzz) for one target. With
 // u = N d and c = d.u:
@@ -162,9 +182,11 @@ __device__ __forceinline__ void eval_pair(const f2 (&q)[NF], f2 px, f2 py, f2 pz
 // of the lane's targets.
 template <int NF, int CAP, bool GUARD, int TPL>
 __device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, const f2 (&px)[TPL], const f2 (&py)[TPL],
-                                          const f2 (&pz)[TPL], f2 e2, f2 (&ax)[TPL], f2 (&ay)[TPL],
-                                          f2 (&az)[TPL]) {
+                                          const f2 (&pz)[TPL], f2 e2, CSum (&acc)[TPL]) {
     const int lane = threadIdx.x & 31;
+    f2 ax[TPL], ay[TPL], az[TPL];
+#pragma unroll
+    for (int i = 0; i < TPL; ++i) ax[i] = ay[i] = az[i] = pk2(0.f, 0.f);
     __syncwarp();
     if (cnt & 1) {  // pad with a massless entry far away: contributes exactly 0
         if (lane < NF) Lst.f[lane][cnt] = (lane < 3) ? 1e30f : 0.0f;
@@ -179,6 +201,8 @@ __device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, const f2
 #pragma unroll
         for (int i = 0; i < TPL; ++i) eval_pair<NF, GUARD>(q, px[i], py[i], pz[i], e2, ax[i], ay[i], az[i]);
     }
+#pragma unroll
+    for (int i = 0; i < TPL; ++i) csum_fold(acc[i], ax[i], ay[i], az[i]);
     __syncwarp();
 }
 
@@ -517,13 +541,14 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
     const f2 e2 = pk2(eps2, eps2);
     // the lane's two targets packed, for the opening vote
     const f2 vx01 = pk2(p[0].x, p[TPL - 1].x), vy01 = pk2(p[0].y, p[TPL - 1].y), vz01 = pk2(p[0].z, p[TPL - 1].z);
-    f2 px[TPL], py[TPL], pz[TPL], ax[TPL], ay[TPL], az[TPL];
+    f2 px[TPL], py[TPL], pz[TPL];
+    CSum bsum[TPL];  // the bodies' compensated sums over the evaluated lists
 #pragma unroll
     for (int i = 0; i < TPL; ++i) {
         px[i] = pk2(p[i].x, p[i].x);
         py[i] = pk2(p[i].y, p[i].y);
         pz[i] = pk2(p[i].z, p[i].z);
-        ax[i] = ay[i] = az[i] = pk2(0.f, 0.f);
+        csum_zero(bsum[i]);
     }
     // Stack entries are sibling ranges (first, end): `first` is the next node to
     // visit, its later siblings follow by skip pointers up to `end`. A pop visits one
@@ -707,7 +732,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
         const unsigned mc = __ballot_sync(0xffffffffu, cellacc);
         const int nc1 = __popc(mc);
         if (Nc + nc1 > CellList::CAP) {
-            eval_list<NFC, CellList::CAP, GUARD, TPL>(Lc, Nc, px, py, pz, e2, ax, ay, az);
+            eval_list<NFC, CellList::CAP, GUARD, TPL>(Lc, Nc, px, py, pz, e2, bsum);
             entries += Nc;
             centries += Nc;
             Nc = 0;
@@ -734,7 +759,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
         const unsigned mb1 = __ballot_sync(0xffffffffu, bodyacc);
         const int nb1 = __popc(mb1);
         if (Nb + nb1 > BodyList::CAP) {
-            eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+            eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, bsum);
             entries += Nb;
             Nb = 0;
         }
@@ -755,7 +780,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
             for (int base = 0; base < c; base += 32) {
                 const int n = min(32, c - base);
                 if (Nb + n > BodyList::CAP) {
-                    eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+                    eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, bsum);
                     entries += Nb;
                     Nb = 0;
                 }
@@ -771,20 +796,16 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
         }
         __syncwarp();
     }
-    eval_list<NFC, CellList::CAP, GUARD, TPL>(Lc, Nc, px, py, pz, e2, ax, ay, az);
-    eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+    eval_list<NFC, CellList::CAP, GUARD, TPL>(Lc, Nc, px, py, pz, e2, bsum);
+    eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, bsum);
     entries += Nc + Nb;
     centries += Nc;
     float rx[TPL], ry[TPL], rz[TPL];
 #pragma unroll
     for (int i = 0; i < TPL; ++i) {
-        float x0, x1, y0, y1, z0, z1;
-        upk2(ax[i], x0, x1);
-        upk2(ay[i], y0, y1);
-        upk2(az[i], z0, z1);
-        rx[i] = x0 + x1;
-        ry[i] = y0 + y1;
-        rz[i] = z0 + z1;
+        rx[i] = bsum[i].sx + bsum[i].cx;
+        ry[i] = bsum[i].sy + bsum[i].cy;
+        rz[i] = bsum[i].sz + bsum[i].cz;
     }
     if (LOCAL) {
         if (lane < Nf) local_add_node<QUAD>(s_lx[warp], lane, s_far[warp][lane], nodeA, nodeQ, lgx, lgy, lgz, eps2);
@@ -960,8 +981,11 @@ __device__ __forceinline__ void eval_pair_masked(const f2 *q, f2 qm, f2 px, f2 p
 template <int NF, int CAP, bool GUARD>
 __device__ __forceinline__ void eval_list_masked(IList<NF + MW_TPL, CAP> &Lst, int cnt, const f2 (&px)[MW_TPL],
                                                  const f2 (&py)[MW_TPL], const f2 (&pz)[MW_TPL], f2 e2,
-                                                 f2 (&ax)[MW_TPL], f2 (&ay)[MW_TPL], f2 (&az)[MW_TPL]) {
+                                                 CSum (&acc)[MW_TPL]) {
     const int lane = threadIdx.x & 31;
+    f2 ax[MW_TPL], ay[MW_TPL], az[MW_TPL];
+#pragma unroll
+    for (int i = 0; i < MW_TPL; ++i) ax[i] = ay[i] = az[i] = pk2(0.f, 0.f);
     __syncwarp();
     if (cnt & 1) {  // pad: far away, massless, empty masks
         if (lane < NF + MW_TPL) Lst.f[lane][cnt] = (lane < 3) ? 1e30f : 0.0f;
@@ -977,6 +1001,8 @@ __device__ __forceinline__ void eval_list_masked(IList<NF + MW_TPL, CAP> &Lst, i
         for (int i = 0; i < MW_TPL; ++i)
             eval_pair_masked<NF, GUARD>(q, q[NF + i], px[i], py[i], pz[i], e2, ax[i], ay[i], az[i]);
     }
+#pragma unroll
+    for (int i = 0; i < MW_TPL; ++i) csum_fold(acc[i], ax[i], ay[i], az[i]);
     __syncwarp();
 }
 
@@ -1025,13 +1051,14 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
         mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
     }
     const f2 e2 = pk2(eps2, eps2);
-    f2 px[TPL], py[TPL], pz[TPL], ax[TPL], ay[TPL], az[TPL];
+    f2 px[TPL], py[TPL], pz[TPL];
+    CSum bsum[TPL];  // the bodies' compensated sums over the evaluated lists
 #pragma unroll
     for (int i = 0; i < TPL; ++i) {
         px[i] = pk2(p[i].x, p[i].x);
         py[i] = pk2(p[i].y, p[i].y);
         pz[i] = pk2(p[i].z, p[i].z);
-        ax[i] = ay[i] = az[i] = pk2(0.f, 0.f);
+        csum_zero(bsum[i]);
     }
     if (lane == 0) stack[0] = make_int4(0, T, int(vmask[0]), int(vmask[1]));
     __syncwarp();
@@ -1139,7 +1166,7 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
         const unsigned mc = __ballot_sync(0xffffffffu, cellacc);
         const int nc1 = __popc(mc);
         if (Nc + nc1 > CellList::CAP) {
-            eval_list_masked<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
+            eval_list_masked<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, bsum);
             Nc = 0;
         }
         if (cellacc) {
@@ -1165,7 +1192,7 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
         const unsigned mb1 = __ballot_sync(0xffffffffu, bodyacc);
         const int nb1 = __popc(mb1);
         if (Nb + nb1 > BodyList::CAP) {
-            eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+            eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, bsum);
             Nb = 0;
         }
         if (bodyacc) {
@@ -1188,7 +1215,7 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
             for (int base = 0; base < c; base += 32) {
                 const int n = min(32, c - base);
                 if (Nb + n > BodyList::CAP) {
-                    eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+                    eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, bsum);
                     Nb = 0;
                 }
                 if (lane < n) {
@@ -1205,18 +1232,14 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
         }
         __syncwarp();
     }
-    eval_list_masked<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, ax, ay, az);
-    eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, ax, ay, az);
+    eval_list_masked<NFC, CellList::CAP, GUARD>(Lc, Nc, px, py, pz, e2, bsum);
+    eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, bsum);
     float rx[TPL], ry[TPL], rz[TPL];
 #pragma unroll
     for (int i = 0; i < TPL; ++i) {
-        float x0, x1, y0, y1, z0, z1;
-        upk2(ax[i], x0, x1);
-        upk2(ay[i], y0, y1);
-        upk2(az[i], z0, z1);
-        rx[i] = x0 + x1;
-        ry[i] = y0 + y1;
-        rz[i] = z0 + z1;
+        rx[i] = bsum[i].sx + bsum[i].cx;
+        ry[i] = bsum[i].sy + bsum[i].cy;
+        rz[i] = bsum[i].sz + bsum[i].cz;
     }
     if (failed) {  // the stack ran out: the per-body cursor walk instead (warp-uniform)
         unsigned na = 0, nv = 0, nc = 0;
@@ -1561,7 +1584,8 @@ int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n
     unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 2;
     int *err = as<int>(S.counters) + 3;
     PT_CUDA(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
-    PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    // within a leapfrog sequence the error word collects every step's errors
+    if (!ctx->keep_errors) PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     const float th2 = theta * theta;
     const float eps2 = softening * softening;
     const bool quad = flags & PT_BH_QUADRUPOLE;
@@ -1575,7 +1599,8 @@ int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n
             PT_TRY(ensure_buf(ctx, S.lhead, sizeof(int) * size_t(groups)));
             PT_TRY(ensure_buf(ctx, S.lcentre, sizeof(float4) * size_t(groups)));
             PT_TRY(ensure_buf(ctx, S.lused, sizeof(int)));
-            if (S.lcap == 0) S.lcap = std::max(1024, 2 * groups);
+            if (S.lcap_fixed > 0) S.lcap = S.lcap_fixed;
+            else if (S.lcap == 0) S.lcap = std::max(1024, 2 * groups);
         }
         const float *gscale = nullptr;
         if (flags & PT_BH_RELATIVE) {
@@ -1602,9 +1627,10 @@ int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n
                 as<float4>(S.sbody), as<int>(S.counters), th2, S.theta_inner * S.theta_inner, LR, eps2, d_out, stats,
                 err, S.stack_cap > 0 ? S.stack_cap : GW_STACK, S.local_ratio, gscale);
             PT_TRY(check_launch(ctx, "bh_walk_group"));
-            // Outside stream capture the record count is checked and the walk rerun
-            // with room for all records; inside, an overflow sets error bit 2.
-            if (!learned || ctx->capturing || attempt > 0) break;
+            // Outside stream capture (and with the automatic capacity) the record count
+            // is checked and the walk rerun with room for all records; otherwise an
+            // overflow sets error bit 2, which the callers report as PT_ERR_CAPACITY.
+            if (!learned || ctx->capturing || attempt > 0 || S.lcap_fixed > 0) break;
             int used = 0;
             PT_CUDA(cudaMemcpyAsync(&used, LR.used, sizeof(int), cudaMemcpyDeviceToHost, st));
             PT_CUDA(cudaStreamSynchronize(st));

@@ -57,6 +57,9 @@ struct pt_ctx {
     void *mlp = nullptr;
     // True while a CUDA graph is being captured on `stream`: buffers must not grow.
     bool capturing = false;
+    // True while a leapfrog step sequence runs: Barnes-Hut walks keep the error word
+    // of earlier steps instead of clearing it, so the sequence's caller sees them all.
+    bool keep_errors = false;
     // Optional phase timing: events recorded at phase boundaries of the last call.
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -85,14 +88,24 @@ inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 
 // (pt_bh.cu): graphs that captured them compare these before a replay.
 struct BhTuning {
     float local_ratio = 0.f, rel_alpha = 0.f, theta_inner = 0.f;
-    int stack_cap = 0;
+    int stack_cap = 0, learned_cap = 0;
     const void *mlp = nullptr;
     bool operator==(const BhTuning &o) const {
         return local_ratio == o.local_ratio && rel_alpha == o.rel_alpha && theta_inner == o.theta_inner &&
-               stack_cap == o.stack_cap && mlp == o.mlp;
+               stack_cap == o.stack_cap && learned_cap == o.learned_cap && mlp == o.mlp;
     }
 };
 BhTuning bh_tuning(pt_ctx *ctx);
+// The Barnes-Hut error word of the context (device int, bit 2 = learned records
+// overflowed), or nullptr before the first Barnes-Hut call.
+int *bh_error_word(pt_ctx *ctx);
+// After a step sequence with PT_BH_LEARNED: synchronises, reads the error word and,
+// when records overflowed, grows the automatic record capacity for the next call and
+// returns PT_ERR_CAPACITY.
+int bh_learned_overflow(pt_ctx *ctx, const char *fn);
+// The brute-force launch plan forced on this thread by pt_bf_set_plan (0 = automatic):
+// part of the shape a captured leapfrog graph was recorded for.
+void bf_forced_plan(int *targets_per_thread, int *slices);
 
 }  // namespace pt
 

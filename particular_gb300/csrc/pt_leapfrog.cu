@@ -58,15 +58,32 @@ struct Graph {
     uint32_t flags = 0;
     cudaStream_t stream = nullptr;
     BhTuning tune;                 // Barnes-Hut settings baked into the captured launches
+    int plan_k = 0, plan_s = 0;    // the brute-force plan forced by pt_bf_set_plan at capture
     unsigned long long epoch = 0;  // the context's buffer addresses it captured
     uint64_t kernels = 0;
     bool same(const void *b, const void *v, const void *a, size_t n_, int s, int m, float d, float t, float e,
-              uint32_t f, cudaStream_t st, const BhTuning &tu, unsigned long long ep) const {
+              uint32_t f, cudaStream_t st, const BhTuning &tu, int pk, int ps, unsigned long long ep) const {
         return exec && body == b && vel == v && acc == a && n == n_ && steps == s && method == m && dt == d &&
                theta == t && softening == e && flags == f && stream == st && epoch == ep &&
-               (method != PT_METHOD_BARNES_HUT || tune == tu);
+               (method != PT_METHOD_BARNES_HUT || tune == tu) &&
+               (method != PT_METHOD_BRUTE_FORCE || (plan_k == pk && plan_s == ps));
     }
 };
+
+// Keeps the Barnes-Hut error word across the steps of one call (restored on return).
+struct KeepErrors {
+    pt_ctx *ctx;
+    bool prev;
+    explicit KeepErrors(pt_ctx *c) : ctx(c), prev(c->keep_errors) { c->keep_errors = true; }
+    ~KeepErrors() { ctx->keep_errors = prev; }
+};
+
+// Clears the Barnes-Hut error word before a step sequence (nothing to clear before
+// the first Barnes-Hut call: the walk then clears it itself).
+static int clear_bh_errors(pt_ctx *ctx) {
+    if (int *e = bh_error_word(ctx)) PT_CUDA(cudaMemsetAsync(e, 0, sizeof(int), ctx->stream));
+    return PT_OK;
+}
 
 struct State {
     Graph graph;
@@ -126,11 +143,20 @@ extern "C" int pt_leapfrog_device(pt_ctx *ctx, float *d_body, float *d_vel, floa
     if (!S) return set_error(PT_ERR_OOM, "leapfrog state allocation failed");
     float4 *body = reinterpret_cast<float4 *>(d_body);
     float4 *vel = reinterpret_cast<float4 *>(d_vel);
-    if (!use_graph)
-        return lf::enqueue_steps(ctx, body, vel, d_acc, n, dt, steps, method, theta, softening, flags);
+    // With the learned correction, record overflows of any step are reported after the
+    // sequence (synchronously) as PT_ERR_CAPACITY.
+    const bool learned = method == PT_METHOD_BARNES_HUT && (flags & PT_BH_LEARNED);
+    lf::KeepErrors keep(ctx);
+    if (!use_graph) {
+        PT_TRY(lf::clear_bh_errors(ctx));
+        PT_TRY(lf::enqueue_steps(ctx, body, vel, d_acc, n, dt, steps, method, theta, softening, flags));
+        return learned ? bh_learned_overflow(ctx, "pt_leapfrog_device") : PT_OK;
+    }
     lf::Graph &G = S->graph;
+    int plan_k = 0, plan_s = 0;
+    bf_forced_plan(&plan_k, &plan_s);
     if (!G.same(d_body, d_vel, d_acc, n, steps, method, dt, theta, softening, flags, ctx->stream,
-                bh_tuning(ctx), ctx->buf_epoch)) {
+                bh_tuning(ctx), plan_k, plan_s, ctx->buf_epoch)) {
         if (G.exec) {
             cudaGraphExecDestroy(G.exec);
             G.exec = nullptr;
@@ -169,10 +195,22 @@ extern "C" int pt_leapfrog_device(pt_ctx *ctx, float *d_body, float *d_vel, floa
         G.flags = flags;
         G.stream = ctx->stream;
         G.tune = bh_tuning(ctx);
+        G.plan_k = plan_k;
+        G.plan_s = plan_s;
         G.epoch = ctx->buf_epoch;  // no buffer grows during the capture
     }
+    PT_TRY(lf::clear_bh_errors(ctx));
     PT_CUDA(cudaGraphLaunch(G.exec, ctx->stream));
     ctx->launches += G.kernels;  // the kernels the replayed graph runs
+    if (learned) {
+        const int rc = bh_learned_overflow(ctx, "pt_leapfrog_device");
+        if (rc != PT_OK) {
+            // captured with too little room for the records: capture again next call
+            cudaGraphExecDestroy(G.exec);
+            G.exec = nullptr;
+        }
+        return rc;
+    }
     return PT_OK;
 }
 

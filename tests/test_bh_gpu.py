@@ -234,19 +234,35 @@ def test_flags_validated(res):
     assert rc == N.PT_ERR_INVALID
 
 
-def test_full_size_sample(res, oracle):
-    """N=1M bulge+disk at theta=0.5: FP64-judged error on a 1024-body sample, no
-    worse than the reference's own walk of the same tree on those bodies."""
+@pytest.fixture(scope="module")
+def bulge_disk_1m(oracle):
+    """The N = 1,048,576 bulge+disk mixture, its oracle tree and an FP64-judged
+    1024-body sample (shared by the theta cases)."""
     b = ics.bulge_disk(1 << 20, seed=31)["bodies"]
-    m = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01))
-    got = m.compute(b)
     idx = np.random.default_rng(1).choice(b.shape[0], 1024, replace=False)
-    ref64 = oracle.bf_f64(b[idx], b, 0.01, True)
-    t = oracle.Tree(b)
-    ref = t.walk(b[idx], 0.5, 0.01, True)
+    return b, idx, oracle.bf_f64(b[idx], b, 0.01, True), oracle.Tree(b)
+
+
+@pytest.mark.parametrize("theta", [0.3, 0.5, 0.8])
+def test_full_size_sample(res, bulge_disk_1m, theta):
+    """N=1M bulge+disk at the three opening angles of the 1M configuration: FP64-judged
+    error on a 1024-body sample, no worse than the reference's own walk of the same
+    tree on those bodies, and per body equal to it up to f32 rounding."""
+    b, idx, ref64, t = bulge_disk_1m
+    m = cuda.BarnesHut(theta, res, AccelerationSoftened(0.01))
+    got = m.compute(b)
+    ref = t.walk(b[idx], theta, 0.01, True)
     e_gpu, e_ref = rel(got[idx], ref64), rel(ref, ref64)
     assert np.percentile(e_gpu, 95) <= np.percentile(e_ref, 95) * 1.02 + 1e-7
     assert np.percentile(rel(got[idx], ref), 99) < 1e-4
+    # the configuration's fast flags (quadrupole, 64-body groups, local expansion of
+    # far nodes) at the same theta: more accurate than the reference rule
+    fast = cuda.BarnesHut(theta, res, AccelerationSoftened(0.01), quadrupole=True, group=True, local=True)
+    e_fast = rel(fast.compute(b)[idx], ref64)
+    print(f"theta {theta}: p50/p95 reference rule {np.median(e_ref):.2e}/{np.percentile(e_ref, 95):.2e}, "
+          f"fast flags {np.median(e_fast):.2e}/{np.percentile(e_fast, 95):.2e}")
+    for q in (50, 95):
+        assert np.percentile(e_fast, q) <= np.percentile(e_ref, q)
 
 
 @pytest.mark.parametrize("kind", ["plummer", "bulge_disk", "cube"])

@@ -60,6 +60,65 @@ def test_ensemble_matches_per_system_leapfrog(res):
     assert np.array_equal(eb[:, 3], b[:, 3])
 
 
+def large_ensemble(seed=65):
+    """Systems in every size class up to 8192 bodies (the autotuner's classes of 2048
+    bodies and more included), Plummer spheres of different scale radii."""
+    sizes = [64, 130, 300, 700, 1500, 2048, 3000, 4500, 6000, 8192]
+    offsets = np.zeros(len(sizes) + 1, np.uint32)
+    offsets[1:] = np.cumsum(sizes)
+    bodies, vel = [], []
+    for k, n in enumerate(sizes):
+        d = ics.plummer(n, a=0.5 + 0.15 * k, seed=seed + k)
+        bodies.append(d["bodies"])
+        vel.append(d["vel"])
+    b = np.concatenate(bodies)
+    v = np.zeros((b.shape[0], 4), np.float32)
+    v[:, :3] = np.concatenate(vel)
+    return offsets, b, v
+
+
+def oracle_kdk(O, b, v, dt, steps, eps):
+    """The kick-drift-kick scheme per system with the oracle's sequential::BruteForce
+    (float32 state), the closing half kick of a step fused with the next opening one as
+    the ensemble kernel does: kicks of dt/2, dt, ..., dt, then dt/2."""
+    b = b.copy()
+    v = v[:, :3].astype(np.float32).copy()
+    a = O.bf_f32(b, b, eps, True)
+    for s in range(steps):
+        v = v + a * np.float32(0.5 * dt if s == 0 else dt)
+        b[:, :3] = b[:, :3] + v * np.float32(dt)
+        a = O.bf_f32(b, b, eps, True)
+    v = v + a * np.float32(0.5 * dt)
+    return b, v
+
+
+@pytest.mark.parametrize("K", [0, 1, 2, 4])
+def test_large_ensemble_matches_oracle(res, oracle, K):
+    """Systems up to 8192 bodies against the oracle's integration, per system: with the
+    autotuner's table (K = 0 runs the tuner first) and with every block shape forced."""
+    import torch
+    offsets, b, v = large_ensemble()
+    L = N.lib()
+    if K == 0:
+        table = np.zeros(8, np.int32)
+        db = torch.from_numpy(b).cuda()
+        N.check(L.pt_ensemble_tune(res.handle, offsets.ctypes.data, len(offsets) - 1, db.data_ptr(), 0.01,
+                                   table.ctypes.data))
+        print(f"autotuned targets per thread per size class: {table.tolist()}")
+    else:
+        N.check(L.pt_ensemble_set_table(res.handle, np.full(8, K, np.int32).ctypes.data))
+    try:
+        eb, ev = run_ensemble(res, offsets, b, v, 3, use_graph=1)
+    finally:
+        N.check(L.pt_ensemble_set_table(res.handle, np.zeros(8, np.int32).ctypes.data))
+    for k in range(len(offsets) - 1):
+        s, e = int(offsets[k]), int(offsets[k + 1])
+        rb, rv = oracle_kdk(oracle, b[s:e], v[s:e], 1e-3, 3, 0.01)
+        assert np.abs(eb[s:e, :3] - rb[:, :3]).max() <= 1e-5 * np.abs(rb[:, :3]).max(), (K, e - s)
+        assert np.abs(ev[s:e, :3] - rv).max() <= 1e-4 * np.abs(rv).max(), (K, e - s)
+        assert np.array_equal(eb[s:e, 3], b[s:e, 3])
+
+
 def test_graph_equals_eager_and_tuning_keeps_results(res):
     offsets, b, v = small_ensemble(40, 62)
     e1 = run_ensemble(res, offsets, b, v, 8, use_graph=0)

@@ -120,3 +120,36 @@ def test_learned_walk_reports_its_effect(res, oracle, trained):
     assert np.median(e1) < 2 * np.median(e0)
     # corrections are summed per group in walk order: the result is reproducible
     np.testing.assert_array_equal(m.compute(b), got)
+
+
+def test_learned_record_overflow_is_reported(res, trained):
+    """With room for one chunk of records, a learned walk cannot keep every marginal
+    cell: the host call and a graph-replayed leapfrog both fail with PT_ERR_CAPACITY
+    instead of dropping corrections silently; with the automatic capacity again the
+    same leapfrog replays cleanly."""
+    import torch
+    L = N.lib()
+    d = ics.bulge_disk(16384, seed=998)
+    b = np.ascontiguousarray(d["bodies"])
+    flags = N.PT_BH_QUADRUPOLE | N.PT_BH_GROUP | N.PT_BH_LEARNED
+    out = np.zeros((b.shape[0], 3), np.float32)
+    try:
+        N.check(L.pt_bh_set_learned_capacity(res.handle, 1))
+        rc = L.pt_bh_accel_f32(res.handle, b.ctypes.data, b.shape[0], b.ctypes.data, b.shape[0], 1.0, 0.01,
+                               flags, out.ctypes.data)
+        assert rc == N.PT_ERR_CAPACITY and "overflowed" in N.last_error()
+        vel = np.zeros((b.shape[0], 4), np.float32)
+        vel[:, :3] = d["vel"]
+        db = torch.from_numpy(b).cuda()
+        dv = torch.from_numpy(vel).cuda()
+        da = torch.zeros((b.shape[0], 3), device="cuda")
+        for _ in range(2):  # the capture call and a replay
+            rc = L.pt_leapfrog_device(res.handle, db.data_ptr(), dv.data_ptr(), da.data_ptr(), b.shape[0], 1e-3,
+                                      3, N.PT_METHOD_BARNES_HUT, 1.0, 0.01, flags, 1)
+            assert rc == N.PT_ERR_CAPACITY and "overflowed" in N.last_error()
+    finally:
+        N.check(L.pt_bh_set_learned_capacity(res.handle, 0))
+    for _ in range(2):
+        N.check(L.pt_leapfrog_device(res.handle, db.data_ptr(), dv.data_ptr(), da.data_ptr(), b.shape[0], 1e-3,
+                                     3, N.PT_METHOD_BARNES_HUT, 1.0, 0.01, flags, 1))
+    assert torch.isfinite(da).all()

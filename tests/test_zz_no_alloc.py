@@ -33,13 +33,16 @@ def test_noalloc_matches_context_entry_point(native_lib):
             d = torch.from_numpy(b).cuda()
             out_na = torch.full((n, 3), float("nan"), dtype=torch.float32, device="cuda")
             out_ctx = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
             free_before = torch.cuda.mem_get_info()[0] if call == 1 else None
             N.check(L.pt_bf_accel_f32_noalloc(d.data_ptr(), n, d.data_ptr(), n, 0.01, 1,
                                               out_na.data_ptr(), None))
             torch.cuda.synchronize()
             if free_before is not None:
-                # after the first call loaded the module, a call allocates nothing
-                assert torch.cuda.mem_get_info()[0] == free_before
+                # After the first call loaded the module, a call allocates nothing. The
+                # device's free memory moves in 2 MiB pages, the smallest step any
+                # cudaMalloc takes; a smaller change comes from elsewhere.
+                assert free_before - torch.cuda.mem_get_info()[0] < 2 << 20
             N.check(L.pt_bf_accel_f32_device(res.handle, d.data_ptr(), n, d.data_ptr(), n, 0.01,
                                              1, 0, out_ctx.data_ptr()))
             res.synchronize()
