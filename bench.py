@@ -672,7 +672,10 @@ class EnsembleWorkload:
         tab = np.zeros(8, np.int32)
         N.check(N.lib().pt_ensemble_tune(res.handle, self.offsets.ctypes.data, 4096,
                                          self.d_b.data_ptr(), self.softening, tab.ctypes.data))
+        tiles = np.zeros(8, np.int32)
+        N.check(N.lib().pt_ensemble_get_shape(res.handle, tab.ctypes.data, tiles.ctypes.data))
         self.table = tab.tolist()
+        self.tiles = tiles.tolist()
         self.h_b = torch.from_numpy(self.bodies).pin_memory()
         self.h_v = torch.from_numpy(self.vel).pin_memory()
 
@@ -707,7 +710,7 @@ class EnsembleWorkload:
                                   "launch of 3 evaluations (1.85 GB), scaled by evaluations",
                 "kernel": "ens_persistent",
                 "algorithmic": "20 flop per pair x sum(n_k^2) x 101 evaluations per step",
-                "autotuned_K_per_size_class": self.table,
+                "autotuned_K_per_size_class": self.table, "autotuned_j_tile_per_size_class": self.tiles,
                 "peak_source": "measured FFMA-chain kernel over all SMs (pt_measure_fp32_peak)"}
 
     def extra(self):
@@ -838,6 +841,160 @@ class LeapfrogBarnesHutWorkload:
                                                 "theta for p95 <= 1e-3), scaled to one leapfrog step"}
 
 
+class CriterionGrid:
+    """The reference's own criterion benchmark (particular/benches/benchmark.rs:77-132):
+    N = 2^10 ... 2^16 bodies uniform in [-5e3, 5e3]^3 with mu uniform in [1e3, 1e9]
+    (SplitMix64, seed 1808: rand's StdRng stream is not reproducible here), unsoftened
+    Acceleration::checked(); one iteration = the accelerations of every body plus the
+    velocity update v += a. Rows: the brute force and Barnes-Hut at theta 0.3 and 0.7,
+    through the host API (host slices in and out, like gpu::BruteForce in that
+    benchmark) and on device-resident buffers; the reference's rayon methods restated
+    (oracle, all host cores) beside them; its published criterion means quoted."""
+
+    name = "criterion_grid"
+    metric = "criterion iterations/s (accelerations + velocity update), brute force N=65536"
+    unit = "iterations/s"
+    sizes = [1 << k for k in range(10, 17)]
+    thetas = (0.3, 0.7)
+    # published criterion means (ms) of particular/benches/results/native-x86-f32-3d.json
+    # (Ryzen 7900X; gpu rows: RTX 3080 through wgpu)
+    published = {
+        ("par_brute_force", 1024): (0.180, "native-x86-f32-3d.json:3749"),
+        ("par_brute_force", 16384): (39.11, "native-x86-f32-3d.json:3926"),
+        ("par_brute_force", 65536): (627.8, "native-x86-f32-3d.json:4500"),
+        ("par_barnes_hut(0.3)", 65536): (85.17, "native-x86-f32-3d.json:1716"),
+        ("par_barnes_hut(0.7)", 65536): (20.21, "native-x86-f32-3d.json:2652"),
+        ("gpu_brute_force", 16384): (0.542, "native-x86-f32-3d.json:190"),
+        ("gpu_brute_force", 65536): (5.886, "native-x86-f32-3d.json:780"),
+    }
+
+    def config(self):
+        return {"workload": self.name, "sizes": self.sizes, "thetas": list(self.thetas),
+                "ic": "uniform positions in [-5e3, 5e3]^3, mu uniform in [1e3, 1e9], v in [-100, 100]^3, "
+                      "SplitMix64 seed 1808",
+                "interaction": "Acceleration::checked(), no softening",
+                "iteration": "accelerations of all bodies + v += a (the reference benchmark's closure)"}
+
+
+def timed_loop(fn, min_s=0.2, max_iter=200, warm=3, sync=None):
+    for _ in range(warm):
+        fn()
+    if sync:
+        sync()
+    k, t0 = 0, time.perf_counter()
+    while True:
+        fn()
+        k += 1
+        if sync:
+            sync()
+        dt = time.perf_counter() - t0
+        if k >= max_iter or (dt >= min_s and k >= 5):
+            return 1e3 * dt / k, k
+
+
+def run_grid(args):
+    """--workload criterion_grid: the table on the GPU (host API and device buffers)
+    and, with --impl reference, the rayon methods restated on the host cores."""
+    from particular_gb300 import ics
+    grid = CriterionGrid()
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    rows = []
+    if args.impl == "reference":
+        from oracle import build as obuild, oracle as O
+        obuild.build()
+        threads = O.max_threads()
+        for n in grid.sizes:
+            d = ics.criterion_bodies(n)
+            b, v = d["bodies"], d["vel"].copy()
+
+            def bf():
+                v[:] += O.bf_f32(b, b, 0.0, True, threads=threads)
+            ms, k = timed_loop(bf, min_s=0.5, max_iter=50, warm=1)
+            rows.append({"method": "par_brute_force", "n": n, "ms": ms, "iterations": k})
+            for th in grid.thetas:
+                def bh():
+                    v[:] += O.Tree(b).walk(b, th, 0.0, True, threads=threads)
+                ms, k = timed_loop(bh, min_s=0.5, max_iter=50, warm=1)
+                rows.append({"method": f"par_barnes_hut({th})", "n": n, "ms": ms, "iterations": k})
+        kind, cores = "port", threads
+    else:
+        import torch
+        from particular_gb300 import CudaResources, build_native
+        from particular_gb300 import _native as N
+        torch.cuda.set_device(local)
+        build_native.build()
+        res = CudaResources(local)
+        L = N.lib()
+        for n in grid.sizes:
+            d = ics.criterion_bodies(n)
+            h_b = torch.from_numpy(d["bodies"]).pin_memory()
+            h_out = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+            v = d["vel"].copy()
+            a = h_out.numpy()
+            d_b = h_b.cuda()
+            d_out = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+            d_v = torch.from_numpy(d["vel"]).cuda()
+            def bf_host():
+                N.check(L.pt_bf_accel_f32(res.handle, h_b.data_ptr(), n, h_b.data_ptr(), n, 0.0, 1, 0,
+                                          h_out.data_ptr()))
+
+            def bf_dev():
+                N.check(L.pt_bf_accel_f32_device(res.handle, d_b.data_ptr(), n, d_b.data_ptr(), n, 0.0, 1, 0,
+                                                 d_out.data_ptr()))
+
+            def bh_host(th):
+                N.check(L.pt_bh_accel_f32(res.handle, h_b.data_ptr(), n, h_b.data_ptr(), n, th, 0.0, 0,
+                                          h_out.data_ptr()))
+
+            def bh_dev(th):
+                N.check(L.pt_bh_accel_f32_device(res.handle, d_b.data_ptr(), n, d_b.data_ptr(), n, th, 0.0, 0,
+                                                 d_out.data_ptr()))
+
+            methods = [("brute_force", bf_host, bf_dev)]
+            for th in grid.thetas:
+                methods.append((f"barnes_hut({th})", lambda th=th: bh_host(th), lambda th=th: bh_dev(th)))
+            for name, host_call, dev_call in methods:
+                def e2e():
+                    host_call()
+                    v[:] += a
+                ms_h, k_h = timed_loop(e2e)
+
+                def dev():
+                    dev_call()
+                    d_v.add_(d_out)
+                ms_d, k_d = timed_loop(dev, sync=torch.cuda.synchronize)
+                rows.append({"method": f"cuda_{name}", "n": n, "ms": ms_h, "iterations": k_h,
+                             "ms_device_buffers": ms_d, "iterations_device_buffers": k_d})
+        res.close()
+        kind, cores = None, None
+    for r in rows:
+        key = (r["method"].replace("cuda_brute_force", "gpu_brute_force"), r["n"])
+        if args.impl == "reference":
+            key = (r["method"], r["n"])
+        if key in grid.published:
+            r["published_ms"], r["published_source"] = grid.published[key]
+    head = [r for r in rows if r["n"] == 65536 and r["method"] in ("cuda_brute_force", "par_brute_force")][0]
+    line = {"metric": grid.metric, "value": 1e3 / head["ms"], "unit": grid.unit, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": grid.config(),
+            "grid": rows,
+            "timing": "wall clock per iteration (host API rows include the host<->device copies and the host "
+                      "velocity update; device rows synchronise each iteration)"}
+    if args.impl == "reference":
+        line.update({"impl": "reference",
+                     "cpu_baseline": {"value": line["value"], "unit": grid.unit, "cores": cores, "kind": kind,
+                                      **host_cores(), "sample": "every grid row, full size"},
+                     "e2e": {"value": line["value"], "unit": grid.unit, "h2d_bytes_per_step": 0,
+                             "d2h_bytes_per_step": 0}})
+    else:
+        line["e2e"] = {"value": line["value"], "unit": grid.unit, "h2d_bytes_per_step": 16 * 65536,
+                       "d2h_bytes_per_step": 12 * 65536}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 WORKLOADS = {BruteForceWorkload.name: BruteForceWorkload,
              BarnesHutWorkload.name: BarnesHutWorkload,
              LeapfrogWorkload.name: LeapfrogWorkload,
@@ -964,7 +1121,7 @@ def secondary_rows(res, torch, stream, flush, sm_mhz):
     rows[en.name] = {"ms_per_call": ms, "timed_calls": k, "leapfrog_steps_per_call": en.steps_per_call,
                      "systems": 4096, "n_bodies": int(en.n),
                      "body_steps_per_s": en.n * en.steps_per_call / (ms * 1e-3),
-                     "autotuned_K_per_size_class": en.table,
+                     "autotuned_K_per_size_class": en.table, "autotuned_j_tile_per_size_class": en.tiles,
                      **fracs(20.0 * en.pairs_per_step * evals / (ms * 1e-3) / 1e12)}
     del en
     torch.cuda.synchronize()
@@ -1092,6 +1249,8 @@ def run_ours(args):
 
 def main():
     args = parse_args()
+    if args.workload == CriterionGrid.name:
+        return run_grid(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

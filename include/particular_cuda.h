@@ -330,14 +330,19 @@ int pt_leapfrog_device(pt_ctx *ctx, float *d_bodies, float *d_vel, float *d_acc,
  * The reference evaluates one system per call; ensembles have no counterpart. */
 int pt_ensemble_run(pt_ctx *ctx, const uint32_t *offsets, uint32_t n_sys, float *d_bodies,
                     float *d_vel, float dt, int steps, float softening, int use_graph);
-/* Autotuner: times 1, 2 and 4 targets per thread (the item's block shape) for each
+/* Autotuner: times every item shape -- 1, 2 or 4 targets per thread (128 threads per
+ * block) times a j-tile of 128, 256 or 512 sources staged in shared memory -- for each
  * system-size class present (class c: 64*2^c <= n < 64*2^(c+1), c = 0..7, the ends
  * open) and keeps the fastest per class for later runs; table_out (8 ints, may be
- * NULL) receives the choice. */
+ * NULL) receives the targets per thread (pt_ensemble_get_shape reports both). */
 int pt_ensemble_tune(pt_ctx *ctx, const uint32_t *offsets, uint32_t n_sys, const float *d_bodies,
                      float softening, int *table_out);
-/* Sets the per-class table directly (8 ints: 0 = default, else 1, 2 or 4). */
+/* Sets the per-class targets per thread directly (8 ints: 0 = default, else 1, 2 or 4). */
 int pt_ensemble_set_table(pt_ctx *ctx, const int *table);
+/* Sets the per-class j-tile directly (8 ints: 0 = default 256, else 128, 256 or 512). */
+int pt_ensemble_set_tiles(pt_ctx *ctx, const int *tiles);
+/* The item shape in use per class (8 ints each, defaults resolved; NULL skips one). */
+int pt_ensemble_get_shape(pt_ctx *ctx, int *table, int *tiles);
 /* Barrier spin limit (iterations of ~64 ns sleeps; default 2^22). stall != 0 makes
  * every barrier wait for one block more than the grid has: a wait nothing ends, to
  * test the timeout path without faulting the GPU. */

@@ -31,5 +31,24 @@ def build(force=False):
     return LIB
 
 
+CEILING_SRC = os.path.join(HERE, "learned_ceiling.c")
+CEILING_BIN = os.path.join(OUT_DIR, "learned_ceiling")
+
+
+def build_ceiling(force=False):
+    """The FP64 model of the group walk that bounds learned corrections
+    (learned_ceiling.c; a program, not part of the library)."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    if not force and os.path.exists(CEILING_BIN) and os.path.getmtime(CEILING_BIN) >= os.path.getmtime(CEILING_SRC):
+        return CEILING_BIN
+    cc = os.environ.get("CC", "gcc")
+    tmp = CEILING_BIN + ".tmp"
+    subprocess.check_call([cc, "-O3", "-std=c11", "-fopenmp", "-Wall", "-Wno-unknown-pragmas", CEILING_SRC,
+                           "-o", tmp, "-lm"])
+    os.replace(tmp, CEILING_BIN)
+    return CEILING_BIN
+
+
 if __name__ == "__main__":
+    build_ceiling(force=True)
     print(build(force=True))

@@ -44,6 +44,8 @@ def lib():
         L.oracle_tree_export.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 6
         L.oracle_bh_walk.argtypes = [ctypes.c_void_p, _f32p, ctypes.c_size_t, ctypes.c_float,
                                      ctypes.c_float, ctypes.c_int, _f32p, _u32p, ctypes.c_int]
+        L.oracle_bh_walk_sum64.argtypes = [ctypes.c_void_p, _f32p, ctypes.c_size_t, ctypes.c_float,
+                                           ctypes.c_float, ctypes.c_int, _f64p, _f64p, ctypes.c_int]
         L.oracle_bh_f32.argtypes = [_f32p, ctypes.c_size_t, _f32p, ctypes.c_size_t,
                                     ctypes.c_float, ctypes.c_float, ctypes.c_int, _f32p, _u32p,
                                     ctypes.c_int]
@@ -243,3 +245,15 @@ class Tree:
         if rc:
             raise RuntimeError(f"oracle_bh_walk failed: {rc}")
         return (out, acc) if accepted else out
+
+    def walk_sum64(self, targets, theta, softening=0.0, checked=True, threads=0):
+        """The same accepted set per body as walk(), its terms computed and summed in
+        double: (FP64 sums, per-body sums of the terms' norms)."""
+        t = _targets(targets)
+        out = np.zeros((t.shape[0], 3), np.float64)
+        l1 = np.zeros(t.shape[0], np.float64)
+        rc = lib().oracle_bh_walk_sum64(self._h, t, t.shape[0], theta, softening, int(checked), out,
+                                        l1, threads)
+        if rc:
+            raise RuntimeError(f"oracle_bh_walk_sum64 failed: {rc}")
+        return out, l1

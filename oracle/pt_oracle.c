@@ -317,3 +317,74 @@ int oracle_bf_pairs_f64(const double *b, size_t n, size_t restrict_len, double s
 #undef SC_FMAX
 #undef PAIR
 #undef BH_NAME
+
+/* ---- precision check of the walk's summation -------------------------------
+ * The reference rule over an f32 orthtree exactly as oracle_bh_walk decides it (the
+ * same accepted set per body), but every accepted node's term computed in double from
+ * its f32 data and summed in double: out = the FP64 sum of the accepted terms, l1 =
+ * the sum of the terms' norms (the scale the FP32 summation error is measured
+ * against). No reference counterpart: it measures how far an FP32 sum over the
+ * reference's accepted set (sequential.rs:497-500 accumulates with +=) strays from the
+ * exact sum of the same terms. */
+int oracle_bh_walk_sum64(const oracle_tree *t, const float *aff, size_t n_aff, float theta, float softening,
+                         int checked, double *out, double *l1, int threads) {
+    if (!t || (n_aff && (!aff || !out))) return OR_ERR_INVALID;
+    set_threads(threads);
+    long long n = (long long)n_aff;
+    float th2 = theta * theta;
+    int fail = 0;
+#pragma omp parallel if (threads != 1)
+    {
+        size_t cap = 256;
+        int32_t *stack = (int32_t *)malloc(cap * sizeof(int32_t));
+        if (!stack) {
+#pragma omp atomic write
+            fail = 1;
+        }
+#pragma omp for schedule(dynamic, 64)
+        for (long long i = 0; i < n; ++i) {
+            if (!stack) continue;
+            float xi = aff[4 * i + 0], yi = aff[4 * i + 1], zi = aff[4 * i + 2];
+            double sx = 0.0, sy = 0.0, sz = 0.0, sa = 0.0;
+            size_t sp = 0;
+            if (t->root >= 0) stack[sp++] = t->root;
+            while (sp) {
+                int32_t id = stack[--sp];
+                const float *p2 = t->data + 4 * (size_t)id;
+                float dx = p2[0] - xi, dy = p2[1] - yi, dz = p2[2] - zi;
+                float d2 = dx * dx + dy * dy + dz * dz;
+                if (d2 == 0.0f) continue;
+                const or_node *nd = &t->nodes[id];
+                float w = nd->max[0] - nd->min[0];
+                if (nd->internal && th2 * d2 < w * w) {
+                    if (sp + 8 > cap) {
+                        cap *= 2;
+                        int32_t *ns = (int32_t *)realloc(stack, cap * sizeof(int32_t));
+                        if (!ns) {
+#pragma omp atomic write
+                            fail = 1;
+                            break;
+                        }
+                        stack = ns;
+                    }
+                    for (int c = 0; c < 8; ++c)
+                        if (nd->child[c] >= 0) stack[sp++] = nd->child[c];
+                } else {
+                    const double q[4] = {p2[0], p2[1], p2[2], p2[3]};
+                    double ax, ay, az;
+                    pair_f64(xi, yi, zi, q, softening, checked, &ax, &ay, &az);
+                    sx += ax;
+                    sy += ay;
+                    sz += az;
+                    sa += sqrt(ax * ax + ay * ay + az * az);
+                }
+            }
+            out[3 * i + 0] = sx;
+            out[3 * i + 1] = sy;
+            out[3 * i + 2] = sz;
+            if (l1) l1[i] = sa;
+        }
+        free(stack);
+    }
+    return fail ? OR_ERR_OOM : OR_OK;
+}

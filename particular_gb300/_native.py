@@ -136,6 +136,8 @@ def _declare(L):
         "pt_ensemble_tune": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_uint32, c_ptr, ctypes.c_float,
                                             c_ptr]),
         "pt_ensemble_set_table": (ctypes.c_int, [c_ptr, c_ptr]),
+        "pt_ensemble_set_tiles": (ctypes.c_int, [c_ptr, c_ptr]),
+        "pt_ensemble_get_shape": (ctypes.c_int, [c_ptr, c_ptr, c_ptr]),
         "pt_ensemble_set_barrier": (ctypes.c_int, [c_ptr, ctypes.c_longlong, ctypes.c_int]),
         "pt_leapfrog": (ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_size, ctypes.c_float, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_float, ctypes.c_float,

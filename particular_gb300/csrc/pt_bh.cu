@@ -336,11 +336,21 @@ int pt_bh_load_tree(pt_ctx *ctx, const int32_t *orthant, const float *bbox, cons
                     for (int a = 0; a < 6; ++a) box[a] = bb[a];
                 st.push_back(~int64_t(k));
                 const int32_t *o = orthant + 8 * size_t(x);
+                int kids = 0;
                 for (int c = 0; c < 8; ++c)  // pushed 0..7: child 7 is opened first
-                    if (o[c] >= 0) st.push_back(o[c]);
+                    if (o[c] >= 0) st.push_back(o[c]), ++kids;
                     else if (o[c] != -1)
                         return set_error(PT_ERR_INVALID, "pt_bh_load_tree: orthant slot %d of node %lld is %d",
                                          c, (long long)x, o[c]);
+                if (kids == 0) {
+                    // Node::Internal with every slot None: opening it adds nothing. The
+                    // walks open a cell into the range of its children, which must not
+                    // be empty, so it gets one massless child at its centre of mass
+                    // (which contributes exactly zero).
+                    B.push_back(make_int4(0, k + 2, int(leaves.size()), 1));
+                    A.push_back(make_float4(d[0], d[1], d[2], 0.f));
+                    leaves.push_back(A.back());
+                }
             } else {
                 B.push_back(make_int4(0, k + 1, int(leaves.size()), 1));
                 leaves.push_back(A.back());

@@ -10,6 +10,8 @@
 //  * lane_walk: the per-body cursor walk the others fall back to when a stack runs out.
 #include "pt_bh.cuh"
 
+#include <type_traits>
+
 namespace pt {
 namespace bh {
 
@@ -139,6 +141,48 @@ __device__ __forceinline__ void csum_fold(CSum &a, f2 tx, f2 ty, f2 tz) {
     two_sum_acc(a.sz, a.cz, l + h);
 }
 
+// Where a warp keeps its bodies' compensated sums: in registers, or, in the kernels
+// whose registers the traversal state fills (the quadrupole group walks, 96 registers
+// for 5 CTAs per SM), in shared memory as [value][lane] (conflict-free; touched once
+// per evaluated chunk).
+template <int TPL>
+struct RegSums {
+    CSum c[TPL];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int i = 0; i < TPL; ++i) csum_zero(c[i]);
+    }
+    __device__ __forceinline__ void fold(int i, f2 tx, f2 ty, f2 tz) { csum_fold(c[i], tx, ty, tz); }
+    __device__ __forceinline__ void total(int i, float &x, float &y, float &z) const {
+        x = c[i].sx + c[i].cx;
+        y = c[i].sy + c[i].cy;
+        z = c[i].sz + c[i].cz;
+    }
+};
+
+template <int TPL>
+struct SmemSums {
+    float (*v)[32];  // [6 * TPL][32]: per body sx, sy, sz, cx, cy, cz
+    int lane;
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int k = 0; k < 6 * TPL; ++k) v[k][lane] = 0.f;
+    }
+    __device__ __forceinline__ void fold(int i, f2 tx, f2 ty, f2 tz) {
+        CSum a;
+        a.sx = v[6 * i][lane], a.sy = v[6 * i + 1][lane], a.sz = v[6 * i + 2][lane];
+        a.cx = v[6 * i + 3][lane], a.cy = v[6 * i + 4][lane], a.cz = v[6 * i + 5][lane];
+        csum_fold(a, tx, ty, tz);
+        v[6 * i][lane] = a.sx, v[6 * i + 1][lane] = a.sy, v[6 * i + 2][lane] = a.sz;
+        v[6 * i + 3][lane] = a.cx, v[6 * i + 4][lane] = a.cy, v[6 * i + 5][lane] = a.cz;
+    }
+    __device__ __forceinline__ void total(int i, float &x, float &y, float &z) const {
+        x = v[6 * i][lane] + v[6 * i + 3][lane];
+        y = v[6 * i + 1][lane] + v[6 * i + 4][lane];
+        z = v[6 * i + 2][lane] + v[6 * i + 5][lane];
+    }
+};
+
 // Two list entries (packed lo/hi: monopole x, y, z, m and, for NF = 10, the negated
 // traceless quadrupole N = -Q as Nxx Nxy Nxz Nyy Nyz Nzz) for one target. With
 // u = N d and c = d.u:
@@ -180,9 +224,9 @@ __device__ __forceinline__ void eval_pair(const f2 (&q)[NF], f2 px, f2 py, f2 pz
 // Evaluates entries [0, cnt) of a list for this lane's TPL targets, two entries per
 // packed instruction; each pair of entries is read from shared memory once for all
 // of the lane's targets.
-template <int NF, int CAP, bool GUARD, int TPL>
+template <int NF, int CAP, bool GUARD, int TPL, class Sums>
 __device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, const f2 (&px)[TPL], const f2 (&py)[TPL],
-                                          const f2 (&pz)[TPL], f2 e2, CSum (&acc)[TPL]) {
+                                          const f2 (&pz)[TPL], f2 e2, Sums &acc) {
     const int lane = threadIdx.x & 31;
     f2 ax[TPL], ay[TPL], az[TPL];
 #pragma unroll
@@ -202,7 +246,7 @@ __device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, const f2
         for (int i = 0; i < TPL; ++i) eval_pair<NF, GUARD>(q, px[i], py[i], pz[i], e2, ax[i], ay[i], az[i]);
     }
 #pragma unroll
-    for (int i = 0; i < TPL; ++i) csum_fold(acc[i], ax[i], ay[i], az[i]);
+    for (int i = 0; i < TPL; ++i) acc.fold(i, ax[i], ay[i], az[i]);
     __syncwarp();
 }
 
@@ -434,10 +478,10 @@ static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
 #define PT_GW_LMINB 5
 #endif
 #ifndef PT_GW_LCELLS
-#define PT_GW_LCELLS 96
+#define PT_GW_LCELLS 72
 #endif
 #ifndef PT_GW_LBODIES
-#define PT_GW_LBODIES 128
+#define PT_GW_LBODIES 96
 #endif
 #ifndef PT_GW_MINB
 #define PT_GW_MINB (GW_TPL == 1 ? 6 : 5)  // CTAs per SM the register budget is set for
@@ -467,6 +511,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
     __shared__ __align__(16) BodyList s_bodies[GW_WARPS];
     __shared__ float s_lx[GW_WARPS][LOCAL ? 19 : 1][32];
     __shared__ int s_far[GW_WARPS][LOCAL ? 64 : 1];
+    __shared__ float s_sums[GW_WARPS][QUAD ? 6 * GW_TPL : 1][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int group = blockIdx.x * GW_WARPS + warp;
     const int g0 = group * GW_GROUP;
@@ -542,13 +587,16 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
     // the lane's two targets packed, for the opening vote
     const f2 vx01 = pk2(p[0].x, p[TPL - 1].x), vy01 = pk2(p[0].y, p[TPL - 1].y), vz01 = pk2(p[0].z, p[TPL - 1].z);
     f2 px[TPL], py[TPL], pz[TPL];
-    CSum bsum[TPL];  // the bodies' compensated sums over the evaluated lists
+    // the bodies' compensated sums over the evaluated lists
+    using Sums = typename std::conditional<QUAD, SmemSums<TPL>, RegSums<TPL>>::type;
+    Sums bsum;
+    if constexpr (QUAD) bsum = Sums{s_sums[warp], lane};
+    bsum.zero();
 #pragma unroll
     for (int i = 0; i < TPL; ++i) {
         px[i] = pk2(p[i].x, p[i].x);
         py[i] = pk2(p[i].y, p[i].y);
         pz[i] = pk2(p[i].z, p[i].z);
-        csum_zero(bsum[i]);
     }
     // Stack entries are sibling ranges (first, end): `first` is the next node to
     // visit, its later siblings follow by skip pointers up to `end`. A pop visits one
@@ -802,11 +850,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
     centries += Nc;
     float rx[TPL], ry[TPL], rz[TPL];
 #pragma unroll
-    for (int i = 0; i < TPL; ++i) {
-        rx[i] = bsum[i].sx + bsum[i].cx;
-        ry[i] = bsum[i].sy + bsum[i].cy;
-        rz[i] = bsum[i].sz + bsum[i].cz;
-    }
+    for (int i = 0; i < TPL; ++i) bsum.total(i, rx[i], ry[i], rz[i]);
     if (LOCAL) {
         if (lane < Nf) local_add_node<QUAD>(s_lx[warp], lane, s_far[warp][lane], nodeA, nodeQ, lgx, lgy, lgz, eps2);
         __syncwarp();
@@ -981,7 +1025,7 @@ __device__ __forceinline__ void eval_pair_masked(const f2 *q, f2 qm, f2 px, f2 p
 template <int NF, int CAP, bool GUARD>
 __device__ __forceinline__ void eval_list_masked(IList<NF + MW_TPL, CAP> &Lst, int cnt, const f2 (&px)[MW_TPL],
                                                  const f2 (&py)[MW_TPL], const f2 (&pz)[MW_TPL], f2 e2,
-                                                 CSum (&acc)[MW_TPL]) {
+                                                 RegSums<MW_TPL> &acc) {
     const int lane = threadIdx.x & 31;
     f2 ax[MW_TPL], ay[MW_TPL], az[MW_TPL];
 #pragma unroll
@@ -1002,7 +1046,7 @@ __device__ __forceinline__ void eval_list_masked(IList<NF + MW_TPL, CAP> &Lst, i
             eval_pair_masked<NF, GUARD>(q, q[NF + i], px[i], py[i], pz[i], e2, ax[i], ay[i], az[i]);
     }
 #pragma unroll
-    for (int i = 0; i < MW_TPL; ++i) csum_fold(acc[i], ax[i], ay[i], az[i]);
+    for (int i = 0; i < MW_TPL; ++i) acc.fold(i, ax[i], ay[i], az[i]);
     __syncwarp();
 }
 
@@ -1052,13 +1096,13 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
     }
     const f2 e2 = pk2(eps2, eps2);
     f2 px[TPL], py[TPL], pz[TPL];
-    CSum bsum[TPL];  // the bodies' compensated sums over the evaluated lists
+    RegSums<TPL> bsum;  // the bodies' compensated sums over the evaluated lists
+    bsum.zero();
 #pragma unroll
     for (int i = 0; i < TPL; ++i) {
         px[i] = pk2(p[i].x, p[i].x);
         py[i] = pk2(p[i].y, p[i].y);
         pz[i] = pk2(p[i].z, p[i].z);
-        csum_zero(bsum[i]);
     }
     if (lane == 0) stack[0] = make_int4(0, T, int(vmask[0]), int(vmask[1]));
     __syncwarp();
@@ -1236,11 +1280,7 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
     eval_list_masked<4, BodyList::CAP, GUARD>(Lb, Nb, px, py, pz, e2, bsum);
     float rx[TPL], ry[TPL], rz[TPL];
 #pragma unroll
-    for (int i = 0; i < TPL; ++i) {
-        rx[i] = bsum[i].sx + bsum[i].cx;
-        ry[i] = bsum[i].sy + bsum[i].cy;
-        rz[i] = bsum[i].sz + bsum[i].cz;
-    }
+    for (int i = 0; i < TPL; ++i) bsum.total(i, rx[i], ry[i], rz[i]);
     if (failed) {  // the stack ran out: the per-body cursor walk instead (warp-uniform)
         unsigned na = 0, nv = 0, nc = 0;
 #pragma unroll

@@ -12,8 +12,9 @@
 // balances systems of 64 ... 8192 bodies. Each item stages its system's sources in
 // shared memory, in SoA form, one 256-body tile at a time, and evaluates them with
 // packed f32x2 math (the brute-force inner loop), compensated across tiles.
-// The number of targets per thread (K, the item's block shape) is chosen per system
-// size class by pt_ensemble_tune, which times each candidate.
+// The item's shape -- targets per thread (K) and the number of sources staged per
+// shared-memory tile (the j-tile J) -- is chosen per system size class by
+// pt_ensemble_tune, which times each candidate.
 // Grid barriers spin with an iteration limit: on expiry the kernel records
 // PT_ERR_TIMEOUT and every block returns, leaving the context usable.
 #include "pt_common.cuh"
@@ -28,8 +29,11 @@ namespace pt {
 namespace ens {
 
 constexpr int THREADS = 128;
-constexpr int TILE = 256;
+constexpr int TILE = 512;   // the largest j-tile: shared memory holds TILE sources
 constexpr int CLASSES = 8;  // size classes by floor(log2(n)) - 6, clamped to [0, 7]
+
+// j-tile codes in an item's word: 0 = 256 (default), 1 = 128, 2 = 512
+inline int tile_code(int J) { return J == 128 ? 1 : J == 512 ? 2 : 0; }
 
 inline int size_class(uint32_t n) {
     int c = 0;
@@ -41,10 +45,12 @@ struct Tile {
     float c[4][TILE + 2];
 };
 
-// Accelerations of targets [s0+t0, s0+t0+cnt) from every body of the system [s0, s0+n).
-template <int K, bool GUARD>
+// Accelerations of targets [s0+t0, s0+t0+cnt) from every body of the system [s0, s0+n),
+// sources staged J at a time.
+template <int K, int J, bool GUARD>
 __device__ void accel_item(const float4 *__restrict__ body, float *__restrict__ acc, int s0, int n, int t0, int cnt,
                            float eps2, Tile &T) {
+    static_assert(J <= TILE, "j-tile larger than the shared tile");
     const int tid = threadIdx.x;
     f2 xi[K], yi[K], zi[K], ax[K], ay[K], az[K];
     float sx[K], sy[K], sz[K], cx[K], cy[K], cz[K];
@@ -59,8 +65,8 @@ __device__ void accel_item(const float4 *__restrict__ body, float *__restrict__ 
         ax[k] = ay[k] = az[k] = zero;
         sx[k] = sy[k] = sz[k] = cx[k] = cy[k] = cz[k] = 0.f;
     }
-    for (int j0 = 0; j0 < n; j0 += TILE) {
-        const int cj = min(TILE, n - j0);
+    for (int j0 = 0; j0 < n; j0 += J) {
+        const int cj = min(J, n - j0);
         __syncthreads();  // the previous tile is consumed
         for (int e = tid; e < cj; e += THREADS) {
             const float4 q = __ldcg(body + s0 + j0 + e);
@@ -108,13 +114,22 @@ __device__ void accel_item(const float4 *__restrict__ body, float *__restrict__ 
     }
 }
 
+template <int K, bool GUARD>
+__device__ __forceinline__ void run_item_k(int jc, const int4 w, int cnt, const float4 *__restrict__ body,
+                                           float *__restrict__ acc, float eps2, Tile &T) {
+    if (jc == 1) accel_item<K, 128, GUARD>(body, acc, w.x, w.y, w.z, cnt, eps2, T);
+    else if (jc == 2) accel_item<K, 512, GUARD>(body, acc, w.x, w.y, w.z, cnt, eps2, T);
+    else accel_item<K, 256, GUARD>(body, acc, w.x, w.y, w.z, cnt, eps2, T);
+}
+
+// item word w = (system start, system size, first target, cnt | K << 24 | j-tile code << 28)
 template <bool GUARD>
 __device__ __forceinline__ void run_item(const int4 w, const float4 *__restrict__ body, float *__restrict__ acc,
                                          float eps2, Tile &T) {
-    const int K = w.w >> 24, cnt = w.w & 0xffffff;
-    if (K == 4) accel_item<4, GUARD>(body, acc, w.x, w.y, w.z, cnt, eps2, T);
-    else if (K == 2) accel_item<2, GUARD>(body, acc, w.x, w.y, w.z, cnt, eps2, T);
-    else accel_item<1, GUARD>(body, acc, w.x, w.y, w.z, cnt, eps2, T);
+    const int K = (w.w >> 24) & 7, jc = (w.w >> 28) & 3, cnt = w.w & 0xffffff;
+    if (K == 4) run_item_k<4, GUARD>(jc, w, cnt, body, acc, eps2, T);
+    else if (K == 2) run_item_k<2, GUARD>(jc, w, cnt, body, acc, eps2, T);
+    else run_item_k<1, GUARD>(jc, w, cnt, body, acc, eps2, T);
 }
 
 // ctrl: [0] barrier arrivals, [1] barrier generation, [2 + p] queue of phase p.
@@ -194,6 +209,7 @@ __global__ void __launch_bounds__(THREADS)
 
 struct State {
     int table[CLASSES] = {0, 0, 0, 0, 0, 0, 0, 0};  // K per size class (0 = default)
+    int tiles[CLASSES] = {0, 0, 0, 0, 0, 0, 0, 0};  // j-tile per size class (0 = default 256)
     long long spin_limit = 1ll << 22;
     int stall = 0;
     DevBuf items, ctrl, acc;
@@ -217,7 +233,8 @@ static State *state(pt_ctx *ctx) {
 static int default_k(int cls) { return cls >= 5 ? 2 : 1; }  // >= 2048 bodies: 2 targets per thread
 
 // Items sorted by cost (targets x sources), largest first.
-static void build_items(const uint32_t *offsets, uint32_t n_sys, const int *table, std::vector<int4> &out) {
+static void build_items(const uint32_t *offsets, uint32_t n_sys, const int *table, const int *tiles,
+                        std::vector<int4> &out) {
     struct Cost {
         int4 w;
         double c;
@@ -228,10 +245,11 @@ static void build_items(const uint32_t *offsets, uint32_t n_sys, const int *tabl
         if (n <= 0) continue;
         const int cls = size_class(uint32_t(n));
         const int K = table[cls] ? table[cls] : default_k(cls);
+        const int jc = tile_code(tiles[cls]);
         const int per = THREADS * K;
         for (int t0 = 0; t0 < n; t0 += per) {
             const int cnt = std::min(per, n - t0);
-            v.push_back({make_int4(s0, n, t0, cnt | (K << 24)), double(cnt) * n});
+            v.push_back({make_int4(s0, n, t0, cnt | (K << 24) | (jc << 28)), double(cnt) * n});
         }
     }
     std::stable_sort(v.begin(), v.end(), [](const Cost &a, const Cost &b) { return a.c > b.c; });
@@ -242,8 +260,9 @@ static void build_items(const uint32_t *offsets, uint32_t n_sys, const int *tabl
 static int upload_items(pt_ctx *ctx, State &S, const uint32_t *offsets, uint32_t n_sys) {
     std::vector<uint32_t> key(offsets, offsets + n_sys + 1);
     key.insert(key.end(), S.table, S.table + CLASSES);
+    key.insert(key.end(), S.tiles, S.tiles + CLASSES);
     if (key == S.key && S.items.ptr) return PT_OK;
-    build_items(offsets, n_sys, S.table, S.host_items);
+    build_items(offsets, n_sys, S.table, S.tiles, S.host_items);
     S.n_items = int(S.host_items.size());
     PT_TRY(ensure_buf(ctx, S.items, sizeof(int4) * std::max<size_t>(1, S.host_items.size())));
     PT_CUDA(cudaMemcpyAsync(S.items.ptr, S.host_items.data(), sizeof(int4) * S.host_items.size(),
@@ -374,7 +393,8 @@ extern "C" int pt_ensemble_run(pt_ctx *ctx, const uint32_t *offsets, uint32_t n_
     return PT_OK;
 }
 
-// Times K in {1, 2, 4} for every size class present and keeps the fastest.
+// Times every (K, J) in {1, 2, 4} x {128, 256, 512} for every size class present and
+// keeps the fastest.
 extern "C" int pt_ensemble_tune(pt_ctx *ctx, const uint32_t *offsets, uint32_t n_sys, const float *d_bodies,
                                 float softening, int *table_out) {
     using namespace pt;
@@ -394,7 +414,7 @@ extern "C" int pt_ensemble_tune(pt_ctx *ctx, const uint32_t *offsets, uint32_t n
     cudaEvent_t e0, e1;
     PT_CUDA(cudaEventCreate(&e0));
     PT_CUDA(cudaEventCreate(&e1));
-    int best_table[ens::CLASSES];
+    int best_table[ens::CLASSES], best_tiles[ens::CLASSES];
     for (int c = 0; c < ens::CLASSES; ++c) {
         std::vector<uint32_t> sub(1, 0);  // the systems of class c, packed as a sub-ensemble
         std::vector<uint32_t> start;
@@ -406,12 +426,15 @@ extern "C" int pt_ensemble_tune(pt_ctx *ctx, const uint32_t *offsets, uint32_t n
             }
         }
         best_table[c] = S->table[c];
+        best_tiles[c] = S->tiles[c];
         if (start.empty()) continue;
         float best = 1e30f;
-        for (int K : {1, 2, 4}) {
+        for (int shape = 0; shape < 9; ++shape) {
+            const int K = 1 << (shape / 3), J = 128 << (shape % 3);
             int tab[ens::CLASSES] = {K, K, K, K, K, K, K, K};
+            int til[ens::CLASSES] = {J, J, J, J, J, J, J, J};
             std::vector<int4> items;
-            ens::build_items(sub.data(), uint32_t(start.size()), tab, items);
+            ens::build_items(sub.data(), uint32_t(start.size()), tab, til, items);
             // map sub-ensemble item starts back to the real system starts
             for (auto &w : items) {
                 const auto it = std::upper_bound(sub.begin(), sub.end(), uint32_t(w.x)) - 1;
@@ -437,12 +460,14 @@ extern "C" int pt_ensemble_tune(pt_ctx *ctx, const uint32_t *offsets, uint32_t n
             if (ms < best) {
                 best = ms;
                 best_table[c] = K;
+                best_tiles[c] = J;
             }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     std::copy(best_table, best_table + ens::CLASSES, S->table);
+    std::copy(best_tiles, best_tiles + ens::CLASSES, S->tiles);
     if (S->exec) {
         cudaGraphExecDestroy(S->exec);
         S->exec = nullptr;
@@ -476,6 +501,33 @@ extern "C" int pt_ensemble_set_barrier(pt_ctx *ctx, long long spin_limit, int st
     if (S->exec) {
         cudaGraphExecDestroy(S->exec);
         S->exec = nullptr;
+    }
+    return PT_OK;
+}
+
+extern "C" int pt_ensemble_set_tiles(pt_ctx *ctx, const int *tiles) {
+    using namespace pt;
+    clear_error();
+    if (!ctx || !tiles) return set_error(PT_ERR_INVALID, "pt_ensemble_set_tiles: NULL argument");
+    ens::State *S = ens::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "ensemble state allocation failed");
+    for (int c = 0; c < ens::CLASSES; ++c)
+        if (tiles[c] != 0 && tiles[c] != 128 && tiles[c] != 256 && tiles[c] != 512)
+            return set_error(PT_ERR_INVALID, "pt_ensemble_set_tiles: the j-tile must be 0, 128, 256 or 512");
+    std::copy(tiles, tiles + ens::CLASSES, S->tiles);
+    S->key.clear();
+    return PT_OK;
+}
+
+extern "C" int pt_ensemble_get_shape(pt_ctx *ctx, int *table, int *tiles) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_ensemble_get_shape: ctx is NULL");
+    ens::State *S = ens::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "ensemble state allocation failed");
+    for (int c = 0; c < ens::CLASSES; ++c) {
+        if (table) table[c] = S->table[c] ? S->table[c] : ens::default_k(c);
+        if (tiles) tiles[c] = S->tiles[c] ? S->tiles[c] : 256;
     }
     return PT_OK;
 }

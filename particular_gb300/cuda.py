@@ -97,6 +97,22 @@ class BruteForce:
         self.vec3a = bool(vec3a)  # glam Vec3A/Vec4 operand order (exact path)
         self.dvec3 = bool(dvec3)
 
+    def load_tree(self, internal, orthant, bbox, data, root=0):
+        """Makes a tree the caller built (the reference's RootedOrthtree over
+        GravitationalField<Vec3, f32>, flattened per node: internal flags, 8 orthant
+        slots with -1 for None, bbox min/max, data (x, y, z, mass); root -1 = None) the
+        resources' current tree; pass the returned DeviceTree as the affecting side of
+        Between to walk it (flags 0 or group only: the tree carries monopoles)."""
+        internal = np.ascontiguousarray(internal, np.uint8)
+        n = internal.shape[0]
+        orthant = np.ascontiguousarray(orthant, np.int32).reshape(n, 8)
+        bbox = np.ascontiguousarray(bbox, np.float32).reshape(n, 6)
+        data = np.ascontiguousarray(data, np.float32).reshape(n, 4)
+        g = ctypes.c_uint64(0)
+        N.check(N.lib().pt_bh_load_tree(self.resources.handle, _ptr(orthant), _ptr(bbox), _ptr(internal),
+                                        _ptr(data), n, int(root), ctypes.byref(g)))
+        return DeviceTree(self.resources, n, g.value)
+
     def compute(self, storage):
         b = as_between(storage)
         if self.dvec3:
@@ -193,6 +209,22 @@ class BarnesHut:
         g = ctypes.c_uint64(0)
         N.check(N.lib().pt_bh_build(self.resources.handle, _ptr(src), src.shape[0], ctypes.byref(g)))
         return DeviceTree(self.resources, src.shape[0], g.value)
+
+    def load_tree(self, internal, orthant, bbox, data, root=0):
+        """Makes a tree the caller built (the reference's RootedOrthtree over
+        GravitationalField<Vec3, f32>, flattened per node: internal flags, 8 orthant
+        slots with -1 for None, bbox min/max, data (x, y, z, mass); root -1 = None) the
+        resources' current tree; pass the returned DeviceTree as the affecting side of
+        Between to walk it (flags 0 or group only: the tree carries monopoles)."""
+        internal = np.ascontiguousarray(internal, np.uint8)
+        n = internal.shape[0]
+        orthant = np.ascontiguousarray(orthant, np.int32).reshape(n, 8)
+        bbox = np.ascontiguousarray(bbox, np.float32).reshape(n, 6)
+        data = np.ascontiguousarray(data, np.float32).reshape(n, 4)
+        g = ctypes.c_uint64(0)
+        N.check(N.lib().pt_bh_load_tree(self.resources.handle, _ptr(orthant), _ptr(bbox), _ptr(internal),
+                                        _ptr(data), n, int(root), ctypes.byref(g)))
+        return DeviceTree(self.resources, n, g.value)
 
     def compute(self, storage):
         b = as_between(storage)

@@ -102,6 +102,19 @@ def uniform_cube(n, seed=1808):
     return {"bodies": _pack(pos, m), "vel": np.zeros((n, 3), np.float32)}
 
 
+def criterion_bodies(n, seed=1808):
+    """The reference benchmark's bodies (particular/benches/benchmark.rs:22-37,97-105):
+    positions uniform in [-5e3, 5e3]^3, every body massive with mu uniform in
+    [1e3, 1e9], velocities uniform in [-100, 100]^3. The reference draws them from
+    rand's StdRng seeded 1808; this generator cannot reproduce that stream, so the same
+    distributions come from SplitMix64 with the same seed."""
+    rng = SplitMix64(seed)
+    pos = rng.uniform(3 * n, -5e3, 5e3).reshape(n, 3)
+    mu = rng.uniform(n, 1e3, 1e9)
+    vel = rng.uniform(3 * n, -100.0, 100.0).reshape(n, 3)
+    return {"bodies": _pack(pos, mu), "vel": vel.astype(np.float32)}
+
+
 def plummer(n, a=1.0, total_mass=1.0, seed=1809):
     rng = SplitMix64(seed)
     pos, vel = plummer_raw(rng, n, a, total_mass)

@@ -92,25 +92,31 @@ def oracle_kdk(O, b, v, dt, steps, eps):
     return b, v
 
 
-@pytest.mark.parametrize("K", [0, 1, 2, 4])
-def test_large_ensemble_matches_oracle(res, oracle, K):
+@pytest.mark.parametrize("K,J", [(0, 0), (1, 128), (1, 512), (2, 256), (4, 128), (4, 512)])
+def test_large_ensemble_matches_oracle(res, oracle, K, J):
     """Systems up to 8192 bodies against the oracle's integration, per system: with the
-    autotuner's table (K = 0 runs the tuner first) and with every block shape forced."""
+    autotuner's shapes (K = 0 runs the tuner first) and with item shapes forced
+    (targets per thread K, j-tile J)."""
     import torch
     offsets, b, v = large_ensemble()
     L = N.lib()
     if K == 0:
         table = np.zeros(8, np.int32)
+        tiles = np.zeros(8, np.int32)
         db = torch.from_numpy(b).cuda()
         N.check(L.pt_ensemble_tune(res.handle, offsets.ctypes.data, len(offsets) - 1, db.data_ptr(), 0.01,
                                    table.ctypes.data))
-        print(f"autotuned targets per thread per size class: {table.tolist()}")
+        N.check(L.pt_ensemble_get_shape(res.handle, table.ctypes.data, tiles.ctypes.data))
+        print(f"autotuned targets per thread {table.tolist()}, j-tiles {tiles.tolist()} per size class")
+        assert set(tiles.tolist()) <= {128, 256, 512}
     else:
         N.check(L.pt_ensemble_set_table(res.handle, np.full(8, K, np.int32).ctypes.data))
+        N.check(L.pt_ensemble_set_tiles(res.handle, np.full(8, J, np.int32).ctypes.data))
     try:
         eb, ev = run_ensemble(res, offsets, b, v, 3, use_graph=1)
     finally:
         N.check(L.pt_ensemble_set_table(res.handle, np.zeros(8, np.int32).ctypes.data))
+        N.check(L.pt_ensemble_set_tiles(res.handle, np.zeros(8, np.int32).ctypes.data))
     for k in range(len(offsets) - 1):
         s, e = int(offsets[k]), int(offsets[k + 1])
         rb, rv = oracle_kdk(oracle, b[s:e], v[s:e], 1e-3, 3, 0.01)
