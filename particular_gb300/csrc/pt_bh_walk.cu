@@ -141,10 +141,12 @@ __device__ __forceinline__ void csum_fold(CSum &a, f2 tx, f2 ty, f2 tz) {
     two_sum_acc(a.sz, a.cz, l + h);
 }
 
-// Where a warp keeps its bodies' compensated sums: in registers, or, in the kernels
-// whose registers the traversal state fills (the quadrupole group walks, 96 registers
-// for 5 CTAs per SM), in shared memory as [value][lane] (conflict-free; touched once
-// per evaluated chunk).
+// Where a warp keeps its bodies' compensated sums: in registers, or, in the kernel
+// whose registers the traversal state fills (the quadrupole group walk with local
+// expansions, 96 registers for 5 CTAs per SM: 56 bytes spilled, walk +15 %), in shared
+// memory as [value][lane] (conflict-free; touched once per evaluated chunk; walk +2.5 %
+// over plain FP32 sums). Measured at N = 4M: the other group walks +1.2 % in registers
+// (+2.7 % in shared memory), the masked walk +1.6 %.
 template <int TPL>
 struct RegSums {
     CSum c[TPL];
@@ -483,6 +485,13 @@ static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
 #ifndef PT_GW_LBODIES
 #define PT_GW_LBODIES 96
 #endif
+// Opened cells with at most this many nodes below them are summed body by body at
+// once instead of being walked level by level (<= 31: one warp-wide load; 0 = off).
+#ifndef PT_GW_FLAT
+#define PT_GW_FLAT 16
+#endif
+constexpr int GW_FLAT = PT_GW_FLAT;
+static_assert(GW_FLAT >= 0 && GW_FLAT <= 31, "a flattened subtree is loaded by one warp");
 #ifndef PT_GW_MINB
 #define PT_GW_MINB (GW_TPL == 1 ? 6 : 5)  // CTAs per SM the register budget is set for
 #endif
@@ -511,7 +520,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
     __shared__ __align__(16) BodyList s_bodies[GW_WARPS];
     __shared__ float s_lx[GW_WARPS][LOCAL ? 19 : 1][32];
     __shared__ int s_far[GW_WARPS][LOCAL ? 64 : 1];
-    __shared__ float s_sums[GW_WARPS][QUAD ? 6 * GW_TPL : 1][32];
+    __shared__ float s_sums[GW_WARPS][QUAD && LOCAL ? 6 * GW_TPL : 1][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int group = blockIdx.x * GW_WARPS + warp;
     const int g0 = group * GW_GROUP;
@@ -588,9 +597,9 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
     const f2 vx01 = pk2(p[0].x, p[TPL - 1].x), vy01 = pk2(p[0].y, p[TPL - 1].y), vz01 = pk2(p[0].z, p[TPL - 1].z);
     f2 px[TPL], py[TPL], pz[TPL];
     // the bodies' compensated sums over the evaluated lists
-    using Sums = typename std::conditional<QUAD, SmemSums<TPL>, RegSums<TPL>>::type;
+    using Sums = typename std::conditional<QUAD && LOCAL, SmemSums<TPL>, RegSums<TPL>>::type;
     Sums bsum;
-    if constexpr (QUAD) bsum = Sums{s_sums[warp], lane};
+    if constexpr (QUAD && LOCAL) bsum = Sums{s_sums[warp], lane};
     bsum.zero();
 #pragma unroll
     for (int i = 0; i < TPL; ++i) {
@@ -735,16 +744,22 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
             learned += nm;
         }
         const bool rest = have && !handed && B.y < range.y;  // later siblings remain
-        const int np = int(rest) + int(open);
+        // An opened cell with at most GW_FLAT nodes below it is not pushed: the bodies
+        // of its leaves go straight to the body list (below). Exact sums instead of its
+        // descendants' multipoles, so never less accurate; it saves the pops and votes
+        // of the tree's last levels.
+        const bool flat = open && B.y - node - 1 <= GW_FLAT;
+        const bool kids = open && !flat;
+        const int np = int(rest) + int(kids);
         // each lane's pushes follow those of the lanes below it
-        const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, open);
+        const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, kids);
         const int total = __popc(mrest) + __popc(mopen);
         int slot = S + __popc(mrest & lt) + __popc(mopen & lt);
         if (slot + np > stack_cap) {
             failed = true;  // never written out of bounds
         } else {
             if (rest) stack[slot++] = make_int2(B.y, range.y);
-            if (open) stack[slot++] = make_int2(node + 1, B.y);  // children on top: popped first
+            if (kids) stack[slot++] = make_int2(node + 1, B.y);  // children on top: popped first
         }
         if (__any_sync(0xffffffffu, failed)) {
             failed = true;
@@ -819,12 +834,8 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
             Lb.f[3][e] = A.w;
         }
         Nb += nb1;
-        unsigned mb = __ballot_sync(0xffffffffu, bucket);
-        while (mb) {  // leaves holding several bodies: one entry per body
-            const int src = __ffs(mb) - 1;
-            mb &= mb - 1;
-            const int f = __shfl_sync(0xffffffffu, B.z, src);
-            const int c = __shfl_sync(0xffffffffu, B.w, src);
+        // bodies [f, f + c) of the key-ordered array -> the body list (warp-uniform f, c)
+        auto append_bodies = [&](int f, int c) {
             for (int base = 0; base < c; base += 32) {
                 const int n = min(32, c - base);
                 if (Nb + n > BodyList::CAP) {
@@ -840,6 +851,47 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
                     Lb.f[3][Nb + lane] = q.w;
                 }
                 Nb += n;
+            }
+        };
+        unsigned mb = __ballot_sync(0xffffffffu, bucket);
+        while (mb) {  // leaves holding several bodies: one entry per body
+            const int src = __ffs(mb) - 1;
+            mb &= mb - 1;
+            append_bodies(__shfl_sync(0xffffffffu, B.z, src), __shfl_sync(0xffffffffu, B.w, src));
+        }
+        unsigned mfl = __ballot_sync(0xffffffffu, flat);
+        while (mfl) {  // small opened subtrees: all their nodes at once, one per lane
+            const int src = __ffs(mfl) - 1;
+            mfl &= mfl - 1;
+            const int f0 = __shfl_sync(0xffffffffu, node, src) + 1;
+            const int f1 = __shfl_sync(0xffffffffu, B.y, src);
+            const int nd = f0 + lane;
+            int4 lb = make_int4(0, 0, -1, 0);
+            float4 la = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (nd < f1) lb = __ldg(nodeB + nd);
+            const bool one = lb.z >= 0 && lb.w == 1;  // a single-body leaf: its record is the body
+            if (one) la = __ldg(nodeA + nd);
+            visits += f1 - f0;
+            const unsigned m1 = __ballot_sync(0xffffffffu, one);
+            const int n1 = __popc(m1);
+            if (Nb + n1 > BodyList::CAP) {
+                eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, bsum);
+                entries += Nb;
+                Nb = 0;
+            }
+            if (one) {
+                const int e = Nb + __popc(m1 & lt);
+                Lb.f[0][e] = la.x;
+                Lb.f[1][e] = la.y;
+                Lb.f[2][e] = la.z;
+                Lb.f[3][e] = la.w;
+            }
+            Nb += n1;
+            unsigned mm = __ballot_sync(0xffffffffu, lb.z >= 0 && lb.w > 1);
+            while (mm) {
+                const int s2 = __ffs(mm) - 1;
+                mm &= mm - 1;
+                append_bodies(__shfl_sync(0xffffffffu, lb.z, s2), __shfl_sync(0xffffffffu, lb.w, s2));
             }
         }
         __syncwarp();

@@ -414,10 +414,14 @@ def test_local_expansion_matches_direct_far_field(res):
     N.check(L.pt_bh_set_local_ratio(res.handle, 1e-4))
     try:
         b = ics.plummer(20000, seed=53)["bodies"]
-        got = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=True, group=True,
-                             local=True).compute(b)
+        m = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=True, group=True, local=True)
+        got = m.compute(b)
+        assert m.stats()["local_nodes"] == 0
         want = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01), quadrupole=True, group=True).compute(b)
-        np.testing.assert_array_equal(got, want)
+        # the same entries; the walks differ only in where their list chunks end, which
+        # moves the compensated sums' rounding
+        r = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+        assert r.max() < 1e-6
     finally:
         N.check(L.pt_bh_set_local_ratio(res.handle, 0.1))
 

@@ -50,19 +50,22 @@ def test_oracle_tree_walked_on_the_gpu(res, oracle, theta, group):
             assert np.percentile(e, q) <= np.percentile(e_ref, q) * 1.01 + 1e-7
 
 
-def test_separate_targets_and_the_device_tree_agree(res, oracle):
-    """The oracle's tree loaded from the host and the device's own build of the same
-    bodies give the same accelerations for separate targets (the device collapses
-    single-child chains, which changes no accepted (centre of mass, mass) pair)."""
+def test_separate_targets_and_the_device_tree(res, oracle):
+    """Separate targets walking the oracle's tree on the GPU get the reference walk's
+    accelerations; the device's own tree of the same bodies is at least as accurate
+    against the FP64 judge (its cell moments are compensated sums, where the
+    reference's f32 sums in body order drift by ~sqrt(count) roundings)."""
     src = ics.bulge_disk(30000, seed=72)["bodies"]
     aff = ics.uniform_cube(3000, 73)["bodies"] * np.float32(3.0)
+    t = oracle.Tree(src)
     m = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01))
-    got = m.compute(Between(aff, load(m, oracle.Tree(src).export())))
+    got = m.compute(Between(aff, load(m, t.export())))
+    r = rel(got, t.walk(aff, 0.5, 0.01, True))
+    assert np.median(r) < 1e-6 and np.percentile(r, 99) < 1e-5
+    ref64 = oracle.bf_f64(aff, src, 0.01, True)
     own = m.compute(Between(aff, src))
-    # centres of mass differ at f32 rounding (the device combines moments compensated,
-    # the reference sums in order), which can flip a decision on the opening boundary
-    r = rel(got, own)
-    assert np.median(r) < 1e-6 and np.percentile(r, 99) < 1e-4
+    for q in (50, 95):
+        assert np.percentile(rel(own, ref64), q) <= np.percentile(rel(got, ref64), q) * 1.01
 
 
 def test_edge_cases(res):
