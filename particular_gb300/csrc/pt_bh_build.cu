@@ -658,6 +658,26 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Levels TOP_LEVELS - 1 .. 0 (at most 8^L cells each, 4681 in all) in one block, a
+// barrier between levels: these levels hold few cells, and one launch each cost ~17 us
+// of latency at N = 4M (85 us for the five).
+constexpr int TOP_LEVELS = 5;
+
+template <class T>
+__global__ void __launch_bounds__(512)
+    cells_top(const int *__restrict__ levels, const int *__restrict__ by_level, const int *__restrict__ pre,
+              const int *__restrict__ kid, const int *__restrict__ nkid, const typename Prec<T>::V4 *__restrict__ nodeG,
+              Record<T> *rec, typename Prec<T>::V4 *nodeA, float4 *nodeQ, int4 *nodeB) {
+    for (int L = TOP_LEVELS - 1; L >= 0; --L) {
+        const int begin = levels[LEVELS + 1 + L], end = begin + levels[L];
+        for (int i = begin + threadIdx.x; i < end; i += blockDim.x) {
+            const int k = by_level[i];
+            cell(pre[k], load_kids(k, kid, nkid), nodeG, rec, nodeA, nodeQ, nodeB);
+        }
+        __syncthreads();  // the level's records (global, read through L2) before its parents
+    }
+}
+
 template <class T>
 int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     using V4 = typename Prec<T>::V4;
@@ -747,7 +767,7 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     PT_TRY(check_launch(ctx, "layout"));
 
     const int lvl_grid = std::max(1, std::min(blocks(n), 8 * ctx->sm_count));
-    for (int L = LEVELS - 1; L >= 0; --L) {
+    for (int L = LEVELS - 1; L >= TOP_LEVELS; --L) {
         // level L holds at most 8^L cells: shallow levels get a grid of their size
         const long long cap = L < 10 ? (1ll << (3 * L)) : (long long)n;
         const int grid = int(std::max(1ll, std::min<long long>(lvl_grid, (std::min<long long>(cap, n) + 255) / 256)));
@@ -756,6 +776,9 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
                                                 nodeQ, as<int4>(S.nodeB));
         PT_TRY(check_launch(ctx, "cells_level"));
     }
+    cells_top<T><<<1, 512, 0, st>>>(levels, as<int>(S.by_level), as<int>(S.pre), as<int>(S.kid), as<int>(S.nkid),
+                                    as<V4>(nG), as<Record<T>>(S.mom), as<V4>(nA), nodeQ, as<int4>(S.nodeB));
+    PT_TRY(check_launch(ctx, "cells_top"));
     S.last_n_src = n;
     S.f64 = F64;
     S.user_tree = false;

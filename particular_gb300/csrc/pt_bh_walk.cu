@@ -488,7 +488,7 @@ static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
 // Opened cells with at most this many nodes below them are summed body by body at
 // once instead of being walked level by level (<= 31: one warp-wide load; 0 = off).
 #ifndef PT_GW_FLAT
-#define PT_GW_FLAT 16
+#define PT_GW_FLAT 31
 #endif
 constexpr int GW_FLAT = PT_GW_FLAT;
 static_assert(GW_FLAT >= 0 && GW_FLAT <= 31, "a flattened subtree is loaded by one warp");
@@ -748,7 +748,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
         // of its leaves go straight to the body list (below). Exact sums instead of its
         // descendants' multipoles, so never less accurate; it saves the pops and votes
         // of the tree's last levels.
-        const bool flat = open && B.y - node - 1 <= GW_FLAT;
+        const bool flat = GW_FLAT > 0 && open && B.y - node - 1 <= GW_FLAT;
         const bool kids = open && !flat;
         const int np = int(rest) + int(kids);
         // each lane's pushes follow those of the lanes below it
@@ -859,39 +859,58 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
             mb &= mb - 1;
             append_bodies(__shfl_sync(0xffffffffu, B.z, src), __shfl_sync(0xffffffffu, B.w, src));
         }
-        unsigned mfl = __ballot_sync(0xffffffffu, flat);
-        while (mfl) {  // small opened subtrees: all their nodes at once, one per lane
-            const int src = __ffs(mfl) - 1;
-            mfl &= mfl - 1;
-            const int f0 = __shfl_sync(0xffffffffu, node, src) + 1;
-            const int f1 = __shfl_sync(0xffffffffu, B.y, src);
-            const int nd = f0 + lane;
-            int4 lb = make_int4(0, 0, -1, 0);
-            float4 la = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (nd < f1) lb = __ldg(nodeB + nd);
-            const bool one = lb.z >= 0 && lb.w == 1;  // a single-body leaf: its record is the body
-            if (one) la = __ldg(nodeA + nd);
-            visits += f1 - f0;
-            const unsigned m1 = __ballot_sync(0xffffffffu, one);
-            const int n1 = __popc(m1);
-            if (Nb + n1 > BodyList::CAP) {
-                eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, bsum);
-                entries += Nb;
-                Nb = 0;
+        // Small opened subtrees, all of this pop's at once: their nodes are numbered
+        // across the warp (a prefix sum of the subtrees' sizes) and loaded 32 at a
+        // time, one per lane; the leaves' bodies go to the body list.
+        if constexpr (GW_FLAT > 0) {
+            const int fcnt = flat ? B.y - node - 1 : 0;
+            int fincl = fcnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, fincl, o);
+                if (lane >= o) fincl += t;
             }
-            if (one) {
-                const int e = Nb + __popc(m1 & lt);
-                Lb.f[0][e] = la.x;
-                Lb.f[1][e] = la.y;
-                Lb.f[2][e] = la.z;
-                Lb.f[3][e] = la.w;
-            }
-            Nb += n1;
-            unsigned mm = __ballot_sync(0xffffffffu, lb.z >= 0 && lb.w > 1);
-            while (mm) {
-                const int s2 = __ffs(mm) - 1;
-                mm &= mm - 1;
-                append_bodies(__shfl_sync(0xffffffffu, lb.z, s2), __shfl_sync(0xffffffffu, lb.w, s2));
+            const int ftot = __shfl_sync(0xffffffffu, fincl, 31);
+            visits += ftot;
+            for (int fb = 0; fb < ftot; fb += 32) {
+                const int j = fb + lane;
+                // the subtree holding node j: the number of lanes whose prefix ends at or before j
+                int o = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int v = __shfl_sync(0xffffffffu, fincl, o + step - 1);
+                    if (v <= j) o += step;
+                }
+                o = min(o, 31);
+                const int first = __shfl_sync(0xffffffffu, node, o) + 1;
+                const int before = __shfl_sync(0xffffffffu, fincl, o) - __shfl_sync(0xffffffffu, fcnt, o);
+                const int nd = first + j - before;
+                int4 lb = make_int4(0, 0, -1, 0);
+                float4 la = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (j < ftot) lb = __ldg(nodeB + nd);
+                const bool one = lb.z >= 0 && lb.w == 1;  // a single-body leaf: its record is the body
+                if (one) la = __ldg(nodeA + nd);
+                const unsigned m1 = __ballot_sync(0xffffffffu, one);
+                const int n1 = __popc(m1);
+                if (Nb + n1 > BodyList::CAP) {
+                    eval_list<4, BodyList::CAP, GUARD, TPL>(Lb, Nb, px, py, pz, e2, bsum);
+                    entries += Nb;
+                    Nb = 0;
+                }
+                if (one) {
+                    const int e = Nb + __popc(m1 & lt);
+                    Lb.f[0][e] = la.x;
+                    Lb.f[1][e] = la.y;
+                    Lb.f[2][e] = la.z;
+                    Lb.f[3][e] = la.w;
+                }
+                Nb += n1;
+                unsigned mm = __ballot_sync(0xffffffffu, lb.z >= 0 && lb.w > 1);
+                while (mm) {
+                    const int s2 = __ffs(mm) - 1;
+                    mm &= mm - 1;
+                    append_bodies(__shfl_sync(0xffffffffu, lb.z, s2), __shfl_sync(0xffffffffu, lb.w, s2));
+                }
             }
         }
         __syncwarp();

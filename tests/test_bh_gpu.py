@@ -110,6 +110,41 @@ def test_tree_matches_reference_orthtree(res, oracle, kind, n):
     assert (np.abs(ref_m - m64) <= rng[:, 1] * 2.0 ** -23 * m64 + 1e-12).all()
 
 
+def test_cell_moments_are_fp64_sums_rounded_at_full_size(res, oracle):
+    """N = 4,194,304 bulge+disk: every cell's stored f32 mass and centre of mass against
+    the exact sums over the cell's bodies, rounded to f32. The moments are combined in
+    compensated FP32 (each value carried as an unevaluated sum hi + lo), not FP64:
+    nearly all values are the correctly rounded sum and the rest are one f32 step away
+    (the hi + lo pair rounds once more when stored)."""
+    if np.finfo(np.longdouble).eps > 1e-18:
+        pytest.skip("long double is not wider than double here")
+    b = ics.bulge_disk(1 << 22, seed=33)["bodies"]
+    m = cuda.BarnesHut(0.5, res, AccelerationSoftened(0.01))
+    m.compute(b)
+    g = m.export_tree()
+    order, e = oracle_preorder(oracle.Tree(b))
+    internal = e["internal"][order].astype(bool)
+    assert np.array_equal(internal, g["links"][:, 2] < 0)
+    rng, perm = e["range"][order][internal], e["perm"]
+    # Prefix sums in extended precision (x86 80-bit, aarch64 128-bit long double): the
+    # difference of two prefixes is exact to far below an f32 step even for two-body
+    # cells, which FP64 prefixes over 4M bodies are not.
+    bp = b[perm].astype(np.longdouble)
+    cs = np.zeros((bp.shape[0] + 1, 4), np.longdouble)
+    cs[1:, 3] = np.cumsum(bp[:, 3])
+    cs[1:, :3] = np.cumsum(bp[:, :3] * bp[:, 3:4], axis=0)
+    lo, hi = rng[:, 0], rng[:, 0] + rng[:, 1]
+    mass = cs[hi, 3] - cs[lo, 3]
+    com = (cs[hi, :3] - cs[lo, :3]) / mass[:, None]
+    want = np.concatenate([com, mass[:, None]], axis=1).astype(np.float64).astype(np.float32)
+    got = g["com_mass"][g["links"][:, 2] < 0].astype(np.float32)
+    steps = np.abs(got.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64))
+    exact = (steps == 0).mean()
+    print(f"{got.shape[0]} cells: {100 * exact:.4f} % of stored values equal the rounded exact sums, "
+          f"largest difference {steps.max()} f32 steps")
+    assert exact > 0.999 and steps.max() <= 1
+
+
 @pytest.mark.parametrize("theta", [0.3, 0.5, 0.8])
 def test_walk_matches_reference(res, oracle, theta):
     b = ics.plummer(20000, seed=24)["bodies"]
