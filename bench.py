@@ -50,7 +50,8 @@ def parse_args():
     p.add_argument("--bodies", type=int, default=0,
                    help="Barnes-Hut workload: bodies (default 4,194,304; smaller cases for profiling)")
     p.add_argument("--method", default=None,
-                   help="Barnes-Hut workload: 'theta,flags[,alpha[,local ratio]]' instead of the calibration "
+                   help="Barnes-Hut workload: 'theta,flags[,alpha[,local ratio[,monopole factor]]]' instead of "
+                        "the calibration "
                         "ladder and the comparison rows (short profiling runs)")
     return p.parse_args()
 
@@ -350,6 +351,7 @@ class BarnesHutWorkload:
             e = rel_err(self.d_out[idx_t].cpu().numpy(), self.ref64)
             return {"theta": theta, "quadrupole": bool(flags & 1), "group": bool(flags & 2),
                     "learned": bool(flags & 4), "local": bool(flags & 8), "relative": alpha,
+                    "monopole_factor": self.mono if (flags & 17) == 17 else None,
                     "local_ratio": ratio if flags & 8 else None, "ms": ms,
                     "bodies_per_s": self.n / (ms * 1e-3), **err_stats(e)}
 
@@ -390,10 +392,15 @@ class BarnesHutWorkload:
         self.selected_holdout = holdout(self.theta, self.flags, self.alpha, self.ratio)
         self.meets_bar = bool(ok) and self.selected_holdout["p95"] <= self.bar
 
+    # PT_BH_RELATIVE with quadrupoles: cells whose quadrupole term is within this
+    # fraction of alpha |a| are evaluated as monopoles (pt_bh_set_relative_monopole)
+    mono = 0.1
+
     def _set_alpha(self, flags):
         from particular_gb300 import _native as N
         if flags & 16:
             N.check(N.lib().pt_bh_set_relative_alpha(self.res.handle, self.alpha))
+            N.check(N.lib().pt_bh_set_relative_monopole(self.res.handle, self.mono))
         N.check(N.lib().pt_bh_set_local_ratio(self.res.handle, self.ratio))
 
     def _run(self, theta, flags):
@@ -480,6 +487,7 @@ class BarnesHutWorkload:
         return {"method": {"name": "cuda::BarnesHut", "theta": self.theta,
                            "quadrupole": bool(self.flags & 1), "group": bool(self.flags & 2),
                            "local": bool(self.flags & 8), "relative_alpha": self.alpha,
+                           "monopole_factor": self.mono if (self.flags & 17) == 17 else None,
                            "local_ratio": self.ratio if self.flags & 8 else None},
                 "selected": self.selected, "selected_holdout": self.selected_holdout,
                 "meets_bar": self.meets_bar,
@@ -1012,6 +1020,8 @@ def make_workload(args):
         parts = args.method.split(",")
         wl.fixed = (float(parts[0]), int(parts[1]), float(parts[2]) if len(parts) > 2 and parts[2] else None,
                     float(parts[3]) if len(parts) > 3 else 0.1)
+        if len(parts) > 4:
+            wl.mono = float(parts[4])
     return wl
 
 

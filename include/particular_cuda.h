@@ -253,6 +253,12 @@ int pt_bh_set_local_ratio(pt_ctx *ctx, float ratio);
 /* The error-bound factor of PT_BH_RELATIVE, in (0, 1]: smaller is more accurate and
  * slower. */
 int pt_bh_set_relative_alpha(pt_ctx *ctx, float alpha);
+/* PT_BH_RELATIVE with PT_BH_QUADRUPOLE: an accepted cell whose monopole truncation
+ * bound M w^2 / d^4 (d from the group's nearest point) stays within beta x alpha |a|
+ * is evaluated without its quadrupole term (20 instead of 58 flops per body). beta in
+ * [0, 1], 0 = every cell keeps its quadrupole; default 0.1, where the FP64-judged
+ * error does not change. */
+int pt_bh_set_relative_monopole(pt_ctx *ctx, float beta);
 /* Caps the PT_BH_GROUP walk's shared-memory stack at `ranges` entries per warp (2 to
  * the compiled capacity; 0 restores the capacity). A warp that runs out takes the
  * per-body walk instead (counted in pt_bh_stats.overflow): a tuning and test hook. */

@@ -99,6 +99,7 @@ def _declare(L):
         "pt_bh_set_learned_capacity": (ctypes.c_int, [c_ptr, ctypes.c_int]),
         "pt_bh_set_local_ratio": (ctypes.c_int, [c_ptr, ctypes.c_float]),
         "pt_bh_set_relative_alpha": (ctypes.c_int, [c_ptr, ctypes.c_float]),
+        "pt_bh_set_relative_monopole": (ctypes.c_int, [c_ptr, ctypes.c_float]),
         "pt_bh_accel_dvec3": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr, ctypes.c_size_t,
                                              ctypes.c_double, ctypes.c_double, ctypes.c_uint32, c_ptr]),
         "pt_bh_accel_dvec3_device": (ctypes.c_int, [c_ptr, c_ptr, ctypes.c_size_t, c_ptr, ctypes.c_size_t,

@@ -469,6 +469,18 @@ int pt_bh_set_relative_alpha(pt_ctx *ctx, float alpha) {
     return PT_OK;
 }
 
+int pt_bh_set_relative_monopole(pt_ctx *ctx, float beta) {
+    using namespace pt;
+    clear_error();
+    if (!ctx) return set_error(PT_ERR_INVALID, "pt_bh_set_relative_monopole: ctx is NULL");
+    if (!(beta >= 0.0f && beta <= 1.0f))
+        return set_error(PT_ERR_INVALID, "pt_bh_set_relative_monopole: %g outside [0, 1]", double(beta));
+    bh::State *S = bh::state(ctx);
+    if (!S) return set_error(PT_ERR_OOM, "Barnes-Hut state allocation failed");
+    S->rel_mono = beta;
+    return PT_OK;
+}
+
 int pt_bh_set_stack_limit(pt_ctx *ctx, int ranges) {
     using namespace pt;
     clear_error();

@@ -78,6 +78,7 @@ struct State {
     bool user_tree = false;           // the current tree came from pt_bh_load_tree (monopoles only)
     float local_ratio = 0.1f;         // PT_BH_LOCAL: far when group radius < ratio * distance
     float rel_alpha = 2.5e-3f;        // PT_BH_RELATIVE: opened where the bound exceeds alpha |a|
+    float rel_mono = 0.1f;            // PT_BH_RELATIVE + quadrupole: monopole-only cells below rel_mono alpha |a|
     const uint32_t *mlp_w = nullptr;  // learned correction: packed BF16 weights (owned by the MLP state)
     const float *mlp_b = nullptr;     // and its bias block
     float theta_inner = 0.5f;

@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
                   const float4 *__restrict__ nodeG, const float4 *__restrict__ sbody, const int *__restrict__ counters,
                   float th2, float th_in2, LearnedRecords LR, float eps2, float *__restrict__ out,
                   unsigned long long *__restrict__ stats, int *__restrict__ err, int stack_cap,
-                  float local_ratio, const float *__restrict__ gscale) {
+                  float local_ratio, const float *__restrict__ gscale, float mono_beta) {
     static_assert(!(LEARNED && LOCAL), "PT_BH_LEARNED and PT_BH_LOCAL are exclusive");
     static_assert(!(LEARNED && REL), "PT_BH_LEARNED and PT_BH_RELATIVE are exclusive");
     constexpr int NFC = QUAD ? 10 : 4;
@@ -540,6 +540,10 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
     // the factor of a cell's (M w^3)^(2/5) kept in its nodeB.w
     const float ginv = (REL && !QUAD) ? gscale[group] : 0.f;
     const float gq = (REL && QUAD) ? __powf(gscale[group], 0.4f) : 0.f;
+    // PT_BH_RELATIVE with quadrupoles: an accepted cell whose monopole truncation bound
+    // M w^2 / d^4 (the quadrupole term it would drop) stays within mono_beta alpha |a|
+    // from every body of the group enters the body list, without its quadrupole.
+    const float gmono = (REL && QUAD && mono_beta > 0.f) ? gscale[group] / mono_beta : 0.f;
     int2 *stack = s_stack[warp];
     const int T = counters[1];
     CellList &Lc = s_cells[warp];
@@ -662,7 +666,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
         // never contradict the per-target values. The remaining cells are voted on one
         // at a time: each lane tests its own target, a ballot collects the votes.
         // PT_BH_RELATIVE adds a second opening radius per cell (rr2), tested the same way.
-        bool maybe = false, sure = false;
+        bool maybe = false, sure = false, monoq = false;
         float w = 0.f, rr2 = 0.f;
         if (have && B.z < 0) {
             w = __int_as_float(B.x);
@@ -672,6 +676,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
             const float e2b = fmaxf(fmaxf(mn2 - A.z, A.z - mx2), 0.f);
             const float emin2 = fmaf(e0, e0, fmaf(e1, e1, e2b * e2b));
             maybe = (LEARNED ? th_in2 : th2) * emin2 < w * w || (REL && emin2 < rr2);
+            if (REL && QUAD) monoq = emin2 * emin2 >= A.w * w * w * gmono && gmono > 0.f;
             const float f0 = fmaxf(A.x - mn0, mx0 - A.x);
             const float f1 = fmaxf(A.y - mn1, mx1 - A.y);
             const float f2b = fmaxf(A.z - mn2, mx2 - A.z);
@@ -789,8 +794,9 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
             }
         }
         const bool bucket = acc && B.z >= 0 && B.w > 1;
-        const bool cellacc = acc && B.z < 0 && !farc;
-        const bool bodyacc = acc && B.z >= 0 && B.w == 1 && !farc;
+        const bool cellacc = acc && B.z < 0 && !farc && !monoq;
+        // single bodies, and cells whose quadrupole term is negligible (monoq): monopoles
+        const bool bodyacc = acc && (B.z >= 0 ? B.w == 1 : monoq) && !farc;
         // accepted cells -> the cell list (with their quadrupoles)
         const unsigned mc = __ballot_sync(0xffffffffu, cellacc);
         const int nc1 = __popc(mc);
@@ -1603,7 +1609,7 @@ using WalkKernel = void (*)(const float4 *, const uint32_t *, int, const float4 
                             const float4 *, const int *, float, float, float *, unsigned long long *);
 using GroupKernel = void (*)(const float4 *, const uint32_t *, int, const float4 *, const int4 *, const float4 *,
                              const float4 *, const float4 *, const int *, float, float, LearnedRecords, float,
-                             float *, unsigned long long *, int *, int, float, const float *);
+                             float *, unsigned long long *, int *, int, float, const float *, float);
 
 static WalkKernel masked_kernel(bool quad, bool guard) {
     if (quad) return guard ? bh_walk_masked<true, true> : bh_walk_masked<true, false>;
@@ -1736,7 +1742,7 @@ int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n
                                                                           32 * GW_WARPS, 0, st>>>(
                 tbody, tidx, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<float4>(S.nodeQ), as<float4>(S.nodeG),
                 as<float4>(S.sbody), as<int>(S.counters), th2, S.theta_inner * S.theta_inner, LR, eps2, d_out, stats,
-                err, S.stack_cap > 0 ? S.stack_cap : GW_STACK, S.local_ratio, gscale);
+                err, S.stack_cap > 0 ? S.stack_cap : GW_STACK, S.local_ratio, gscale, S.rel_mono);
             PT_TRY(check_launch(ctx, "bh_walk_group"));
             // Outside stream capture (and with the automatic capacity) the record count
             // is checked and the walk rerun with room for all records; otherwise an

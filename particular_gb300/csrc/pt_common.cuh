@@ -87,12 +87,13 @@ inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 
 // Barnes-Hut settings held by the context that its launches take as parameters
 // (pt_bh.cu): graphs that captured them compare these before a replay.
 struct BhTuning {
-    float local_ratio = 0.f, rel_alpha = 0.f, theta_inner = 0.f;
+    float local_ratio = 0.f, rel_alpha = 0.f, rel_mono = 0.f, theta_inner = 0.f;
     int stack_cap = 0, learned_cap = 0;
     const void *mlp = nullptr;
     bool operator==(const BhTuning &o) const {
-        return local_ratio == o.local_ratio && rel_alpha == o.rel_alpha && theta_inner == o.theta_inner &&
-               stack_cap == o.stack_cap && learned_cap == o.learned_cap && mlp == o.mlp;
+        return local_ratio == o.local_ratio && rel_alpha == o.rel_alpha && rel_mono == o.rel_mono &&
+               theta_inner == o.theta_inner && stack_cap == o.stack_cap && learned_cap == o.learned_cap &&
+               mlp == o.mlp;
     }
 };
 BhTuning bh_tuning(pt_ctx *ctx);

@@ -176,11 +176,13 @@ class BarnesHut:
     pt_bh_set_local_ratio); its truncation error is judged against FP64.
     relative=alpha (with group) also opens a cell where its truncation bound
     M w^3 / d^5 (M w^2 / d^4 without quadrupoles) exceeds alpha |a|, |a| estimated
-    once per group; theta stays the geometric cap.
+    once per group; theta stays the geometric cap. monopole=beta (with relative and
+    quadrupole) evaluates an accepted cell without its quadrupole where the term it
+    drops, M w^2 / d^4, stays within beta alpha |a| (pt_bh_set_relative_monopole).
     """
 
     def __init__(self, theta, resources, interaction, quadrupole=False, group=False,
-                 learned=False, local=False, dvec3=False, relative=None):
+                 learned=False, local=False, dvec3=False, relative=None, monopole=None):
         self.dvec3 = bool(dvec3)  # glam DVec3 bodies: the f64 method (reference rule only)
         self.theta64 = float(theta)
         self.theta = float(np.float32(theta))
@@ -191,6 +193,9 @@ class BarnesHut:
         self.learned = bool(learned)  # needs a model (particular_gb300.learned) and group
         self.local = bool(local)      # far nodes through the group's local expansion
         self.relative = None if relative is None else float(relative)  # error-bound factor alpha
+        # with relative and quadrupole: cells whose quadrupole term stays within
+        # monopole x alpha |a| are evaluated without it (None: the resources' setting)
+        self.monopole = None if monopole is None else float(monopole)
 
     @property
     def flags(self):
@@ -201,6 +206,8 @@ class BarnesHut:
     def _set_alpha(self):
         if self.relative is not None:
             N.check(N.lib().pt_bh_set_relative_alpha(self.resources.handle, self.relative))
+        if self.monopole is not None:
+            N.check(N.lib().pt_bh_set_relative_monopole(self.resources.handle, self.monopole))
 
     def build(self, affecting):
         """Builds the tree over `affecting` (any storage of particles) once; pass the

@@ -30,12 +30,33 @@ def test_opens_at_least_what_the_cap_opens(res, oracle, quad):
     geo = bh(res, 0.6, quadrupole=quad)
     e0 = rel(geo.compute(b)[::10], ref64)
     s0 = geo.stats()
-    m = bh(res, 0.6, quadrupole=quad, relative=2.5e-3)
+    m = bh(res, 0.6, quadrupole=quad, relative=2.5e-3, monopole=0.0)
     e1 = rel(m.compute(b)[::10], ref64)
     s1 = m.stats()
     assert s1["interactions"] > s0["interactions"] and s1["overflow"] == 0
     for q in (50, 95, 99):
         assert np.percentile(e1, q) <= np.percentile(e0, q) * 1.01 + 1e-7, q
+
+
+@pytest.mark.parametrize("local", [False, True])
+def test_monopole_cells_keep_the_error(res, oracle, local):
+    """With the quadrupole, accepted cells whose quadrupole term is within beta alpha |a|
+    are evaluated as monopoles: at beta 0.1 a large share of the list's cells drop the
+    term while the FP64-judged error stays where it was."""
+    b = ics.bulge_disk(60000, seed=69)["bodies"]
+    ref64 = oracle.bf_f64(b[::20], b, 0.01, True)
+    rows = {}
+    for beta in (0.0, 0.1):
+        m = bh(res, 1.0, quadrupole=True, relative=2.5e-3, monopole=beta, local=local)
+        e = rel(m.compute(b)[::20], ref64)
+        rows[beta] = (m.stats(), np.percentile(e, 50), np.percentile(e, 95))
+    (s0, p50a, p95a), (s1, p50b, p95b) = rows[0.0], rows[0.1]
+    print(f"local {local}: cells {s0['cell_interactions']} -> {s1['cell_interactions']} of "
+          f"{s0['interactions']} entries; p50 {p50a:.3e} -> {p50b:.3e}, p95 {p95a:.3e} -> {p95b:.3e}")
+    assert s1["interactions"] == s0["interactions"]      # the same accepted nodes
+    assert s1["cell_interactions"] < 0.8 * s0["cell_interactions"]
+    assert p95b <= 1.05 * p95a and p50b <= 1.1 * p50a
+    N.check(N.lib().pt_bh_set_relative_monopole(res.handle, 0.1))
 
 
 def test_tiny_alpha_is_the_direct_sum(res, oracle):
@@ -128,3 +149,7 @@ def test_relative_flag_validation(res):
         with pytest.raises(N.CudaError):
             N.check(L.pt_bh_set_relative_alpha(res.handle, bad))
     N.check(L.pt_bh_set_relative_alpha(res.handle, 2.5e-3))
+    for bad in (-0.1, 1.5, float("nan")):
+        with pytest.raises(N.CudaError):
+            N.check(L.pt_bh_set_relative_monopole(res.handle, bad))
+    N.check(L.pt_bh_set_relative_monopole(res.handle, 0.1))
