@@ -274,7 +274,9 @@ class BarnesHutWorkload:
               (1.0, 19, 1.5e-3, 0.1), (1.0, 19, 2e-3, 0.1), (1.0, 19, 2.5e-3, 0.1), (1.0, 19, 3e-3, 0.1),
               (1.0, 27, 2e-3, 0.1), (1.0, 27, 2.5e-3, 0.1), (1.0, 27, 2.75e-3, 0.1), (1.0, 27, 3e-3, 0.1),
               (1.0, 27, 2.5e-3, 0.13), (1.0, 27, 2.75e-3, 0.13), (1.0, 27, 3e-3, 0.13),
-              (1.0, 27, 2.5e-3, 0.15), (1.0, 27, 2.6e-3, 0.14), (1.0, 27, 2.75e-3, 0.14)]
+              (1.0, 27, 2.5e-3, 0.15), (1.0, 27, 2.6e-3, 0.14), (1.0, 27, 2.75e-3, 0.14),
+              (1.0, 27, 3e-3, 0.12), (1.0, 27, 3.25e-3, 0.12), (1.0, 27, 3.5e-3, 0.12),
+              (1.0, 27, 3.5e-3, 0.1), (1.0, 27, 4e-3, 0.1), (1.0, 27, 3e-3, 0.14), (1.0, 27, 3.25e-3, 0.14)]
 
     def __init__(self, n=4194304, softening=0.01, sample=2048, holdout=4096):
         from particular_gb300 import ics

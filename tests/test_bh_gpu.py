@@ -112,10 +112,11 @@ def test_tree_matches_reference_orthtree(res, oracle, kind, n):
 
 def test_cell_moments_are_fp64_sums_rounded_at_full_size(res, oracle):
     """N = 4,194,304 bulge+disk: every cell's stored f32 mass and centre of mass against
-    the exact sums over the cell's bodies, rounded to f32. The moments are combined in
-    compensated FP32 (each value carried as an unevaluated sum hi + lo), not FP64:
-    nearly all values are the correctly rounded sum and the rest are one f32 step away
-    (the hi + lo pair rounds once more when stored)."""
+    the exact sums over the cell's bodies. The moments are combined in compensated FP32
+    (each value carried as an unevaluated sum hi + lo, centres of mass as offsets from
+    the cell's geometric centre), not FP64: most stored values are the exact sum
+    rounded to f32, and every one is within two f32 steps of it at the cell's scale (a
+    centre-of-mass coordinate at the scale of the cell's width when it lies near zero)."""
     if np.finfo(np.longdouble).eps > 1e-18:
         pytest.skip("long double is not wider than double here")
     b = ics.bulge_disk(1 << 22, seed=33)["bodies"]
@@ -124,7 +125,8 @@ def test_cell_moments_are_fp64_sums_rounded_at_full_size(res, oracle):
     g = m.export_tree()
     order, e = oracle_preorder(oracle.Tree(b))
     internal = e["internal"][order].astype(bool)
-    assert np.array_equal(internal, g["links"][:, 2] < 0)
+    cells = g["links"][:, 2] < 0
+    assert np.array_equal(internal, cells)
     rng, perm = e["range"][order][internal], e["perm"]
     # Prefix sums in extended precision (x86 80-bit, aarch64 128-bit long double): the
     # difference of two prefixes is exact to far below an f32 step even for two-body
@@ -136,13 +138,18 @@ def test_cell_moments_are_fp64_sums_rounded_at_full_size(res, oracle):
     lo, hi = rng[:, 0], rng[:, 0] + rng[:, 1]
     mass = cs[hi, 3] - cs[lo, 3]
     com = (cs[hi, :3] - cs[lo, :3]) / mass[:, None]
-    want = np.concatenate([com, mass[:, None]], axis=1).astype(np.float64).astype(np.float32)
-    got = g["com_mass"][g["links"][:, 2] < 0].astype(np.float32)
-    steps = np.abs(got.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64))
-    exact = (steps == 0).mean()
-    print(f"{got.shape[0]} cells: {100 * exact:.4f} % of stored values equal the rounded exact sums, "
-          f"largest difference {steps.max()} f32 steps")
-    assert exact > 0.999 and steps.max() <= 1
+    exact = np.concatenate([com, mass[:, None]], axis=1).astype(np.float64)
+    got = g["com_mass"][cells].astype(np.float64)
+    rounded = (got == exact.astype(np.float32).astype(np.float64)).mean()
+    w = g["width"][cells].astype(np.float64)
+    scale = np.maximum(np.abs(exact), np.concatenate([np.repeat(w[:, None], 3, 1), np.zeros((w.size, 1))], 1))
+    step = 2.0 ** (np.floor(np.log2(scale)) - 23)
+    worst = (np.abs(got - exact) / step).max(axis=0)
+    print(f"{got.shape[0]} cells: {100 * rounded:.3f} % of stored values are the exact sums rounded to f32; "
+          f"largest error in f32 steps at the cell's scale: x {worst[0]:.2f} y {worst[1]:.2f} z {worst[2]:.2f} "
+          f"mass {worst[3]:.2f}")
+    assert rounded > 0.97
+    assert worst.max() <= 2.0
 
 
 @pytest.mark.parametrize("theta", [0.3, 0.5, 0.8])
