@@ -432,11 +432,13 @@ class BarnesHutWorkload:
 
     def walk_flops(self, st):
         # monopole: 20 per accepted node (the GPU Gems convention); the quadrupole
-        # term adds 38 per accepted cell (single bodies carry none); a far node taken
-        # by the local expansion costs its lane 85 flops (180 with the quadrupole)
+        # term adds 38 per accepted cell evaluated with it (single bodies and
+        # monopole-only cells carry none); a far node taken by the local expansion
+        # costs its lane 85 flops, 180 when added with its quadrupole
         quad = bool(self.flags & 1)
         return (20 * st.interactions + (self.QUAD_FLOPS * st.cell_interactions if quad else 0)
-                + self.LOCAL_FLOPS[quad] * st.local_nodes)
+                + self.LOCAL_FLOPS[0] * st.local_nodes
+                + (self.LOCAL_FLOPS[1] - self.LOCAL_FLOPS[0]) * st.local_quad_nodes)
 
     def roofline(self, res, step_ms):
         import ctypes
@@ -481,9 +483,10 @@ class BarnesHutWorkload:
                 "interactions_per_body": st.interactions / self.n,
                 "cell_interactions_per_body": st.cell_interactions / self.n,
                 "local_nodes_per_body": st.local_nodes / self.n,
-                "algorithmic": "20 flop per accepted node per body (+38 per accepted cell with "
-                               "the quadrupole) + 85 (180 with the quadrupole) per far node taken "
-                               "by a group's local expansion, x the walk's own counts",
+                "local_quad_nodes_per_body": st.local_quad_nodes / self.n,
+                "algorithmic": "20 flop per accepted node per body (+38 per accepted cell evaluated "
+                               "with its quadrupole) + 85 per far node taken by a group's local "
+                               "expansion (180 when added with its quadrupole), x the walk's own counts",
                 "peak_source": "measured FFMA-chain kernel over all SMs (pt_measure_fp32_peak)"}
 
     def extra(self):
@@ -823,13 +826,15 @@ class LeapfrogBarnesHutWorkload:
         N.check(N.lib().pt_bh_last_stats(res.handle, ctypes.byref(st)))
         peak = ctypes.c_double(0)
         N.check(N.lib().pt_measure_fp32_peak(res.handle, ctypes.byref(peak)))
-        flops = (20 * st.interactions + 38 * st.cell_interactions + 180 * st.local_nodes) * self.steps_per_call
+        flops = (20 * st.interactions + 38 * st.cell_interactions + 85 * st.local_nodes
+                 + 95 * st.local_quad_nodes) * self.steps_per_call
         achieved = flops / (step_ms * 1e-3) / 1e12
         return {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                 "frac": achieved / peak.value, "traffic": None,
                 "kernel": "bh_walk_group (whole leapfrog step timed, tree build included)",
                 "algorithmic": "per evaluation: 20 flop per accepted node per body + 38 per accepted cell "
-                               "+ 180 per far node of a local expansion (counts of the last evaluation)"
+                               "+ 85 per far node of a local expansion (180 with its quadrupole; counts of the "
+                               "last evaluation)"
                                " x 10 evaluations per step",
                 "peak_source": "measured FFMA-chain kernel over all SMs (pt_measure_fp32_peak)"}
 

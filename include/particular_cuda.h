@@ -204,6 +204,9 @@ typedef struct pt_bh_stats {
                                    quadrupole term to) */
     uint64_t local_nodes;  /* PT_BH_LOCAL: far nodes added to the groups' local
                               expansions (per group and node) */
+    uint64_t local_quad_nodes; /* the far nodes of local_nodes that are cells added with
+                                  their quadrupole (PT_BH_QUADRUPOLE; monopole-only
+                                  cells of PT_BH_RELATIVE are not) */
 } pt_bh_stats;
 
 /* cuda::BarnesHut over host buffers (synchronous). Layouts as pt_bf_accel_f32. */

@@ -40,7 +40,7 @@ class BhStats(ctypes.Structure):
                 ("visits", ctypes.c_uint64), ("warps", ctypes.c_uint64),
                 ("max_stack", ctypes.c_uint64), ("overflow", ctypes.c_uint64),
                 ("learned", ctypes.c_uint64), ("cell_interactions", ctypes.c_uint64),
-                ("local_nodes", ctypes.c_uint64)]
+                ("local_nodes", ctypes.c_uint64), ("local_quad_nodes", ctypes.c_uint64)]
 
 _NAMES = {PT_ERR_INVALID: "PT_ERR_INVALID", PT_ERR_CUDA: "PT_ERR_CUDA", PT_ERR_OOM: "PT_ERR_OOM",
           PT_ERR_CAPACITY: "PT_ERR_CAPACITY", PT_ERR_TIMEOUT: "PT_ERR_TIMEOUT",

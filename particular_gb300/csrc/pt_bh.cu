@@ -366,7 +366,7 @@ int pt_bh_load_tree(pt_ctx *ctx, const int32_t *orthant, const float *bbox, cons
         PT_TRY(ensure_buf(ctx, S->nodeQ, 32 * T));
         PT_TRY(ensure_buf(ctx, S->sbody, 16 * std::max<size_t>(L, 1)));
     }
-    PT_TRY(ensure_buf(ctx, S->counters, 4 * sizeof(int) + 8 * sizeof(unsigned long long)));
+    PT_TRY(ensure_buf(ctx, S->counters, sizeof(unsigned long long) * 16));
     PT_TRY(ensure_buf(ctx, S->box, sizeof(float) * 8));
     cudaStream_t st = ctx->stream;
     const int counts[4] = {int(L), int(T), cells, 0};
@@ -376,7 +376,7 @@ int pt_bh_load_tree(pt_ctx *ctx, const int32_t *orthant, const float *bbox, cons
         PT_CUDA(cudaMemsetAsync(S->nodeQ.ptr, 0, 32 * T, st));
         if (L) PT_CUDA(cudaMemcpyAsync(S->sbody.ptr, leaves.data(), 16 * L, cudaMemcpyHostToDevice, st));
     }
-    PT_CUDA(cudaMemsetAsync(S->counters.ptr, 0, 4 * sizeof(int) + 8 * sizeof(unsigned long long), st));
+    PT_CUDA(cudaMemsetAsync(S->counters.ptr, 0, sizeof(unsigned long long) * 16, st));
     PT_CUDA(cudaMemcpyAsync(S->counters.ptr, counts, sizeof(counts), cudaMemcpyHostToDevice, st));
     PT_CUDA(cudaMemcpyAsync(S->box.ptr, box, sizeof(box), cudaMemcpyHostToDevice, st));
     PT_CUDA(cudaStreamSynchronize(st));  // the host arrays are freed on return
@@ -513,7 +513,7 @@ int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out) {
     auto *S = static_cast<bh::State *>(ctx->bh);
     if (!S || !S->counters.ptr) return set_error(PT_ERR_INVALID, "pt_bh_last_stats: no Barnes-Hut call yet");
     PT_CUDA(cudaSetDevice(ctx->device));
-    unsigned long long h[10];
+    unsigned long long h[11];
     PT_CUDA(cudaMemcpyAsync(h, S->counters.ptr, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
     PT_CUDA(cudaStreamSynchronize(ctx->stream));
     const int *hi = reinterpret_cast<const int *>(h);
@@ -522,6 +522,7 @@ int pt_bh_last_stats(pt_ctx *ctx, pt_bh_stats *out) {
     out->cells = uint64_t(hi[2]);
     out->overflow = h[8];
     out->local_nodes = h[9];
+    out->local_quad_nodes = h[10];
     out->interactions = h[2];
     out->visits = h[3];
     out->warps = h[4];

@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
     const float far2 = LOCAL ? rg2 / (local_ratio * local_ratio) : 0.f;
     if (LOCAL)
         for (int k = 0; k < 19; ++k) s_lx[warp][k][lane] = 0.f;
-    unsigned nlocal = 0;  // warp-uniform
+    unsigned nlocal = 0, nlocalq = 0;  // warp-uniform: far nodes, those with a quadrupole
     int Nf = 0;                     // queued far nodes
     // learned: the warp's current record chunk and its fill; the previous chunk links to
     // the next one (head of the group's chain first)
@@ -781,7 +781,10 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
         if (LOCAL) {
             const unsigned mf = __ballot_sync(0xffffffffu, farc);
             if (mf) {
-                if (farc) s_far[warp][Nf + __popc(mf & lt)] = 2 * node + (B.z < 0 ? 1 : 0);
+                // the low bit asks for the cell's quadrupole (not for monopole-only cells)
+                const bool farq = farc && B.z < 0 && !monoq;
+                if (farc) s_far[warp][Nf + __popc(mf & lt)] = 2 * node + (farq ? 1 : 0);
+                if (QUAD) nlocalq += __popc(__ballot_sync(0xffffffffu, farq));
                 Nf += __popc(mf);
                 nlocal += __popc(mf);
                 __syncwarp();
@@ -988,7 +991,10 @@ __global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MIN
         atomicAdd(stats + 0, s_acc);
         atomicAdd(stats + 1, s_vis);
         if (LEARNED) atomicAdd(stats + 4, learned);
-        if (LOCAL && !failed) atomicAdd(stats + 7, nlocal);
+        if (LOCAL && !failed) {
+            atomicAdd(stats + 7, nlocal);
+            if (QUAD) atomicAdd(stats + 8, nlocalq);
+        }
         atomicAdd(stats + 5, s_cell);
         atomicAdd(stats + 2, 1ull);
         atomicMax(stats + 3, (unsigned long long)maxS);
@@ -1678,7 +1684,7 @@ int run64(pt_ctx *ctx, const double4_32a *d_aff, int n_aff, const double4_32a *d
     const uint32_t *tidx = same ? as<uint32_t>(S.idx) : as<uint32_t>(S.tidx);
     unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 2;
     int *err = as<int>(S.counters) + 3;
-    PT_CUDA(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
+    PT_CUDA(cudaMemsetAsync(stats, 0, 9 * sizeof(unsigned long long), st));
     PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     mark(ctx, 1);
     bh_walk64<<<(n_aff + 32 * W64_WARPS - 1) / (32 * W64_WARPS), 32 * W64_WARPS, 0, st>>>(
@@ -1700,7 +1706,7 @@ int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n
     // fell back to the per-body walk, far nodes taken by the local expansion}
     unsigned long long *stats = reinterpret_cast<unsigned long long *>(S.counters.ptr) + 2;
     int *err = as<int>(S.counters) + 3;
-    PT_CUDA(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
+    PT_CUDA(cudaMemsetAsync(stats, 0, 9 * sizeof(unsigned long long), st));
     // within a leapfrog sequence the error word collects every step's errors
     if (!ctx->keep_errors) PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     const float th2 = theta * theta;
@@ -1754,7 +1760,7 @@ int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n
             if (used <= S.lcap) break;
             S.lcap = used + used / 4;
             PT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-            PT_CUDA(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
+            PT_CUDA(cudaMemsetAsync(stats, 0, 9 * sizeof(unsigned long long), st));
         }
         if (learned) {
             bh_learned_eval<<<ctx->sm_count * 4, 128, 0, st>>>(LR, as<float4>(S.nodeA), as<float4>(S.nodeQ),
