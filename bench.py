@@ -53,6 +53,9 @@ def parse_args():
                    help="Barnes-Hut workload: 'theta,flags[,alpha[,local ratio[,monopole factor]]]' instead of "
                         "the calibration "
                         "ladder and the comparison rows (short profiling runs)")
+    p.add_argument("--stack-limit", type=int, default=0,
+                   help="Barnes-Hut workload: cap the group walk's stack at this many ranges (2 sends every "
+                        "warp to the per-body skip-pointer walk: the stackless traversal, for comparison)")
     return p.parse_args()
 
 
@@ -1194,6 +1197,9 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     res.set_stream(stream.cuda_stream)
+    if args.stack_limit:
+        from particular_gb300 import _native as N
+        N.check(N.lib().pt_bh_set_stack_limit(res.handle, args.stack_limit))
     wl.setup_gpu(res, torch, stream)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
