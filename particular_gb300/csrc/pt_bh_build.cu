@@ -658,10 +658,11 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// Levels TOP_LEVELS - 1 .. 0 (at most 8^L cells each, 4681 in all) in one block, a
-// barrier between levels: these levels hold few cells, and one launch each cost ~17 us
-// of latency at N = 4M (85 us for the five).
-constexpr int TOP_LEVELS = 5;
+// Levels TOP_LEVELS - 1 .. 0 (at most 8^L cells each, 585 in all) in one block, a
+// barrier between levels: these levels hold few cells, and one launch each cost
+// ~17 us of latency at N = 4M. (Level 4 too, up to 4096 cells at several cells per
+// thread, made the block take 66 us.)
+constexpr int TOP_LEVELS = 4;
 
 template <class T>
 __global__ void __launch_bounds__(512)
