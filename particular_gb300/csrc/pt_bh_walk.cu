@@ -1033,105 +1033,30 @@ __device__ __forceinline__ void scale_cursor_walk(float cx, float cy, float cz, 
     }
 }
 
-// One warp per group: the group's box from its bodies (one load per lane and body
-// slot), then the walk from the box centre with a shared-memory stack of sibling
-// ranges, one node per lane and pop, as the group walk pops them: the chain of
-// dependent loads is the tree's depth, not every visited node (one thread per group
-// walking the cursor took 125 us at N = 4M with 6 % of warps active). The accepted
-// nodes are the cursor walk's; a warp whose stack runs out takes that walk instead.
-constexpr int GS_WARPS = 4;
-constexpr int GS_STACK = 192;
-__global__ void __launch_bounds__(32 * GS_WARPS)
+// One thread per group: the group's box, then the cursor walk from its centre. (One
+// warp per group walking with a range stack, one node per lane and pop, was slower at
+// N = 4M, 125 -> ~290 us: 65536 warps take several waves, each pop a round trip to
+// L2, while the threads' cursor walks mostly hit L1 in the tree's upper levels.)
+__global__ void __launch_bounds__(128)
     bh_group_scale(const float4 *__restrict__ tbody, int n_aff, const float4 *__restrict__ nodeA,
                    const int4 *__restrict__ nodeB, const int *__restrict__ counters, float eps2, float alpha,
                    float *__restrict__ gscale) {
-    __shared__ int2 s_stack[GS_WARPS][GS_STACK];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = blockIdx.x * GS_WARPS + warp;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int g0 = g * GW_GROUP;
     if (g0 >= n_aff) return;
-    const float4 p0 = tbody[g0];
-    float mn0 = p0.x, mn1 = p0.y, mn2 = p0.z, mx0 = p0.x, mx1 = p0.y, mx2 = p0.z;
-    for (int i = lane; i < GW_GROUP; i += 32) {
-        const int t = g0 + i;
-        if (t < n_aff) {
-            const float4 p = tbody[t];
-            mn0 = fminf(mn0, p.x), mn1 = fminf(mn1, p.y), mn2 = fminf(mn2, p.z);
-            mx0 = fmaxf(mx0, p.x), mx1 = fmaxf(mx1, p.y), mx2 = fmaxf(mx2, p.z);
-        }
+    const int g1 = min(n_aff, g0 + GW_GROUP);
+    float4 p = tbody[g0];
+    float mn0 = p.x, mn1 = p.y, mn2 = p.z, mx0 = p.x, mx1 = p.y, mx2 = p.z;
+    for (int t = g0 + 1; t < g1; ++t) {
+        p = tbody[t];
+        mn0 = fminf(mn0, p.x), mn1 = fminf(mn1, p.y), mn2 = fminf(mn2, p.z);
+        mx0 = fmaxf(mx0, p.x), mx1 = fmaxf(mx1, p.y), mx2 = fmaxf(mx2, p.z);
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mn0 = fminf(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
-        mn1 = fminf(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
-        mn2 = fminf(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
-        mx0 = fmaxf(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
-        mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
-        mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
-    }
-    const float cx = 0.5f * (mn0 + mx0), cy = 0.5f * (mn1 + mx1), cz = 0.5f * (mn2 + mx2);
-    const int T = counters[1];
-    const unsigned lt = (1u << lane) - 1u;
-    int2 *stack = s_stack[warp];
-    if (lane == 0) stack[0] = make_int2(0, T);
-    __syncwarp();
-    int S = 1;
-    bool failed = false;
     float ax = 0.f, ay = 0.f, az = 0.f;
-    while (S > 0) {
-        const int k = min(min(32, S), max(1, (GS_STACK - S) / 2));
-        const bool have = lane < k;
-        const int2 range = have ? stack[S - 1 - lane] : make_int2(0, 0);
-        __syncwarp();
-        S -= k;
-        const int node = range.x;
-        float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
-        int4 B = make_int4(0, 0, 0, 0);
-        if (have) {
-            A = __ldg(nodeA + node);
-            B = __ldg(nodeB + node);
-        }
-        const float dx = A.x - cx, dy = A.y - cy, dz = A.z - cz;
-        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float w = __int_as_float(B.x);
-        const bool open = have && B.z < 0 && 2.25f * d2 < w * w;
-        if (have && !open && d2 > 0.f) {
-            const float inv = rsqrt_ftz(d2 + eps2);
-            const float s = (A.w * inv) * (inv * inv);
-            ax = fmaf(dx, s, ax);
-            ay = fmaf(dy, s, ay);
-            az = fmaf(dz, s, az);
-        }
-        const bool rest = have && B.y < range.y;  // later siblings remain
-        const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, open);
-        int slot = S + __popc(mrest & lt) + __popc(mopen & lt);
-        if (slot + int(rest) + int(open) > GS_STACK) {
-            failed = true;  // never written out of bounds
-        } else {
-            if (rest) stack[slot++] = make_int2(B.y, range.y);
-            if (open) stack[slot++] = make_int2(node + 1, B.y);
-        }
-        if (__any_sync(0xffffffffu, failed)) {
-            failed = true;
-            break;
-        }
-        S += __popc(mrest) + __popc(mopen);
-        __syncwarp();
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        ax += __shfl_xor_sync(0xffffffffu, ax, o);
-        ay += __shfl_xor_sync(0xffffffffu, ay, o);
-        az += __shfl_xor_sync(0xffffffffu, az, o);
-    }
-    if (lane == 0) {
-        if (failed) {
-            ax = ay = az = 0.f;
-            scale_cursor_walk(cx, cy, cz, nodeA, nodeB, T, eps2, ax, ay, az);
-        }
-        const float a = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
-        gscale[g] = 1.f / (alpha * fmaxf(a, 1e-30f));
-    }
+    scale_cursor_walk(0.5f * (mn0 + mx0), 0.5f * (mn1 + mx1), 0.5f * (mn2 + mx2), nodeA, nodeB, counters[1], eps2,
+                      ax, ay, az);
+    const float a = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+    gscale[g] = 1.f / (alpha * fmaxf(a, 1e-30f));
 }
 
 // ---- masked group walk: the reference's rule, per body, with shared traversal ----
@@ -1812,8 +1737,7 @@ int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n
         const float *gscale = nullptr;
         if (flags & PT_BH_RELATIVE) {
             PT_TRY(ensure_buf(ctx, S.gscale, sizeof(float) * size_t(groups)));
-            bh_group_scale<<<(groups + GS_WARPS - 1) / GS_WARPS, 32 * GS_WARPS, 0, st>>>(
-                tbody, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB),
+            bh_group_scale<<<blocks(groups, 128), 128, 0, st>>>(tbody, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB),
                                                                 as<int>(S.counters), eps2, S.rel_alpha,
                                                                 as<float>(S.gscale));
             PT_TRY(check_launch(ctx, "bh_group_scale"));
