@@ -137,3 +137,42 @@ def test_graph_recaptured_when_settings_change(res):
         N.check(L.pt_bh_set_local_ratio(res.handle, 0.1))
     assert np.array_equal(outs[0][0], outs[1][0])
     assert np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_graph_recaptured_when_buffers_grow():
+    """A captured leapfrog holds the addresses of the context's grow-only buffers. A
+    bigger Barnes-Hut call on the same context between two replays reallocates them
+    (every reallocation bumps the context's buffer epoch), so the next replay
+    captures again and still equals the eager steps."""
+    import torch
+    from particular_gb300 import CudaResources
+    n, n_big = 20000, 400000
+    d = ics.plummer(n, seed=55)
+    big = ics.plummer(n_big, seed=56)
+    L = N.lib()
+    fl = N.PT_BH_QUADRUPOLE | N.PT_BH_GROUP | N.PT_BH_LOCAL
+    outs = []
+    for use_graph in (0, 1):
+        r = CudaResources(0)
+        try:
+            b = torch.from_numpy(d["bodies"]).cuda()
+            v = torch.zeros((n, 4), device="cuda")
+            v[:, :3] = torch.from_numpy(d["vel"]).cuda()
+            a = torch.zeros((n, 3), device="cuda")
+            bb = torch.from_numpy(big["bodies"]).cuda()
+            ab = torch.zeros((n_big, 3), device="cuda")
+            torch.cuda.synchronize()
+            N.check(L.pt_bh_accel_f32_device(r.handle, b.data_ptr(), n, b.data_ptr(), n,
+                                             0.5, 0.01, fl, a.data_ptr()))
+            for k in range(3):
+                N.check(L.pt_leapfrog_device(r.handle, b.data_ptr(), v.data_ptr(), a.data_ptr(), n,
+                                             1e-3, 3, N.PT_METHOD_BARNES_HUT, 0.5, 0.01, fl, use_graph))
+                if k == 0:  # grows the tree buffers between the capture and the replays
+                    N.check(L.pt_bh_accel_f32_device(r.handle, bb.data_ptr(), n_big, bb.data_ptr(),
+                                                     n_big, 0.5, 0.01, fl, ab.data_ptr()))
+            r.synchronize()
+            outs.append((b.cpu().numpy(), v.cpu().numpy()))
+        finally:
+            r.close()
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
