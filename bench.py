@@ -279,7 +279,10 @@ class BarnesHutWorkload:
               (1.0, 27, 2.5e-3, 0.13), (1.0, 27, 2.75e-3, 0.13), (1.0, 27, 3e-3, 0.13),
               (1.0, 27, 2.5e-3, 0.15), (1.0, 27, 2.6e-3, 0.14), (1.0, 27, 2.75e-3, 0.14),
               (1.0, 27, 3e-3, 0.12), (1.0, 27, 3.25e-3, 0.12), (1.0, 27, 3.5e-3, 0.12),
-              (1.0, 27, 3.5e-3, 0.1), (1.0, 27, 4e-3, 0.1), (1.0, 27, 3e-3, 0.14), (1.0, 27, 3.25e-3, 0.14)]
+              (1.0, 27, 3.5e-3, 0.1), (1.0, 27, 4e-3, 0.1), (1.0, 27, 3e-3, 0.14), (1.0, 27, 3.25e-3, 0.14),
+              # looser geometric caps: the error bound decides more of the openings
+              (1.2, 27, 2.75e-3, 0.1), (1.5, 27, 2.5e-3, 0.1), (1.5, 27, 2.75e-3, 0.1), (1.5, 27, 3e-3, 0.1),
+              (1.5, 27, 2.5e-3, 0.12), (1.5, 27, 2.75e-3, 0.12), (2.0, 27, 2.75e-3, 0.1)]
 
     def __init__(self, n=4194304, softening=0.01, sample=2048, holdout=4096):
         from particular_gb300 import ics
@@ -360,7 +363,11 @@ class BarnesHutWorkload:
                     "local_ratio": ratio if flags & 8 else None, "ms": ms,
                     "bodies_per_s": self.n / (ms * 1e-3), **err_stats(e)}
 
+        model = os.path.join(ROOT, "particular_gb300", "data", "mlp_bulge_disk.npz")
         if self.fixed:
+            if self.fixed[1] & 4:  # the learned correction: the shipped model
+                from particular_gb300 import learned as LM
+                LM.load(res, model)
             row = measure(*self.fixed)
             self.table, self.plain, self.learned_row, self.selected = [row], None, None, row
             self.theta, self.flags, self.alpha, self.ratio = self.fixed
@@ -371,7 +378,6 @@ class BarnesHutWorkload:
         # the learned correction at theta 1.0 (model trained by `python -m
         # particular_gb300.learned`, shipped in particular_gb300/data)
         self.learned_row = None
-        model = os.path.join(ROOT, "particular_gb300", "data", "mlp_bulge_disk.npz")
         if os.path.exists(model):
             from particular_gb300 import learned as LM
             meta = LM.load(res, model)
@@ -1038,17 +1044,40 @@ def make_workload(args):
 
 
 # --------------------------------------------------------------------------- secondary rows
-def secondary_rows(res, torch, stream, flush, sm_mhz):
+def secondary_rows(res, torch, stream, flush, sm_mhz, cpu=True):
     """The other configurations' numbers, measured in the same run as the headline
     (one GPU, device-resident inputs, L2 flushed between timed calls, CUDA events on
-    the launching stream): the brute force at N = 131072 against the FP32 FMA peak,
-    the 10-step brute-force leapfrog (N = 131072), the 10-step Barnes-Hut leapfrog
-    at N = 1,048,576 for theta 0.3 / 0.5 / 0.8 (reference rule and the fast flags)
-    with first-evaluation errors, and the 4096-system ensemble (100 steps)."""
+    the launching stream): the brute force at N = 1024 (uniform cube, softening 1e-3)
+    and at N = 131072 against the FP32 FMA peak, with errors against the FP64 brute
+    force, the 10-step brute-force leapfrog (N = 131072), the 10-step Barnes-Hut
+    leapfrog at N = 1,048,576 for theta 0.3 / 0.5 / 0.8 (reference rule and the fast
+    flags) with first-evaluation errors, and the 4096-system ensemble (100 steps).
+    With `cpu`, each row also carries `cpu_baseline`: the reference's CPU method
+    restated (the oracle: sequential::BruteForce for N = 1024, parallel::BruteForce and
+    parallel::BarnesHut otherwise) timed on the host cores on a bounded sample."""
     import ctypes
     from particular_gb300 import _native as N, ics
     L = N.lib()
     rows = {}
+    threads = 1
+    if cpu:
+        from oracle import build as obuild, oracle as O
+        obuild.build()
+        threads = O.max_threads()
+
+    def cpu_leg(fn, unit, cores=None):
+        if not cpu:
+            return {}
+        value, info = fn()
+        return {"cpu_baseline": {"value": value, "unit": unit, "cores": cores or threads, "kind": "port",
+                                 **info}}
+
+    def f64_ref(d_t, nt, d_s, ns, eps):
+        out = torch.empty((nt, 3), dtype=torch.float64, device="cuda")
+        N.check(L.pt_bf_accel_f64_device(res.handle, d_t.data_ptr(), nt, d_s.data_ptr(), ns, eps, 1,
+                                         out.data_ptr()))
+        torch.cuda.synchronize()
+        return out.cpu().numpy()
 
     def time_calls(fn, warm, k):
         for _ in range(warm):
@@ -1080,14 +1109,49 @@ def secondary_rows(res, torch, stream, flush, sm_mhz):
         return {"tflops": tflops, "frac_probe": tflops / peak.value, "frac_formula": tflops / formula,
                 "frac_formula_2070": tflops / formula_max}
 
-    # brute force, one evaluation
+    # brute force, N = 1024 uniform cube, softening 1e-3, one evaluation: the exact
+    # path (the reference's sequential f32 sum, bit for bit) and the fast path
+    n1, eps1 = 1024, 1e-3
+    c1 = ics.uniform_cube(n1)["bodies"]
+    d1 = torch.from_numpy(c1).cuda()
+    o1 = torch.empty((n1, 3), dtype=torch.float32, device="cuda")
+    r1 = f64_ref(d1, n1, d1, n1, eps1)
+    c1_rows = []
+    for flags, label in ((N.PT_BF_EXACT, "exact (the reference's f32 sum order)"),
+                         (0, "fast (f32x2, compensated)")):
+        def c1_call(flags=flags):
+            N.check(L.pt_bf_accel_f32_device(res.handle, d1.data_ptr(), n1, d1.data_ptr(), n1, eps1, 1, flags,
+                                             o1.data_ptr()))
+        ms, k = time_calls(c1_call, 5, 20)
+        c1_rows.append({"path": label, "flags": int(flags), "ms": ms, "timed_calls": k,
+                        "pairs_per_s": n1 * n1 / (ms * 1e-3),
+                        "error": err_stats(rel_err(o1.cpu().numpy(), r1))})
+
+    def c1_cpu():
+        reps = 20
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            O.bf_f32(c1, c1, eps1, True, threads=1)
+        t = (time.perf_counter() - t0) / reps
+        return n1 / t, {"ms": t * 1e3, "sample": f"full evaluation, mean of {reps}, one thread "
+                                                  "(sequential::BruteForce restated)"}
+    rows["bf_uniform_1024"] = {"n_bodies": n1, "softening": eps1, "ic": "uniform [-1,1]^3, masses [0.5,1.5]",
+                               "error_judge": "FP64 brute force, every body", "rows": c1_rows,
+                               **cpu_leg(c1_cpu, "bodies/s", cores=1)}
+    del d1, o1
+    # brute force, N = 131072 Plummer, one evaluation
     bf = BruteForceWorkload()
     bf.setup_gpu(res, torch, stream)
     ms, k = time_calls(bf.step_device, 3, 5)
+    bidx = torch.from_numpy(np.sort(np.random.default_rng(5).choice(bf.n, 2048, replace=False))).cuda()
+    bref = f64_ref(bf.d_b[bidx].contiguous(), 2048, bf.d_b, bf.n, bf.softening)
     rows[bf.name] = {"ms": ms, "timed_calls": k, "pairs_per_s": bf.n * bf.n / (ms * 1e-3),
                      "bodies_per_s": bf.n / (ms * 1e-3),
                      **fracs(20.0 * bf.n * bf.n / (ms * 1e-3) / 1e12),
-                     "algorithmic": "20 flop per pair interaction, N^2 pairs"}
+                     "algorithmic": "20 flop per pair interaction, N^2 pairs",
+                     "error": err_stats(rel_err(bf.d_out[bidx].cpu().numpy(), bref)),
+                     "error_judge": "FP64 brute force on 2048 seeded bodies",
+                     **cpu_leg(lambda: bf.cpu_reference(threads), "bodies/s")}
     del bf
     # brute-force leapfrog, 10 steps in one graph
     lf = LeapfrogWorkload()
@@ -1095,7 +1159,8 @@ def secondary_rows(res, torch, stream, flush, sm_mhz):
     ms, k = time_calls(lf.step_device, 2, 3)
     rows[lf.name] = {"ms_per_call": ms, "timed_calls": k, "leapfrog_steps_per_call": lf.steps_per_call,
                      "body_steps_per_s": lf.n * lf.steps_per_call / (ms * 1e-3),
-                     **fracs(20.0 * lf.n * lf.n * lf.steps_per_call / (ms * 1e-3) / 1e12)}
+                     **fracs(20.0 * lf.n * lf.n * lf.steps_per_call / (ms * 1e-3) / 1e12),
+                     **cpu_leg(lambda: lf.cpu_reference(threads), "body-steps/s")}
     del lf
     # Barnes-Hut leapfrog at N = 1M: 10 steps with a tree rebuild each, one graph
     n = 1048576
@@ -1130,9 +1195,32 @@ def secondary_rows(res, torch, stream, flush, sm_mhz):
             ms, k = time_calls(call, 1, 3)
             bh_rows.append({"theta": th, "flags": flags, "method": label, "ms_per_call": ms, "timed_calls": k,
                             "body_steps_per_s": n * 10 / (ms * 1e-3), "first_evaluation_error": e})
+    bh_cpu = {}
+    if cpu:
+        # parallel::BarnesHut restated: one sequential build, the walk of the 2048 judged
+        # bodies over all host threads (time scaled to N), per theta
+        jn = js.cpu().numpy()
+        t0 = time.perf_counter()
+        tree = O.Tree(d["bodies"])
+        t_build = time.perf_counter() - t0
+        cpu_rows = []
+        for th in (0.3, 0.5, 0.8):
+            t0 = time.perf_counter()
+            a = tree.walk(jn, th, 0.01, True, threads=threads)
+            t_walk = (time.perf_counter() - t0) * (n / 2048)
+            cpu_rows.append({"theta": th, "body_steps_per_s": n / (t_build + t_walk),
+                             "ms_per_step": (t_build + t_walk) * 1e3,
+                             "first_evaluation_error": err_stats(rel_err(a, ref))})
+        del tree
+        bh_cpu = {"cpu_baseline": {"kind": "port", "cores": threads, "unit": "body-steps/s",
+                                   "build_ms": t_build * 1e3, "rows": cpu_rows,
+                                   "sample": "sequential tree build over all bodies + walk of the 2048 "
+                                             "judged bodies, scaled to one leapfrog step (kick/drift cost "
+                                             "ignored)"}}
     rows["leapfrog_bh_bulge_disk_1048576"] = {
         "n_bodies": n, "leapfrog_steps_per_call": 10, "dt": 1e-3, "softening": 0.01,
-        "error_judge": "FP64 brute force on 2048 seeded bodies, first evaluation", "rows": bh_rows}
+        "error_judge": "FP64 brute force on 2048 seeded bodies, first evaluation", "rows": bh_rows,
+        **bh_cpu}
     del db, dv, da, b0, v0
     # ensemble: 4096 systems, 100 steps in one persistent launch replayed from a graph
     en = EnsembleWorkload()
@@ -1143,7 +1231,8 @@ def secondary_rows(res, torch, stream, flush, sm_mhz):
                      "systems": 4096, "n_bodies": int(en.n),
                      "body_steps_per_s": en.n * en.steps_per_call / (ms * 1e-3),
                      "autotuned_K_per_size_class": en.table, "autotuned_j_tile_per_size_class": en.tiles,
-                     **fracs(20.0 * en.pairs_per_step * evals / (ms * 1e-3) / 1e12)}
+                     **fracs(20.0 * en.pairs_per_step * evals / (ms * 1e-3) / 1e12),
+                     **cpu_leg(lambda: en.cpu_reference(threads), "body-steps/s")}
     del en
     torch.cuda.synchronize()
     return rows
@@ -1246,7 +1335,8 @@ def run_ours(args):
     roof = wl.roofline(res, step_ms)
     secondary = None
     if rank == 0 and isinstance(wl, BarnesHutWorkload) and not args.method and not args.no_secondary:
-        secondary = secondary_rows(res, torch, stream, flush, clk.get("sm_mhz"))
+        secondary = secondary_rows(res, torch, stream, flush, clk.get("sm_mhz"),
+                                   cpu=not args.no_cpu_baseline)
     if rank != 0:
         return 0
     line = {"metric": wl.metric, "value": value, "unit": wl.unit, "n_gpus": world,

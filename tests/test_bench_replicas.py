@@ -77,5 +77,7 @@ def test_method_and_bodies_options(monkeypatch):
     wl = bench.make_workload(bench.parse_args())
     assert wl.fixed == (0.5, 0, None, 0.1)
     for theta, flags, alpha, ratio in bench.BarnesHutWorkload.ladder:
-        assert (alpha is not None) == bool(flags & 16) and 0 < ratio <= 0.5 and 0 < theta <= 1.0
+        assert (alpha is not None) == bool(flags & 16) and 0 < ratio <= 0.5
+        # with the error-bound opening theta is only the geometric cap
+        assert 0 < theta <= (2.0 if flags & 16 else 1.0)
 
