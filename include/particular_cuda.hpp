@@ -354,6 +354,16 @@ struct CudaTree {
     }
 };
 
+// A tree the caller built: the reference's RootedOrthtree over GravitationalField<Vec3,
+// f32> (tree/mod.rs:13-60) flattened per node, as pt_bh_load_tree takes it.
+struct OrthtreeNodes {
+    std::vector<uint8_t> internal;  // 1 = Node::Internal, 0 = Node::External
+    std::vector<int32_t> orthant;   // 8 per node: child NodeID, -1 for None
+    std::vector<float> bbox;        // 6 per node: min x, y, z then max x, y, z
+    std::vector<float> data;        // 4 per node: centre of mass x, y, z, mass
+    int32_t root = 0;               // RootedOrthtree::root(), -1 for None
+};
+
 template <class S, class T>
 struct BarnesHut {
     S theta;
@@ -361,6 +371,20 @@ struct BarnesHut {
     T interaction;
     uint32_t flags = 0;  // PT_BH_QUADRUPOLE | PT_BH_GROUP | PT_BH_LOCAL | PT_BH_RELATIVE
     float alpha = 0.f;   // PT_BH_RELATIVE: the error-bound factor (0: the resources' current one)
+    float local_ratio = 0.f;  // PT_BH_LOCAL: group radius / distance of far nodes (0: current one)
+    float monopole = -1.f;    // PT_BH_RELATIVE: monopole-only factor in [0, 1] (< 0: current one)
+
+    // Makes a tree the caller built the resources' current tree (monopoles: walk it
+    // with flags 0 or PT_BH_GROUP).
+    CudaTree load_tree(const OrthtreeNodes &t) {
+        const size_t n = t.internal.size();
+        if (t.orthant.size() != 8 * n || t.bbox.size() != 6 * n || t.data.size() != 4 * n)
+            throw Error(PT_ERR_INVALID, "particular cuda: OrthtreeNodes arrays of unequal node counts");
+        CudaTree tr{&resources, n, 0};
+        check(pt_bh_load_tree(resources.get(), t.orthant.data(), t.bbox.data(), t.internal.data(), t.data.data(), n,
+                              t.root, &tr.generation));
+        return tr;
+    }
 
     // Builds the tree over the affecting particles of `storage` once.
     template <class Storage>
@@ -413,6 +437,9 @@ struct BarnesHut {
   private:
     void set_alpha() {
         if ((flags & PT_BH_RELATIVE) && alpha > 0.f) check(pt_bh_set_relative_alpha(resources.get(), alpha));
+        if ((flags & PT_BH_RELATIVE) && monopole >= 0.f)
+            check(pt_bh_set_relative_monopole(resources.get(), monopole));
+        if ((flags & PT_BH_LOCAL) && local_ratio > 0.f) check(pt_bh_set_local_ratio(resources.get(), local_ratio));
     }
 
     template <class P1, class P2>

@@ -110,7 +110,17 @@ __device__ __forceinline__ void lane_walk(float4 p, bool valid, int T, const flo
 // targets (so never less accurate than that rule), and appends accepted nodes to a
 // shared-memory interaction list. A full list is evaluated densely: every lane runs its target
 // against all entries, two entries per packed f32x2 instruction.
-constexpr int GW_WARPS = 4;
+// Warps (groups) per CTA of the group walk. A CTA's slot is held until its slowest
+// warp ends; with 2 warps per CTA the neighbouring groups' unequal work idles fewer
+// warp slots while 20 warps per SM stay resident. Measured at N = 4M (walk ms, 4 / 2 /
+// 1 warps per CTA): headline configuration 5.47 / 5.39 / 5.42, quadrupole + group at
+// theta 0.52 16.40 / 16.29 / 16.33, with the local expansion 12.43 / 12.17 / 11.88 (one
+// warp per CTA holds 19 warps per SM there: shared memory). Persistent warps taking
+// groups from a counter instead spilled (96 -> 116 bytes) and were slower (5.85 ms).
+#ifndef PT_GW_WARPS
+#define PT_GW_WARPS 2
+#endif
+constexpr int GW_WARPS = PT_GW_WARPS;
 
 
 // Interaction lists in structure-of-arrays form. Cells carry their quadrupole
@@ -472,10 +482,10 @@ constexpr int GW_TPL = PT_GW_TPL;
 constexpr int GW_GROUP = 32 * GW_TPL;
 constexpr int GW_SHIFT = GW_TPL == 1 ? 5 : GW_TPL == 2 ? 6 : 7;
 static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
-// PT_BH_LOCAL walk: CTAs per SM and list capacities. Both registers (96) and shared
-// memory (44 KB) hold it at 5 CTAs per SM; 6 CTAs with lists of 64 cells and 96
-// bodies (80 registers, 84 bytes spilled, 37 KB) measured 6.9 ms against 6.1 ms at
-// N = 4M.
+// PT_BH_LOCAL walk: occupancy (counted in CTAs of 4 warps per SM, so 5 = 20 warps)
+// and list capacities. Both registers (96) and shared memory (11 KB per warp) hold it
+// at 20 warps per SM; 24 warps with lists of 64 cells and 96 bodies (80 registers, 84
+// bytes spilled) measured 6.9 ms against 6.1 ms at N = 4M.
 #ifndef PT_GW_LMINB
 #define PT_GW_LMINB 5
 #endif
@@ -493,10 +503,10 @@ static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
 constexpr int GW_FLAT = PT_GW_FLAT;
 static_assert(GW_FLAT >= 0 && GW_FLAT <= 31, "a flattened subtree is loaded by one warp");
 #ifndef PT_GW_MINB
-#define PT_GW_MINB (GW_TPL == 1 ? 6 : 5)  // CTAs per SM the register budget is set for
+#define PT_GW_MINB (GW_TPL == 1 ? 6 : 5)  // 4-warp CTAs per SM the register budget is set for
 #endif
 template <bool QUAD, bool GUARD, bool LEARNED, bool LOCAL, bool REL>
-__global__ void __launch_bounds__(32 * GW_WARPS, LOCAL ? PT_GW_LMINB : PT_GW_MINB)
+__global__ void __launch_bounds__(32 * GW_WARPS, (LOCAL ? PT_GW_LMINB : PT_GW_MINB) * 4 / GW_WARPS)
     bh_walk_group(const float4 *__restrict__ tbody, const uint32_t *__restrict__ tidx, int n_aff,
                   const float4 *__restrict__ nodeA, const int4 *__restrict__ nodeB, const float4 *__restrict__ nodeQ,
                   const float4 *__restrict__ nodeG, const float4 *__restrict__ sbody, const int *__restrict__ counters,

@@ -4,8 +4,8 @@
 // totals; the totals are scanned recursively and added back.
 // radix_sort_u64: 8-bit digits; per digit a histogram pass (per-tile counts), a row
 // scan (one block per digit value over the tiles) and a scatter pass. The scatter
-// ranks keys stably inside a 2048-key tile with warp match/popc and a per-digit
-// running offset, so equal digits keep their input order, stages the tile in shared
+// ranks keys stably inside a tile (each warp its own run of keys, with warp
+// match/popc), so equal digits keep their input order, stages the tile in shared
 // memory in digit order and writes every digit's run contiguously.
 #include "pt_prims.cuh"
 
@@ -76,7 +76,10 @@ __global__ void scan_total(uint32_t *__restrict__ out, int n, const uint32_t *__
 
 // ---- radix sort ------------------------------------------------------------
 constexpr int RS_THREADS = 256;
-constexpr int RS_ROUNDS = 8;
+#ifndef PT_RS_ROUNDS
+#define PT_RS_ROUNDS 8
+#endif
+constexpr int RS_ROUNDS = PT_RS_ROUNDS;  // keys per thread of a tile
 constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
 constexpr int RS_WARPS = RS_THREADS / 32;
 
@@ -139,67 +142,75 @@ __global__ void __launch_bounds__(RS_THREADS)
     if (threadIdx.x == 0) rowsum[d] = total;
 }
 
-// Ranks the tile's keys stably by digit (warp match/popc, per-digit running offsets),
-// stages them in shared memory in digit order, then writes each digit's run to its
-// global range: consecutive threads write consecutive addresses.
+// Ranks the tile's keys stably by digit, stages them in shared memory in digit order,
+// then writes each digit's run to its global range (consecutive threads write
+// consecutive addresses). Warp w owns the tile's w-th run of 32 * RS_ROUNDS keys and
+// ranks them round by round with warp match/popc against its own digit counters (no
+// block barrier between rounds); one scan over the warps per digit then orders the
+// warps, so equal digits keep their input order.
 __global__ void __launch_bounds__(RS_THREADS)
     rs_scatter(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin, uint64_t *__restrict__ kout,
-               uint32_t *__restrict__ vout, int n, int shift, const uint32_t *__restrict__ hist,
-               const uint32_t *__restrict__ offs, const uint32_t *__restrict__ rowsum, int nblocks) {
+               uint32_t *__restrict__ vout, int n, int shift, const uint32_t *__restrict__ offs,
+               const uint32_t *__restrict__ rowsum, int nblocks) {
     __shared__ uint64_t skeys[RS_TILE];
     __shared__ uint32_t svals[RS_TILE];
-    __shared__ uint32_t warp_cnt[RS_WARPS][256];
-    __shared__ uint32_t warp_off[RS_WARPS][256];
-    __shared__ uint32_t lrun[256], tstart[256], gbase[256];
+    __shared__ uint32_t wcnt[RS_WARPS][256];
+    __shared__ uint32_t tstart[256], gbase[256];
     __shared__ uint32_t wsum[RS_WARPS + 1];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int b = blockIdx.x;
     // digit t's global start for this tile: all smaller digits, then earlier tiles
     gbase[t] = block_excl_scan(rowsum[t], wsum, nullptr) + offs[size_t(t) * nblocks + b];
-    // digit t's start in this tile's staged (digit-ordered) copy
-    const uint32_t ts = block_excl_scan(hist[size_t(t) * nblocks + b], wsum, nullptr);
-    tstart[t] = ts;
-    lrun[t] = ts;
 #pragma unroll
-    for (int w = 0; w < RS_WARPS; ++w) warp_cnt[w][t] = 0;
+    for (int w = 0; w < RS_WARPS; ++w) wcnt[w][t] = 0;
     __syncthreads();
     const uint32_t lt = (1u << lane) - 1u;
-    const size_t base = size_t(b) * RS_TILE;
-    for (int r = 0; r < RS_ROUNDS; ++r) {
-        const size_t i = base + size_t(r) * RS_THREADS + t;
-        const bool valid = i < size_t(n);
-        const uint64_t key = valid ? kin[i] : 0ull;
-        const uint32_t val = valid ? vin[i] : 0u;
-        const uint32_t d = valid ? uint32_t((key >> shift) & 255u) : 256u;
-        const uint32_t peers = __match_any_sync(0xffffffffu, d);
-        const uint32_t rank = __popc(peers & lt);
-        if (valid && rank == 0) warp_cnt[warp][d] = __popc(peers);
-        __syncthreads();
-        {
-            uint32_t acc = lrun[t];
+    const size_t wbase = size_t(b) * RS_TILE + size_t(warp) * (32 * RS_ROUNDS);
+    uint64_t key[RS_ROUNDS];
+    uint32_t val[RS_ROUNDS], rank[RS_ROUNDS];
 #pragma unroll
-            for (int w = 0; w < RS_WARPS; ++w) {
-                const uint32_t c = warp_cnt[w][t];
-                warp_off[w][t] = acc;
-                warp_cnt[w][t] = 0;
-                acc += c;
-            }
-            lrun[t] = acc;
-        }
-        __syncthreads();
-        if (valid) {
-            const uint32_t pos = warp_off[warp][d] + rank;
-            skeys[pos] = key;
-            svals[pos] = val;
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const size_t i = wbase + size_t(r) * 32 + lane;
+        const bool valid = i < size_t(n);
+        key[r] = valid ? kin[i] : 0ull;
+        val[r] = valid ? vin[i] : 0u;
+        const uint32_t d = valid ? uint32_t((key[r] >> shift) & 255u) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        // keys of digit d in this warp's earlier rounds, then the lanes below
+        const uint32_t before = valid ? wcnt[warp][d] : 0u;
+        __syncwarp();
+        if (valid && (peers & lt) == 0u) wcnt[warp][d] = before + __popc(peers);
+        __syncwarp();
+        rank[r] = before + __popc(peers & lt);
+    }
+    __syncthreads();
+    // digit t: the warps' starts within the digit, then the digit's start in the tile
+    uint32_t tot = 0;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; ++w) {
+        const uint32_t c = wcnt[w][t];
+        wcnt[w][t] = tot;
+        tot += c;
+    }
+    tstart[t] = block_excl_scan(tot, wsum, nullptr);
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const size_t i = wbase + size_t(r) * 32 + lane;
+        if (i < size_t(n)) {
+            const uint32_t d = uint32_t((key[r] >> shift) & 255u);
+            const uint32_t pos = tstart[d] + wcnt[warp][d] + rank[r];
+            skeys[pos] = key[r];
+            svals[pos] = val[r];
         }
     }
     __syncthreads();
-    const int cnt = int(min(size_t(RS_TILE), size_t(n) - base));
+    const int cnt = int(min(size_t(RS_TILE), size_t(n) - size_t(b) * RS_TILE));
     for (int i = t; i < cnt; i += RS_THREADS) {
-        const uint64_t key = skeys[i];
-        const uint32_t d = uint32_t(key >> shift) & 255u;
+        const uint64_t k = skeys[i];
+        const uint32_t d = uint32_t(k >> shift) & 255u;
         const uint32_t pos = gbase[d] + (uint32_t(i) - tstart[d]);
-        kout[pos] = key;
+        kout[pos] = k;
         vout[pos] = svals[i];
     }
 }
@@ -270,7 +281,7 @@ int radix_sort_u64(pt_ctx *ctx, PrimScratch &s, uint64_t *keys, uint32_t *vals, 
         PT_TRY(check_launch(ctx, "rs_hist"));
         rs_rowscan<<<256, RS_THREADS, 0, st>>>(hist, offs, rowsum, nblocks);
         PT_TRY(check_launch(ctx, "rs_rowscan"));
-        rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, shift, hist, offs, rowsum, nblocks);
+        rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, shift, offs, rowsum, nblocks);
         PT_TRY(check_launch(ctx, "rs_scatter"));
         std::swap(ka, kb);
         std::swap(va, vb);

@@ -181,6 +181,65 @@ int main() {
     }
     std::printf("%-40s %s\n", "BarnesHut tree reuse (build once, walk)", reuse && refused ? "ok" : "FAIL");
     ok &= reuse && refused;
+
+    // a tree the caller built (a RootedOrthtree flattened per node): root [-4, 4]^3 with
+    // an internal child [-4, 0]^3 over two bodies and an external child. At theta 0 its
+    // walk sums the leaves (the brute force over them); a far target takes the root's
+    // monopole.
+    {
+        const std::vector<Body> lb = {{Vec3(-3.f, -1.f, -2.f), 2.f}, {Vec3(-1.f, -3.f, -0.5f), 1.f},
+                                      {Vec3(2.f, 3.f, 1.f), 4.f}};
+        cuda::OrthtreeNodes t;
+        t.internal = {1, 1, 0, 0, 0};
+        t.orthant.assign(40, -1);
+        t.bbox.assign(30, 0.f);
+        t.data.assign(20, 0.f);
+        for (int c = 0; c < 3; ++c) {
+            t.bbox[c] = -4.f, t.bbox[3 + c] = 4.f;      // node 0
+            t.bbox[6 + c] = -4.f, t.bbox[9 + c] = 0.f;  // node 1
+        }
+        t.orthant[0] = 1, t.orthant[7] = 4;
+        t.orthant[8 + 0] = 2, t.orthant[8 + 3] = 3;
+        auto put = [&](int k, std::initializer_list<int> members) {
+            double m = 0, x = 0, y = 0, z = 0;
+            for (int i : members) {
+                m += lb[i].mu;
+                x += double(lb[i].mu) * lb[i].position.x;
+                y += double(lb[i].mu) * lb[i].position.y;
+                z += double(lb[i].mu) * lb[i].position.z;
+            }
+            t.data[4 * k] = float(x / m), t.data[4 * k + 1] = float(y / m), t.data[4 * k + 2] = float(z / m);
+            t.data[4 * k + 3] = float(m);
+        };
+        put(0, {0, 1, 2});
+        put(1, {0, 1});
+        put(2, {0});
+        put(3, {1});
+        put(4, {2});
+        const std::vector<Body> targets = {{Vec3(0.5f, 0.25f, -1.f), 0.f}, {Vec3(-2.f, 2.f, 3.f), 0.f},
+                                           {Vec3(100.f, 50.f, -30.f), 0.f}};
+        cuda::BarnesHut<float, AccelerationSoftened<float, true>> bh0{0.f, res, softened_checked(0.01f)};
+        const cuda::CudaTree ut = bh0.load_tree(t);
+        const auto u0 = bh0.compute(between(Slice<Body>(targets), ut));
+        const auto d0 = cuda::BruteForce<AccelerationSoftened<float, true>>{res, softened_checked(0.01f)}.compute(
+            between(Slice<Body>(targets), Slice<Body>(lb)));
+        bool user = u0.size() == 3 && d0.size() == 3;
+        for (size_t i = 0; user && i < 3; ++i) {
+            const float s = std::fabs(d0[i].x) + std::fabs(d0[i].y) + std::fabs(d0[i].z);
+            user = std::fabs(u0[i].x - d0[i].x) + std::fabs(u0[i].y - d0[i].y) + std::fabs(u0[i].z - d0[i].z) <=
+                   1e-6f * s;
+        }
+        cuda::BarnesHut<float, AccelerationSoftened<float, true>> bh1{1.f, res, softened_checked(0.01f)};
+        const cuda::CudaTree ut1 = bh1.load_tree(t);
+        const auto u1 = bh1.compute(between(Slice<Body>(targets), ut1));
+        const double dx = t.data[0] - 100.0, dy = t.data[1] - 50.0, dz = t.data[2] + 30.0;
+        const double r2 = dx * dx + dy * dy + dz * dz + 1e-4, q = t.data[3] / (r2 * std::sqrt(r2));
+        user = user && u1.size() == 3 && std::fabs(u1[2].x - dx * q) <= 1e-5 * std::fabs(dx * q) &&
+               std::fabs(u1[2].y - dy * q) <= 1e-5 * std::fabs(dy * q) &&
+               std::fabs(u1[2].z - dz * q) <= 1e-5 * std::fabs(dz * q);
+        std::printf("%-40s %s\n", "BarnesHut over a caller-built tree", user ? "ok" : "FAIL");
+        ok &= user;
+    }
     std::printf("%s\n", ok ? "ALL OK" : "SOME FAILED");
     return ok ? 0 : 1;
 }
