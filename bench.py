@@ -1186,6 +1186,10 @@ def secondary_rows(res, torch, stream, flush, sm_mhz, cpu=True):
                                              da.data_ptr()))
             torch.cuda.synchronize()
             e = err_stats(rel_err(da[jidx].cpu().numpy(), ref))
+            st = N.BhStats()
+            N.check(L.pt_bh_last_stats(res.handle, ctypes.byref(st)))
+            e["interactions_per_body"] = st.interactions / n
+            e["fallback_warps"] = int(st.overflow)
             db.copy_(b0)
             dv.copy_(v0)
 

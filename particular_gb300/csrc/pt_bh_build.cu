@@ -423,19 +423,26 @@ __device__ void cell(int pv, const Kids &K, const float4 *__restrict__ nodeG, Re
     float mh = 0.f, ml = 0.f, px = 0.f, py = 0.f, pz = 0.f;
     float sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
     int count = 0;
+    // Straight-line over the 8 slots (no early exit): every slot's address is valid (an
+    // empty slot names the first child), so all the children's loads can be in flight at
+    // once; the sums still run slot by slot.
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        if (i >= K.n) break;
-        const int c = K.e[i] >> 1;
-        const float4 a = ld_cg(nodeA + c);
-        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), s0 = lo, s1 = lo;
+        const bool v = i < K.n;
+        const int ke = v ? K.e[i] : K.e[0];
+        const int c = ke >> 1;
+        const bool has_rec = v && !(ke & 1);
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 a = v ? ld_cg(nodeA + c) : zero;
+        float4 lo = zero, s0 = zero, s1 = zero;
         int cn = 1;
-        if (!(K.e[i] & 1)) {
+        if (has_rec) {
             lo = ld_cg(&rec[c].lo);
             s0 = ld_cg(&rec[c].s0);
             s1 = ld_cg(&rec[c].s1);
             cn = __float_as_int(s1.z);
         }
+        if (!v) continue;
         const float dx = __fsub_rn(a.x, g.x) + lo.x, dy = __fsub_rn(a.y, g.y) + lo.y, dz = __fsub_rn(a.z, g.z) + lo.z;
         float e;
         mh = two_sum(mh, a.w, e);

@@ -111,14 +111,15 @@ __device__ __forceinline__ void lane_walk(float4 p, bool valid, int T, const flo
 // shared-memory interaction list. A full list is evaluated densely: every lane runs its target
 // against all entries, two entries per packed f32x2 instruction.
 // Warps (groups) per CTA of the group walk. A CTA's slot is held until its slowest
-// warp ends; with 2 warps per CTA the neighbouring groups' unequal work idles fewer
-// warp slots while 20 warps per SM stay resident. Measured at N = 4M (walk ms, 4 / 2 /
-// 1 warps per CTA): headline configuration 5.47 / 5.39 / 5.42, quadrupole + group at
-// theta 0.52 16.40 / 16.29 / 16.33, with the local expansion 12.43 / 12.17 / 11.88 (one
-// warp per CTA holds 19 warps per SM there: shared memory). Persistent warps taking
+// warp ends, so with one warp per CTA no warp slot idles behind a neighbouring group's
+// longer walk; the local-expansion lists are sized (64 cells, 88 bodies) so that 20
+// one-warp CTAs fit an SM's shared memory. Measured at N = 4M (walk ms): headline
+// configuration 5.40 with 2 warps per CTA (72 / 96 entries) -> 5.25 with 1 (64 / 88);
+// quadrupole + group + local at theta 0.52 12.19 -> 11.74; quadrupole + group at theta
+// 0.52 16.30 -> 15.19 (4 warps per CTA: 5.47, 12.43, 16.40). Persistent warps taking
 // groups from a counter instead spilled (96 -> 116 bytes) and were slower (5.85 ms).
 #ifndef PT_GW_WARPS
-#define PT_GW_WARPS 2
+#define PT_GW_WARPS 1
 #endif
 constexpr int GW_WARPS = PT_GW_WARPS;
 
@@ -490,10 +491,10 @@ static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
 #define PT_GW_LMINB 5
 #endif
 #ifndef PT_GW_LCELLS
-#define PT_GW_LCELLS 72
+#define PT_GW_LCELLS 64
 #endif
 #ifndef PT_GW_LBODIES
-#define PT_GW_LBODIES 96
+#define PT_GW_LBODIES 88
 #endif
 // Opened cells with at most this many nodes below them are summed body by body at
 // once instead of being walked level by level (<= 31: one warp-wide load; 0 = off).
