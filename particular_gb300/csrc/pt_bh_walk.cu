@@ -1017,12 +1017,11 @@ __global__ void __launch_bounds__(32 * GW_WARPS, (LOCAL ? PT_GW_LMINB : PT_GW_MI
 // = 1.5 with monopoles; gscale[g] = 1 / (alpha |a|), the factor of the group walk's
 // error bound. (At N = 4M bulge+disk, estimates from theta 1.0 and 1.5 walks select
 // the same cells up to 0.2 %; 1.5 visits about half the nodes.)
-// The per-point cursor walk over the preorder nodes [first, end) (a subtree, or the
-// whole tree): the node index only grows, so the loop ends.
+// The per-point cursor walk: the node index only grows, so the loop ends.
 __device__ __forceinline__ void scale_cursor_walk(float cx, float cy, float cz, const float4 *__restrict__ nodeA,
-                                                  const int4 *__restrict__ nodeB, int first, int end, float eps2,
-                                                  float &ax, float &ay, float &az) {
-    for (int node = first; node < end;) {
+                                                  const int4 *__restrict__ nodeB, int T, float eps2, float &ax,
+                                                  float &ay, float &az) {
+    for (int node = 0; node < T;) {
         const float4 A = __ldg(nodeA + node);
         const int4 B = __ldg(nodeB + node);
         const float dx = A.x - cx, dy = A.y - cy, dz = A.z - cz;
@@ -1045,73 +1044,33 @@ __device__ __forceinline__ void scale_cursor_walk(float cx, float cy, float cz, 
     }
 }
 
-// Eight threads per group: the group's box from eight bodies each, then the root,
-// accepted whole (thread 0 adds it) or opened, in which case thread k walks the
-// subtree of the root's k-th child (the last thread also any later children) and the
-// eight partial sums are added. (One thread per group walking the whole tree took
-// 0.124 ms at N = 4M; one warp per group with a range stack made the walk phase slower,
-// 5.68 -> 5.85 ms: 65536 warps in several waves, each pop a round trip to L2.)
-constexpr int SCALE_SPLIT = 8;
+// One thread per group: the group's box, then the cursor walk from its centre. (One
+// warp per group walking with a range stack, one node per lane and pop, was slower at
+// N = 4M: the walk phase, which includes this kernel, went from 5.68 to 5.85 ms. Its
+// 65536 warps take several waves, each pop a round trip to L2, while the threads'
+// cursor walks mostly hit L1 in the tree's upper levels. Eight threads per group, each
+// walking one of the root's children's subtrees, took the same 0.124 ms: the group's
+// own octant holds most of the visits.)
 __global__ void __launch_bounds__(128)
     bh_group_scale(const float4 *__restrict__ tbody, int n_aff, const float4 *__restrict__ nodeA,
                    const int4 *__restrict__ nodeB, const int *__restrict__ counters, float eps2, float alpha,
                    float *__restrict__ gscale) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int g = t / SCALE_SPLIT, sub = t % SCALE_SPLIT;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int g0 = g * GW_GROUP;
-    const bool live = g0 < n_aff;  // the same for the eight threads of a group
-    float mn0 = INFINITY, mn1 = INFINITY, mn2 = INFINITY, mx0 = -INFINITY, mx1 = -INFINITY, mx2 = -INFINITY;
-    if (live) {
-        const int g1 = min(n_aff, g0 + GW_GROUP);
-        for (int i = g0 + sub; i < g1; i += SCALE_SPLIT) {
-            const float4 p = tbody[i];
-            mn0 = fminf(mn0, p.x), mn1 = fminf(mn1, p.y), mn2 = fminf(mn2, p.z);
-            mx0 = fmaxf(mx0, p.x), mx1 = fmaxf(mx1, p.y), mx2 = fmaxf(mx2, p.z);
-        }
-    }
-#pragma unroll
-    for (int o = 1; o < SCALE_SPLIT; o <<= 1) {
-        mn0 = fminf(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
-        mn1 = fminf(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
-        mn2 = fminf(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
-        mx0 = fmaxf(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
-        mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
-        mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
+    if (g0 >= n_aff) return;
+    const int g1 = min(n_aff, g0 + GW_GROUP);
+    float4 p = tbody[g0];
+    float mn0 = p.x, mn1 = p.y, mn2 = p.z, mx0 = p.x, mx1 = p.y, mx2 = p.z;
+    for (int t = g0 + 1; t < g1; ++t) {
+        p = tbody[t];
+        mn0 = fminf(mn0, p.x), mn1 = fminf(mn1, p.y), mn2 = fminf(mn2, p.z);
+        mx0 = fmaxf(mx0, p.x), mx1 = fmaxf(mx1, p.y), mx2 = fmaxf(mx2, p.z);
     }
     float ax = 0.f, ay = 0.f, az = 0.f;
-    const int T = counters[1];
-    if (live && T > 0) {
-        const float cx = 0.5f * (mn0 + mx0), cy = 0.5f * (mn1 + mx1), cz = 0.5f * (mn2 + mx2);
-        const float4 A = __ldg(nodeA);
-        const int4 B = __ldg(nodeB);
-        bool open = false;
-        if (B.z < 0) {
-            const float dx = A.x - cx, dy = A.y - cy, dz = A.z - cz;
-            const float w = __int_as_float(B.x);
-            open = 2.25f * fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < w * w;
-        }
-        if (!open) {
-            if (sub == 0) scale_cursor_walk(cx, cy, cz, nodeA, nodeB, 0, T, eps2, ax, ay, az);
-        } else {
-            // the root's children are node 1 and its chain of skip pointers, up to B.y
-            int c = 1;
-            for (int k = 0; k < sub && c < B.y; ++k) c = __ldg(nodeB + c).y;
-            if (c < B.y) {
-                const int e = sub == SCALE_SPLIT - 1 ? B.y : __ldg(nodeB + c).y;
-                scale_cursor_walk(cx, cy, cz, nodeA, nodeB, c, e, eps2, ax, ay, az);
-            }
-        }
-    }
-#pragma unroll
-    for (int o = 1; o < SCALE_SPLIT; o <<= 1) {
-        ax += __shfl_xor_sync(0xffffffffu, ax, o);
-        ay += __shfl_xor_sync(0xffffffffu, ay, o);
-        az += __shfl_xor_sync(0xffffffffu, az, o);
-    }
-    if (live && sub == 0) {
-        const float a = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
-        gscale[g] = 1.f / (alpha * fmaxf(a, 1e-30f));
-    }
+    scale_cursor_walk(0.5f * (mn0 + mx0), 0.5f * (mn1 + mx1), 0.5f * (mn2 + mx2), nodeA, nodeB, counters[1], eps2,
+                      ax, ay, az);
+    const float a = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+    gscale[g] = 1.f / (alpha * fmaxf(a, 1e-30f));
 }
 
 // ---- masked group walk: the reference's rule, per body, with shared traversal ----
@@ -1798,9 +1757,9 @@ int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n
         const float *gscale = nullptr;
         if (flags & PT_BH_RELATIVE) {
             PT_TRY(ensure_buf(ctx, S.gscale, sizeof(float) * size_t(groups)));
-            bh_group_scale<<<blocks(groups * SCALE_SPLIT, 128), 128, 0, st>>>(
-                tbody, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<int>(S.counters), eps2, S.rel_alpha,
-                as<float>(S.gscale));
+            bh_group_scale<<<blocks(groups, 128), 128, 0, st>>>(tbody, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB),
+                                                                as<int>(S.counters), eps2, S.rel_alpha,
+                                                                as<float>(S.gscale));
             PT_TRY(check_launch(ctx, "bh_group_scale"));
             gscale = as<float>(S.gscale);
         }
