@@ -266,7 +266,7 @@ class BarnesHutWorkload:
     bar = 1e-3
     # the calibration selects with a margin so that the bar holds on the held-out sample
     select_bar = 0.9e-3
-    # (theta, flags, alpha, local ratio) candidates: quadrupole + group opening; the
+    # (theta, flags, alpha, local ratio[, monopole factor]) candidates: quadrupole + group opening; the
     # reference's own monopole per-body walk at theta 0.5 is measured alongside as
     # "plain". flags: 1 quadrupole, 2 group, 8 local expansion of far nodes (group
     # radius < ratio x distance), 16 error-bound opening (alpha; theta is then the
@@ -282,7 +282,10 @@ class BarnesHutWorkload:
               (1.0, 27, 3.5e-3, 0.1), (1.0, 27, 4e-3, 0.1), (1.0, 27, 3e-3, 0.14), (1.0, 27, 3.25e-3, 0.14),
               # looser geometric caps: the error bound decides more of the openings
               (1.2, 27, 2.75e-3, 0.1), (1.5, 27, 2.5e-3, 0.1), (1.5, 27, 2.75e-3, 0.1), (1.5, 27, 3e-3, 0.1),
-              (1.5, 27, 2.5e-3, 0.12), (1.5, 27, 2.75e-3, 0.12), (2.0, 27, 2.75e-3, 0.1)]
+              (1.5, 27, 2.5e-3, 0.12), (1.5, 27, 2.75e-3, 0.12), (2.0, 27, 2.75e-3, 0.1),
+              (2.0, 27, 2.85e-3, 0.1), (2.0, 27, 2.75e-3, 0.11), (2.0, 27, 2.6e-3, 0.12), (2.0, 27, 2.5e-3, 0.13),
+              # a fifth entry: the monopole-only factor (else `mono`)
+              (2.0, 27, 2.75e-3, 0.1, 0.1), (2.0, 27, 2.6e-3, 0.1, 0.2), (2.0, 27, 2.75e-3, 0.1, 0.2)]
 
     def __init__(self, n=4194304, softening=0.01, sample=2048, holdout=4096):
         from particular_gb300 import ics
@@ -388,12 +391,16 @@ class BarnesHutWorkload:
             self.learned_row = row
             self.plain_theta1 = measure(1.0, 3)
         ok = []
-        for theta, flags, alpha, ratio in self.ladder:
+        default_mono = self.mono
+        for entry in self.ladder:
+            theta, flags, alpha, ratio = entry[:4]
+            self.mono = entry[4] if len(entry) > 4 else default_mono
             row = measure(theta, flags, alpha, ratio)
             self.table.append(row)
             if row["p95"] <= self.select_bar:
                 ok.append(row)
         best = max(ok, key=lambda r: r["bodies_per_s"]) if ok else min(self.table, key=lambda r: r["p95"])
+        self.mono = best.get("monopole_factor") or default_mono
         self.theta = best["theta"]
         self.alpha = best.get("relative")
         self.ratio = best.get("local_ratio") or 0.1

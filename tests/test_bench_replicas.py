@@ -76,7 +76,9 @@ def test_method_and_bodies_options(monkeypatch):
     monkeypatch.setattr(sys, "argv", ["bench.py", "--bodies", "2048", "--method", "0.5,0"])
     wl = bench.make_workload(bench.parse_args())
     assert wl.fixed == (0.5, 0, None, 0.1)
-    for theta, flags, alpha, ratio in bench.BarnesHutWorkload.ladder:
+    for entry in bench.BarnesHutWorkload.ladder:
+        theta, flags, alpha, ratio = entry[:4]
+        assert len(entry) == 4 or (len(entry) == 5 and 0.0 <= entry[4] <= 1.0 and (flags & 17) == 17)
         assert (alpha is not None) == bool(flags & 16) and 0 < ratio <= 0.5
         # with the error-bound opening theta is only the geometric cap
         assert 0 < theta <= (2.0 if flags & 16 else 1.0)
