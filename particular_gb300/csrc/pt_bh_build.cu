@@ -637,8 +637,8 @@ __global__ void layout(int *counters, const int *__restrict__ bfirst,
         const int f = int(ufirst[k]);
         const int nb = int(ufirst[k + 1]) - f;
         nodeB[pk] = make_int4(0, pk + 1, f, nb);
-        nodeG[pk] = P::make(T(0), T(0), T(0), T(0));
-        nodeR[pk] = make_int2(f, int(ufirst[k + 1]));
+        // (no nodeG / nodeR for leaves: the cell centre and body range are read for
+        // cells only, by the f64 walk's widths and the learned features and samples)
         const int op = loparent[k];
         if (op >= 0) kid[8 * op + lslot[k]] = 2 * pk + (nb == 1 ? 1 : 0);
         leaf(pk, f, f + nb, sbody, rec, nodeA, nodeQ);  // the leaf's moment record
