@@ -154,7 +154,7 @@ __device__ __forceinline__ void csum_fold(CSum &a, f2 tx, f2 ty, f2 tz) {
 
 // Where a warp keeps its bodies' compensated sums: in registers, or, in the kernel
 // whose registers the traversal state fills (the quadrupole group walk with local
-// expansions, 96 registers for 5 CTAs per SM: 56 bytes spilled, walk +15 %), in shared
+// expansions, 96 registers for 20 warps per SM: 56 bytes spilled, walk +15 %), in shared
 // memory as [value][lane] (conflict-free; touched once per evaluated chunk; walk +2.5 %
 // over plain FP32 sums). Measured at N = 4M: the other group walks +1.2 % in registers
 // (+2.7 % in shared memory), the masked walk +1.6 %.
@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, (LOCAL ? PT_GW_LMINB : PT_GW_MI
     // PT_BH_LOCAL keeps its 19 expansion coefficients per lane in shared memory
     // ([coefficient][lane]: no bank conflicts) and queues far nodes (up to 63) so that
     // they are expanded 32 at a time, one per lane, instead of by the few lanes that
-    // popped them; the stack is trimmed to 288 ranges so that 5 CTAs stay resident.
+    // popped them; the stack is trimmed to 288 ranges so that 20 warps stay resident per SM.
     constexpr int STK = LOCAL ? 288 : GW_STACK;
     stack_cap = min(stack_cap, STK);
     __shared__ int2 s_stack[GW_WARPS][STK];
