@@ -1223,18 +1223,40 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
     bool failed = false;
     while (S > 0) {
         const int k = min(min(32, S), max(1, (MW_STACK - S) / 2));
-        const bool have = lane < k;
-        const int4 r = have ? stack[S - 1 - lane] : make_int4(0, 0, 0, 0);
+        const bool first = lane < k;
+        int4 r = first ? stack[S - 1 - lane] : make_int4(0, 0, 0, 0);
         __syncwarp();
         S -= k;
-        const int node = r.x;
-        const unsigned mk0 = unsigned(r.z), mk1 = unsigned(r.w);
+        int node = r.x;
         float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
         int4 B = make_int4(0, 0, 0, 0);
-        if (have) {
+        if (first) {
             A = __ldg(nodeA + node);
             B = __ldg(nodeB + node);
         }
+        // A pop of fewer than 32 ranges leaves lanes idle: lane k + i then also takes
+        // the second node of range i (its first node's skip pointer) with the range's
+        // masks, and the rest of the range passes to it. Each range still pushes at
+        // most three ranges, within the room k was sized for (2 per popped range).
+        bool second = false;
+        if (k < 32) {
+            const int src = lane >= k ? lane - k : lane;
+            const int nxt = __shfl_sync(0xffffffffu, B.y, src);
+            const int end = __shfl_sync(0xffffffffu, r.y, src);
+            const int m0 = __shfl_sync(0xffffffffu, r.z, src), m1 = __shfl_sync(0xffffffffu, r.w, src);
+            if (lane >= k && src < k && nxt < end) {
+                second = true;
+                node = nxt;
+                r = make_int4(nxt, end, m0, m1);
+                A = __ldg(nodeA + node);
+                B = __ldg(nodeB + node);
+            }
+        }
+        const unsigned msecond = __ballot_sync(0xffffffffu, second);
+        // its rest went to lane + k
+        const bool handed = first && lane + k < 32 && ((msecond >> (lane + k)) & 1u);
+        const bool have = first || second;
+        const unsigned mk0 = unsigned(r.z), mk1 = unsigned(r.w);
         visit_pairs += __popc(mk0) + __popc(mk1);
         // Per node: which of its bodies open it and which accept it. The bodies' box
         // settles most nodes; a node whose centre of mass lies inside the box (a body
@@ -1296,7 +1318,7 @@ __global__ void __launch_bounds__(32 * MW_WARPS)
             }
         }
         // push: later siblings share the parent's masks; children get the opening bodies
-        const bool rest = have && (mk0 | mk1) && B.y < r.y;
+        const bool rest = have && !handed && (mk0 | mk1) && B.y < r.y;
         const bool opn = (op0 | op1) != 0u;
         const unsigned mrest = __ballot_sync(0xffffffffu, rest), mopen = __ballot_sync(0xffffffffu, opn);
         const int total = __popc(mrest) + __popc(mopen);
