@@ -496,6 +496,11 @@ static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
 #ifndef PT_GW_LBODIES
 #define PT_GW_LBODIES 88
 #endif
+// Stack ranges per warp of the PT_BH_LOCAL walk. (21 warps per SM, with lists of 56
+// cells / 80 bodies and 272 ranges, measured the same as 20: 5.21 against 5.20 ms.)
+#ifndef PT_GW_LSTACK
+#define PT_GW_LSTACK 288
+#endif
 // Opened cells with at most this many nodes below them are summed body by body at
 // once instead of being walked level by level (<= 31: one warp-wide load; 0 = off).
 #ifndef PT_GW_FLAT
@@ -524,7 +529,7 @@ __global__ void __launch_bounds__(32 * GW_WARPS, (LOCAL ? PT_GW_LMINB : PT_GW_MI
     // ([coefficient][lane]: no bank conflicts) and queues far nodes (up to 63) so that
     // they are expanded 32 at a time, one per lane, instead of by the few lanes that
     // popped them; the stack is trimmed to 288 ranges so that 20 warps stay resident per SM.
-    constexpr int STK = LOCAL ? 288 : GW_STACK;
+    constexpr int STK = LOCAL ? PT_GW_LSTACK : GW_STACK;
     stack_cap = min(stack_cap, STK);
     __shared__ int2 s_stack[GW_WARPS][STK];
     __shared__ __align__(16) CellList s_cells[GW_WARPS];
