@@ -1049,118 +1049,35 @@ __device__ __forceinline__ void scale_cursor_walk(float cx, float cy, float cz, 
     }
 }
 
-// Four lanes per group: the group's box from 16 bodies each, then a walk in which the
-// four lanes pop up to four sibling ranges of the group's shared-memory stack per step
-// (one node each, as the group walk does with 32), so the chain of dependent node
-// loads is about a quarter of a one-thread cursor walk's (one thread per group:
-// 0.115 ms at N = 1M and 0.124 ms at 4M, set by that chain, not by the number of
-// groups; one warp per group walking with a range stack made the walk phase slower,
-// 5.68 -> 5.85 ms at 4M; eight threads walking the root's eight subtrees took the same
-// time as one: the group's own octant holds most of the visits). A group whose stack
-// would overflow redoes its estimate with the one-thread cursor walk.
-constexpr int GS_LANES = 4;
-constexpr int GS_STACK = 96;  // sibling ranges per group
+// One thread per group: the group's box, then the cursor walk from its centre. (One
+// warp per group walking with a range stack, one node per lane and pop, was slower at
+// N = 4M: the walk phase, which includes this kernel, went from 5.68 to 5.85 ms. Its
+// 65536 warps take several waves, each pop a round trip to L2, while the threads'
+// cursor walks mostly hit L1 in the tree's upper levels. Eight threads per group, each
+// walking one of the root's children's subtrees, took the same 0.124 ms: the group's
+// own octant holds most of the visits. Four lanes per group popping up to four ranges
+// of a shared-memory stack per step took 0.18 ms: a walk from one point keeps few
+// ranges open, so the steps stayed nearly as many and each cost more.)
 __global__ void __launch_bounds__(128)
     bh_group_scale(const float4 *__restrict__ tbody, int n_aff, const float4 *__restrict__ nodeA,
                    const int4 *__restrict__ nodeB, const int *__restrict__ counters, float eps2, float alpha,
                    float *__restrict__ gscale) {
-    __shared__ int2 s_stack[128 / GS_LANES][GS_STACK];
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int g = t / GS_LANES, j = t % GS_LANES;
-    int2 *stack = s_stack[threadIdx.x / GS_LANES];
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int g0 = g * GW_GROUP;
-    const bool live = g0 < n_aff;  // the same for the group's four lanes
-    float mn0 = INFINITY, mn1 = INFINITY, mn2 = INFINITY, mx0 = -INFINITY, mx1 = -INFINITY, mx2 = -INFINITY;
-    if (live) {
-        const int g1 = min(n_aff, g0 + GW_GROUP);
-        for (int i = g0 + j; i < g1; i += GS_LANES) {
-            const float4 p = tbody[i];
-            mn0 = fminf(mn0, p.x), mn1 = fminf(mn1, p.y), mn2 = fminf(mn2, p.z);
-            mx0 = fmaxf(mx0, p.x), mx1 = fmaxf(mx1, p.y), mx2 = fmaxf(mx2, p.z);
-        }
+    if (g0 >= n_aff) return;
+    const int g1 = min(n_aff, g0 + GW_GROUP);
+    float4 p = tbody[g0];
+    float mn0 = p.x, mn1 = p.y, mn2 = p.z, mx0 = p.x, mx1 = p.y, mx2 = p.z;
+    for (int t = g0 + 1; t < g1; ++t) {
+        p = tbody[t];
+        mn0 = fminf(mn0, p.x), mn1 = fminf(mn1, p.y), mn2 = fminf(mn2, p.z);
+        mx0 = fmaxf(mx0, p.x), mx1 = fmaxf(mx1, p.y), mx2 = fmaxf(mx2, p.z);
     }
-#pragma unroll
-    for (int o = 1; o < GS_LANES; o <<= 1) {
-        mn0 = fminf(mn0, __shfl_xor_sync(0xffffffffu, mn0, o));
-        mn1 = fminf(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
-        mn2 = fminf(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
-        mx0 = fmaxf(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
-        mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
-        mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
-    }
-    const float cx = 0.5f * (mn0 + mx0), cy = 0.5f * (mn1 + mx1), cz = 0.5f * (mn2 + mx2);
-    const int T = counters[1];
     float ax = 0.f, ay = 0.f, az = 0.f;
-    int S = 0;  // the group's stack size, the same in its four lanes
-    if (live && T > 0) {
-        if (j == 0) stack[0] = make_int2(0, T);
-        S = 1;
-    }
-    __syncwarp();
-    bool failed = false;
-    // every lane takes part in every step (the shuffles stay within a group's lanes)
-    while (__any_sync(0xffffffffu, S > 0)) {
-        const int k = S > 0 ? min(min(GS_LANES, S), max(1, (GS_STACK - S) / 2)) : 0;
-        const bool have = j < k;
-        const int2 r = have ? stack[S - 1 - j] : make_int2(0, 0);
-        __syncwarp();
-        S -= k;
-        bool open = false, rest = false;
-        int nxt = 0;
-        if (have) {
-            const float4 A = __ldg(nodeA + r.x);
-            const int4 B = __ldg(nodeB + r.x);
-            const float dx = A.x - cx, dy = A.y - cy, dz = A.z - cz;
-            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (B.z < 0) {
-                const float w = __int_as_float(B.x);
-                open = 2.25f * d2 < w * w;  // theta = 1.5
-            }
-            if (!open && d2 > 0.f) {
-                const float inv = rsqrt_ftz(d2 + eps2);
-                const float sc = (A.w * inv) * (inv * inv);
-                ax = fmaf(dx, sc, ax);
-                ay = fmaf(dy, sc, ay);
-                az = fmaf(dz, sc, az);
-            }
-            nxt = B.y;
-            rest = nxt < r.y;  // later siblings remain
-        }
-        // pushes of the lanes below this one in the group: an exclusive prefix sum
-        const int np = int(rest) + int(open);
-        int pre = np;
-#pragma unroll
-        for (int o = 1; o < GS_LANES; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, pre, o, GS_LANES);
-            if (j >= o) pre += v;
-        }
-        const int total = __shfl_sync(0xffffffffu, pre, GS_LANES - 1, GS_LANES);
-        pre -= np;
-        if (S + total > GS_STACK) {  // never written out of bounds: redo it below
-            failed = true;
-            S = 0;
-        } else {
-            int sl = S + pre;
-            if (rest) stack[sl++] = make_int2(nxt, r.y);
-            if (open) stack[sl++] = make_int2(r.x + 1, nxt);  // children on top: popped first
-            S += total;
-        }
-        __syncwarp();
-    }
-#pragma unroll
-    for (int o = 1; o < GS_LANES; o <<= 1) {
-        ax += __shfl_xor_sync(0xffffffffu, ax, o);
-        ay += __shfl_xor_sync(0xffffffffu, ay, o);
-        az += __shfl_xor_sync(0xffffffffu, az, o);
-    }
-    if (live && j == 0) {
-        if (failed) {
-            ax = ay = az = 0.f;
-            scale_cursor_walk(cx, cy, cz, nodeA, nodeB, T, eps2, ax, ay, az);
-        }
-        const float a = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
-        gscale[g] = 1.f / (alpha * fmaxf(a, 1e-30f));
-    }
+    scale_cursor_walk(0.5f * (mn0 + mx0), 0.5f * (mn1 + mx1), 0.5f * (mn2 + mx2), nodeA, nodeB, counters[1], eps2,
+                      ax, ay, az);
+    const float a = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+    gscale[g] = 1.f / (alpha * fmaxf(a, 1e-30f));
 }
 
 // ---- masked group walk: the reference's rule, per body, with shared traversal ----
@@ -1869,9 +1786,9 @@ int walk(pt_ctx *ctx, State &S, const float4 *tbody, const uint32_t *tidx, int n
         const float *gscale = nullptr;
         if (flags & PT_BH_RELATIVE) {
             PT_TRY(ensure_buf(ctx, S.gscale, sizeof(float) * size_t(groups)));
-            bh_group_scale<<<blocks(groups * GS_LANES, 128), 128, 0, st>>>(
-                tbody, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB), as<int>(S.counters), eps2, S.rel_alpha,
-                as<float>(S.gscale));
+            bh_group_scale<<<blocks(groups, 128), 128, 0, st>>>(tbody, n_aff, as<float4>(S.nodeA), as<int4>(S.nodeB),
+                                                                as<int>(S.counters), eps2, S.rel_alpha,
+                                                                as<float>(S.gscale));
             PT_TRY(check_launch(ctx, "bh_group_scale"));
             gscale = as<float>(S.gscale);
         }
