@@ -153,3 +153,39 @@ def test_relative_flag_validation(res):
         with pytest.raises(N.CudaError):
             N.check(L.pt_bh_set_relative_monopole(res.handle, bad))
     N.check(L.pt_bh_set_relative_monopole(res.handle, 0.1))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 63, 64, 65, 129])
+def test_headline_configuration_edge_sizes(res, oracle, n):
+    """The headline configuration (quadrupole + group + local expansion + error-bound
+    opening, theta cap 2.0) on sizes at and around the 64-body group boundary: a
+    single body feels nothing, and the rest stay within the bench's bar against the
+    FP64 brute force."""
+    b = ics.plummer(n, seed=70 + n)["bodies"] if n > 1 else np.array([[1, 2, 3, 4]], np.float32)
+    m = bh(res, 2.0, quadrupole=True, local=True, relative=2.75e-3, monopole=0.15)
+    got = m.compute(b)
+    assert got.shape == (n, 3) and np.isfinite(got).all()
+    if n == 1:
+        assert not got.any()
+        return
+    ref64 = oracle.bf_f64(b, b, 0.01, True)
+    e = rel(got, ref64)
+    assert np.percentile(e, 95) <= 1e-3 and e.max() < 1e-2
+
+
+def test_headline_configuration_degenerate_inputs(res, oracle):
+    """Coincident bodies (one bucket leaf), an all-massless set (|a| = 0 everywhere:
+    the estimate's floor keeps the opening radius finite and the result zero), no
+    sources, and no targets."""
+    m = bh(res, 2.0, quadrupole=True, local=True, relative=2.75e-3, monopole=0.15)
+    b = ics.uniform_cube(3000, 71)["bodies"]
+    same = np.concatenate([np.tile(np.array([[0.25, -0.5, 0.5, 1.0]], np.float32), (80, 1)), b])
+    got = m.compute(same)
+    assert np.isfinite(got).all()
+    ref64 = oracle.bf_f64(same, same, 0.01, True)
+    assert np.percentile(rel(got, ref64), 95) < 5e-3
+    massless = b.copy()
+    massless[:, 3] = 0.0
+    assert not m.compute(massless).any()
+    assert not m.compute(Between(b, np.zeros((0, 4), np.float32))).any()
+    assert m.compute(Between(np.zeros((0, 4), np.float32), b)).shape == (0, 3)
