@@ -83,3 +83,20 @@ def test_method_and_bodies_options(monkeypatch):
         # with the error-bound opening theta is only the geometric cap
         assert 0 < theta <= (2.0 if flags & 16 else 1.0)
 
+
+
+def test_reference_arm_small_case():
+    """`--impl reference` on a small Barnes-Hut case, on CPU: the restated
+    parallel::BarnesHut walks every target once over the K steps and prints the
+    contract's line (value, e2e with no copies, cpu_baseline describing the run)."""
+    import json
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--bodies", "4096",
+                        "--steps", "2", "--warmup", "1"], capture_output=True, text=True, timeout=600,
+                       env=dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0"))
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads([x for x in r.stdout.splitlines() if x.startswith("{")][-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "bodies/s"
+    assert line["e2e"]["value"] == line["value"] and line["e2e"]["h2d_bytes_per_step"] == 0
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
+    assert line["config"]["n_bodies"] == 4096
