@@ -84,3 +84,28 @@ def test_brute_force_pairs_semantics(res, oracle, ordered):
         assert np.abs(got - want32).max() < 1e-5 * scale, exact
     got64 = cuda.BruteForce(res, AccelerationSoftened(0.01), dvec3=True).compute(storage64)
     assert np.abs(got64 - want64).max() < 1e-12 * scale
+
+
+def test_in_order_fold_of_the_reference_doctest(res):
+    """The fold that particular's brute force documents (lib.rs:212-262: forces[i] is
+    the sum of the pair terms in j order from zero, the self term included as zero),
+    for that doctest's sun / earth / jupiter bodies (AU, solar masses, G = 4 pi^2)
+    with the acceleration interaction (unsoftened, checked) in double, each pair term
+    as gravity/impls/mod.rs:150-166 computes it: bit for bit."""
+    G = 4.0 * np.pi * np.pi
+    b = np.array([[0.0, 0.0, 0.0, 1.0 * G], [1.0, 0.0, 0.0, 3.0027e-6 * G], [5.2, 0.0, 0.0, 0.000954588 * G]],
+                 np.float64)
+    got = cuda.BruteForce(res, Acceleration.checked(), dvec3=True).compute(b)
+
+    def pair(i, j):
+        d = b[j, :3] - b[i, :3]
+        n = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]
+        if n == 0.0:
+            return d
+        return d * (b[j, 3] / (n * np.sqrt(n)))
+
+    for i in range(3):
+        acc = np.zeros(3)
+        for j in range(3):
+            acc = acc + pair(i, j)
+        assert np.array_equal(got[i], acc), (i, got[i], acc)
