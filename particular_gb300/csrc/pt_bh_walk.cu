@@ -1096,7 +1096,14 @@ __global__ void __launch_bounds__(128)
 #define PT_MW_WARPS 1
 #endif
 constexpr int MW_WARPS = PT_MW_WARPS;
-constexpr int MW_STACK = 384;
+// Stack ranges per warp of the masked walk: 320 fit 20 one-warp CTAs per SM in shared
+// memory (384: 18). Walk at N = 4M, 384 -> 320: theta 0.5 13.96 -> 13.81 ms, with
+// quadrupoles 22.51 -> 22.38, theta 0.3 39.40 -> 39.03 (12 of 65536 warps then run out
+// of stack and take the per-body cursor walk: the same accepted sets).
+#ifndef PT_MW_STACK
+#define PT_MW_STACK 320
+#endif
+constexpr int MW_STACK = PT_MW_STACK;
 constexpr int MW_TPL = 2;  // bodies per lane; mask word i covers bodies g0 + 32 i + lane
 
 // Entry pair (packed lo/hi) for one body, weighted by the body's bits of the two
