@@ -284,7 +284,9 @@ struct LearnedRecords {
 };
 
 // One warp per chunk (grid-stride): features of the 128 recorded cells at the group
-// centre, four 32-row tensor-core batches, the chunk's sum into part[chunk].
+// centre, four 32-row tensor-core batches, the chunk's sum into part[chunk]. (It holds
+// 2 CTAs per SM at ~242 registers; capped at 168 for 3 CTAs it spills 128 bytes and
+// the learned step at N = 4M went from 9.95 to 10.69 ms.)
 // Cells whose size/distance ratio at the group centre lies outside the range the
 // model was trained on ([lo, hi]) get no correction.
 __global__ void __launch_bounds__(128) bh_learned_eval(LearnedRecords L, const float4 *__restrict__ nodeA,
