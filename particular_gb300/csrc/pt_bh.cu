@@ -120,6 +120,9 @@ void pt_bh_state_free(pt_ctx *ctx) {
                      &S->lnext,    &S->lpart,  &S->lhead, &S->lcentre, &S->lused, &S->sbody64, &S->nodeA64,
                      &S->nodeG64,  &S->tbody64, &S->gscale};
     for (DevBuf *b : all) free_buf(ctx, *b);
+    if (S->fork) cudaEventDestroy(S->fork);
+    if (S->join) cudaEventDestroy(S->join);
+    if (S->aux) cudaStreamDestroy(S->aux);
     delete S;
     ctx->bh = nullptr;
 }

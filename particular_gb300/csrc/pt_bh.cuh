@@ -84,6 +84,10 @@ struct State {
     float theta_inner = 0.5f;
     int cap_n = 0;
     int last_n_src = 0;
+    // a second stream for build work that does not depend on the tree chain (the
+    // sorted bodies' gather), joined back before the layout
+    cudaStream_t aux = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 inline State *state(pt_ctx *ctx) {

@@ -739,8 +739,18 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     make_keys<T><<<blocks(n), 256, 0, st>>>(d_src, n, as<T>(S.box), as<uint64_t>(S.keys), as<uint32_t>(S.idx));
     PT_TRY(check_launch(ctx, "make_keys"));
     PT_TRY(radix_sort_u64(ctx, S.prims, as<uint64_t>(S.keys), as<uint32_t>(S.idx), n, 3 * LEVELS));
-    gather_bodies<V4><<<blocks(n), 256, 0, st>>>(d_src, as<uint32_t>(S.idx), n, as<V4>(sb));
+    // The bodies' gather into key order runs on a second stream beside the tree chain
+    // (unit flags .. octree links) and joins before the layout, its first reader.
+    if (!S.aux) {
+        PT_CUDA(cudaStreamCreateWithFlags(&S.aux, cudaStreamNonBlocking));
+        PT_CUDA(cudaEventCreateWithFlags(&S.fork, cudaEventDisableTiming));
+        PT_CUDA(cudaEventCreateWithFlags(&S.join, cudaEventDisableTiming));
+    }
+    PT_CUDA(cudaEventRecord(S.fork, st));
+    PT_CUDA(cudaStreamWaitEvent(S.aux, S.fork, 0));
+    gather_bodies<V4><<<blocks(n), 256, 0, S.aux>>>(d_src, as<uint32_t>(S.idx), n, as<V4>(sb));
     PT_TRY(check_launch(ctx, "gather_bodies"));
+    PT_CUDA(cudaEventRecord(S.join, S.aux));
     unit_flags<<<blocks(n), 256, 0, st>>>(as<uint64_t>(S.keys), n, as<uint32_t>(S.flags));
     PT_TRY(check_launch(ctx, "unit_flags"));
     PT_TRY(scan_u32(ctx, S.prims, as<uint32_t>(S.flags), as<uint32_t>(S.uscan), n));
@@ -765,6 +775,7 @@ int build_t(pt_ctx *ctx, State &S, const typename Prec<T>::V4 *d_src, int n) {
     level_offsets<<<1, 32, 0, st>>>(levels);
     PT_TRY(check_launch(ctx, "level_offsets"));
     PT_TRY(scan_u32(ctx, S.prims, as<uint32_t>(S.cnt), as<uint32_t>(S.pscan), n + 1));
+    PT_CUDA(cudaStreamWaitEvent(st, S.join, 0));  // the gathered bodies
     layout<T><<<blocks(n), 256, 0, st>>>(counters, as<int>(S.bfirst), as<int>(S.blast), as<int>(S.bdelta),
                                      as<uint8_t>(S.top), as<int>(S.oparent), as<uint32_t>(S.cnt),
                                      as<uint32_t>(S.pscan), as<uint64_t>(S.ukey), as<uint32_t>(S.ufirst),
