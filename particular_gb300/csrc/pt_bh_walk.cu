@@ -104,12 +104,12 @@ __device__ __forceinline__ void lane_walk(float4 p, bool valid, int T, const flo
 }
 
 // ---- group walk (PT_BH_GROUP) ----------------------------------------------
-// One warp walks for 32 key-adjacent targets. Each step pops up to 32 nodes from a
-// shared-memory stack of sibling ranges (independent loads, one per lane), opens a
-// cell when the reference's per-body rule opens it for at least one of the 32
-// targets (so never less accurate than that rule), and appends accepted nodes to a
-// shared-memory interaction list. A full list is evaluated densely: every lane runs its target
-// against all entries, two entries per packed f32x2 instruction.
+// One warp walks for 32 x GW_TPL (64) key-adjacent targets. Each step pops up to 32
+// nodes from a shared-memory stack of sibling ranges (independent loads, one per
+// lane), opens a cell when the reference's per-body rule opens it for at least one of
+// the targets (so never less accurate than that rule), and appends accepted nodes to
+// shared-memory interaction lists. A full list is evaluated densely: every lane runs
+// its targets against all entries, two entries per packed f32x2 instruction.
 // Warps (groups) per CTA of the group walk. A CTA's slot is held until its slowest
 // warp ends, so with one warp per CTA no warp slot idles behind a neighbouring group's
 // longer walk; the local-expansion lists are sized (64 cells, 88 bodies) so that 20
