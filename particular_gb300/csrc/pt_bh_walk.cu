@@ -266,7 +266,7 @@ __device__ __forceinline__ void eval_list(IList<NF, CAP> &Lst, int cnt, const f2
 // ---- learned correction: records of marginal cells ---------------------------
 // The walk (PT_BH_LEARNED) does not evaluate the network itself: it records the
 // node index of every marginal cell (accepted at theta, opened at theta_inner) in
-// chunks of LCHUNK entries that each belong to one warp (one group of 32 targets),
+// chunks of LCHUNK entries that each belong to one warp (one group of 64 targets),
 // chained per group in walk order, and the group's centre. A tensor-core kernel then
 // evaluates all records (bh_learned_eval) and bh_learned_apply adds each group's
 // sum, chunk by chunk in chain order, so results do not depend on scheduling.
