@@ -504,12 +504,15 @@ static_assert(GW_GROUP == (1 << GW_SHIFT), "targets per lane: 1, 2 or 4");
 #define PT_GW_LSTACK 288
 #endif
 // Opened cells with at most this many nodes below them are summed body by body at
-// once instead of being walked level by level (<= 31: one warp-wide load; 0 = off).
+// once instead of being walked level by level (loaded 32 nodes per round; 0 = off).
+// The calibrated headline at N = 4M (fastest configuration within the error margin)
+// for limits 7 / 15 / 31 / 47 / 63 / 95 / 127: 5.26 / 5.65 / 6.07 / 6.10 / 6.05 /
+// 5.92 / 5.77 e8 bodies/s.
 #ifndef PT_GW_FLAT
 #define PT_GW_FLAT 31
 #endif
 constexpr int GW_FLAT = PT_GW_FLAT;
-static_assert(GW_FLAT >= 0 && GW_FLAT <= 31, "a flattened subtree is loaded by one warp");
+static_assert(GW_FLAT >= 0 && GW_FLAT <= 1023, "flattened subtree size");
 #ifndef PT_GW_MINB
 #define PT_GW_MINB (GW_TPL == 1 ? 6 : 5)  // 4-warp CTAs per SM the register budget is set for
 #endif
