@@ -288,7 +288,8 @@ class BarnesHutWorkload:
               (1.5, 27, 2.5e-3, 0.12), (1.5, 27, 2.75e-3, 0.12), (2.0, 27, 2.75e-3, 0.1),
               (2.0, 27, 2.85e-3, 0.1), (2.0, 27, 2.75e-3, 0.11), (2.0, 27, 2.6e-3, 0.12), (2.0, 27, 2.5e-3, 0.13),
               # a fifth entry: the monopole-only factor (else `mono`)
-              (2.0, 27, 2.75e-3, 0.1, 0.1), (2.0, 27, 2.6e-3, 0.1, 0.2), (2.0, 27, 2.75e-3, 0.1, 0.2)]
+              (2.0, 27, 2.75e-3, 0.1, 0.1), (2.0, 27, 2.6e-3, 0.1, 0.2), (2.0, 27, 2.75e-3, 0.1, 0.2),
+              (2.0, 27, 2.9e-3, 0.1), (2.0, 27, 3e-3, 0.1), (2.0, 27, 2.85e-3, 0.11), (2.0, 27, 2.9e-3, 0.1, 0.2)]
 
     def __init__(self, n=4194304, softening=0.01, sample=2048, holdout=4096):
         from particular_gb300 import ics
