@@ -189,3 +189,24 @@ def test_headline_configuration_degenerate_inputs(res, oracle):
     assert not m.compute(massless).any()
     assert not m.compute(Between(b, np.zeros((0, 4), np.float32))).any()
     assert m.compute(Between(np.zeros((0, 4), np.float32), b)).shape == (0, 3)
+
+
+def test_headline_configuration_at_full_size(res, oracle):
+    """The bench's headline configuration (theta cap 2.0, quadrupole + group + local
+    expansion at ratio 0.11, alpha 2.75e-3, monopole factor 0.15) on another seed of
+    the N = 4,194,304 bulge+disk mixture: FP64-judged p95 on 2048 bodies within the
+    bench's bar (the calibration keeps a 10 % margin for samples like this one)."""
+    b = ics.bulge_disk(1 << 22, seed=4242)["bodies"]
+    idx = np.sort(np.random.default_rng(11).choice(b.shape[0], 2048, replace=False))
+    m = cuda.BarnesHut(2.0, res, AccelerationSoftened(0.01), quadrupole=True, group=True, local=True,
+                       relative=2.75e-3, monopole=0.15)
+    N.check(N.lib().pt_bh_set_local_ratio(res.handle, 0.11))
+    try:
+        got = m.compute(b)
+    finally:  # the context's defaults again
+        N.check(N.lib().pt_bh_set_local_ratio(res.handle, 0.1))
+        N.check(N.lib().pt_bh_set_relative_alpha(res.handle, 2.5e-3))
+        N.check(N.lib().pt_bh_set_relative_monopole(res.handle, 0.1))
+    e = rel(got[idx], oracle.bf_f64(b[idx], b, 0.01, True))
+    assert np.isfinite(got).all()
+    assert np.percentile(e, 95) <= 1.05e-3, np.percentile(e, 95)
